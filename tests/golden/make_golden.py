@@ -1,0 +1,217 @@
+"""Record golden vectors by running the upstream fluidimage PIV code itself.
+
+Run from the repository root (needs the upstream sources, not needed afterwards):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [case ...]
+
+Each case writes ``tests/golden/<case>.npz`` holding the input images, the
+parameters (JSON) and the upstream outputs of ``WorkPIV.calcul`` (every pass:
+displacements, positions, peak values, errors, interpolated fields) or of the
+per-window correlation plugin ``CorrelFFTNumpy``.  Upstream runs with
+``method_correl = "np.fft"`` in pure-Python transonic mode (see refharness.py).
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(ROOT))
+
+import refharness  # noqa: E402
+
+refharness.install()
+
+from fluidimage.calcul.correl import CorrelFFTNumpy  # noqa: E402
+from fluidimage.calcul.errors import PIVError  # noqa: E402
+from fluidimage.works.piv import WorkPIV  # noqa: E402
+
+from fluidimage_gb300 import synthetic  # noqa: E402
+
+PASS_KEYS = [
+    "deltaxs", "deltays", "xs", "ys", "correls_max", "deltaxs_input", "deltays_input",
+    "deltaxs_approx", "deltays_approx", "ixvecs_approx", "iyvecs_approx",
+    "deltaxs_final", "deltays_final", "ixvecs_final", "iyvecs_final",
+    "deltaxs_smooth", "deltays_smooth", "xs_smooth", "ys_smooth",
+]
+
+
+def _encode_dict(prefix, d, out):
+    keys = np.array(sorted(d.keys()), dtype=np.int64)
+    out[prefix + "_keys"] = keys
+    vals = [d[int(k)] for k in keys]
+    if vals and isinstance(vals[0], str):
+        out[prefix + "_vals"] = np.array(vals, dtype=str) if vals else np.array([], dtype=str)
+    else:
+        out[prefix + "_vals"] = np.array(vals, dtype=np.float64)
+
+
+def run_workpiv(name, im0, im1, settings, keep_planes=False):
+    params = WorkPIV.create_default_params()
+    params.piv0.method_correl = "np.fft"
+    for path, value in settings.items():
+        obj = params
+        parts = path.split(".")
+        for p in parts[:-1]:
+            obj = getattr(obj, p)
+        setattr(obj, parts[-1], value)
+    work = WorkPIV(params)
+    result = work.calcul({"arrays": (im0, im1), "names": ("im0", "im1")})
+    out = {
+        "im0": im0,
+        "im1": im1,
+        "settings": np.array(json.dumps(settings)),
+        "numpy_version": np.array(np.__version__),
+        "nb_passes": np.array(len(result.passes)),
+    }
+    for ip, r in enumerate(result.passes):
+        work_piv = work.works_piv[ip]
+        out[f"p{ip}_ixvecs"] = np.asarray(work_piv.ixvecs)
+        out[f"p{ip}_iyvecs"] = np.asarray(work_piv.iyvecs)
+        out[f"p{ip}_shape_crop"] = np.asarray(work_piv.shape_crop_im0)
+        for key in PASS_KEYS:
+            if hasattr(r, key):
+                out[f"p{ip}_{key}"] = np.asarray(getattr(r, key))
+        _encode_dict(f"p{ip}_errors", r.errors, out)
+        for key in ("deltaxs_wrong", "deltays_wrong"):
+            if hasattr(r, key):
+                _encode_dict(f"p{ip}_{key}", getattr(r, key), out)
+        if keep_planes:
+            n0, n1 = work_piv.shape_crop_im0
+            planes = np.full((len(r.correls), n0, n1), np.nan, dtype=np.float32)
+            for i, c in enumerate(r.correls):
+                if c is not None:
+                    planes[i] = c
+            out[f"p{ip}_planes"] = planes
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"wrote {name}.npz")
+
+
+def case_correl_window():
+    """Per-window plugin: planes, norms, peaks and subpix of CorrelFFTNumpy."""
+    out = {"numpy_version": np.array(np.__version__)}
+    rng_cases = [
+        ("sq32", (32, 32), (3.3, 5.8), None),
+        ("sq32_dmax", (32, 32), (3.3, 5.8), "50%"),
+        ("sq16", (16, 16), (-2.4, 1.6), None),
+        ("sq64", (64, 64), (7.7, -4.2), None),
+    ]
+    for icase, (tag, shape, shift, dmax) in enumerate(rng_cases):
+        model = synthetic.ParticleModel(density=0.06, noise=2.0, dtype="uint8")
+        big0, big1 = synthetic.make_pair((shape[0] + 40, shape[1] + 40),
+                                         synthetic.uniform_shift(*shift), model,
+                                         seed=100 + icase, as_float32=True)
+        im0 = np.ascontiguousarray(big0[20:20 + shape[0], 20:20 + shape[1]])
+        im1 = np.ascontiguousarray(big1[20:20 + shape[0], 20:20 + shape[1]])
+        correl = CorrelFFTNumpy(shape, shape, method_subpix="2d_gaussian2",
+                                nsubpix=None, displacement_max=dmax)
+        for pair_tag, (a, b) in (("same", (im0, im0)), ("shift", (im0, im1))):
+            key = f"{tag}_{pair_tag}"
+            plane, norm = correl(a, b)
+            out[key + "_im0"] = a
+            out[key + "_im1"] = b
+            out[key + "_plane"] = plane.copy()
+            out[key + "_norm"] = np.array(norm)
+            try:
+                dx, dy, cmax, _ = correl.compute_displacements_from_correl(plane, norm)
+                err = ""
+            except PIVError as e:
+                dx, dy, cmax = e.results
+                err = e.explanation
+            out[key + "_peak"] = np.array([dx, dy, cmax], dtype=np.float64)
+            out[key + "_err"] = np.array(err)
+            out[key + "_plane_after"] = plane
+            if not err:
+                sdx, sdy = correl.apply_subpix(dx, dy, plane)
+                out[key + "_subpix"] = np.array([sdx, sdy], dtype=np.float64)
+            out[key + "_dmax"] = np.array(json.dumps(dmax))
+    np.savez_compressed(HERE / "correl_window.npz", **out)
+    print("wrote correl_window.npz")
+
+
+def case_single_pass_c1():
+    """512x512 float32-from-uint8, shift (3.3, -1.7), 32 px windows, overlap 0.5."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0),
+                                    intensity=(128, 255), noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((512, 512), synthetic.uniform_shift(3.3, -1.7),
+                                   model, seed=1000, as_float32=True)
+    run_workpiv("single_pass_c1", im0, im1, {
+        "piv0.shape_crop_im0": 32, "piv0.grid.overlap": 0.5,
+        "piv0.method_subpix": "2d_gaussian2", "multipass.number": 1,
+        "fix.threshold_diff_neighbour": None, "fix.correl_min": float("-inf"),
+    })
+
+
+def case_multipass_small():
+    """Config-2 recipe on a 384x384 uint16 Oseen pair: 64->32->16, TPS every pass."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0),
+                                    intensity=(1000, 4000), noise=20.0, dtype="uint16")
+    field = synthetic.oseen_vortex((384, 384), d_max=8.0, rc=60.0)
+    im0, im1 = synthetic.make_pair((384, 384), field, model, seed=2000)
+    run_workpiv("multipass_small", im0, im1, {
+        "piv0.shape_crop_im0": 64, "piv0.grid.overlap": 0.5,
+        "multipass.number": 3, "multipass.coeff_zoom": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 200, "multipass.smoothing_coef": 0.5,
+        "fix.threshold_diff_neighbour": 2,
+    })
+
+
+def case_dmax():
+    """displacement_max='50%' mask, two passes with TPS, uint8 sinusoid field."""
+    model = synthetic.ParticleModel(density=0.05, noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((256, 256), synthetic.sinusoid(4.0, 256.0), model,
+                                   seed=3000)
+    run_workpiv("dmax_two_pass", im0, im1, {
+        "piv0.shape_crop_im0": 32, "piv0.grid.overlap": 0.5,
+        "piv0.displacement_max": "50%",
+        "multipass.number": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 100, "multipass.smoothing_coef": 2.0,
+        "fix.displacement_max": 10, "fix.threshold_diff_neighbour": 3,
+    }, keep_planes=True)
+
+
+def case_edges():
+    """Peaks beyond the window (boundary errors, second chance), a blank region
+    (zero-variance windows) and image borders, 16 px windows, single pass."""
+    model = synthetic.ParticleModel(density=0.04, noise=3.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((160, 192), synthetic.uniform_shift(6.6, -7.3), model,
+                                   seed=4000)
+    im0[40:100, 60:130] = 17
+    im1[40:100, 60:130] = 17
+    run_workpiv("edges_single_pass", im0, im1, {
+        "piv0.shape_crop_im0": 16, "piv0.grid.overlap": 0.5,
+        "multipass.number": 1, "multipass.use_tps": False,
+        "fix.threshold_diff_neighbour": None,
+    }, keep_planes=True)
+
+
+def case_griddata():
+    """Two passes with the default ``use_tps='last'`` (griddata between passes)."""
+    model = synthetic.ParticleModel(density=0.05, noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((256, 256), synthetic.uniform_shift(-2.2, 3.6), model,
+                                   seed=5000)
+    run_workpiv("griddata_two_pass", im0, im1, {
+        "piv0.shape_crop_im0": 32, "piv0.grid.overlap": 0.5,
+        "multipass.number": 2, "multipass.use_tps": "last",
+    })
+
+
+CASES = {
+    "correl_window": case_correl_window,
+    "single_pass_c1": case_single_pass_c1,
+    "multipass_small": case_multipass_small,
+    "dmax_two_pass": case_dmax,
+    "edges_single_pass": case_edges,
+    "griddata_two_pass": case_griddata,
+}
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        CASES[name]()
