@@ -1,0 +1,367 @@
+"""Benchmark: PIV vectors/s of the multipass drop-in on one GB300.
+
+Workload ("config2"): one 2048x2048 uint16 (12-bit) particle-image pair, Oseen
+vortex (rc 200 px, peak 8 px), three passes 64 -> 32 -> 16 px windows with
+overlap 0.5, WorkFIX neighbour threshold 2, thin-plate-spline interpolation
+between passes and at the end (subdomains of 200 vectors, smoothing 0.5).
+One step = ``WorkPIV.calcul`` of one pair; the counted vectors are the final
+field's (65025 per pair).
+
+* ``value``: device-resident images, CUDA events around each step, L2 flushed
+  (a 512 MiB write) between steps outside the timed events.
+* ``e2e``: the public API ``WorkPIV.calcul`` from pinned host images to host
+  ``MultipassPIVResults`` (host<->device copies inside the timed region).
+* ``roofline``: the dominant kernel, timed with CUDA events inside the timed
+  steps, against MEASURED_PEAKS.json.
+* ``cpu_baseline``: the CPU oracle (numpy restatement of the reference path), one
+  thread, on a 512x512 crop of the same workload.
+
+``--impl reference`` times that CPU oracle on all host cores (one process per
+core, one 512x512 sample pair per process and step) with the same metric.
+
+Multi-GPU: replicas only (pairs are independent; no collective on the data path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "PIV vectors/s at <=0.005 px vs FP64; plain FP32 vs batched tensor-core form"
+UNIT = "vectors/s"
+WORKLOAD = "config2: 2048x2048 uint16 pair, Oseen vortex, 3 passes 64/32/16 px, overlap 0.5, fix thr 2, TPS subdom 200 smoothing 0.5"
+SAMPLE_SHAPE = (512, 512)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------
+# CPU oracle (reference arm and cpu_baseline): runs in separate processes
+# ------------------------------------------------------------------------------------
+def _oracle_sample(pair):
+    """Run the oracle multipass on one 512x512 sample pair; returns (vectors, seconds)."""
+    from fluidimage_gb300 import WorkPIV, workloads
+    from oracle import piv as O
+
+    (im0, im1), _ = workloads.config2_images(pair=pair, shape=SAMPLE_SHAPE)
+    params = workloads.config2_params(WorkPIV.create_default_params())
+    t0 = time.perf_counter()
+    res = O.multipass(im0, im1, params)
+    dt = time.perf_counter() - t0
+    return int(res[-1].deltaxs.size), dt
+
+
+def _oracle_worker(pair, q):
+    q.put(_oracle_sample(pair))
+
+
+def cpu_baseline_single():
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    code = ("import sys, json; sys.path.insert(0, %r); import bench; "
+            "print(json.dumps(bench._oracle_sample(0)))" % str(ROOT))
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         timeout=600)
+    if out.returncode != 0:
+        return None
+    nvec, dt = json.loads(out.stdout.strip().splitlines()[-1])
+    return {"value": nvec / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"one {SAMPLE_SHAPE[0]}x{SAMPLE_SHAPE[1]} pair of the same workload "
+                      f"({nvec} final vectors, 3 passes + fix + TPS) in {dt:.2f} s, "
+                      "numpy oracle, 1 thread"}
+
+
+def run_reference(args):
+    """Reference arm: the CPU oracle on all host cores, one process per core."""
+    import multiprocessing as mp
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    os.environ.update(OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    step_times, nvec_total = [], 0
+    for step in range(args.warmup + args.steps):
+        q = ctx.Queue()
+        procs = [ctx.Process(target=_oracle_worker, args=(1000 * step + c, q))
+                 for c in range(cores)]
+        t0 = time.perf_counter()
+        for p in procs:
+            p.start()
+        res = [q.get() for _ in procs]
+        for p in procs:
+            p.join()
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            step_times.append(dt)
+            nvec_total = sum(r[0] for r in res)
+    ms = 1e3 * statistics.mean(step_times)
+    value = nvec_total / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD,
+                                        "sample": f"{cores} pairs of {SAMPLE_SHAPE} per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x one {SAMPLE_SHAPE[0]}x"
+                                   f"{SAMPLE_SHAPE[1]} pair each per step (numpy oracle)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_gpu(args):
+    import torch
+
+    from fluidimage_gb300 import WorkPIV, _lib, engine, workloads
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_
+
+        dist_.init_process_group("nccl")
+        dist = dist_
+    lib = _lib.load()
+
+    (im0, im1), _ = workloads.config2_images(pair=rank)
+    params = workloads.config2_params(WorkPIV.create_default_params())
+    work = WorkPIV(params, device=dev)
+    t0 = torch.from_numpy(im0.view(np.int16)).to(dev)
+    t1 = torch.from_numpy(im1.view(np.int16)).to(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(args.warmup):
+        outs = work.calcul_device(t0, t1)
+    torch.cuda.synchronize()
+    nvec_final = outs[-1].layout.nvec
+
+    timer = engine.KernelTimer()
+    clocks = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.fi_launch_count()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        engine.TIMER = timer
+        ev0.record()
+        outs = work.calcul_device(t0, t1)
+        ev1.record()
+        engine.TIMER = None
+        torch.cuda.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = lib.fi_launch_count() - launches0
+    if dist is not None:
+        dist.barrier()
+    ms = statistics.mean(step_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nvec_final / (ms / 1e3)
+
+    # ---- end to end through the public API (pinned host images -> host results)
+    h0 = torch.from_numpy(im0.view(np.int16)).pin_memory()
+    h1 = torch.from_numpy(im1.view(np.int16)).pin_memory()
+    res = work.calcul({"arrays": (h0, h1), "names": ("im0", "im1")})
+    d2h = _result_bytes(res)
+    e2e_ms = []
+    for _ in range(args.e2e_steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t_start = time.perf_counter()
+        res = work.calcul({"arrays": (h0, h1), "names": ("im0", "im1")})
+        torch.cuda.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t_start))
+    e2e_value = world * nvec_final / (statistics.mean(e2e_ms) / 1e3)
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    kern = timer.summary()
+    dominant = max(kern.items(), key=lambda kv: kv[1]["total_ms"])
+    peaks, peak_kind = _peaks()
+    roof = roofline(dominant, outs, work, peaks, peak_kind, args.steps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FFT correlation), f64 (TPS solve)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs_per_step_per_gpu": 1,
+                   "final_vectors_per_pair": nvec_final,
+                   "l2": "512 MiB flush write between timed steps (untimed)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(im0.nbytes + im1.nbytes),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
+        "gpu_launches": int(launches),
+        "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kern.items()},
+        "roofline": roof,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_single()
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _result_bytes(res):
+    total = 0
+    for r in res.passes:
+        for v in vars(r).values():
+            if isinstance(v, np.ndarray):
+                total += v.nbytes
+    return total
+
+
+def roofline(dominant, outs, work, peaks, peak_kind, steps):
+    """Roofline of the dominant library entry point (algorithmic work per launch)."""
+    name, stats = dominant
+    avg_s = stats["avg_ms"] / 1e3
+    if name == "fi_tps_solve":
+        # FP64 LU of (N+3)^2 systems: 2/3 (N+3)^3 flops per subdomain; bound by the
+        # FP64 pipe (no measured FP64 peak: nominal 1.25 TFLOP/s)
+        flops = 0.0
+        nlaunch = 0
+        for pd in outs:
+            for tps in (pd.tps_next, pd.tps_final):
+                if tps is not None:
+                    n = tps.counts.astype(np.float64) + 3
+                    flops += float((2.0 / 3.0 * n**3).sum())
+                    nlaunch += 1
+        per_launch = flops / max(nlaunch, 1)
+        achieved = per_launch / avg_s / 1e12
+        peak = 1.25
+        return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
+                "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
+    # correlation / other: HBM bound by the unique image bytes + outputs
+    nbytes = 0.0
+    nlaunch = 0
+    for pd in outs:
+        H, W = work._pipelines[next(iter(work._pipelines))].imshape, None
+        lay = pd.layout
+        nbytes += 2 * H[0] * H[1] * 2 + 16 * lay.nvec
+        nlaunch += 1
+    per_launch = nbytes / max(nlaunch, 1)
+    achieved = per_launch / avg_s / 1e9
+    peak = float(peaks["hbm_gbs"])
+    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+            "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

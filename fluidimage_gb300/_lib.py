@@ -1,0 +1,142 @@
+"""ctypes binding of ``libfluidimage_gb300.so`` (the C ABI in include/fluidimage_gb300.h).
+
+The library is built in-tree by ``fluidimage_gb300.build``; loading fails loudly
+when it is missing — there is no fallback implementation.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import build as _build
+
+FI_OK = 0
+FI_U8, FI_U16, FI_F32 = 0, 1, 2
+
+VEC_OK = 0
+VEC_PEAK_BOUNDARY = 1
+VEC_PEAK_NAN = 2
+VEC_WRONG_SUBPIX = 3
+VEC_BAD_CROP = 4
+VEC_ALL_NAN = 5
+
+FLAG_NEAR_TIE = 1
+
+FIX_CORREL_MIN = 1
+FIX_DISPLACEMENT = 2
+FIX_NEIGHBOUR = 4
+
+P = C.c_void_p
+
+
+class PivPassArgs(C.Structure):
+    _fields_ = [
+        ("im0", P), ("im1", P), ("dtype", C.c_int), ("height", C.c_int), ("width", C.c_int),
+        ("im_min", P), ("n", C.c_int), ("ixvecs", P), ("nx", C.c_int), ("iyvecs", P),
+        ("ny", C.c_int), ("dxin", P), ("dyin", P), ("mask", P),
+        ("box_i0_start", C.c_int), ("box_i0_stop", C.c_int), ("box_i1_start", C.c_int),
+        ("box_i1_stop", C.c_int), ("particle_radius", C.c_int), ("apply_subpix", C.c_int),
+        ("deltaxs", P), ("deltays", P), ("correls_max", P), ("errors", P), ("xs", P),
+        ("ys", P), ("norms", P), ("planes", P), ("flags", P),
+    ]
+
+
+class FixArgs(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("deltaxs", P), ("deltays", P), ("correls_max", P),
+        ("errors", P), ("correl_min", C.c_float), ("use_displacement_max", C.c_int),
+        ("displacement_max", C.c_float), ("use_threshold", C.c_int), ("threshold", C.c_float),
+        ("deltaxs_out", P), ("deltays_out", P), ("fix_flags", P), ("diff2", P), ("work", P),
+    ]
+
+
+class TpsPlan(C.Structure):
+    _fields_ = [
+        ("num_centers", C.c_int), ("nb_subdomx", C.c_int), ("nb_subdomy", C.c_int),
+        ("status", C.c_int), ("smoothing", C.c_double), ("x_min", C.c_double),
+        ("x_max", C.c_double), ("y_min", C.c_double), ("y_max", C.c_double),
+        ("buffer_x", C.c_double), ("buffer_y", C.c_double),
+    ]
+
+
+_SIGNATURES = {
+    "fi_last_error": (C.c_char_p, []),
+    "fi_version": (C.c_char_p, []),
+    "fi_abi_sizes": (C.c_int, [P]),
+    "fi_launch_count": (C.c_longlong, []),
+    "fi_images_min": (C.c_int, [P, P, C.c_int, C.c_int64, P, P]),
+    "fi_piv_pass": (C.c_int, [P, P]),
+    "fi_correl_windows": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P]),
+    "fi_peaks_from_planes": (
+        C.c_int,
+        [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+         P, P, P, P, P, P, P],
+    ),
+    "fi_subpix_at": (C.c_int, [P, C.c_int, C.c_int, P, P, P, P, P, P]),
+    "fi_fix": (C.c_int, [P, P]),
+    "fi_tps_plan_make": (
+        C.c_int,
+        [P, P, P, P, C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, P, P, P],
+    ),
+    "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P]),
+    "fi_tps_solve": (
+        C.c_int,
+        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, C.c_double, C.c_int, P, P, P, P,
+         P, P, P, P, P],
+    ),
+    "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
+    "fi_tps_interpolate": (
+        C.c_int,
+        [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,
+         P, P, P, P, P],
+    ),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.library_path()
+
+
+def load() -> C.CDLL:
+    """Load the CUDA library (build it first with ``fluidimage_gb300.build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise RuntimeError(
+            f"{path} is missing: build it with `python -m fluidimage_gb300.build` "
+            "(the GB300 path has no CPU fallback)"
+        )
+    lib = C.CDLL(str(path))
+    for name, (restype, argtypes) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _lib = lib
+    return lib
+
+
+class CudaLibError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str = ""):
+    if rc != FI_OK:
+        msg = load().fi_last_error().decode(errors="replace")
+        raise CudaLibError(f"{what or 'fluidimage_gb300'} failed ({rc}): {msg}")
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a torch tensor (None for None)."""
+    return None if t is None else t.data_ptr()
+
+
+def stream_handle(stream=None) -> int:
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

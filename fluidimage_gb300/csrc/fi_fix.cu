@@ -1,0 +1,148 @@
+// False-vector removal of one pass: WorkFIX.calcul (works/piv/fix.py:66-133) with
+// the NaN-aware 8-neighbour mean mean_neighbors_xy (calcul/mean_neighbors.py:5-155).
+//
+// Stage A (elementwise): vectors with a correlation error, with
+// correls_max < correl_min or with |d|^2 > displacement_max^2 become NaN.
+// Stage B (3x3 stencil on the vector grid): |d - mean8(d)|^2 > threshold^2 -> NaN.
+// All arithmetic is float32 in the upstream operation order; comparisons use the
+// float32-rounded thresholds (numpy 2 scalar promotion).
+#include "fi_common.cuh"
+
+namespace fi {
+
+__global__ void k_fix_a(fi_fix_args a, int nvec, float cmin, float dmax2, float* ox, float* oy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  float dx = a.deltaxs[i], dy = a.deltays[i];
+  bool wrong = a.errors[i] != 0;
+  uint8_t flags = 0;
+  if (wrong) dx = dy = NAN;
+  if (a.correls_max[i] < cmin) {
+    flags |= FI_FIX_CORREL_MIN;
+    if (!wrong) dx = dy = NAN;
+    wrong = true;
+  }
+  if (a.use_displacement_max) {
+    const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    if (d2 > dmax2) {
+      flags |= FI_FIX_DISPLACEMENT;
+      if (!wrong) dx = dy = NAN;
+      wrong = true;
+    }
+  }
+  ox[i] = dx;
+  oy[i] = dy;
+  a.fix_flags[i] = flags;
+  if (a.diff2) a.diff2[i] = NAN;
+}
+
+// a[i0][i1] (0 where NaN) and validity b, read from the stage-A output.
+struct Grid {
+  const float* x;
+  const float* y;
+  int n0, n1;
+  __device__ __forceinline__ bool ok(int i0, int i1) const {
+    const int k = i0 * n1 + i1;
+    return !(isnan(x[k]) || isnan(y[k]));
+  }
+  __device__ __forceinline__ float ax(int i0, int i1) const {
+    return ok(i0, i1) ? x[i0 * n1 + i1] : 0.0f;
+  }
+  __device__ __forceinline__ float ay(int i0, int i1) const {
+    return ok(i0, i1) ? y[i0 * n1 + i1] : 0.0f;
+  }
+  __device__ __forceinline__ float b(int i0, int i1) const { return ok(i0, i1) ? 1.0f : 0.0f; }
+};
+
+// Sum over the neighbours in the order of _mean_neighbors (mean_neighbors.py:5-125).
+template <int C>  // C = 0: x, 1: y, 2: count
+__device__ __forceinline__ float nsum(const Grid& g, int i0, int i1) {
+  auto v = [&](int r, int c) -> float {
+    if (C == 0) return g.ax(r, c);
+    if (C == 1) return g.ay(r, c);
+    return g.b(r, c);
+  };
+  const int n0 = g.n0, n1 = g.n1;
+  const bool top = i0 == 0, bot = i0 == n0 - 1, lef = i1 == 0, rig = i1 == n1 - 1;
+  if ((top || bot) && (lef || rig)) {  // corners
+    const int d0 = top ? 1 : -1, d1 = lef ? 1 : -1;
+    return __fadd_rn(__fadd_rn(v(i0 + d0, i1), v(i0 + d0, i1 + d1)), v(i0, i1 + d1));
+  }
+  if (top || bot) {
+    const int dn = top ? 1 : -1;
+    float s = __fadd_rn(v(i0, i1 - 1), v(i0, i1 + 1));
+    s = __fadd_rn(s, v(i0 + dn, i1 + 1));
+    s = __fadd_rn(s, v(i0 + dn, i1));
+    s = __fadd_rn(s, v(i0 + dn, i1 - 1));
+    return s;
+  }
+  if (lef || rig) {
+    const int dn = lef ? 1 : -1;
+    float s = __fadd_rn(v(i0 - 1, i1), v(i0 + 1, i1));
+    s = __fadd_rn(s, v(i0 - 1, i1 + dn));
+    s = __fadd_rn(s, v(i0, i1 + dn));
+    s = __fadd_rn(s, v(i0 + 1, i1 + dn));
+    return s;
+  }
+  float s = __fadd_rn(v(i0, i1 - 1), v(i0, i1 + 1));
+  s = __fadd_rn(s, __fadd_rn(v(i0 - 1, i1 + 1), v(i0 + 1, i1 + 1)));
+  s = __fadd_rn(s, __fadd_rn(v(i0 - 1, i1), v(i0 + 1, i1)));
+  s = __fadd_rn(s, __fadd_rn(v(i0 - 1, i1 - 1), v(i0 + 1, i1 - 1)));
+  return s;
+}
+
+__global__ void k_fix_b(fi_fix_args a, const float* ix, const float* iy, float thr2) {
+  const int nvec = a.nx * a.ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  Grid g{ix, iy, a.ny, a.nx};
+  const int i0 = i / a.nx, i1 = i % a.nx;
+  const float dx = ix[i], dy = iy[i];
+  float ox = dx, oy = dy;
+  if (g.ok(i0, i1)) {
+    const float cnt = nsum<2>(g, i0, i1);
+    if (cnt != 0.0f) {
+      const float mx = __fdiv_rn(nsum<0>(g, i0, i1), cnt);
+      const float my = __fdiv_rn(nsum<1>(g, i0, i1), cnt);
+      const float ex = __fsub_rn(mx, dx), ey = __fsub_rn(my, dy);
+      const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+      if (a.diff2) a.diff2[i] = d2;
+      if (d2 > thr2) {
+        a.fix_flags[i] |= FI_FIX_NEIGHBOUR;
+        ox = oy = NAN;
+      }
+    }
+  }
+  a.deltaxs_out[i] = ox;
+  a.deltays_out[i] = oy;
+}
+
+}  // namespace fi
+
+using namespace fi;
+
+extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
+  FI_REQUIRE(args, "fi_fix: null args");
+  const fi_fix_args& a = *args;
+  FI_REQUIRE(a.nx >= 2 && a.ny >= 2, "fi_fix: vector grid must be at least 2 x 2");
+  FI_REQUIRE(a.deltaxs && a.deltays && a.correls_max && a.errors && a.deltaxs_out &&
+                 a.deltays_out && a.fix_flags,
+             "fi_fix: null pointer");
+  FI_REQUIRE(!a.use_threshold || a.work, "fi_fix: the neighbour test needs work[2*nvec]");
+  const int nvec = a.nx * a.ny;
+  cudaStream_t s = (cudaStream_t)stream;
+  const float dmax2 = (float)((double)a.displacement_max * (double)a.displacement_max);
+  const float thr2 = (float)((double)a.threshold * (double)a.threshold);
+  const int threads = 256, blocks = (nvec + threads - 1) / threads;
+  if (a.use_threshold) {
+    float* wx = a.work;
+    float* wy = a.work + nvec;
+    k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
+    k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
+    add_launches(1);
+  } else {
+    k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
+                                       a.deltays_out);
+  }
+  return check_launch("fi_fix");
+}

@@ -1,0 +1,664 @@
+// Thin-plate-spline subdomain smoothing/interpolation in FP64:
+// ThinPlateSplineSubdom (calcul/interpolate/thin_plate_spline_subdom.py:25-280) with
+// compute_tps_weights / compute_tps_matrix (calcul/interpolate/thin_plate_spline.py:
+// 108-216), as called by BaseWorkPIV.apply_interp (works/piv/singlepass.py:466-548).
+//
+// Stages (host-driven, see the C ABI):
+//   plan     : ordered selection of the valid vectors, subdomain layout (1 block)
+//   members  : per-subdomain ordered membership, counts then CSR indices + norm coefs
+//   solve    : per subdomain (one block): build [[K + lambda I, P], [P^T, 0]] in
+//              column-major FP64, LU with partial pivoting, then the iterative
+//              outlier replacement (threshold_tps, <= 10 re-solves) for x and y
+//              reusing the same factors (the matrix depends on the centres only)
+//   blend    : smoothed values at the centres, weighted by the subdomain norm coefs
+//   eval     : interpolation at new positions, both components per kernel evaluation
+//
+// Layout arithmetic (linspace, buffers, norm coefs) uses round-to-nearest
+// intrinsics so that it reproduces numpy's float64 results bit for bit.
+#include <cmath>
+
+#include "fi_common.cuh"
+
+namespace fi {
+
+__device__ __forceinline__ double linspace_at(double start, double stop, int num, int j) {
+  if (num > 1 && j == num - 1) return stop;
+  if (num <= 1) return start;
+  const double div = (double)(num - 1);
+  const double delta = __dsub_rn(stop, start);
+  const double step = __ddiv_rn(delta, div);
+  if (step == 0.0) return __dadd_rn(__dmul_rn(__ddiv_rn((double)j, div), delta), start);
+  return __dadd_rn(__dmul_rn((double)j, step), start);
+}
+
+struct Limits {
+  double lminx, lmaxx, lminy, lmaxy;
+};
+
+__device__ __forceinline__ Limits subdom_limits(const fi_tps_plan& p, int ix, int iy) {
+  Limits L;
+  L.lminx = __dsub_rn(linspace_at(p.x_min, p.x_max, p.nb_subdomx + 1, ix), p.buffer_x);
+  L.lmaxx = __dadd_rn(linspace_at(p.x_min, p.x_max, p.nb_subdomx + 1, ix + 1), p.buffer_x);
+  L.lminy = __dsub_rn(linspace_at(p.y_min, p.y_max, p.nb_subdomy + 1, iy), p.buffer_y);
+  L.lmaxy = __dadd_rn(linspace_at(p.y_min, p.y_max, p.nb_subdomy + 1, iy + 1), p.buffer_y);
+  return L;
+}
+
+__device__ __forceinline__ bool inside(const Limits& L, double x, double y) {
+  return x >= L.lminx && x < L.lmaxx && y >= L.lminy && y < L.lmaxy;
+}
+
+// _compute_coef_norm (thin_plate_spline_subdom.py:208-222)
+__device__ __forceinline__ double coef_norm(const Limits& L, double x, double y) {
+  const double xc = __dmul_rn(0.5, __dadd_rn(L.lminx, L.lmaxx));
+  const double yc = __dmul_rn(0.5, __dadd_rn(L.lminy, L.lmaxy));
+  const double dxm = __dsub_rn(L.lmaxx, xc), dym = __dsub_rn(L.lmaxy, yc);
+  const double ddx = __dsub_rn(x, xc), ddy = __dsub_rn(y, yc);
+  const double dx2 = __ddiv_rn(__dmul_rn(ddx, ddx), __dmul_rn(dxm, dxm));
+  const double dy2 = __ddiv_rn(__dmul_rn(ddy, ddy), __dmul_rn(dym, dym));
+  return __dadd_rn(__dmul_rn(__dsub_rn(1.0, dx2), __dsub_rn(1.0, dy2)), 0.001);
+}
+
+// r^2 log(r^2) / 2 with r^2 = (y1 - y0)^2 + (x1 - x0)^2 (thin_plate_spline.py:136-145)
+__device__ __forceinline__ double tps_phi(double x0, double y0, double x1, double y1) {
+  const double dy = __dsub_rn(y1, y0), dx = __dsub_rn(x1, x0);
+  const double r2 = __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx));
+  if (r2 == 0.0) return 0.0;
+  return __ddiv_rn(__dmul_rn(r2, log(r2)), 2.0);
+}
+
+// ---------------------------------------------------------------------------
+// block-wide ordered compaction helper (blockDim.x multiple of 32, <= 1024)
+// returns the exclusive position of this thread's element and the chunk total.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int block_scan_flag(bool flag, int* warp_tot, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned b = __ballot_sync(0xffffffffu, flag);
+  const int in_warp = __popc(b & ((1u << lane) - 1u));
+  if (lane == 0) warp_tot[wid] = __popc(b);
+  __syncthreads();
+  if (wid == 0) {
+    int v = lane < nw ? warp_tot[lane] : 0;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane < nw) warp_tot[lane] = incl - v;
+    if (lane == 31) warp_tot[32] = incl;
+  }
+  __syncthreads();
+  const int pos = warp_tot[wid] + in_warp;
+  *total = warp_tot[32];
+  __syncthreads();
+  return pos;
+}
+
+__device__ __forceinline__ double block_reduce_d(double v, double* sh, bool is_max) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = is_max ? fmax(v, u) : fmin(v, u);
+  }
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < nw ? sh[lane] : (is_max ? -INFINITY : INFINITY);
+    for (int o = 16; o > 0; o >>= 1) {
+      const double u = __shfl_xor_sync(0xffffffffu, v, o);
+      v = is_max ? fmax(v, u) : fmin(v, u);
+    }
+    if (lane == 0) sh[32] = v;
+  }
+  __syncthreads();
+  v = sh[32];
+  __syncthreads();
+  return v;
+}
+
+__global__ void __launch_bounds__(1024)
+    k_tps_plan(const float* xs, const float* ys, const float* dx, const float* dy, int nvec,
+               int subdom_size, double smoothing_coef, double pct, fi_tps_plan* plan, double* cx,
+               double* cy, float* ux, float* uy, int32_t* sel) {
+  __shared__ int warp_tot[33];
+  __shared__ double red[33];
+  double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+  int base = 0;
+  for (int c0 = 0; c0 < nvec; c0 += blockDim.x) {
+    const int i = c0 + threadIdx.x;
+    bool ok = false;
+    float vx = 0.f, vy = 0.f;
+    if (i < nvec) {
+      vx = dx[i];
+      vy = dy[i];
+      ok = !(isnan(vx) || isnan(vy));
+    }
+    int total;
+    const int pos = base + block_scan_flag(ok, warp_tot, &total);
+    if (ok) {
+      const double x = (double)xs[i], y = (double)ys[i];
+      cx[pos] = x;
+      cy[pos] = y;
+      ux[pos] = vx;
+      uy[pos] = vy;
+      if (sel) sel[pos] = i;
+      xmin = fmin(xmin, x);
+      xmax = fmax(xmax, x);
+      ymin = fmin(ymin, y);
+      ymax = fmax(ymax, y);
+    }
+    base += total;
+  }
+  xmin = block_reduce_d(xmin, red, false);
+  xmax = block_reduce_d(xmax, red, true);
+  ymin = block_reduce_d(ymin, red, false);
+  ymax = block_reduce_d(ymax, red, true);
+  if (threadIdx.x != 0) return;
+  fi_tps_plan p{};
+  p.num_centers = base;
+  if (base == 0) {
+    p.status = 1;
+    *plan = p;
+    return;
+  }
+  p.x_min = xmin;
+  p.x_max = xmax;
+  p.y_min = ymin;
+  p.y_max = ymax;
+  const double range_x = __dsub_rn(xmax, xmin), range_y = __dsub_rn(ymax, ymin);
+  const double aspect = __ddiv_rn(range_y, range_x);
+  const double nb_subdom = __ddiv_rn((double)base, (double)subdom_size);
+  const double fx = floor(__dsqrt_rn(__ddiv_rn(nb_subdom, aspect)));
+  const double fy = ceil(__dsqrt_rn(__dmul_rn(nb_subdom, aspect)));
+  if (!(fx < 1e6) || !(fy < 1e6)) {  // upstream fails (int(inf) / int(nan))
+    p.status = 2;
+    *plan = p;
+    return;
+  }
+  int nbx = (int)fx, nby = (int)fy;
+  if (nbx == 0) nbx = 1;
+  if (nby == 0) nby = 1;
+  p.nb_subdomx = nbx;
+  p.nb_subdomy = nby;
+  const double x0 = linspace_at(xmin, xmax, nbx + 1, 0), x1 = linspace_at(xmin, xmax, nbx + 1, 1);
+  const double y0 = linspace_at(ymin, ymax, nby + 1, 0), y1 = linspace_at(ymin, ymax, nby + 1, 1);
+  const double per = __ddiv_rn((double)base, (double)(nbx * nby));
+  p.smoothing = __dmul_rn(
+      smoothing_coef, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dsub_rn(x1, x0), __dsub_rn(y1, y0)), per)));
+  const double coef_buffer = __ddiv_rn(pct, 100.0);
+  p.buffer_x = __ddiv_rn(__dmul_rn(coef_buffer, range_x), (double)nbx);
+  p.buffer_y = __ddiv_rn(__dmul_rn(coef_buffer, range_y), (double)nby);
+  p.status = 0;
+  *plan = p;
+}
+
+// Ordered membership of points in subdomain blockIdx.x; mode 0 counts, mode 1 fills.
+__global__ void __launch_bounds__(512)
+    k_tps_members(const fi_tps_plan* plan_ptr, const double* px, const double* py, int npts,
+                  int mode, int32_t* counts, const int64_t* offsets, int32_t* indices,
+                  double* coefs) {
+  __shared__ int warp_tot[33];
+  const fi_tps_plan p = *plan_ptr;
+  const int i = blockIdx.x;
+  const int iy = i / p.nb_subdomx, ix = i % p.nb_subdomx;
+  const Limits L = subdom_limits(p, ix, iy);
+  int base = 0;
+  const int64_t off = (mode == 1) ? offsets[i] : 0;
+  for (int c0 = 0; c0 < npts; c0 += blockDim.x) {
+    const int q = c0 + threadIdx.x;
+    bool in = false;
+    double x = 0.0, y = 0.0;
+    if (q < npts) {
+      x = px[q];
+      y = py[q];
+      in = inside(L, x, y);
+    }
+    int total;
+    const int pos = base + block_scan_flag(in, warp_tot, &total);
+    if (in && mode == 1) {
+      indices[off + pos] = q;
+      coefs[off + pos] = coef_norm(L, x, y);
+    }
+    base += total;
+  }
+  if (threadIdx.x == 0 && mode == 0) counts[i] = base;
+}
+
+// Block argmax of |col[k..n-1]| with the first index on ties (LAPACK idamax).
+__device__ __forceinline__ int block_argmax_abs(const double* col, int k, int n, double* shv,
+                                                int* shi) {
+  double best = -1.0;
+  int bi = n;
+  for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
+    const double v = fabs(col[r]);
+    if (v > best) {
+      best = v;
+      bi = r;
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ov > best || (ov == best && oi < bi)) {
+      best = ov;
+      bi = oi;
+    }
+  }
+  if (lane == 0) {
+    shv[wid] = best;
+    shi[wid] = bi;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    best = lane < nw ? shv[lane] : -1.0;
+    bi = lane < nw ? shi[lane] : n;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) shi[32] = bi;
+  }
+  __syncthreads();
+  const int r = shi[32];
+  __syncthreads();
+  return r;
+}
+
+// Solve (LU, pivots) x = rhs in place; y in shared memory (n doubles).
+__device__ void lu_solve(const double* A, const int32_t* piv, int n, double* y) {
+  for (int k = 0; k < n; ++k) {  // row interchanges in order (dgetrs / dlaswp)
+    if (threadIdx.x == 0) {
+      const int p = piv[k];
+      if (p != k) {
+        const double t = y[k];
+        y[k] = y[p];
+        y[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {  // L (unit diagonal), column oriented
+    const double yk = y[k];
+    const double* col = A + (int64_t)k * n;
+    for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) y[r] -= col[r] * yk;
+    __syncthreads();
+  }
+  for (int k = n - 1; k >= 0; --k) {  // U
+    const double* col = A + (int64_t)k * n;
+    if (threadIdx.x == 0) y[k] = y[k] / col[k];
+    __syncthreads();
+    const double xk = y[k];
+    for (int r = threadIdx.x; r < k; r += blockDim.x) y[r] -= col[r] * xk;
+    __syncthreads();
+  }
+}
+
+// One block per subdomain: build, factorise, iterate the two components.
+__global__ void __launch_bounds__(512)
+    k_tps_solve(const fi_tps_plan* plan_ptr, const double* cx, const double* cy, const float* ux,
+                const float* uy, const int32_t* counts, const int64_t* offsets,
+                const int32_t* indices, const int64_t* mat_off, double* matrices, int32_t* pivots,
+                double threshold, int use_threshold, const int64_t* w_off, double* weights,
+                double* smoothed_x, double* smoothed_y, int32_t* iters, int32_t* nfixed,
+                int32_t* singular, double* max_udiff) {
+  extern __shared__ double sh[];
+  __shared__ double shv[33];
+  __shared__ int shi[33];
+  __shared__ int s_any;
+  const fi_tps_plan p = *plan_ptr;
+  const int sd = blockIdx.x;
+  const int N = counts[sd];
+  const int n = N + 3;
+  const int64_t off = offsets[sd];
+  const int32_t* idx = indices + off;
+  double* A = matrices + mat_off[sd];
+  int32_t* piv = pivots + (off + 3 * (int64_t)sd);
+  double* y = sh;             // n doubles
+  float* vals = reinterpret_cast<float*>(sh + n);  // N floats
+  const double lam = p.smoothing;
+
+  // ---- build IM = [[K + lam I, P], [P^T, 0]], column-major (symmetric) ----
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int c = wid; c < n; c += nw) {
+    double* col = A + (int64_t)c * n;
+    if (c < N) {
+      const int b = idx[c];
+      const double bx = cx[b], by = cy[b];
+      for (int r = lane; r < n; r += 32) {
+        double v;
+        if (r < N) {
+          const int a = idx[r];
+          v = (r == c) ? lam : tps_phi(bx, by, cx[a], cy[a]);
+        } else {
+          v = (r == N) ? 1.0 : ((r == N + 1) ? by : bx);
+        }
+        col[r] = v;
+      }
+    } else {
+      for (int r = lane; r < n; r += 32) {
+        double v = 0.0;
+        if (r < N) {
+          const int a = idx[r];
+          v = (c == N) ? 1.0 : ((c == N + 1) ? cy[a] : cx[a]);
+        }
+        col[r] = v;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- LU with partial pivoting (right-looking, column-major) ----
+  int sing = 0;
+  for (int k = 0; k < n; ++k) {
+    double* colk = A + (int64_t)k * n;
+    const int pr = block_argmax_abs(colk, k, n, shv, shi);
+    const double pv = colk[pr];
+    if (pv == 0.0) {
+      sing = 1;
+      break;
+    }
+    if (threadIdx.x == 0) piv[k] = pr;
+    if (pr != k)
+      for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        double* col = A + (int64_t)c * n;
+        const double t = col[k];
+        col[k] = col[pr];
+        col[pr] = t;
+      }
+    __syncthreads();
+    const double d = colk[k];
+    for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) colk[r] = colk[r] / d;
+    __syncthreads();
+    for (int c = k + 1 + wid; c < n; c += nw) {
+      double* col = A + (int64_t)c * n;
+      const double akc = col[k];
+      for (int r = k + 1 + lane; r < n; r += 32) col[r] -= colk[r] * akc;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) singular[sd] = sing;
+  if (sing) return;
+
+  // ---- iterative outlier replacement, compute_tps_weights_iter (subdom.py:236-280) ----
+  for (int comp = 0; comp < 2; ++comp) {
+    const float* u = comp == 0 ? ux : uy;
+    double* sm = comp == 0 ? smoothed_x : smoothed_y;
+    double* w = weights + w_off[sd] + (int64_t)comp * n;
+    for (int r = threadIdx.x; r < N; r += blockDim.x) vals[r] = u[idx[r]];
+    __syncthreads();
+    int count = 1, fixed = 0;
+    while (true) {
+      for (int r = threadIdx.x; r < n; r += blockDim.x) y[r] = (r < N) ? (double)vals[r] : 0.0;
+      __syncthreads();
+      lu_solve(A, piv, n, y);
+      // smoothed = EM @ w = values - lam * w (rows < N of IM w = rhs)
+      if (threadIdx.x == 0) s_any = 0;
+      __syncthreads();
+      double mx = 0.0;
+      int nbad = 0;
+      for (int r = threadIdx.x; r < N; r += blockDim.x) {
+        const double s = __dsub_rn((double)vals[r], __dmul_rn(lam, y[r]));
+        sm[off + r] = s;
+        const double dif = fabs(__dsub_rn(s, (double)vals[r]));
+        mx = fmax(mx, dif);
+        if (use_threshold && dif > threshold) nbad++;
+      }
+      mx = block_reduce_d(mx, shv, true);
+      if (count == 1 && threadIdx.x == 0) max_udiff[2 * sd + comp] = mx;
+      if (nbad) atomicAdd(&s_any, nbad);
+      __syncthreads();
+      const int bad = s_any;
+      if (!use_threshold || bad == 0 || count > 10) break;
+      fixed += bad;
+      for (int r = threadIdx.x; r < N; r += blockDim.x) {
+        const double s = sm[off + r];
+        const double dif = fabs(__dsub_rn(s, (double)vals[r]));
+        if (dif > threshold) vals[r] = (float)s;
+      }
+      __syncthreads();
+      count++;
+    }
+    for (int r = threadIdx.x; r < n; r += blockDim.x) w[r] = y[r];
+    if (threadIdx.x == 0) {
+      iters[2 * sd + comp] = count;
+      nfixed[2 * sd + comp] = fixed;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Smoothed values at the centres: sum over containing subdomains, in order.
+__global__ void k_tps_blend_centers(const fi_tps_plan* plan_ptr, const double* cx,
+                                    const double* cy, const int32_t* counts,
+                                    const int64_t* offsets, const int32_t* indices,
+                                    const double* coefs, const double* smx, const double* smy,
+                                    double* outx, double* outy) {
+  const fi_tps_plan p = *plan_ptr;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.num_centers) return;
+  const double x = cx[q], y = cy[q];
+  const double wx = __ddiv_rn(__dsub_rn(p.x_max, p.x_min), (double)p.nb_subdomx);
+  const double wy = __ddiv_rn(__dsub_rn(p.y_max, p.y_min), (double)p.nb_subdomy);
+  const int ixc = (wx > 0) ? (int)floor((x - p.x_min) / wx) : 0;
+  const int iyc = (wy > 0) ? (int)floor((y - p.y_min) / wy) : 0;
+  double sx = 0.0, sy = 0.0, nrm = 0.0;
+  for (int iy = clampi(iyc - 2, 0, p.nb_subdomy - 1); iy <= clampi(iyc + 2, 0, p.nb_subdomy - 1); ++iy)
+    for (int ix = clampi(ixc - 2, 0, p.nb_subdomx - 1); ix <= clampi(ixc + 2, 0, p.nb_subdomx - 1); ++ix) {
+      const Limits L = subdom_limits(p, ix, iy);
+      if (!inside(L, x, y)) continue;
+      const int sd = iy * p.nb_subdomx + ix;
+      const int64_t off = offsets[sd];
+      int lo = 0, hi = counts[sd] - 1;
+      while (lo < hi) {  // members are sorted: find q
+        const int mid = (lo + hi) >> 1;
+        if (indices[off + mid] < q) lo = mid + 1; else hi = mid;
+      }
+      const double c = coefs[off + lo];
+      sx = __dadd_rn(sx, __dmul_rn(c, smx[off + lo]));
+      sy = __dadd_rn(sy, __dmul_rn(c, smy[off + lo]));
+      nrm = __dadd_rn(nrm, c);
+    }
+  outx[q] = __ddiv_rn(sx, nrm);
+  outy[q] = __ddiv_rn(sy, nrm);
+}
+
+// Interpolation at the new positions of subdomain blockIdx.y:
+// part[k] = coef_k * (sum_j w_j phi(|q_k - c_j|^2) + w_N + w_N+1 y + w_N+2 x).
+__global__ void __launch_bounds__(256)
+    k_tps_eval(const int32_t* counts, const int64_t* offsets, const int32_t* indices,
+               const int64_t* w_off, const double* weights, const double* cx, const double* cy,
+               const int32_t* ncounts, const int64_t* noffsets, const int32_t* nindices,
+               const double* ncoefs, const double* px, const double* py, double* partx,
+               double* party) {
+  extern __shared__ double sh[];
+  const int sd = blockIdx.y;
+  const int N = counts[sd], n = N + 3, M = ncounts[sd];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x * blockDim.x >= M) return;
+  double* scx = sh;
+  double* scy = sh + N;
+  double* swx = sh + 2 * N;
+  double* swy = sh + 2 * N + n;
+  const int64_t off = offsets[sd];
+  const double* w = weights + w_off[sd];
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    const int a = indices[off + j];
+    scx[j] = cx[a];
+    scy[j] = cy[a];
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    swx[j] = w[j];
+    swy[j] = w[n + j];
+  }
+  __syncthreads();
+  if (k >= M) return;
+  const int64_t noff = noffsets[sd];
+  const int q = nindices[noff + k];
+  const double x = px[q], y = py[q];
+  double vx = 0.0, vy = 0.0;
+  for (int j = 0; j < N; ++j) {
+    const double f = tps_phi(scx[j], scy[j], x, y);
+    vx = fma(swx[j], f, vx);
+    vy = fma(swy[j], f, vy);
+  }
+  vx = fma(swx[N + 2], x, fma(swx[N + 1], y, __dadd_rn(vx, swx[N])));
+  vy = fma(swy[N + 2], x, fma(swy[N + 1], y, __dadd_rn(vy, swy[N])));
+  const double c = ncoefs[noff + k];
+  partx[noff + k] = __dmul_rn(c, vx);
+  party[noff + k] = __dmul_rn(c, vy);
+}
+
+// Gather the interpolated values per new position (subdomain order) and round.
+__global__ void k_tps_gather(const fi_tps_plan* plan_ptr, const int32_t* ncounts,
+                             const int64_t* noffsets, const int32_t* nindices,
+                             const double* ncoefs, const double* partx, const double* party,
+                             const double* px, const double* py, int npts, double* outx,
+                             double* outy, int32_t* rx, int32_t* ry) {
+  const fi_tps_plan p = *plan_ptr;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= npts) return;
+  const double x = px[q], y = py[q];
+  const double wx = __ddiv_rn(__dsub_rn(p.x_max, p.x_min), (double)p.nb_subdomx);
+  const double wy = __ddiv_rn(__dsub_rn(p.y_max, p.y_min), (double)p.nb_subdomy);
+  const int ixc = (wx > 0) ? (int)floor((x - p.x_min) / wx) : 0;
+  const int iyc = (wy > 0) ? (int)floor((y - p.y_min) / wy) : 0;
+  double sx = 0.0, sy = 0.0, nrm = 0.0;
+  for (int iy = clampi(iyc - 2, 0, p.nb_subdomy - 1); iy <= clampi(iyc + 2, 0, p.nb_subdomy - 1); ++iy)
+    for (int ix = clampi(ixc - 2, 0, p.nb_subdomx - 1); ix <= clampi(ixc + 2, 0, p.nb_subdomx - 1); ++ix) {
+      const Limits L = subdom_limits(p, ix, iy);
+      if (!inside(L, x, y)) continue;
+      const int sd = iy * p.nb_subdomx + ix;
+      const int64_t off = noffsets[sd];
+      int lo = 0, hi = ncounts[sd] - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (nindices[off + mid] < q) lo = mid + 1; else hi = mid;
+      }
+      sx = __dadd_rn(sx, partx[off + lo]);
+      sy = __dadd_rn(sy, party[off + lo]);
+      nrm = __dadd_rn(nrm, ncoefs[off + lo]);
+    }
+  const double vx = __ddiv_rn(sx, nrm), vy = __ddiv_rn(sy, nrm);
+  outx[q] = vx;
+  outy[q] = vy;
+  if (rx) rx[q] = (int32_t)rint(vx);
+  if (ry) ry[q] = (int32_t)rint(vy);
+}
+
+}  // namespace fi
+
+using namespace fi;
+
+extern "C" int fi_tps_plan_make(const float* xs, const float* ys, const float* dx, const float* dy,
+                                int nvec, int subdom_size, double smoothing_coef,
+                                double percent_buffer_area, fi_tps_plan* plan, double* cx,
+                                double* cy, float* ux, float* uy, int32_t* selection,
+                                void* stream) {
+  FI_REQUIRE(xs && ys && dx && dy && plan && cx && cy && ux && uy, "fi_tps_plan_make: null pointer");
+  FI_REQUIRE(nvec > 0 && subdom_size > 0, "fi_tps_plan_make: bad sizes");
+  k_tps_plan<<<1, 1024, 0, (cudaStream_t)stream>>>(xs, ys, dx, dy, nvec, subdom_size,
+                                                   smoothing_coef, percent_buffer_area, plan, cx,
+                                                   cy, ux, uy, selection);
+  return check_launch("fi_tps_plan_make");
+}
+
+extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px,
+                              const double* py, int npts, int mode, int32_t* counts,
+                              const int64_t* offsets, int32_t* indices, double* coefs,
+                              void* stream) {
+  FI_REQUIRE(plan && px && py && nb_subdom > 0 && npts > 0, "fi_tps_members: bad arguments");
+  FI_REQUIRE(mode == 0 ? counts != nullptr : (offsets && indices && coefs),
+             "fi_tps_members: missing outputs");
+  k_tps_members<<<nb_subdom, 512, 0, (cudaStream_t)stream>>>(plan, px, py, npts, mode, counts,
+                                                            offsets, indices, coefs);
+  return check_launch("fi_tps_members");
+}
+
+extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members,
+                            const double* cx, const double* cy, const float* ux,
+                            const float* uy, const int32_t* counts, const int64_t* offsets,
+                            const int32_t* indices, const int64_t* mat_offsets, double* matrices,
+                            int32_t* pivots, double threshold, int use_threshold,
+                            const int64_t* w_offsets, double* weights, double* smoothed_x,
+                            double* smoothed_y, int32_t* iters, int32_t* nfixed,
+                            int32_t* singular, double* max_udiff, void* stream) {
+  FI_REQUIRE(plan && counts && offsets && indices && mat_offsets && matrices && pivots &&
+                 w_offsets && weights && smoothed_x && smoothed_y && iters && nfixed &&
+                 singular && max_udiff,
+             "fi_tps_solve: null pointer");
+  FI_REQUIRE(nb_subdom > 0, "fi_tps_solve: no subdomain");
+  const size_t smem = (size_t)(max_members + 3) * sizeof(double) + (size_t)max_members * 4 + 16;
+  FI_REQUIRE(smem <= 200 * 1024, "fi_tps_solve: subdomain of %d vectors too large", max_members);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    attr = smem;
+  }
+  k_tps_solve<<<nb_subdom, 512, smem, (cudaStream_t)stream>>>(
+      plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, pivots, threshold,
+      use_threshold, w_offsets, weights, smoothed_x, smoothed_y, iters, nfixed, singular,
+      max_udiff);
+  return check_launch("fi_tps_solve");
+}
+
+extern "C" int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, const double* cx,
+                                    const double* cy, const int32_t* counts,
+                                    const int64_t* offsets, const int32_t* indices,
+                                    const double* coefs, const double* smoothed_x,
+                                    const double* smoothed_y, double* out_x, double* out_y,
+                                    void* stream) {
+  FI_REQUIRE(plan && cx && cy && counts && offsets && indices && coefs && out_x && out_y,
+             "fi_tps_blend_centers: null pointer");
+  if (num_centers <= 0) return FI_OK;
+  const int threads = 256;
+  k_tps_blend_centers<<<(num_centers + threads - 1) / threads, threads, 0, (cudaStream_t)stream>>>(
+      plan, cx, cy, counts, offsets, indices, coefs, smoothed_x, smoothed_y, out_x, out_y);
+  return check_launch("fi_tps_blend_centers");
+}
+
+extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
+                                  int max_new_members, const double* cx, const double* cy,
+                                  const int32_t* counts, const int64_t* offsets,
+                                  const int32_t* indices, const int64_t* w_offsets,
+                                  const double* weights, const double* px, const double* py,
+                                  int npts, const int32_t* ncounts, const int64_t* noffsets,
+                                  const int32_t* nindices, const double* ncoefs, double* partx,
+                                  double* party, double* out_x, double* out_y, int32_t* out_rx,
+                                  int32_t* out_ry, void* stream) {
+  FI_REQUIRE(plan && cx && cy && counts && offsets && indices && w_offsets && weights && px &&
+                 py && ncounts && noffsets && nindices && ncoefs && partx && party && out_x &&
+                 out_y,
+             "fi_tps_interpolate: null pointer");
+  FI_REQUIRE(nb_subdom > 0 && npts > 0, "fi_tps_interpolate: bad sizes");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t smem = (size_t)(4 * max_members + 6) * sizeof(double);
+  FI_REQUIRE(smem <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
+             max_members);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_eval, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    attr = smem;
+  }
+  if (max_new_members > 0) {
+    const int threads = 256;
+    dim3 grid((max_new_members + threads - 1) / threads, nb_subdom);
+    k_tps_eval<<<grid, threads, smem, s>>>(counts, offsets, indices, w_offsets, weights, cx, cy,
+                                           ncounts, noffsets, nindices, ncoefs, px, py, partx,
+                                           party);
+    add_launches(1);
+  }
+  const int threads = 256;
+  k_tps_gather<<<(npts + threads - 1) / threads, threads, 0, s>>>(
+      plan, ncounts, noffsets, nindices, ncoefs, partx, party, px, py, npts, out_x, out_y, out_rx,
+      out_ry);
+  return check_launch("fi_tps_interpolate");
+}

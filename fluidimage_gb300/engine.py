@@ -1,0 +1,498 @@
+"""Device pipeline of the multipass PIV (one image pair at a time, one GPU).
+
+``PIVPipeline`` holds everything that depends only on the parameters and the
+image shape (window grids, displacement_max masks, device buffers) and runs the
+passes of ``WorkPIV.calcul`` (works/piv/multipass.py:172-190) on device:
+
+    pass 0        fi_piv_pass (grid windows)            -> fi_fix
+    pass k >= 1   TPS(previous pass -> this grid)       -> fi_piv_pass (shifted) -> fi_fix
+    final         TPS(last pass -> its own grid)
+
+Only the window grid and the masks are computed on the host (they depend on
+the parameters, not on the images).  The TPS stages read back a few integers
+(number of valid vectors, subdomain populations) to size their buffers.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib as L
+from .errors import ERROR_STRINGS, InterpError  # noqa: F401  (ERROR_STRINGS re-exported)
+
+_DTYPES = {np.dtype(np.uint8): L.FI_U8, np.dtype(np.uint16): L.FI_U16,
+           np.dtype(np.float32): L.FI_F32}
+
+SUPPORTED_WINDOWS = (16, 24, 32, 48, 64)
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+class KernelTimer:
+    """CUDA-event timing of each library entry point on the launching stream."""
+
+    def __init__(self):
+        self.events = {}
+
+    def record(self, name):
+        torch = _torch()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+        self.events.setdefault(name, []).append((start, end))
+        return end
+
+    def summary(self):
+        torch = _torch()
+        torch.cuda.synchronize()
+        out = {}
+        for name, pairs in self.events.items():
+            ms = [a.elapsed_time(b) for a, b in pairs]
+            out[name] = {"launches": len(ms), "total_ms": float(sum(ms)),
+                         "avg_ms": float(sum(ms) / len(ms))}
+        return out
+
+
+#: set to a KernelTimer to time every library call (benchmark instrumentation)
+TIMER = None
+
+
+class _timed:
+    def __init__(self, name):
+        self.name = name
+        self.end = None
+
+    def __enter__(self):
+        if TIMER is not None:
+            self.end = TIMER.record(self.name)
+        return self
+
+    def __exit__(self, *exc):
+        if self.end is not None:
+            self.end.record()
+        return False
+
+
+# --------------------------------------------------------------------------------
+# host-side layout (parameters only): works/piv/singlepass.py:108-141, 363-389
+# --------------------------------------------------------------------------------
+def crop_start_stop(shape_crop):
+    n0, n1 = shape_crop
+    return (n0 // 2, n1 // 2), (n0 // 2 + n0 % 2, n1 // 2 + n1 % 2)
+
+
+def make_grid(imshape, shape_crop, overlap):
+    """Window-centre vectors ``ixvecs, iyvecs`` (singlepass.py:108-141)."""
+    len_y, len_x = imshape
+    start, stop = crop_start_stop(shape_crop)
+    stepy = shape_crop[0] - int(np.round(overlap * shape_crop[0]))
+    stepx = shape_crop[1] - int(np.round(overlap * shape_crop[1]))
+    if stepy < 1 or stepx < 1:
+        raise ValueError("overlap too large for the window size")
+    ixvec_max = len_x - stop[1]
+    ixvecs = np.arange(start[1], ixvec_max, stepx, dtype=int)
+    iyvec_max = len_y - stop[0]
+    iyvecs = np.arange(start[0], iyvec_max, stepy, dtype=int)
+    if ixvecs.size == 0 or iyvecs.size == 0:
+        raise ValueError("image smaller than the interrogation window")
+    if ixvec_max - ixvecs[-1] > stepx // 2.5:
+        ixvecs = np.append(ixvecs, ixvec_max)
+    if iyvec_max - iyvecs[-1] > stepy // 2.5:
+        iyvecs = np.append(iyvecs, iyvec_max)
+    return ixvecs, iyvecs
+
+
+def parse_displacement_max(displ_max, shape):
+    if isinstance(displ_max, str) and displ_max.endswith("%"):
+        return float(displ_max[:-1]) / 100 * max(shape)
+    return displ_max
+
+
+def displacement_mask(n, displacement_max):
+    """``where_large_displacement`` and search box (calcul/correl.py:518-547)."""
+    if displacement_max is None:
+        return None, (0, n, 0, n)
+    ix0 = iy0 = n // 2 - 1
+    mask = np.zeros((n, n), dtype=bool)
+    for i0 in range(n):
+        for i1 in range(n):
+            dx, dy = ix0 - i1, iy0 - i0
+            mask[i0, i1] = math.sqrt(dx**2 + dy**2) > displacement_max
+    rows = ~mask.all(axis=1)
+    cols = ~mask.all(axis=0)
+    i0s = int(np.argmax(rows)) if rows.any() else n - 1
+    i1s = int(np.argmax(cols)) if cols.any() else n - 1
+    i0e = int(n - np.argmax(rows[::-1])) if rows.any() else 1
+    i1e = int(n - np.argmax(cols[::-1])) if cols.any() else 1
+    return mask, (i0s, i0e, i1s, i1e)
+
+
+def pass_shapes(shape_crop_im0, number, coeff_zoom):
+    """Window shape per pass (works/piv/multipass.py:120-165)."""
+    if isinstance(shape_crop_im0, (int, np.integer)):
+        shape = (int(shape_crop_im0), int(shape_crop_im0))
+    elif isinstance(shape_crop_im0, (tuple, list)) and len(shape_crop_im0) == 2:
+        shape = tuple(shape_crop_im0)
+    else:
+        raise NotImplementedError("For now, shape_crop_im0 has to be one or two integer!")
+    if isinstance(coeff_zoom, int):
+        coeffs = [coeff_zoom] * (number - 1)
+    elif len(coeff_zoom) == number - 1:
+        coeffs = list(coeff_zoom)
+    else:
+        raise ValueError(
+            "params.multipass.coeff_zoom has to be an integer or "
+            "an iterable of length params.multipass.number - 1"
+        )
+    shapes = [tuple(int(s) for s in shape)]
+    for i in range(1, number):
+        shape = (shape[0] / coeffs[i - 1], shape[1] / coeffs[i - 1])
+        shapes.append(tuple(int(s) for s in shape))
+    return shapes
+
+
+@dataclass
+class PassLayout:
+    index: int
+    n: int
+    ixvecs: np.ndarray
+    iyvecs: np.ndarray
+    gx: np.ndarray
+    gy: np.ndarray
+    displacement_max: Optional[float]
+    mask: Optional[np.ndarray]
+    box: tuple
+    apply_subpix: bool
+    dev: dict = field(default_factory=dict)
+
+    @property
+    def nvec(self):
+        return self.gx.size
+
+
+# --------------------------------------------------------------------------------
+# TPS driver (device)
+# --------------------------------------------------------------------------------
+@dataclass
+class TpsOutput:
+    out_x: object  # float64 [npts] device
+    out_y: object
+    rx: object     # int32 [npts] device (rounded)
+    ry: object
+    smooth_x: object = None  # float64 [num_centers] (blend at the centres)
+    smooth_y: object = None
+    selection: object = None  # int32 [num_centers]: index of each centre in the pass
+    num_centers: int = 0
+    nb_subdom: int = 0
+    counts: object = None
+    w_offsets: object = None
+    weights: object = None
+    singular: object = None
+    iters: object = None
+    nfixed: object = None
+    max_udiff: object = None
+
+
+def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
+            threshold, want_smooth, stream):
+    """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548)."""
+    torch = _torch()
+    lib = L.load()
+    dev = xs.device
+    s = L.stream_handle(stream)
+    f64 = dict(dtype=torch.float64, device=dev)
+    i32 = dict(dtype=torch.int32, device=dev)
+    plan = torch.empty(C.sizeof(L.TpsPlan), dtype=torch.uint8, device=dev)
+    cx = torch.empty(nvec, **f64)
+    cy = torch.empty(nvec, **f64)
+    ux = torch.empty(nvec, dtype=torch.float32, device=dev)
+    uy = torch.empty(nvec, dtype=torch.float32, device=dev)
+    sel = torch.empty(nvec, **i32)
+    with _timed("fi_tps_plan_make"):
+        L.check(lib.fi_tps_plan_make(L.ptr(xs), L.ptr(ys), L.ptr(dx), L.ptr(dy), nvec,
+                                     int(subdom_size), float(smoothing_coef), 20.0, L.ptr(plan),
+                                     L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy), L.ptr(sel), s),
+                "fi_tps_plan_make")
+    hdr = L.TpsPlan.from_buffer_copy(plan.cpu().numpy().tobytes())
+    if hdr.status == 1:
+        raise InterpError("Only nan.")
+    if hdr.status != 0:
+        raise ValueError("TPS subdomain layout is degenerate (all vectors on one line)")
+    nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
+    counts = torch.empty(nsub, **i32)
+    ncounts = torch.empty(nsub, **i32)
+    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 0, L.ptr(counts),
+                               None, None, None, s), "fi_tps_members")
+    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 0,
+                               L.ptr(ncounts), None, None, None, s), "fi_tps_members")
+    both = torch.cat([counts, ncounts]).cpu().numpy().astype(np.int64)
+    ch, nch = both[:nsub], both[nsub:]
+    off = np.concatenate([[0], np.cumsum(ch)[:-1]]).astype(np.int64)
+    noff = np.concatenate([[0], np.cumsum(nch)[:-1]]).astype(np.int64)
+    msz = (ch + 3) ** 2
+    moff = np.concatenate([[0], np.cumsum(msz)[:-1]]).astype(np.int64)
+    wsz = 2 * (ch + 3)
+    woff = np.concatenate([[0], np.cumsum(wsz)[:-1]]).astype(np.int64)
+    tot, ntot = int(ch.sum()), int(nch.sum())
+    offs = torch.from_numpy(np.concatenate([off, noff, moff, woff])).to(dev, non_blocking=True)
+    off_d, noff_d, moff_d, woff_d = offs[:nsub], offs[nsub:2 * nsub], offs[2 * nsub:3 * nsub], offs[3 * nsub:]
+    idx = torch.empty(max(tot, 1), **i32)
+    coefs = torch.empty(max(tot, 1), **f64)
+    nidx = torch.empty(max(ntot, 1), **i32)
+    ncoefs = torch.empty(max(ntot, 1), **f64)
+    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 1, None,
+                               L.ptr(off_d), L.ptr(idx), L.ptr(coefs), s), "fi_tps_members")
+    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 1, None,
+                               L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), s), "fi_tps_members")
+    matrices = torch.empty(int(msz.sum()), **f64)
+    pivots = torch.empty(tot + 3 * nsub, **i32)
+    weights = torch.empty(int(wsz.sum()), **f64)
+    smx = torch.empty(max(tot, 1), **f64)
+    smy = torch.empty(max(tot, 1), **f64)
+    iters = torch.empty(2 * nsub, **i32)
+    nfixed = torch.empty(2 * nsub, **i32)
+    singular = torch.empty(nsub, **i32)
+    max_udiff = torch.empty(2 * nsub, **f64)
+    use_thr = threshold is not None
+    with _timed("fi_tps_solve"):
+      L.check(lib.fi_tps_solve(L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux),
+                             L.ptr(uy), L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d),
+                             L.ptr(matrices), L.ptr(pivots),
+                             float(threshold) if use_thr else 0.0, int(use_thr), L.ptr(woff_d),
+                             L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
+                             L.ptr(nfixed), L.ptr(singular), L.ptr(max_udiff), s),
+            "fi_tps_solve")
+    out = TpsOutput(
+        out_x=torch.empty(npts, **f64), out_y=torch.empty(npts, **f64),
+        rx=torch.empty(npts, **i32), ry=torch.empty(npts, **i32), selection=sel,
+        num_centers=nv, nb_subdom=nsub, counts=ch, w_offsets=woff, weights=weights,
+        singular=singular, iters=iters, nfixed=nfixed, max_udiff=max_udiff,
+    )
+    if want_smooth:
+        out.smooth_x = torch.empty(nv, **f64)
+        out.smooth_y = torch.empty(nv, **f64)
+        L.check(lib.fi_tps_blend_centers(L.ptr(plan), nv, L.ptr(cx), L.ptr(cy), L.ptr(counts),
+                                         L.ptr(off_d), L.ptr(idx), L.ptr(coefs), L.ptr(smx),
+                                         L.ptr(smy), L.ptr(out.smooth_x), L.ptr(out.smooth_y), s),
+                "fi_tps_blend_centers")
+    partx = torch.empty(max(ntot, 1), **f64)
+    party = torch.empty(max(ntot, 1), **f64)
+    with _timed("fi_tps_interpolate"):
+      L.check(lib.fi_tps_interpolate(L.ptr(plan), nsub, int(ch.max()), int(nch.max()), L.ptr(cx),
+                                   L.ptr(cy), L.ptr(counts), L.ptr(off_d), L.ptr(idx),
+                                   L.ptr(woff_d), L.ptr(weights), L.ptr(px), L.ptr(py), npts,
+                                   L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),
+                                   L.ptr(partx), L.ptr(party), L.ptr(out.out_x),
+                                   L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry), s),
+            "fi_tps_interpolate")
+    return out
+
+
+# --------------------------------------------------------------------------------
+# the pipeline
+# --------------------------------------------------------------------------------
+@dataclass
+class PassDevice:
+    """Device outputs of one pass."""
+
+    layout: PassLayout
+    deltaxs_raw: object
+    deltays_raw: object
+    correls_max: object
+    errors: object
+    xs: object
+    ys: object
+    flags: object
+    deltaxs: object  # after fix
+    deltays: object
+    fix_flags: object
+    diff2: object
+    planes: object = None
+    dxin: object = None
+    dyin: object = None
+    tps_next: Optional[TpsOutput] = None  # interpolation of this pass on the next grid
+    tps_final: Optional[TpsOutput] = None
+
+
+class PIVPipeline:
+    """Compiled multipass configuration for one image shape and dtype."""
+
+    def __init__(self, params, imshape, dtype, device=None, keep_correls=False,
+                 interp_last=True):
+        torch = _torch()
+        self.params = params
+        self.imshape = tuple(int(s) for s in imshape)
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in _DTYPES:
+            raise TypeError(f"image dtype {self.dtype} not supported (uint8, uint16, float32)")
+        self.device = torch.device(device if device is not None else "cuda")
+        self.keep_correls = keep_correls
+        self.interp_last = interp_last
+        p0, mp = params.piv0, params.multipass
+        if p0.nb_peaks_to_search != 1:
+            raise NotImplementedError("nb_peaks_to_search > 1 is not provided by this backend")
+        if p0.method_subpix != "2d_gaussian2":
+            raise NotImplementedError("method_subpix must be '2d_gaussian2' on this backend")
+        if mp.number > 1 and mp.use_tps is not True:
+            raise NotImplementedError(
+                "interpolation between passes needs params.multipass.use_tps = True "
+                "(the griddata path is not provided by this backend)"
+            )
+        if mp.use_tps is False and interp_last:
+            raise NotImplementedError(
+                "the final griddata interpolation is not provided (use_tps=False); "
+                "pass interp_last=False to skip it")
+        shapes = pass_shapes(p0.shape_crop_im0, mp.number, mp.coeff_zoom)
+        if p0.shape_crop_im1 is not None:
+            s1 = p0.shape_crop_im1
+            s1 = (s1, s1) if isinstance(s1, (int, np.integer)) else tuple(s1)
+            if tuple(s1) != shapes[0]:
+                raise ValueError("with this correlation method the input images have to "
+                                 "have the same shape.")
+        self.layouts: List[PassLayout] = []
+        for ip, shape in enumerate(shapes):
+            if shape[0] != shape[1] or shape[0] not in SUPPORTED_WINDOWS:
+                raise NotImplementedError(
+                    f"window {shape} not supported (square {SUPPORTED_WINDOWS})")
+            n = shape[0]
+            ixvecs, iyvecs = make_grid(self.imshape, shape, p0.grid.overlap)
+            gx, gy = np.meshgrid(ixvecs, iyvecs)
+            dmax = parse_displacement_max(p0.displacement_max, shape)
+            mask, box = displacement_mask(n, dmax)
+            lay = PassLayout(ip, n, ixvecs, iyvecs, gx.flatten(), gy.flatten(), dmax, mask, box,
+                             apply_subpix=(ip == mp.number - 1))
+            lay.dev["ixvecs"] = torch.as_tensor(ixvecs.astype(np.int32), device=self.device)
+            lay.dev["iyvecs"] = torch.as_tensor(iyvecs.astype(np.int32), device=self.device)
+            lay.dev["px"] = torch.as_tensor(lay.gx.astype(np.float64), device=self.device)
+            lay.dev["py"] = torch.as_tensor(lay.gy.astype(np.float64), device=self.device)
+            lay.dev["mask"] = (None if mask is None else
+                               torch.as_tensor(mask.astype(np.uint8), device=self.device))
+            self.layouts.append(lay)
+        self.im_min = torch.empty(2, dtype=torch.float32, device=self.device)
+
+    # ----------------------------------------------------------------------
+    def run(self, im0, im1, stream=None) -> List[PassDevice]:
+        """Run all passes on device images (torch tensors, same dtype/shape)."""
+        torch = _torch()
+        lib = L.load()
+        if tuple(im0.shape) != self.imshape or tuple(im1.shape) != self.imshape:
+            raise ValueError("image shape differs from the pipeline's")
+        im0 = im0.contiguous()
+        im1 = im1.contiguous()
+        s = L.stream_handle(stream)
+        dt = _DTYPES[self.dtype]
+        H, W = self.imshape
+        L.check(lib.fi_images_min(L.ptr(im0), L.ptr(im1), dt, H * W, L.ptr(self.im_min), s),
+                "fi_images_min")
+        mp, fx = self.params.multipass, self.params.fix
+        outs: List[PassDevice] = []
+        prev: Optional[PassDevice] = None
+        for lay in self.layouts:
+            dxin = dyin = None
+            if prev is not None:
+                prev.tps_next = run_tps(
+                    prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                    lay.dev["px"], lay.dev["py"], lay.nvec, mp.subdom_size, mp.smoothing_coef,
+                    mp.threshold_tps, False, stream)
+                dxin, dyin = prev.tps_next.rx, prev.tps_next.ry
+            cur = self._run_pass(lay, im0, im1, dxin, dyin, dt, s)
+            self._run_fix(cur, fx, s)
+            outs.append(cur)
+            prev = cur
+        if not self.interp_last:
+            return outs
+        try:
+            prev.tps_final = run_tps(
+                prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                prev.layout.dev["px"], prev.layout.dev["py"], prev.layout.nvec,
+                mp.subdom_size, mp.smoothing_coef, mp.threshold_tps, True, stream)
+        except InterpError as e:
+            print("Warning: InterpError at the end of the last piv pass:", e)
+        return outs
+
+    def _run_pass(self, lay, im0, im1, dxin, dyin, dt, s) -> PassDevice:
+        torch = _torch()
+        lib = L.load()
+        nvec, dev = lay.nvec, self.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        u8 = dict(dtype=torch.uint8, device=dev)
+        out = PassDevice(
+            layout=lay, deltaxs_raw=torch.empty(nvec, **f32), deltays_raw=torch.empty(nvec, **f32),
+            correls_max=torch.empty(nvec, **f32), errors=torch.empty(nvec, **u8),
+            xs=torch.empty(nvec, **f32), ys=torch.empty(nvec, **f32),
+            flags=torch.empty(nvec, **u8), deltaxs=torch.empty(nvec, **f32),
+            deltays=torch.empty(nvec, **f32), fix_flags=torch.empty(nvec, **u8),
+            diff2=torch.empty(nvec, **f32), dxin=dxin, dyin=dyin,
+        )
+        if self.keep_correls:
+            out.planes = torch.empty(nvec * lay.n * lay.n, **f32)
+        H, W = self.imshape
+        a = L.PivPassArgs()
+        a.im0, a.im1, a.dtype, a.height, a.width = L.ptr(im0), L.ptr(im1), dt, H, W
+        a.im_min = L.ptr(self.im_min)
+        a.n = lay.n
+        a.ixvecs, a.nx = L.ptr(lay.dev["ixvecs"]), lay.ixvecs.size
+        a.iyvecs, a.ny = L.ptr(lay.dev["iyvecs"]), lay.iyvecs.size
+        a.dxin, a.dyin = L.ptr(dxin), L.ptr(dyin)
+        a.mask = L.ptr(lay.dev["mask"])
+        a.box_i0_start, a.box_i0_stop, a.box_i1_start, a.box_i1_stop = lay.box
+        a.particle_radius = int(self.params.piv0.particle_radius)
+        a.apply_subpix = int(lay.apply_subpix)
+        a.deltaxs, a.deltays = L.ptr(out.deltaxs_raw), L.ptr(out.deltays_raw)
+        a.correls_max, a.errors = L.ptr(out.correls_max), L.ptr(out.errors)
+        a.xs, a.ys = L.ptr(out.xs), L.ptr(out.ys)
+        a.norms = None
+        a.planes = L.ptr(out.planes)
+        a.flags = L.ptr(out.flags)
+        with _timed("fi_piv_pass"):
+            L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
+        return out
+
+    def _run_fix(self, cur: PassDevice, fx, s):
+        torch = _torch()
+        lib = L.load()
+        lay = cur.layout
+        a = L.FixArgs()
+        a.nx, a.ny = lay.ixvecs.size, lay.iyvecs.size
+        a.deltaxs, a.deltays = L.ptr(cur.deltaxs_raw), L.ptr(cur.deltays_raw)
+        a.correls_max, a.errors = L.ptr(cur.correls_max), L.ptr(cur.errors)
+        a.correl_min = float(fx.correl_min)
+        a.use_displacement_max = int(bool(fx.displacement_max))
+        a.displacement_max = float(fx.displacement_max or 0.0)
+        a.use_threshold = int(fx.threshold_diff_neighbour is not None)
+        a.threshold = float(fx.threshold_diff_neighbour or 0.0)
+        a.deltaxs_out, a.deltays_out = L.ptr(cur.deltaxs), L.ptr(cur.deltays)
+        a.fix_flags, a.diff2 = L.ptr(cur.fix_flags), L.ptr(cur.diff2)
+        work = torch.empty(2 * lay.nvec, dtype=torch.float32, device=self.device)
+        a.work = L.ptr(work)
+        with _timed("fi_fix"):
+            L.check(lib.fi_fix(C.byref(a), s), "fi_fix")
+
+
+# --------------------------------------------------------------------------------
+# device -> host results
+# --------------------------------------------------------------------------------
+def error_dict(err, fix_flags, diff2, threshold):
+    """Rebuild ``errors`` of _loop_vectors + WorkFIX (fix.py:66-133) from the codes."""
+    errors = {}
+    for i in np.nonzero((err != 0) | (fix_flags != 0))[0]:
+        i = int(i)
+        s = ERROR_STRINGS.get(int(err[i])) if err[i] else None
+        f = int(fix_flags[i])
+        for bit, text in ((1, "correl < correl_min"), (2, "delta2 < displacement_max2"),
+                          (4, "diff neighbour too large")):
+            if f & bit:
+                s = text if s is None else s + " + " + text
+        if f & 4:
+            s += f" (diff = {np.sqrt(np.float64(diff2[i])):.2f})"
+        errors[i] = s
+    return errors

@@ -1,0 +1,298 @@
+"""``WorkPIV``: multipass PIV on one GB300, with the upstream work API.
+
+Mirrors ``fluidimage.works.piv.WorkPIV`` (works/piv/multipass.py:17-190),
+``FirstWorkPIV`` / ``WorkPIVFromDisplacement`` (works/piv/singlepass.py:566-870)
+and ``WorkFIX`` (works/piv/fix.py:21-243): same parameter tree
+(``create_default_params``), same ``calcul(couple)`` / ``calcul_from_arrays``
+entry points, same ``MultipassPIVResults`` / ``HeavyPIVResults`` attributes.
+All windows of a pass are processed by one kernel launch; the passes, the
+false-vector removal and the TPS interpolation run on the GPU.
+"""
+
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .data_objects import ArrayCouple, HeavyPIVResults, MultipassPIVResults
+from .engine import PIVPipeline, error_dict
+from .errors import InterpError
+from .params import ParamContainer
+
+#: correlation tags computed by this backend (FFT cross-correlation semantics of
+#: CorrelFFTNumpy / CorrelFFTW, calcul/correl.py:639-692)
+FFT_TAGS = ("gb300", "np.fft", "fftw")
+
+
+def _complete_params_piv0(params):
+    params._set_child("piv0", attribs={
+        "shape_crop_im0": 48,
+        "shape_crop_im1": None,
+        "displacement_max": None,
+        "displacement_mean": None,
+        "method_correl": "gb300",
+        "method_subpix": "2d_gaussian2",
+        "nsubpix": None,
+        "nb_peaks_to_search": 1,
+        "particle_radius": 3,
+    })
+    params.piv0._set_child("grid", attribs={"overlap": 0.5, "from": "overlap"})
+    params._set_child("mask", attribs={"strcrop": None})
+
+
+def _complete_params_fix(params, tag="fix"):
+    params._set_child(tag, attribs={
+        "correl_min": 0.2,
+        "threshold_diff_neighbour": 10,
+        "displacement_max": None,
+    })
+
+
+def _complete_params_multipass(params):
+    params._set_child("multipass", attribs={
+        "number": 1,
+        "coeff_zoom": 2,
+        "use_tps": "last",
+        "subdom_size": 200,
+        "smoothing_coef": 5.0,
+        "threshold_tps": 1.5,
+    })
+
+
+def _complete_params_series(params):
+    params._set_child("series", attribs={
+        "path": "",
+        "str_subset": "pairs",
+        "ind_start": "first",
+        "ind_stop": None,
+        "ind_step": 1,
+    })
+
+
+class LazyWeights:
+    """Per-subdomain TPS weights (``deltaxs_tps``), copied to the host on first use."""
+
+    def __init__(self, tps, comp):
+        self._tps = tps
+        self._comp = comp
+        self._items = None
+
+    def _load(self):
+        if self._items is None:
+            w = self._tps.weights.cpu().numpy()
+            items = []
+            for i, cnt in enumerate(self._tps.counts):
+                n = int(cnt) + 3
+                o = int(self._tps.w_offsets[i]) + self._comp * n
+                items.append(w[o:o + n].copy())
+            self._items = items
+        return self._items
+
+    def __len__(self):
+        return self._tps.nb_subdom
+
+    def __getitem__(self, i):
+        return self._load()[i]
+
+    def __iter__(self):
+        return iter(self._load())
+
+
+class WorkPIV:
+    """Multipass PIV work (works/piv/multipass.py:17-190) on the GPU.
+
+    Parameters
+    ----------
+    params : ParamContainer from :meth:`create_default_params`.
+    keep_correls : store the correlation planes in ``HeavyPIVResults.correls``
+        (upstream always stores them; here they cost a device-to-host copy).
+    device : torch device (default ``cuda``).
+    interp_last : compute the final interpolation (``deltaxs_final``...); it is
+        TPS here, so ``use_tps=False`` (upstream: griddata) needs ``False``.
+    """
+
+    @classmethod
+    def create_default_params(cls):
+        params = ParamContainer(tag="params")
+        _complete_params_series(params)
+        _complete_params_piv0(params)
+        _complete_params_fix(params)
+        _complete_params_multipass(params)
+        return params
+
+    def __init__(self, params=None, keep_correls=False, device=None, verbose=False,
+                 interp_last=True):
+        if params is None:
+            params = self.create_default_params()
+        self.params = params
+        if params.piv0.method_correl not in FFT_TAGS:
+            from .correl import correlation_classes
+
+            raise ValueError(
+                "params.piv0.method_correl should be in " + str(list(correlation_classes))
+            )
+        if params.piv0.grid.overlap >= 1:
+            raise ValueError("params.piv0.grid.overlap has to be smaller than 1")
+        self.keep_correls = keep_correls
+        self.interp_last = interp_last
+        self.device = device
+        self.verbose = verbose
+        self._pipelines = {}
+
+    # --------------------------------------------------------------------
+    def _pipeline(self, imshape, dtype):
+        key = (tuple(imshape), np.dtype(dtype).str)
+        if key not in self._pipelines:
+            self._pipelines[key] = PIVPipeline(self.params, imshape, dtype, device=self.device,
+                                               keep_correls=self.keep_correls,
+                                               interp_last=self.interp_last)
+        return self._pipelines[key]
+
+    def _xy_offsets(self):
+        strcrop = self.params.mask.strcrop
+        if strcrop is None:
+            return 0, 0
+        from .data_objects import get_slices_from_strcrop
+
+        sl = get_slices_from_strcrop(strcrop)
+        return (sl[1].start or 0), (sl[0].start or 0)
+
+    def calcul_device(self, im0, im1, stream=None):
+        """Run the passes on device images (torch tensors); returns device outputs."""
+        pipe = self._pipeline(tuple(im0.shape), _np_dtype(im0))
+        return pipe.run(im0, im1, stream=stream)
+
+    def calcul(self, couple):
+        """Compute a multipass PIV field from a couple of images."""
+        import torch
+
+        if isinstance(couple, dict):
+            couple = ArrayCouple(**couple)
+        if not isinstance(couple, ArrayCouple):
+            raise ValueError(f"not isinstance(couple, ArrayCouple), {type(couple) = }")
+        couple.apply_mask(self.params.mask)
+        im0, im1 = couple.get_arrays()
+        dev = torch.device(self.device or "cuda")
+        t0 = _to_device(im0, dev)
+        t1 = _to_device(im1, dev)
+        outs = self.calcul_device(t0, t1)
+        return self.results_to_host(outs, couple)
+
+    def calcul_from_arrays(self, *arrays, names=None):
+        names = [f"array{i}" for i in range(len(arrays))]
+        t_start = time.perf_counter()
+        result = self.calcul({"arrays": arrays, "names": names})
+        if self.verbose:
+            print(f"Calcul done in {time.perf_counter() - t_start:.2f} s")
+        return result
+
+    # --------------------------------------------------------------------
+    def results_to_host(self, outs, couple=None):
+        """Device outputs -> ``MultipassPIVResults`` (upstream attributes and dtypes)."""
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        fx = self.params.fix
+        offx, offy = self._xy_offsets()
+        results = MultipassPIVResults()
+        hosts = []
+        for pd in outs:
+            lay = pd.layout
+            h = {k: getattr(pd, k).cpu().numpy() for k in (
+                "deltaxs_raw", "deltays_raw", "correls_max", "errors", "xs", "ys", "flags",
+                "deltaxs", "deltays", "fix_flags", "diff2")}
+            errors = error_dict(h["errors"], h["fix_flags"], h["diff2"],
+                                fx.threshold_diff_neighbour)
+            if lay.index == 0:
+                xs = lay.gx + offx
+                ys = lay.gy + offy
+            else:
+                xs = h["xs"].astype(np.float64) + offx
+                ys = h["ys"].astype(np.float64) + offy
+            nvec = lay.nvec
+            if pd.planes is not None:
+                planes = pd.planes.view(nvec, lay.n, lay.n).cpu().numpy()
+                correls = [None if h["errors"][i] == 4 else planes[i] for i in range(nvec)]
+            else:
+                correls = [None] * nvec
+            r = HeavyPIVResults(
+                h["deltaxs"], h["deltays"], xs, ys, errors, correls_max=h["correls_max"],
+                correls=correls, couple=couple, params=self.params,
+                secondary_peaks=[None] * nvec,
+            )
+            r.indices_no_displacement = (lay.n // 2 - 1, lay.n // 2 - 1)
+            r.displacement_max = lay.displacement_max
+            r.near_ties = int(np.count_nonzero(h["flags"] & 1))
+            if fx.threshold_diff_neighbour is not None:
+                r.deltaxs_wrong = {i: h["deltaxs_raw"][i] for i in errors}
+                r.deltays_wrong = {i: h["deltays_raw"][i] for i in errors}
+            if pd.dxin is not None:
+                r.deltaxs_input = pd.dxin.cpu().numpy()
+                r.deltays_input = pd.dyin.cpu().numpy()
+            hosts.append((r, h))
+            results.append(r)
+        for k, pd in enumerate(outs):
+            r, h = hosts[k]
+            if pd.tps_next is not None:
+                nxt = outs[k + 1].layout
+                self._check_tps(pd.tps_next)
+                r.deltaxs_approx = pd.tps_next.out_x.cpu().numpy()
+                r.deltays_approx = pd.tps_next.out_y.cpu().numpy()
+                r.ixvecs_approx = nxt.gx + offx
+                r.iyvecs_approx = nxt.gy + offy
+                r.deltaxs_tps = LazyWeights(pd.tps_next, 0)
+                r.deltays_tps = LazyWeights(pd.tps_next, 1)
+            if pd.tps_final is not None:
+                tps = pd.tps_final
+                self._check_tps(tps)
+                lay = pd.layout
+                fx_ = tps.out_x.cpu().numpy()
+                fy_ = tps.out_y.cpu().numpy()
+                r.ixvecs_final = lay.gx + offx
+                r.iyvecs_final = lay.gy + offy
+                r.deltaxs_final = fx_
+                r.deltays_final = fy_
+                sel = tps.selection[: tps.num_centers].cpu().numpy().astype(np.int64)
+                xs_s = r.ixvecs_final.copy().astype(np.float32)
+                xs_s[sel] = r.xs[sel]
+                ys_s = r.iyvecs_final.copy().astype(np.float32)
+                ys_s[sel] = r.ys[sel]
+                dxs = fx_.copy()
+                dxs[sel] = tps.smooth_x.cpu().numpy()
+                dys = fy_.copy()
+                dys[sel] = tps.smooth_y.cpu().numpy()
+                r.xs_smooth, r.ys_smooth = xs_s, ys_s
+                r.deltaxs_smooth, r.deltays_smooth = dxs, dys
+                r.deltaxs_tps = LazyWeights(tps, 0)
+                r.deltays_tps = LazyWeights(tps, 1)
+        return results
+
+    @staticmethod
+    def _check_tps(tps):
+        if int(tps.singular.sum().item()) != 0:
+            raise np.linalg.LinAlgError(
+                "Singular TPS subdomain system (upstream falls back to griddata, "
+                "which this backend does not provide)"
+            )
+
+
+def _np_dtype(t):
+    """Image element type of a device tensor; uint16 images travel as int16 storage."""
+    import torch
+
+    return {torch.uint8: np.uint8, torch.int16: np.uint16, torch.float32: np.float32}[t.dtype]
+
+
+def _to_device(a, dev):
+    """Host image -> device tensor (uint16 data kept bit for bit in an int16 tensor)."""
+    import torch
+
+    if isinstance(a, torch.Tensor):
+        return a.to(dev).contiguous()
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.uint16:
+        a = a.view(np.int16)
+    elif a.dtype not in (np.uint8, np.float32):
+        raise TypeError(f"image dtype {a.dtype} not supported (uint8, uint16, float32)")
+    return torch.from_numpy(a).to(dev)

@@ -45,6 +45,7 @@ class ParticleModel:
     intensity: Tuple[float, float] = (128.0, 255.0)
     noise: float = 2.0
     dtype: str = "uint8"
+    max_value: Optional[float] = None  # clip level (default: dtype maximum)
     extra: dict = field(default_factory=dict)
 
 
@@ -91,25 +92,25 @@ def sinusoid(amplitude=5.0, wavelength=512.0) -> Callable:
     return field_
 
 
-def _render(shape, xs, ys, diam, peak, dtype_float=np.float64):
+def _render(shape, xs, ys, diam, peak, chunk=65536):
+    """Sum of Gaussian spots, as separable (rows x columns) patches per particle."""
     ny, nx = shape
-    out = np.zeros(ny * nx, dtype=dtype_float)
+    out = np.zeros(ny * nx, dtype=np.float64)
     radius = int(np.ceil(1.5 * diam.max())) + 1
-    ix0 = np.floor(xs).astype(np.int64)
-    iy0 = np.floor(ys).astype(np.int64)
-    inv = -8.0 / (diam * diam)
-    for oy in range(-radius, radius + 1):
-        iy = iy0 + oy
-        oky = (iy >= 0) & (iy < ny)
-        ddy = (iy - ys) ** 2
-        for ox in range(-radius, radius + 1):
-            ix = ix0 + ox
-            ok = oky & (ix >= 0) & (ix < nx)
-            if not ok.any():
-                continue
-            r2 = ddy[ok] + (ix[ok] - xs[ok]) ** 2
-            val = peak[ok] * np.exp(inv[ok] * r2)
-            out +=np.bincount(iy[ok] * nx + ix[ok], weights=val, minlength=ny * nx)
+    offs = np.arange(-radius, radius + 1)
+    for c0 in range(0, xs.size, chunk):
+        x = xs[c0:c0 + chunk]
+        y = ys[c0:c0 + chunk]
+        inv = -8.0 / (diam[c0:c0 + chunk] ** 2)
+        ix = np.floor(x).astype(np.int64)[:, None] + offs[None, :]
+        iy = np.floor(y).astype(np.int64)[:, None] + offs[None, :]
+        gx = np.exp(inv[:, None] * (ix - x[:, None]) ** 2)
+        gy = np.exp(inv[:, None] * (iy - y[:, None]) ** 2)
+        gx[(ix < 0) | (ix >= nx)] = 0.0
+        gy[(iy < 0) | (iy >= ny)] = 0.0
+        vals = (peak[c0:c0 + chunk, None, None] * gy[:, :, None]) * gx[:, None, :]
+        flat = np.clip(iy, 0, ny - 1)[:, :, None] * nx + np.clip(ix, 0, nx - 1)[:, None, :]
+        out += np.bincount(flat.ravel(), weights=vals.ravel(), minlength=ny * nx)
     return out.reshape(shape)
 
 
@@ -150,7 +151,8 @@ def make_pair(
         im = _render(shape, xs, ys, diam, peak)
         if model.noise > 0:
             im = im + rng.normal(0.0, model.noise, size=shape)
-        im = np.clip(np.rint(im), info.min, info.max).astype(model.dtype)
+        top = info.max if model.max_value is None else model.max_value
+        im = np.clip(np.rint(im), info.min, top).astype(model.dtype)
         if as_float32:
             im = im.astype(np.float32)
         images.append(im)

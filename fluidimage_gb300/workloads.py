@@ -1,0 +1,49 @@
+"""Synthetic PIV workloads used by the tests and the benchmark.
+
+``config1``: one 512x512 pair, float32 built from uint8, uniform shift (3.3, -1.7),
+32 px windows, overlap 0.5, '2d_gaussian2', no neighbour filter.
+``config2``: one 2048x2048 uint16 (12-bit) pair, Oseen vortex (rc = 200 px, peak
+8 px), noise 20 counts; three passes 64 -> 32 -> 16 px, overlap 0.5, neighbour
+threshold 2, TPS between passes (subdomains of 200 vectors, smoothing 0.5).
+Seeds follow ``seed = config_index * 1000 + pair_index``.
+"""
+
+from __future__ import annotations
+
+from . import synthetic
+
+
+def config1_images(pair=0, shape=(512, 512)):
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(128, 255),
+                                    noise=2.0, dtype="uint8")
+    field = synthetic.uniform_shift(3.3, -1.7)
+    return synthetic.make_pair(shape, field, model, seed=1000 + pair, as_float32=True), field
+
+
+def config1_params(params):
+    params.piv0.shape_crop_im0 = 32
+    params.piv0.grid.overlap = 0.5
+    params.piv0.method_subpix = "2d_gaussian2"
+    params.multipass.number = 1
+    params.fix.threshold_diff_neighbour = None
+    params.fix.correl_min = float("-inf")
+    return params
+
+
+def config2_images(pair=0, shape=(2048, 2048)):
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = synthetic.oseen_vortex(shape, d_max=8.0, rc=200.0)
+    return synthetic.make_pair(shape, field, model, seed=2000 + pair), field
+
+
+def config2_params(params):
+    params.piv0.shape_crop_im0 = 64
+    params.piv0.grid.overlap = 0.5
+    params.multipass.number = 3
+    params.multipass.coeff_zoom = 2
+    params.multipass.use_tps = True
+    params.multipass.subdom_size = 200
+    params.multipass.smoothing_coef = 0.5
+    params.fix.threshold_diff_neighbour = 2
+    return params

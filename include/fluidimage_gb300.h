@@ -1,0 +1,264 @@
+/*
+ * fluidimage_gb300 — C ABI of the GB300 (sm_103a) PIV hot path.
+ *
+ * Every entry point takes plain device pointers and sizes plus a CUDA stream
+ * (passed as void*, NULL = legacy default stream), enqueues its kernels on that
+ * stream and returns immediately.  The return value is FI_OK (0) or a negative
+ * FI_ERR_* code; fi_last_error() gives the message of the calling thread's last
+ * failure.  No entry point allocates device memory or synchronises the stream
+ * unless stated.  Buffers are owned by the caller.
+ *
+ * Each entry point cites the upstream fluidimage 0.5.3 interface it replaces
+ * (paths inside the fluidimage project).
+ */
+#ifndef FLUIDIMAGE_GB300_H
+#define FLUIDIMAGE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FI_OK 0
+#define FI_ERR_INVALID (-1)
+#define FI_ERR_CUDA (-2)
+#define FI_ERR_UNSUPPORTED (-3)
+
+/* image element types */
+#define FI_U8 0
+#define FI_U16 1
+#define FI_F32 2
+
+/* per-vector error codes written by fi_piv_pass (upstream PIVError strings) */
+#define FI_VEC_OK 0
+#define FI_VEC_PEAK_BOUNDARY 1 /* "Correlation peak touching boundary." */
+#define FI_VEC_PEAK_NAN 2      /* "Correlation peak touching nan."      */
+#define FI_VEC_WRONG_SUBPIX 3  /* "wrong subpix" (integer peak kept)     */
+#define FI_VEC_BAD_CROP 4      /* "Bad im_crop shape."                   */
+#define FI_VEC_ALL_NAN 5       /* plane without finite value (upstream asserts) */
+#define FI_VEC_CLOSE_BOUNDARY 6 /* "close boundary" (fi_subpix_at only)   */
+
+/* per-vector flag bits written by fi_piv_pass */
+#define FI_FLAG_NEAR_TIE 1 /* top two plane values within 1e-6 relative */
+
+/* fix flag bits written by fi_fix */
+#define FI_FIX_CORREL_MIN 1     /* "correl < correl_min"        */
+#define FI_FIX_DISPLACEMENT 2   /* "delta2 < displacement_max2" */
+#define FI_FIX_NEIGHBOUR 4      /* "diff neighbour too large"   */
+
+const char* fi_last_error(void);
+
+/* Library version string. */
+const char* fi_version(void);
+
+/* Number of kernels launched by the library since it was loaded. */
+long long fi_launch_count(void);
+
+/* sizeof of fi_piv_pass_args, fi_fix_args and fi_tps_plan (host-only, for bindings). */
+int fi_abi_sizes(int64_t* out3);
+
+/*
+ * Minimum of two images, written as two floats to out_min[0..1] (device).
+ * Replaces the "im - im.min()" of BaseWorkPIV._pad_images
+ * (works/piv/singlepass.py:196-208).
+ */
+int fi_images_min(const void* im0, const void* im1, int dtype, int64_t count,
+                  float* out_min, void* stream);
+
+/* Arguments of one PIV pass (one window size, all windows of one image pair). */
+typedef struct fi_piv_pass_args {
+  const void* im0;          /* image 0, row-major height x width (dtype)      */
+  const void* im1;          /* image 1, same shape and dtype                  */
+  int dtype;                /* FI_U8, FI_U16 or FI_F32                        */
+  int height, width;
+  const float* im_min;      /* device [2]: minima of im0, im1 (fi_images_min) */
+  int n;                    /* window size n x n (16, 24, 32, 48, 64)         */
+  const int32_t* ixvecs;    /* grid x centres (nx), device                    */
+  int nx;
+  const int32_t* iyvecs;    /* grid y centres (ny), device                    */
+  int ny;
+  const int32_t* dxin;      /* nullable: integer input shift per vector       */
+  const int32_t* dyin;      /*   (passes >= 1), device [nx*ny]                */
+  const uint8_t* mask;      /* nullable: n*n, 1 where |d| > displacement_max  */
+  int box_i0_start, box_i0_stop, box_i1_start, box_i1_stop; /* search box    */
+  int particle_radius;      /* second-chance NaN box half width (3)           */
+  int apply_subpix;         /* 1: '2d_gaussian2' (+ centroid fallback)        */
+  float* deltaxs;           /* out [nvec]                                     */
+  float* deltays;           /* out [nvec]                                     */
+  float* correls_max;       /* out [nvec]                                     */
+  uint8_t* errors;          /* out [nvec] FI_VEC_*                            */
+  float* xs;                /* out [nvec] vector x position (midpoint)        */
+  float* ys;                /* out [nvec]                                     */
+  double* norms;            /* nullable out [nvec]: sqrt(S0 * S1)             */
+  float* planes;            /* nullable out [nvec*n*n], fftshift layout       */
+  uint8_t* flags;           /* nullable out [nvec] FI_FLAG_*                  */
+} fi_piv_pass_args;
+
+/*
+ * One PIV pass, fused: window extraction (with the integer window shift of
+ * passes >= 1), FFT cross-correlation of the mean-removed windows, peak search
+ * with the displacement_max mask and the second-chance search, and the
+ * '2d_gaussian2' subpixel fit.  One thread group per window, FP32 FFTs in
+ * registers, FP64 window energies.
+ * Replaces BaseWorkPIV._loop_vectors (works/piv/singlepass.py:262-361) with
+ * CorrelFFTNumpy.__call__ (calcul/correl.py:671-685),
+ * CorrelBase.compute_displacements_from_correl (calcul/correl.py:226-275),
+ * nan_indices_max (calcul/correl.py:88-132) and SubPix.compute_subpix
+ * (calcul/subpix.py:107-218), plus the window positions of
+ * WorkPIVFromDisplacement (works/piv/singlepass.py:787-870).
+ */
+int fi_piv_pass(const fi_piv_pass_args* args, void* stream);
+
+/*
+ * Per-window plugin contract: correlation planes and norms of `count` window
+ * pairs (float32, n x n each, C order), like CorrelFFTNumpy.__call__
+ * (calcul/correl.py:671-685) applied to each pair.  planes are written in the
+ * "_like_fftshift" layout (calcul/correl.py:596-636).
+ */
+int fi_correl_windows(const float* win0, const float* win1, int count, int n,
+                      float* planes, double* norms, void* stream);
+
+/*
+ * Peak search (+ optional subpixel fit) on planes already in device memory,
+ * with the semantics of CorrelFFTBase.compute_displacements_from_correl
+ * (calcul/correl.py:561-568, 226-275) and CorrelBase.apply_subpix
+ * (calcul/correl.py:277-281).  When mask is NULL the second-chance NaN box is
+ * written into `planes` in place, as upstream does.  Outputs as fi_piv_pass
+ * (integer displacements when apply_subpix == 0), plus the peak indices.
+ */
+int fi_peaks_from_planes(float* planes, const double* norms, int count, int n,
+                         const uint8_t* mask, int box_i0_start, int box_i0_stop,
+                         int box_i1_start, int box_i1_stop, int particle_radius,
+                         int apply_subpix, float* deltaxs, float* deltays,
+                         float* correls_max, uint8_t* errors, int32_t* peak_i0,
+                         int32_t* peak_i1, void* stream);
+
+/*
+ * '2d_gaussian2' subpixel fit (with its centroid fallback) at given peak indices
+ * (peak_i0 = row, peak_i1 = column) on planes in device memory: the
+ * CorrelBase.apply_subpix / SubPix.compute_subpix pair (calcul/correl.py:277-281,
+ * calcul/subpix.py:107-218).  Writes displacements and FI_VEC_* codes
+ * (FI_VEC_WRONG_SUBPIX, FI_VEC_CLOSE_BOUNDARY keep the integer displacement).
+ */
+int fi_subpix_at(const float* planes, int count, int n, const int32_t* peak_i0,
+                 const int32_t* peak_i1, float* deltaxs, float* deltays, uint8_t* errors,
+                 void* stream);
+
+/* Arguments of the false-vector removal of one pass. */
+typedef struct fi_fix_args {
+  int nx, ny;                  /* vector grid                                  */
+  const float* deltaxs;        /* in [nvec] (pass output)                      */
+  const float* deltays;
+  const float* correls_max;    /* in [nvec]                                    */
+  const uint8_t* errors;       /* in [nvec] FI_VEC_*                           */
+  float correl_min;            /* -inf to disable                              */
+  int use_displacement_max;
+  float displacement_max;      /* fix.displacement_max                         */
+  int use_threshold;
+  float threshold;             /* fix.threshold_diff_neighbour                 */
+  float* deltaxs_out;          /* out [nvec]: NaN where removed                */
+  float* deltays_out;
+  uint8_t* fix_flags;          /* out [nvec] FI_FIX_*                          */
+  float* diff2;                /* out [nvec]: |d - mean8(d)|^2 (float32)       */
+  float* work;                 /* scratch [2*nvec] (floats)                    */
+} fi_fix_args;
+
+/*
+ * WorkFIX.calcul without secondary peaks (works/piv/fix.py:66-133) with
+ * mean_neighbors_xy (calcul/mean_neighbors.py:128-155).
+ */
+int fi_fix(const fi_fix_args* args, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Thin-plate-spline subdomain interpolation (FP64), the apply_interp of
+ * works/piv/singlepass.py:409-563 with ThinPlateSplineSubdom
+ * (calcul/interpolate/thin_plate_spline_subdom.py:25-280).
+ * The host drives the stages; sizes that depend on data (number of valid
+ * vectors, subdomain populations) are read back between stages.
+ * ------------------------------------------------------------------------- */
+
+/* Header of a TPS plan (device memory, written by fi_tps_plan). */
+typedef struct fi_tps_plan {
+  int num_centers;      /* valid (non-NaN) vectors                        */
+  int nb_subdomx, nb_subdomy;
+  int status;           /* 0, or 1 when there is no valid vector          */
+  double smoothing;     /* smoothing_coef normalised by subdomain area     */
+  double x_min, x_max, y_min, y_max;
+  double buffer_x, buffer_y;
+} fi_tps_plan;
+
+/*
+ * Select the valid vectors (non-NaN dx and dy, order kept) and compute the
+ * subdomain layout (ThinPlateSplineSubdom.__init__, thin_plate_spline_subdom.py:
+ * 38-126).  xs, ys, dx, dy: float32 [nvec].  Outputs the centres cx, cy (float64),
+ * the values ux, uy (float32) and, if not NULL, the original index of each
+ * selected vector.  The header *plan is written in device memory; the host reads
+ * num_centers, nb_subdomx, nb_subdomy and status from it before the next stages.
+ */
+int fi_tps_plan_make(const float* xs, const float* ys, const float* dx, const float* dy,
+                     int nvec, int subdom_size, double smoothing_coef,
+                     double percent_buffer_area, fi_tps_plan* plan, double* cx, double* cy,
+                     float* ux, float* uy, int32_t* selection, void* stream);
+
+/*
+ * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
+ * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
+ * counts), the point indices and their norm coefficients
+ * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).
+ */
+int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
+                   int npts, int mode, int32_t* counts, const int64_t* offsets,
+                   int32_t* indices, double* coefs, void* stream);
+
+/*
+ * Per subdomain: build [[K + smoothing I, P], [P^T, 0]] (compute_tps_weights,
+ * thin_plate_spline.py:168-216), LU-factorise it once with partial pivoting and
+ * run the iterative outlier replacement of compute_tps_weights_iter
+ * (thin_plate_spline_subdom.py:236-280) for both components on the same factors.
+ * matrices: scratch, (n_i+3)^2 doubles at mat_offsets[i]; pivots: scratch,
+ * n_i+3 ints at offsets[i] + 3 i; weights: 2 (n_i+3) doubles at w_offsets[i]
+ * (x then y); smoothed_x/y: n_i doubles at offsets[i].  iters, nfixed,
+ * max_udiff: [2 * nb_subdom] (x, y); singular: [nb_subdom] (1 = zero pivot,
+ * where upstream raises LinAlgError).
+ */
+int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
+                 const double* cy, const float* ux, const float* uy, const int32_t* counts,
+                 const int64_t* offsets, const int32_t* indices, const int64_t* mat_offsets,
+                 double* matrices, int32_t* pivots, double threshold, int use_threshold,
+                 const int64_t* w_offsets, double* weights, double* smoothed_x,
+                 double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* singular,
+                 double* max_udiff, void* stream);
+
+/*
+ * Smoothed values at the centres, blended over the subdomains that contain them
+ * (compute_tps_weights_subdom, thin_plate_spline_subdom.py:128-159).
+ */
+int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, const double* cx,
+                         const double* cy, const int32_t* counts, const int64_t* offsets,
+                         const int32_t* indices, const double* coefs, const double* smoothed_x,
+                         const double* smoothed_y, double* out_x, double* out_y, void* stream);
+
+/*
+ * Interpolation at npts new positions (init_with_new_positions + interpolate,
+ * thin_plate_spline_subdom.py:161-234): out_x/out_y float64 and, if not NULL,
+ * out_rx/out_ry = round-half-even to int32 (the window shifts of the next pass,
+ * works/piv/singlepass.py:752-753).  ncounts/noffsets/nindices/ncoefs: membership
+ * of the new positions (fi_tps_members); partx/party: scratch of the same size
+ * as nindices.
+ */
+int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
+                       int max_new_members, const double* cx, const double* cy,
+                       const int32_t* counts, const int64_t* offsets, const int32_t* indices,
+                       const int64_t* w_offsets, const double* weights, const double* px,
+                       const double* py, int npts, const int32_t* ncounts,
+                       const int64_t* noffsets, const int32_t* nindices, const double* ncoefs,
+                       double* partx, double* party, double* out_x, double* out_y,
+                       int32_t* out_rx, int32_t* out_ry, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUIDIMAGE_GB300_H */
