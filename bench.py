@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", type=int, default=2048,
+                    help="image side (2048 = the config; smaller sizes for profiling)")
     return ap.parse_args()
 
 
@@ -216,7 +218,7 @@ def run_gpu(args):
         dist = dist_
     lib = _lib.load()
 
-    (im0, im1), _ = workloads.config2_images(pair=rank)
+    (im0, im1), _ = workloads.config2_images(pair=rank, shape=(args.size, args.size))
     params = workloads.config2_params(WorkPIV.create_default_params())
     work = WorkPIV(params, device=dev)
     t0 = torch.from_numpy(im0.view(np.int16)).to(dev)
@@ -290,7 +292,9 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FFT correlation), f64 (TPS solve)",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "pairs_per_step_per_gpu": 1,
+        "config": {"workload": WORKLOAD if args.size == 2048 else
+                   WORKLOAD.replace("2048x2048", f"{args.size}x{args.size}"),
+                   "pairs_per_step_per_gpu": 1,
                    "final_vectors_per_pair": nvec_final,
                    "l2": "512 MiB flush write between timed steps (untimed)",
                    "parallelism": f"replicas x{world}"},

@@ -22,6 +22,7 @@ VEC_BAD_CROP = 4
 VEC_ALL_NAN = 5
 
 FLAG_NEAR_TIE = 1
+FLAG_SUBPIX_TIE = 2
 
 FIX_CORREL_MIN = 1
 FIX_DISPLACEMENT = 2

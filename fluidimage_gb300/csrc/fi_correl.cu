@@ -249,7 +249,7 @@ __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchB
 // operation order, then the centroid fallback of SubPix.compute_subpix
 // (subpix.py:184-216).  Returns 0 or FI_VEC_WRONG_SUBPIX; (dx, dy) displacement.
 __device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix0, int iy0,
-                                     float* dxo, float* dyo) {
+                                     float* dxo, float* dyo, bool* min_tie) {
   float n[9];
   float cmin = c[0];
 #pragma unroll
@@ -259,11 +259,16 @@ __device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix
   float cmx = n[0];
 #pragma unroll
   for (int k = 1; k < 9; ++k) cmx = (n[k] > cmx) ? n[k] : cmx;
+  int nlow = 0;  // crop values within 1e-5 of the minimum (relative to the range)
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     n[k] = __fdiv_rn(n[k], cmx);
+    nlow += (n[k] < 1e-5f) ? 1 : 0;
     if (n[k] == 0.0f) n[k] = 1e-8f;
   }
+  // two or more values at the minimum: the 1e-8 floor makes the fit depend on
+  // which of them rounds to exactly zero (a near-tie of the subpixel fit)
+  *min_tie = nlow >= 2;
   float c10 = 0.f, c01 = 0.f, c11 = 0.f, c20 = 0.f, c02 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -323,7 +328,19 @@ __device__ int subpix_gaussian2(const float* PL, int i0, int i1, float* dxo, flo
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) c[3 * a + b] = PL[(i0 - 1 + a) * Cfg<N>::LDP + (i1 - 1 + b)];
-  return subpix_gaussian2_vals(c, i0, i1, N / 2 - 1, N / 2 - 1, dxo, dyo);
+  bool tie;
+  return subpix_gaussian2_vals(c, i0, i1, N / 2 - 1, N / 2 - 1, dxo, dyo, &tie);
+}
+
+template <int N>
+__device__ int subpix_gaussian2_tie(const float* PL, int i0, int i1, float* dxo, float* dyo,
+                                    bool* tie) {
+  float c[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) c[3 * a + b] = PL[(i0 - 1 + a) * Cfg<N>::LDP + (i1 - 1 + b)];
+  return subpix_gaussian2_vals(c, i0, i1, N / 2 - 1, N / 2 - 1, dxo, dyo, tie);
 }
 
 // SubPix.compute_subpix at given peak indices on planes in global memory
@@ -346,7 +363,8 @@ __global__ void k_subpix_at(const float* planes, int count, int n, const int32_t
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) c[3 * a + b] = P[(i0 - 1 + a) * n + (i1 - 1 + b)];
   float dx, dy;
-  errs[w] = (uint8_t)subpix_gaussian2_vals(c, i0, i1, ix0, iy0, &dx, &dy);
+  bool tie;
+  errs[w] = (uint8_t)subpix_gaussian2_vals(c, i0, i1, ix0, iy0, &dx, &dy, &tie);
   dxs[w] = dx;
   dys[w] = dy;
 }
@@ -364,7 +382,8 @@ struct VecResult {
   int err;
   float dx, dy, cmax;
   int i0, i1;
-  bool tie;
+  bool tie;        // near-tie of the two largest plane values (either attempt)
+  bool subpix_tie; // tied minimum in the 3x3 subpixel crop
   NanBox nb;
 };
 
@@ -376,6 +395,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
   PeakOut p1 = find_peak<N>(PL, pa.mask, pa.box, nb, norm, t, g, red);
   VecResult r;
   r.tie = p1.tie;
+  r.subpix_tie = false;
   r.nb = nb;
   PeakOut fin = p1;
   if (p1.err == FI_VEC_PEAK_BOUNDARY || p1.err == FI_VEC_PEAK_NAN) {
@@ -385,6 +405,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
     if (r1 > r0 && c1 > c0) nb = NanBox{r0, r1, c0, c1};
     r.nb = nb;
     PeakOut p2 = find_peak<N>(PL, pa.mask, pa.box, nb, norm, t, g, red);
+    r.tie = r.tie || p2.tie;
     if (p2.err == FI_VEC_OK) {
       fin = p2;
     } else {
@@ -405,7 +426,9 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
   if (fin.err == FI_VEC_OK && pa.apply_subpix) {
     if (t == 0) {
       float sx, sy;
-      const int e = subpix_gaussian2<N>(PL, fin.i0, fin.i1, &sx, &sy);
+      bool stie;
+      const int e = subpix_gaussian2_tie<N>(PL, fin.i0, fin.i1, &sx, &sy, &stie);
+      r.subpix_tie = stie;
       r.err = e;
       r.dx = sx;
       r.dy = sy;
@@ -619,7 +642,10 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
       a.deltays[w] = dyo;
       a.correls_max[w] = cm;
       a.errors[w] = (uint8_t)err;
-      if (a.flags) a.flags[w] = (valid && res.tie) ? FI_FLAG_NEAR_TIE : 0;
+      if (a.flags)
+        a.flags[w] = valid ? (uint8_t)((res.tie ? FI_FLAG_NEAR_TIE : 0) |
+                                       (res.subpix_tie ? FI_FLAG_SUBPIX_TIE : 0))
+                           : (uint8_t)0;
       if (!FROM_WINDOWS) {
         a.xs[w] = (float)((double)(ixs0 + ixs1) * 0.5);
         a.ys[w] = (float)((double)(iys0 + iys1) * 0.5);

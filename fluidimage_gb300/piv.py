@@ -223,7 +223,11 @@ class WorkPIV:
             )
             r.indices_no_displacement = (lay.n // 2 - 1, lay.n // 2 - 1)
             r.displacement_max = lay.displacement_max
-            r.near_ties = int(np.count_nonzero(h["flags"] & 1))
+            # per-vector near-tie flags (bit 0: top-two plane values within 1e-6
+            # relative; bit 1: tied minimum in the subpixel crop); on these vectors
+            # the upstream result depends on float rounding
+            r.near_tie_flags = h["flags"]
+            r.near_ties = int(np.count_nonzero(h["flags"]))
             if fx.threshold_diff_neighbour is not None:
                 r.deltaxs_wrong = {i: h["deltaxs_raw"][i] for i in errors}
                 r.deltays_wrong = {i: h["deltays_raw"][i] for i in errors}

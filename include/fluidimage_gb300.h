@@ -41,7 +41,10 @@ extern "C" {
 #define FI_VEC_CLOSE_BOUNDARY 6 /* "close boundary" (fi_subpix_at only)   */
 
 /* per-vector flag bits written by fi_piv_pass */
-#define FI_FLAG_NEAR_TIE 1 /* top two plane values within 1e-6 relative */
+#define FI_FLAG_NEAR_TIE 1   /* top two plane values within 1e-6 relative        */
+#define FI_FLAG_SUBPIX_TIE 2 /* two 3x3 crop values at the minimum (within 1e-5 of
+                                the range): the '2d_gaussian2' 1e-8 floor then
+                                depends on float rounding                         */
 
 /* fix flag bits written by fi_fix */
 #define FI_FIX_CORREL_MIN 1     /* "correl < correl_min"        */
