@@ -52,6 +52,11 @@ __device__ __forceinline__ float load_px(const void* im, int dtype, int64_t idx)
   }
 }
 
+__device__ __forceinline__ int load_px_int(const void* im, int dtype, int64_t idx) {
+  return (dtype == FI_U8) ? (int)__ldg(reinterpret_cast<const uint8_t*>(im) + idx)
+                          : (int)__ldg(reinterpret_cast<const uint16_t*>(im) + idx);
+}
+
 // Order-preserving float <-> uint32 keys (for atomicMin over floats).
 __device__ __forceinline__ uint32_t float_to_key(float f) {
   uint32_t u = __float_as_uint(f);

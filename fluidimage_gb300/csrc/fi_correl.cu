@@ -91,6 +91,28 @@ __device__ __forceinline__ void gsum4(double (&v)[4], int g, double* red) {
   }
 }
 
+// Sum of 4 unsigned 64-bit integers over the group (exact).
+template <int G>
+__device__ __forceinline__ void gsum4u(unsigned long long (&v)[4], int g, double* red) {
+  constexpr int W = G < 32 ? G : 32;
+  const unsigned m = seg_mask<G>();
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] += __shfl_xor_sync(m, v[i], o, W);
+  if constexpr (G == 64) {
+    unsigned long long* ru = reinterpret_cast<unsigned long long*>(red);
+    const int wi = (threadIdx.x >> 5) & 1;
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) ru[4 * wi + i] = v[i];
+    gsync<G>(g);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = ru[i] + ru[4 + i];
+    gsync<G>(g);
+  }
+}
+
 // min/max of 4 floats over the group: v[0], v[1] min; v[2], v[3] max.
 template <int G>
 __device__ __forceinline__ void gminmax4(float (&v)[4], int g, double* red) {
@@ -496,12 +518,19 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
     x10 = s1x - npad;
   }
 
-  // ---- stage the two windows, FP64 sums, min/max ----
-  double sums[4] = {0.0, 0.0, 0.0, 0.0};
+  // ---- stage the two windows; exact window sums ----
+  // Integer images: exact integer sums of v and v^2 (INT pipe).  Float images and
+  // plugin windows: float32 sums with a compensated sum of squares.  FP64 is used
+  // only once per window (the FP64 pipe of this GPU is narrow).
+  const bool intpath = !FROM_WINDOWS && a.dtype != FI_F32;
+  unsigned si0 = 0u, si1 = 0u;
+  unsigned long long qi0 = 0ull, qi1 = 0ull;
+  float sf0 = 0.f, sf1 = 0.f, qf0 = 0.f, qf1 = 0.f, cf0 = 0.f, cf1 = 0.f;
   float mm[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
   if (t < N) {
     const float min0 = FROM_WINDOWS ? 0.f : __ldg(a.im_min + 0);
     const float min1 = FROM_WINDOWS ? 0.f : __ldg(a.im_min + 1);
+    const int mini0 = (int)min0, mini1 = (int)min1;
     const int H = a.height, W = a.width;
 #pragma unroll 4
     for (int r = 0; r < N; ++r) {
@@ -510,26 +539,54 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
         v0 = __ldg(win0 + ((int64_t)w * N + r) * N + t);
         v1 = __ldg(win1 + ((int64_t)w * N + r) * N + t);
       } else if (valid) {
-        int y = y00 + r, x = x00 + t;
-        if (y >= 0 && y < H && x >= 0 && x < W)
-          v0 = __fsub_rn(load_px(a.im0, a.dtype, (int64_t)y * W + x), min0);
-        y = y10 + r;
-        x = x10 + t;
-        if (y >= 0 && y < H && x >= 0 && x < W)
-          v1 = __fsub_rn(load_px(a.im1, a.dtype, (int64_t)y * W + x), min1);
+        const int y0 = y00 + r, x0 = x00 + t, y1 = y10 + r, x1 = x10 + t;
+        const bool in0 = y0 >= 0 && y0 < H && x0 >= 0 && x0 < W;
+        const bool in1 = y1 >= 0 && y1 < H && x1 >= 0 && x1 < W;
+        if (intpath) {
+          const int i0v = in0 ? load_px_int(a.im0, a.dtype, (int64_t)y0 * W + x0) - mini0 : 0;
+          const int i1v = in1 ? load_px_int(a.im1, a.dtype, (int64_t)y1 * W + x1) - mini1 : 0;
+          v0 = (float)i0v;
+          v1 = (float)i1v;
+          si0 += (unsigned)i0v;
+          si1 += (unsigned)i1v;
+          qi0 += (unsigned long long)((unsigned)i0v * (unsigned)i0v);
+          qi1 += (unsigned long long)((unsigned)i1v * (unsigned)i1v);
+        } else {
+          if (in0) v0 = __fsub_rn(load_px(a.im0, a.dtype, (int64_t)y0 * W + x0), min0);
+          if (in1) v1 = __fsub_rn(load_px(a.im1, a.dtype, (int64_t)y1 * W + x1), min1);
+        }
       }
       Z[r * C::LD + t] = make_float2(v0, v1);
-      sums[0] += (double)v0;
-      sums[1] += (double)v0 * (double)v0;
-      sums[2] += (double)v1;
-      sums[3] += (double)v1 * (double)v1;
+      if (!intpath) {
+        sf0 += v0;
+        sf1 += v1;
+        // Kahan-compensated sums of squares
+        float yk = fmaf(v0, v0, -cf0), tk = qf0 + yk;
+        cf0 = (tk - qf0) - yk;
+        qf0 = tk;
+        yk = fmaf(v1, v1, -cf1);
+        tk = qf1 + yk;
+        cf1 = (tk - qf1) - yk;
+        qf1 = tk;
+      }
       mm[0] = fminf(mm[0], v0);
       mm[1] = fminf(mm[1], v1);
       mm[2] = fmaxf(mm[2], v0);
       mm[3] = fmaxf(mm[3], v1);
     }
   }
-  gsum4<C::G>(sums, g, red);
+  double sums[4];
+  if (intpath) {
+    unsigned long long u[4] = {si0, qi0, si1, qi1};
+    gsum4u<C::G>(u, g, red);
+    for (int i = 0; i < 4; ++i) sums[i] = (double)u[i];
+  } else {
+    sums[0] = (double)sf0;
+    sums[1] = (double)qf0 - (double)cf0;
+    sums[2] = (double)sf1;
+    sums[3] = (double)qf1 - (double)cf1;
+    gsum4<C::G>(sums, g, red);
+  }
   gminmax4<C::G>(mm, g, red);
   const double NN = (double)N * (double)N;
   // a constant window has an exactly zero spectrum (and plane) upstream
