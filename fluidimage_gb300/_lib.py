@@ -27,6 +27,7 @@ FLAG_SUBPIX_TIE = 2
 FIX_CORREL_MIN = 1
 FIX_DISPLACEMENT = 2
 FIX_NEIGHBOUR = 4
+FIX_STATIC_MAX_VECTORS = 262144
 
 P = C.c_void_p
 
@@ -76,6 +77,7 @@ _SIGNATURES = {
     ),
     "fi_subpix_at": (C.c_int, [P, C.c_int, C.c_int, P, P, P, P, P, P]),
     "fi_fix": (C.c_int, [P, P]),
+    "fi_fix_static": (C.c_int, [P, P]),
     "fi_tps_plan_make": (
         C.c_int,
         [P, P, P, P, C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, P, P, P],

@@ -6,9 +6,38 @@
 // Stage B (3x3 stencil on the vector grid): |d - mean8(d)|^2 > threshold^2 -> NaN.
 // All arithmetic is float32 in the upstream operation order; comparisons use the
 // float32-rounded thresholds (numpy 2 scalar promotion).
+#include <mutex>
+
 #include "fi_common.cuh"
 
 namespace fi {
+
+// Scratch of fi_fix_static: the stage-A output (x then y) of up to
+// FI_FIX_STATIC_MAX_VECTORS vectors.  Every GPU that loads this library holds it
+// (2 MiB) until the process exits; all calls on a device share it.
+static __device__ __align__(256) float g_fix_scratch[2 * FI_FIX_STATIC_MAX_VECTORS];
+
+// Device address of g_fix_scratch on the current device, looked up once per device.
+// (The host-side name g_fix_scratch is only a stand-in and must never be passed to
+// a kernel.)
+static int fix_scratch_address(float** out) {
+  static std::mutex lock;
+  static float* addr[64] = {};
+  int dev = 0;
+  FI_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("fi_fix_static: device index %d out of range", dev);
+    return FI_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> guard(lock);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    FI_CUDA_TRY(cudaGetSymbolAddress(&p, g_fix_scratch));
+    addr[dev] = static_cast<float*>(p);
+  }
+  *out = addr[dev];
+  return FI_OK;
+}
 
 __global__ void k_fix_a(fi_fix_args a, int nvec, float cmin, float dmax2, float* ox, float* oy) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,4 +174,39 @@ extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
                                        a.deltays_out);
   }
   return check_launch("fi_fix");
+}
+
+// Allocation-free variant of fi_fix: same kernels, scratch in g_fix_scratch.
+extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
+  FI_REQUIRE(args, "fi_fix_static: null args");
+  const fi_fix_args& a = *args;
+  FI_REQUIRE(a.nx >= 2 && a.ny >= 2, "fi_fix_static: vector grid must be at least 2 x 2");
+  FI_REQUIRE((int64_t)a.nx * a.ny <= FI_FIX_STATIC_MAX_VECTORS,
+             "fi_fix_static: %lld vectors exceed the static scratch limit of %d vectors "
+             "(use fi_fix with a caller-provided work buffer)",
+             (long long)a.nx * a.ny, FI_FIX_STATIC_MAX_VECTORS);
+  FI_REQUIRE(a.deltaxs && a.deltays && a.correls_max && a.errors && a.deltaxs_out &&
+                 a.deltays_out && a.fix_flags,
+             "fi_fix_static: null pointer");
+  float* scratch = nullptr;
+  const int rc = fix_scratch_address(&scratch);
+  if (rc != FI_OK) return rc;
+  const int nvec = a.nx * a.ny;
+  cudaStream_t s = (cudaStream_t)stream;
+  const float dmax2 = (float)((double)a.displacement_max * (double)a.displacement_max);
+  const float thr2 = (float)((double)a.threshold * (double)a.threshold);
+  const int threads = 256, blocks = (nvec + threads - 1) / threads;
+  if (a.use_threshold) {
+    // stage A writes every scratch entry it uses before stage B reads it, so
+    // nothing left by an earlier call is ever read
+    float* wx = scratch;
+    float* wy = scratch + nvec;
+    k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
+    k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
+    add_launches(1);
+  } else {
+    k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
+                                       a.deltays_out);
+  }
+  return check_launch("fi_fix_static");
 }

@@ -174,6 +174,24 @@ typedef struct fi_fix_args {
  */
 int fi_fix(const fi_fix_args* args, void* stream);
 
+/*
+ * fi_fix without a caller-provided work buffer, for callers that cannot allocate
+ * device memory (a host framework that owns a fixed device-memory budget, or a
+ * latency-critical loop where cudaMalloc and its implicit device synchronisation
+ * are not allowed).  No counterpart in the reference: it is the same WorkFIX
+ * computation as fi_fix, with its scratch (args->work is ignored) in a static
+ * device array of 2 * FI_FIX_STATIC_MAX_VECTORS floats (2 MiB) that every GPU
+ * loading this library holds until the process exits.  Grids of more than
+ * FI_FIX_STATIC_MAX_VECTORS vectors are rejected with FI_ERR_INVALID.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  It allocates nothing (no cudaMalloc, no cudaFree).  All
+ * calls on a device share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ */
+#define FI_FIX_STATIC_MAX_VECTORS 262144
+int fi_fix_static(const fi_fix_args* args, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Thin-plate-spline subdomain interpolation (FP64), the apply_interp of
  * works/piv/singlepass.py:409-563 with ThinPlateSplineSubdom
