@@ -301,6 +301,10 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(im0.nbytes + im1.nbytes),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": statistics.mean(e2e_ms)},
         "gpu_launches": int(launches),
+        "tps_subdomains": int(sum(t.nb_subdom for pd in outs for t in (pd.tps_next, pd.tps_final)
+                                  if t is not None)),
+        "tps_lu_fallbacks": int(sum(int(t.mp_status.sum().item()) for pd in outs
+                                    for t in (pd.tps_next, pd.tps_final) if t is not None)),
         "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kern.items()},
         "roofline": roof,
         "clocks": clk,

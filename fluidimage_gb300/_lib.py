@@ -86,13 +86,19 @@ _SIGNATURES = {
     "fi_tps_solve": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, C.c_double, C.c_int, P, P, P, P,
-         P, P, P, P, P],
+         P, P, P, P, P, P],
+    ),
+    "fi_tps_phi_table": (C.c_int, [P, C.c_int64, P]),
+    "fi_tps_solve_mp": (
+        C.c_int,
+        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, C.c_double,
+         C.c_int, P, P, P, P, P, P, P, P, P],
     ),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
     "fi_tps_interpolate": (
         C.c_int,
         [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,
-         P, P, P, P, P],
+         P, P, P, P, P, C.c_int64, P],
     ),
 }
 

@@ -67,6 +67,21 @@ __device__ __forceinline__ double tps_phi(double x0, double y0, double x1, doubl
   return __ddiv_rn(__dmul_rn(r2, log(r2)), 2.0);
 }
 
+// Same value from a table of phi(k / 4) when 4 r^2 is an integer k < tsize (centres
+// and grid points on the half-integer lattice); bit-identical to tps_phi.
+__device__ __forceinline__ double tps_phi_tab(double x0, double y0, double x1, double y1,
+                                              const double* table, int64_t tsize) {
+  const double dy = __dsub_rn(y1, y0), dx = __dsub_rn(x1, x0);
+  const double r2 = __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx));
+  const double q = 4.0 * r2;
+  if (table != nullptr && q < (double)tsize) {
+    const int64_t k = (int64_t)q;
+    if ((double)k == q) return __ldg(table + k);
+  }
+  if (r2 == 0.0) return 0.0;
+  return __ddiv_rn(__dmul_rn(r2, log(r2)), 2.0);
+}
+
 // ---------------------------------------------------------------------------
 // block-wide ordered compaction helper (blockDim.x multiple of 32, <= 1024)
 // returns the exclusive position of this thread's element and the chunk total.
@@ -305,13 +320,17 @@ __global__ void __launch_bounds__(512)
                 const int32_t* indices, const int64_t* mat_off, double* matrices, int32_t* pivots,
                 double threshold, int use_threshold, const int64_t* w_off, double* weights,
                 double* smoothed_x, double* smoothed_y, int32_t* iters, int32_t* nfixed,
-                int32_t* singular, double* max_udiff) {
+                int32_t* singular, double* max_udiff, const int32_t* only_failed) {
   extern __shared__ double sh[];
   __shared__ double shv[33];
   __shared__ int shi[33];
   __shared__ int s_any;
   const fi_tps_plan p = *plan_ptr;
   const int sd = blockIdx.x;
+  if (only_failed != nullptr && only_failed[sd] == 0) {  // solved by the mixed-precision path
+    if (threadIdx.x == 0) singular[sd] = 0;
+    return;
+  }
   const int N = counts[sd];
   const int n = N + 3;
   const int64_t off = offsets[sd];
@@ -476,7 +495,7 @@ __global__ void __launch_bounds__(256)
                const int64_t* w_off, const double* weights, const double* cx, const double* cy,
                const int32_t* ncounts, const int64_t* noffsets, const int32_t* nindices,
                const double* ncoefs, const double* px, const double* py, double* partx,
-               double* party) {
+               double* party, const double* table, int64_t tsize) {
   extern __shared__ double sh[];
   const int sd = blockIdx.y;
   const int N = counts[sd], n = N + 3, M = ncounts[sd];
@@ -504,7 +523,7 @@ __global__ void __launch_bounds__(256)
   const double x = px[q], y = py[q];
   double vx = 0.0, vy = 0.0;
   for (int j = 0; j < N; ++j) {
-    const double f = tps_phi(scx[j], scy[j], x, y);
+    const double f = tps_phi_tab(scx[j], scy[j], x, y, table, tsize);
     vx = fma(swx[j], f, vx);
     vy = fma(swy[j], f, vy);
   }
@@ -588,7 +607,8 @@ extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_memb
                             int32_t* pivots, double threshold, int use_threshold,
                             const int64_t* w_offsets, double* weights, double* smoothed_x,
                             double* smoothed_y, int32_t* iters, int32_t* nfixed,
-                            int32_t* singular, double* max_udiff, void* stream) {
+                            int32_t* singular, double* max_udiff, const int32_t* only_failed,
+                            void* stream) {
   FI_REQUIRE(plan && counts && offsets && indices && mat_offsets && matrices && pivots &&
                  w_offsets && weights && smoothed_x && smoothed_y && iters && nfixed &&
                  singular && max_udiff,
@@ -605,7 +625,7 @@ extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_memb
   k_tps_solve<<<nb_subdom, 512, smem, (cudaStream_t)stream>>>(
       plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, pivots, threshold,
       use_threshold, w_offsets, weights, smoothed_x, smoothed_y, iters, nfixed, singular,
-      max_udiff);
+      max_udiff, only_failed);
   return check_launch("fi_tps_solve");
 }
 
@@ -632,7 +652,8 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                                   int npts, const int32_t* ncounts, const int64_t* noffsets,
                                   const int32_t* nindices, const double* ncoefs, double* partx,
                                   double* party, double* out_x, double* out_y, int32_t* out_rx,
-                                  int32_t* out_ry, void* stream) {
+                                  int32_t* out_ry, const double* phi_table, int64_t table_size,
+                                  void* stream) {
   FI_REQUIRE(plan && cx && cy && counts && offsets && indices && w_offsets && weights && px &&
                  py && ncounts && noffsets && nindices && ncoefs && partx && party && out_x &&
                  out_y,
@@ -653,7 +674,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
     dim3 grid((max_new_members + threads - 1) / threads, nb_subdom);
     k_tps_eval<<<grid, threads, smem, s>>>(counts, offsets, indices, w_offsets, weights, cx, cy,
                                            ncounts, noffsets, nindices, ncoefs, px, py, partx,
-                                           party);
+                                           party, phi_table, table_size);
     add_launches(1);
   }
   const int threads = 256;

@@ -1,0 +1,712 @@
+// Mixed-precision solver of the smoothed TPS subdomain systems.
+//
+// Upstream (calcul/interpolate/thin_plate_spline.py:168-216,
+// thin_plate_spline_subdom.py:236-280) solves [[K + lam I, P], [P^T, 0]] [w; a] =
+// [u; 0] with LAPACK gesv in FP64, for x and y and again after each outlier
+// replacement.  That saddle-point matrix has condition numbers ~1e13-1e15, but its
+// null-space form is benign: with P = Q [R; 0] (Householder, Q = H1 H2 H3),
+// w = Q2 z and
+//     B z = Q2^T u,   B = Q2^T (K + lam I) Q2   (SPD, cond ~1e4 for lam > 0),
+//     a = R^-1 (Q1^T u - Q1^T (K + lam I) w),   smoothed = u - lam w.
+// On this GPU FP32 runs 73x faster than FP64, so B (projected in FP64) is rounded
+// to FP32 and factorised there (blocked Cholesky, ~N^3/6 flops), and the solution
+// is refined with FP64 residuals t = u - (K + lam I) w (2 N^2 FP64 flops per step
+// for both components, a few steps).  Refinement stops when the correction is below
+// 1e-13 of the solution, or stagnates below 1e-9; a subdomain that does not
+// converge (or whose P has rank < 3, or whose Cholesky meets a non-positive pivot)
+// is flagged and re-solved by the FP64 LU kernel (k_tps_solve).
+//
+// K entries come from a table of phi(r^2) = r^2 log(r^2) / 2 indexed by 4 r^2,
+// exact for window centres on the half-integer lattice (the integer window shifts
+// put every PIV vector there); other distances use log() directly.
+#include <cmath>
+
+#include "fi_common.cuh"
+
+namespace fi {
+
+// ------------------------------------------------------------------ phi
+__device__ __forceinline__ double phi_direct(double r2) {
+  if (r2 == 0.0) return 0.0;
+  return __ddiv_rn(__dmul_rn(r2, log(r2)), 2.0);
+}
+
+// phi(r^2) for the centre pair (a, b); table lookup when 4 r^2 is an integer in range.
+__device__ __forceinline__ double phi_pair(double xa, double ya, double xb, double yb,
+                                           const double* table, int64_t tsize) {
+  const double dy = __dsub_rn(ya, yb), dx = __dsub_rn(xa, xb);
+  const double r2 = __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx));
+  const double q = 4.0 * r2;
+  if (table != nullptr && q < (double)tsize) {
+    const int64_t k = (int64_t)q;
+    if ((double)k == q) return __ldg(table + k);
+  }
+  return phi_direct(r2);
+}
+
+__global__ void k_phi_table(double* table, int64_t count) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count;
+       k += (int64_t)gridDim.x * blockDim.x)
+    table[k] = phi_direct((double)k * 0.25);
+}
+
+// ------------------------------------------------------------------ block helpers
+template <int NT>
+__device__ __forceinline__ double bsum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < NT / 32 ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[32] = v;
+  }
+  __syncthreads();
+  v = sh[32];
+  __syncthreads();
+  return v;
+}
+
+template <int NT>
+__device__ __forceinline__ double2 bsum2(double2 v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  if (lane == 0) {
+    sh[2 * wid] = v.x;
+    sh[2 * wid + 1] = v.y;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    v.x = lane < NT / 32 ? sh[2 * lane] : 0.0;
+    v.y = lane < NT / 32 ? sh[2 * lane + 1] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    if (lane == 0) {
+      sh[64] = v.x;
+      sh[65] = v.y;
+    }
+  }
+  __syncthreads();
+  v.x = sh[64];
+  v.y = sh[65];
+  __syncthreads();
+  return v;
+}
+
+template <int NT>
+__device__ __forceinline__ double bmax(double v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < NT / 32 ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[32] = v;
+  }
+  __syncthreads();
+  v = sh[32];
+  __syncthreads();
+  return v;
+}
+
+constexpr int MP_THREADS = 512;
+
+// t = u - A w for two right-hand sides; A (n x n, symmetric, column-major) in FP64.
+__device__ void residual2(const double* A, int n, const double* wx, const double* wy,
+                          const float* ux, const float* uy, double* tx, double* ty) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+  for (int c = wid; c < n; c += nw) {
+    const double* col = A + (int64_t)c * n;  // row c = column c
+    double ax = 0.0, ay = 0.0;
+    for (int r = lane; r < n; r += 32) {
+      const double a = col[r];
+      ax = fma(a, wx[r], ax);
+      ay = fma(a, wy[r], ay);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, o);
+      ay += __shfl_xor_sync(0xffffffffu, ay, o);
+    }
+    if (lane == 0) {
+      tx[c] = (double)ux[c] - ax;
+      ty[c] = (double)uy[c] - ay;
+    }
+  }
+  __syncthreads();
+}
+constexpr int NB = 32;     // Cholesky panel width
+constexpr int PLD = NB + 1;
+
+// Apply H_k = I - tau_k v_k v_k^T (k in order) to the two vectors x, y (length n).
+template <bool REVERSE>
+__device__ void apply_reflectors2(const double* V, const double* tau, int n, double* x,
+                                  double* y, double* sh) {
+  for (int kk = 0; kk < 3; ++kk) {
+    const int k = REVERSE ? 2 - kk : kk;
+    const double* v = V + (int64_t)k * n;
+    double2 d = make_double2(0.0, 0.0);
+    for (int i = threadIdx.x; i < n; i += MP_THREADS) {
+      d.x += v[i] * x[i];
+      d.y += v[i] * y[i];
+    }
+    d = bsum2<MP_THREADS>(d, sh);
+    const double cx = tau[k] * d.x, cy = tau[k] * d.y;
+    for (int i = threadIdx.x; i < n; i += MP_THREADS) {
+      x[i] -= cx * v[i];
+      y[i] -= cy * v[i];
+    }
+    __syncthreads();
+  }
+}
+
+// Solve (L L^T) x = r in place for two right-hand sides (float), L lower m x m,
+// column-major with leading dimension ld; blocks of NB columns.
+__device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry, float* diag) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+  // forward: L y = r
+  for (int J = 0; J < m; J += NB) {
+    const int jb = min(NB, m - J);
+    for (int e = threadIdx.x; e < jb * jb; e += MP_THREADS) {
+      const int r = e % jb, c = e / jb;
+      diag[r * PLD + c] = (c <= r) ? L[(int64_t)(J + c) * ld + J + r] : 0.f;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      float vx = lane < jb ? rx[J + lane] : 0.f, vy = lane < jb ? ry[J + lane] : 0.f;
+      for (int k = 0; k < jb; ++k) {
+        const float d = diag[k * PLD + k];
+        const float xk = __shfl_sync(0xffffffffu, vx, k) / d;
+        const float yk = __shfl_sync(0xffffffffu, vy, k) / d;
+        if (lane == k) {
+          vx = xk;
+          vy = yk;
+        } else if (lane > k && lane < jb) {
+          const float l = diag[lane * PLD + k];
+          vx -= l * xk;
+          vy -= l * yk;
+        }
+      }
+      if (lane < jb) {
+        rx[J + lane] = vx;
+        ry[J + lane] = vy;
+      }
+    }
+    __syncthreads();
+    for (int r = J + jb + threadIdx.x; r < m; r += MP_THREADS) {
+      float ax = 0.f, ay = 0.f;
+      for (int c = 0; c < jb; ++c) {
+        const float l = L[(int64_t)(J + c) * ld + r];
+        ax += l * rx[J + c];
+        ay += l * ry[J + c];
+      }
+      rx[r] -= ax;
+      ry[r] -= ay;
+    }
+    __syncthreads();
+  }
+  // backward: L^T x = y
+  for (int J = ((m - 1) / NB) * NB; J >= 0; J -= NB) {
+    const int jb = min(NB, m - J);
+    // y[J:J+jb] -= L[J+jb:m, J:J+jb]^T x[J+jb:m]
+    for (int c = wid; c < jb; c += nw) {
+      const float* col = L + (int64_t)(J + c) * ld;
+      float ax = 0.f, ay = 0.f;
+      for (int r = J + jb + lane; r < m; r += 32) {
+        ax += col[r] * rx[r];
+        ay += col[r] * ry[r];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+      }
+      if (lane == 0) {
+        rx[J + c] -= ax;
+        ry[J + c] -= ay;
+      }
+    }
+    for (int e = threadIdx.x; e < jb * jb; e += MP_THREADS) {
+      const int r = e % jb, c = e / jb;
+      diag[r * PLD + c] = (c <= r) ? L[(int64_t)(J + c) * ld + J + r] : 0.f;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      float vx = lane < jb ? rx[J + lane] : 0.f, vy = lane < jb ? ry[J + lane] : 0.f;
+      for (int k = jb - 1; k >= 0; --k) {
+        const float d = diag[k * PLD + k];
+        const float xk = __shfl_sync(0xffffffffu, vx, k) / d;
+        const float yk = __shfl_sync(0xffffffffu, vy, k) / d;
+        if (lane == k) {
+          vx = xk;
+          vy = yk;
+        } else if (lane < k) {
+          const float l = diag[k * PLD + lane];
+          vx -= l * xk;
+          vy -= l * yk;
+        }
+      }
+      if (lane < jb) {
+        rx[J + lane] = vx;
+        ry[J + lane] = vy;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Blocked right-looking Cholesky (lower) of the m x m matrix B (column-major, ld).
+// Returns false on a non-positive pivot.
+__device__ bool chol_factor(float* B, int m, int ld, float* panel, int* s_flag) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) *s_flag = 0;
+  for (int J = 0; J < m; J += NB) {
+    const int jb = min(NB, m - J);
+    const int rows = m - J;
+    for (int e = threadIdx.x; e < rows * jb; e += MP_THREADS) {
+      const int r = e % rows, c = e / rows;
+      panel[r * PLD + c] = B[(int64_t)(J + c) * ld + J + r];
+    }
+    __syncthreads();
+    // diagonal block by warp 0 (lane = row)
+    if (wid == 0) {
+      for (int k = 0; k < jb; ++k) {
+        float dkk = panel[k * PLD + k];
+        if (!(dkk > 0.f)) {
+          if (lane == 0) *s_flag = 1;
+          dkk = 1.f;
+        }
+        const float d = sqrtf(dkk);
+        if (lane == k) panel[k * PLD + k] = d;
+        __syncwarp();
+        if (lane > k && lane < jb) panel[lane * PLD + k] /= d;
+        __syncwarp();
+        if (lane > k && lane < jb) {
+          const float lk = panel[lane * PLD + k];
+          for (int c = k + 1; c <= lane; ++c) panel[lane * PLD + c] -= lk * panel[c * PLD + k];
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // rows below the diagonal block: L21 = A21 L11^-T (one row per thread)
+    for (int r = jb + threadIdx.x; r < rows; r += MP_THREADS) {
+      float* pr = panel + r * PLD;
+      for (int k = 0; k < jb; ++k) {
+        float v = pr[k];
+        for (int c = 0; c < k; ++c) v -= pr[c] * panel[k * PLD + c];
+        pr[k] = v / panel[k * PLD + k];
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * jb; e += MP_THREADS) {
+      const int r = e % rows, c = e / rows;
+      if (r >= c) B[(int64_t)(J + c) * ld + J + r] = panel[r * PLD + c];
+    }
+    // trailing update of the lower triangle: B22 -= L21 L21^T, 4x4 tiles
+    const int t0 = J + jb, tn = m - t0;
+    if (tn > 0) {
+      const int nt = (tn + 3) / 4;
+      const int ntiles = nt * (nt + 1) / 2;
+      for (int tile = threadIdx.x; tile < ntiles; tile += MP_THREADS) {
+        // tile -> (ti, tj) with tj <= ti
+        int ti = (int)((sqrtf(8.f * tile + 1.f) - 1.f) * 0.5f);
+        while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
+        while (ti * (ti + 1) / 2 > tile) --ti;
+        const int tj = tile - ti * (ti + 1) / 2;
+        float acc[4][4] = {};
+        const int rb = jb + 4 * ti, cb = jb + 4 * tj;
+        for (int k = 0; k < jb; ++k) {
+          float a[4], b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            a[q] = (rb + q < rows) ? panel[(rb + q) * PLD + k] : 0.f;
+            b[q] = (cb + q < rows) ? panel[(cb + q) * PLD + k] : 0.f;
+          }
+#pragma unroll
+          for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a[p], b[q], acc[p][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int c = t0 + 4 * tj + q;
+          if (c >= m) continue;
+          float* col = B + (int64_t)c * ld;
+#pragma unroll
+          for (int p = 0; p < 4; ++p) {
+            const int r = t0 + 4 * ti + p;
+            if (r < m && r >= c) col[r] -= acc[p][q];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    (void)lane;
+  }
+  return *s_flag == 0;
+}
+
+// One block per subdomain.  Status per subdomain: 0 solved here, 1 needs the FP64
+// LU fallback (rank-deficient P, Cholesky breakdown or no convergence).
+__global__ void __launch_bounds__(MP_THREADS)
+    k_tps_solve_mp(const fi_tps_plan* plan_ptr, const double* cx, const double* cy,
+                   const float* ux, const float* uy, const int32_t* counts,
+                   const int64_t* offsets, const int32_t* indices, const int64_t* mat_off,
+                   double* matrices, double* work64, float* matrices32, const double* phi_table,
+                   int64_t table_size, double threshold, int use_threshold,
+                   const int64_t* w_off, double* weights, double* smoothed_x,
+                   double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
+                   double* max_udiff, int max_refine) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ double sh[80];
+  __shared__ double s_tau[3];
+  __shared__ double s_R[9];
+  __shared__ int s_flag, s_bad[2];
+  const fi_tps_plan p = *plan_ptr;
+  const int sd = blockIdx.x;
+  const int N = counts[sd];
+  const int m = N - 3;
+  const int64_t off = offsets[sd];
+  const int32_t* idx = indices + off;
+  const double lam = p.smoothing;
+  if (threadIdx.x == 0) status[sd] = 1;
+  if (m < 1) return;  // fewer than 4 centres: FP64 LU path
+
+  // shared layout (doubles first)
+  double* V = reinterpret_cast<double*>(smraw);  // 3 N
+  double* xc = V + 3 * N;                         // N
+  double* yc = xc + N;                            // N
+  double* wx = yc + N;                            // N  (weights w, then scratch)
+  double* wy = wx + N;
+  double* tx = wy + N;                            // N  (residual / projections)
+  double* ty = tx + N;
+  double* zx = ty + N;                            // m (+3 padding)
+  double* zy = zx + N;
+  float* vx = reinterpret_cast<float*>(zy + N);  // N current values (float32)
+  float* vy = vx + N;
+  float* rx = vy + N;                             // m correction (float)
+  float* ry = rx + N;
+  float* panel = ry + N;                          // N * PLD
+
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+  const double* A64 = matrices + mat_off[sd];  // N x N, K + lam I (kept for residuals)
+  double* W64 = work64 + mat_off[sd];          // N x N, projected copy
+  float* B = matrices32 + mat_off[sd];         // N x N float
+
+  for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+    const int a = idx[i];
+    xc[i] = cx[a];
+    yc[i] = cy[a];
+  }
+  __syncthreads();
+  // ---- A = K + lam I in FP64 (column-major), and the copy that gets projected
+  for (int c = wid; c < N; c += nw) {
+    const double bx = xc[c], by = yc[c];
+    double* col = matrices + mat_off[sd] + (int64_t)c * N;
+    double* colw = W64 + (int64_t)c * N;
+    for (int r = lane; r < N; r += 32) {
+      const double v = (r == c) ? lam : phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
+      col[r] = v;
+      colw[r] = v;
+    }
+  }
+  // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
+  {
+    double* P0 = tx;  // scratch columns
+    double* P1 = ty;
+    double* P2 = wx;
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+      P0[i] = 1.0;
+      P1[i] = yc[i];
+      P2[i] = xc[i];
+    }
+    __syncthreads();
+    double* cols[3] = {P0, P1, P2};
+    bool rank_ok = true;
+    for (int k = 0; k < 3; ++k) {
+      double* x = cols[k];
+      double nrm2 = 0.0;
+      for (int i = k + threadIdx.x; i < N; i += MP_THREADS) nrm2 += x[i] * x[i];
+      nrm2 = bsum<MP_THREADS>(nrm2, sh);
+      const double x0 = x[k];
+      const double nrm = sqrt(nrm2);
+      if (!(nrm > 0.0)) {
+        rank_ok = false;
+        break;
+      }
+      const double alpha = (x0 >= 0.0) ? -nrm : nrm;
+      double* v = V + (int64_t)k * N;
+      for (int i = threadIdx.x; i < N; i += MP_THREADS) v[i] = (i < k) ? 0.0 : x[i];
+      __syncthreads();
+      if (threadIdx.x == 0) v[k] = x0 - alpha;
+      __syncthreads();
+      double vv = 0.0;
+      for (int i = k + threadIdx.x; i < N; i += MP_THREADS) vv += v[i] * v[i];
+      vv = bsum<MP_THREADS>(vv, sh);
+      if (!(vv > 0.0)) {
+        rank_ok = false;
+        break;
+      }
+      const double tau = 2.0 / vv;
+      if (threadIdx.x == 0) {
+        s_tau[k] = tau;
+        s_R[k * 3 + k] = alpha;
+      }
+      for (int j = k + 1; j < 3; ++j) {  // apply H_k to the remaining columns
+        double* y = cols[j];
+        double d = 0.0;
+        for (int i = k + threadIdx.x; i < N; i += MP_THREADS) d += v[i] * y[i];
+        d = bsum<MP_THREADS>(d, sh);
+        for (int i = k + threadIdx.x; i < N; i += MP_THREADS) y[i] -= tau * d * v[i];
+        __syncthreads();
+        if (threadIdx.x == 0) s_R[k * 3 + j] = y[k];
+        __syncthreads();
+      }
+      if (fabs(alpha) < 1e-9 * sqrt((double)N)) rank_ok = false;  // collinear centres
+    }
+    __syncthreads();
+    if (!rank_ok) return;
+  }
+  __syncthreads();
+  // ---- Q^T A Q in FP64 (three two-sided reflections on the copy W64): the
+  // projection cancels the large affine part of K, so it needs FP64; only the
+  // projected block B22 (norm ~ its condition number times lam) is rounded to FP32.
+  for (int k = 0; k < 3; ++k) {
+    const double* v = V + (int64_t)k * N;
+    const double tau = s_tau[k];
+    for (int c = wid; c < N; c += nw) {  // p = A v (A symmetric: row c = column c)
+      const double* col = W64 + (int64_t)c * N;
+      double acc = 0.0;
+      for (int r = k + lane; r < N; r += 32) acc = fma(col[r], v[r], acc);
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) tx[c] = acc;
+    }
+    __syncthreads();
+    double vp = 0.0;
+    for (int i = k + threadIdx.x; i < N; i += MP_THREADS) vp += v[i] * tx[i];
+    vp = bsum<MP_THREADS>(vp, sh);
+    const double beta = 0.5 * tau * tau * vp;
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) ty[i] = tau * tx[i] - beta * v[i];
+    __syncthreads();
+    for (int c = wid; c < N; c += nw) {  // A -= v w^T + w v^T
+      double* col = W64 + (int64_t)c * N;
+      const double vc = v[c], wc = ty[c];
+      for (int r = lane; r < N; r += 32) col[r] -= fma(v[r], wc, ty[r] * vc);
+    }
+    __syncthreads();
+  }
+  for (int c = wid; c < N; c += nw) {  // B = float(Q^T A Q), lower triangle of B22 used
+    const double* col = W64 + (int64_t)c * N;
+    float* colb = B + (int64_t)c * N;
+    for (int r = c + lane; r < N; r += 32) colb[r] = (float)col[r];
+  }
+  __syncthreads();
+  // ---- FP32 Cholesky of B22 = B[3:, 3:]
+  float* B22 = B + 3 + 3 * (int64_t)N;
+  if (!chol_factor(B22, m, N, panel, &s_flag)) return;
+
+  // ---- outlier iterations with refined solves (x and y in lockstep)
+  for (int r = threadIdx.x; r < N; r += MP_THREADS) {
+    vx[r] = ux[idx[r]];
+    vy[r] = uy[idx[r]];
+  }
+  for (int r = threadIdx.x; r < N; r += MP_THREADS) zx[r] = zy[r] = 0.0;
+  __syncthreads();
+  int count[2] = {1, 1}, fixed[2] = {0, 0};
+  bool done[2] = {false, false};
+  bool converged_all = true;
+  while (true) {
+    // refine z for the current values
+    bool conv = false;
+    double prev = INFINITY;
+    for (int it = 0; it < max_refine; ++it) {
+      // w = Q [0; z]
+      for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+        wx[i] = (i < 3) ? 0.0 : zx[i - 3];
+        wy[i] = (i < 3) ? 0.0 : zy[i - 3];
+      }
+      __syncthreads();
+      apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
+      residual2(A64, N, wx, wy, vx, vy, tx, ty);
+      // rho = (Q^T t)[3:]
+      apply_reflectors2<false>(V, s_tau, N, tx, ty, sh);
+      for (int i = threadIdx.x; i < m; i += MP_THREADS) {
+        rx[i] = (float)tx[i + 3];
+        ry[i] = (float)ty[i + 3];
+      }
+      __syncthreads();
+      chol_solve2(B22, m, N, rx, ry, panel);
+      double dmax = 0.0, zmax = 0.0;
+      for (int i = threadIdx.x; i < m; i += MP_THREADS) {
+        if (!done[0]) zx[i] += (double)rx[i];
+        if (!done[1]) zy[i] += (double)ry[i];
+        dmax = fmax(dmax, fmax(done[0] ? 0.0 : fabs((double)rx[i]),
+                               done[1] ? 0.0 : fabs((double)ry[i])));
+        zmax = fmax(zmax, fmax(fabs(zx[i]), fabs(zy[i])));
+      }
+      dmax = bmax<MP_THREADS>(dmax, sh);
+      zmax = bmax<MP_THREADS>(zmax, sh);
+      if (dmax <= 1e-13 * zmax || dmax == 0.0) {
+        conv = true;
+        break;
+      }
+      if (it >= 2 && dmax > 0.5 * prev) {  // at the FP64 residual floor
+        conv = dmax <= 1e-9 * zmax;
+        break;
+      }
+      prev = dmax;
+    }
+    if (!conv) {
+      converged_all = false;
+      break;
+    }
+    // final w, s = A w is in t before projection: recompute t = u - A w for a
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+      wx[i] = (i < 3) ? 0.0 : zx[i - 3];
+      wy[i] = (i < 3) ? 0.0 : zy[i - 3];
+    }
+    __syncthreads();
+    apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
+    residual2(A64, N, wx, wy, vx, vy, tx, ty);
+    // a = R^-1 (Q1^T (u - A w))
+    apply_reflectors2<false>(V, s_tau, N, tx, ty, sh);
+    double ax3[3], ay3[3];
+    for (int k = 2; k >= 0; --k) {
+      double sxk = tx[k], syk = ty[k];
+      for (int j = k + 1; j < 3; ++j) {
+        sxk -= s_R[k * 3 + j] * ax3[j];
+        syk -= s_R[k * 3 + j] * ay3[j];
+      }
+      ax3[k] = sxk / s_R[k * 3 + k];
+      ay3[k] = syk / s_R[k * 3 + k];
+    }
+    // smoothed = u - lam w; outlier test (compute_tps_weights_iter, subdom.py:236-280)
+    if (threadIdx.x == 0) s_bad[0] = s_bad[1] = 0;
+    __syncthreads();
+    double mxx = 0.0, mxy = 0.0;
+    int bx = 0, by = 0;
+    for (int r = threadIdx.x; r < N; r += MP_THREADS) {
+      const double sxv = __dsub_rn((double)vx[r], __dmul_rn(lam, wx[r]));
+      const double syv = __dsub_rn((double)vy[r], __dmul_rn(lam, wy[r]));
+      const double dfx = fabs(__dsub_rn(sxv, (double)vx[r]));
+      const double dfy = fabs(__dsub_rn(syv, (double)vy[r]));
+      if (!done[0]) {
+        smoothed_x[off + r] = sxv;
+        mxx = fmax(mxx, dfx);
+        if (use_threshold && dfx > threshold) bx++;
+      }
+      if (!done[1]) {
+        smoothed_y[off + r] = syv;
+        mxy = fmax(mxy, dfy);
+        if (use_threshold && dfy > threshold) by++;
+      }
+    }
+    mxx = bmax<MP_THREADS>(mxx, sh);
+    mxy = bmax<MP_THREADS>(mxy, sh);
+    if (bx) atomicAdd(&s_bad[0], bx);
+    if (by) atomicAdd(&s_bad[1], by);
+    __syncthreads();
+    const int nbx = s_bad[0], nby = s_bad[1];
+    if (threadIdx.x == 0) {
+      if (count[0] == 1 && !done[0]) max_udiff[2 * sd] = mxx;
+      if (count[1] == 1 && !done[1]) max_udiff[2 * sd + 1] = mxy;
+    }
+    // store the weights of the components finishing now
+    const int n3 = N + 3;
+    double* wxo = weights + w_off[sd];
+    double* wyo = wxo + n3;
+    bool fin[2];
+    fin[0] = !done[0] && (!use_threshold || nbx == 0 || count[0] > 10);
+    fin[1] = !done[1] && (!use_threshold || nby == 0 || count[1] > 10);
+    for (int r = threadIdx.x; r < N; r += MP_THREADS) {
+      if (fin[0]) wxo[r] = wx[r];
+      if (fin[1]) wyo[r] = wy[r];
+    }
+    if (threadIdx.x == 0) {
+      if (fin[0])
+        for (int k = 0; k < 3; ++k) wxo[N + k] = ax3[k];
+      if (fin[1])
+        for (int k = 0; k < 3; ++k) wyo[N + k] = ay3[k];
+    }
+    // replace the erratic values (rounded to float32 like upstream's array)
+    for (int r = threadIdx.x; r < N; r += MP_THREADS) {
+      if (!done[0] && !fin[0]) {
+        const double sv = smoothed_x[off + r];
+        if (fabs(__dsub_rn(sv, (double)vx[r])) > threshold) vx[r] = (float)sv;
+      }
+      if (!done[1] && !fin[1]) {
+        const double sv = smoothed_y[off + r];
+        if (fabs(__dsub_rn(sv, (double)vy[r])) > threshold) vy[r] = (float)sv;
+      }
+    }
+    for (int c = 0; c < 2; ++c) {
+      if (done[c]) continue;
+      if (fin[c]) {
+        done[c] = true;
+      } else {
+        fixed[c] += (c == 0) ? nbx : nby;
+        count[c]++;
+      }
+    }
+    __syncthreads();
+    if (done[0] && done[1]) break;
+  }
+  if (!converged_all) return;
+  if (threadIdx.x == 0) {
+    iters[2 * sd] = count[0];
+    iters[2 * sd + 1] = count[1];
+    nfixed[2 * sd] = fixed[0];
+    nfixed[2 * sd + 1] = fixed[1];
+    status[sd] = 0;
+  }
+}
+
+}  // namespace fi
+
+using namespace fi;
+
+extern "C" int fi_tps_phi_table(double* table, int64_t count, void* stream) {
+  FI_REQUIRE(table && count > 0, "fi_tps_phi_table: bad arguments");
+  k_phi_table<<<1024, 256, 0, (cudaStream_t)stream>>>(table, count);
+  return check_launch("fi_tps_phi_table");
+}
+
+extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members,
+                               const double* cx, const double* cy, const float* ux,
+                               const float* uy, const int32_t* counts, const int64_t* offsets,
+                               const int32_t* indices, const int64_t* mat_offsets,
+                               double* matrices, double* work64, float* matrices32,
+                               const double* phi_table,
+                               int64_t table_size, double threshold, int use_threshold,
+                               const int64_t* w_offsets, double* weights, double* smoothed_x,
+                               double* smoothed_y, int32_t* iters, int32_t* nfixed,
+                               int32_t* status, double* max_udiff, void* stream) {
+  FI_REQUIRE(plan && cx && cy && ux && uy && counts && offsets && indices && mat_offsets &&
+                 matrices && work64 && matrices32 && w_offsets && weights && smoothed_x &&
+                 smoothed_y &&
+                 iters && nfixed && status && max_udiff,
+             "fi_tps_solve_mp: null pointer");
+  FI_REQUIRE(nb_subdom > 0, "fi_tps_solve_mp: no subdomain");
+  const int N = max_members > 4 ? max_members : 4;
+  const size_t smem = (size_t)N * 11 * sizeof(double) + (size_t)N * 4 * sizeof(float) +
+                      (size_t)N * PLD * sizeof(float) + 64;
+  FI_REQUIRE(smem <= 220 * 1024, "fi_tps_solve_mp: subdomain of %d vectors too large",
+             max_members);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_solve_mp,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
+  }
+  k_tps_solve_mp<<<nb_subdom, MP_THREADS, smem, (cudaStream_t)stream>>>(
+      plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, work64, matrices32,
+      phi_table, table_size, threshold, use_threshold, w_offsets, weights, smoothed_x,
+      smoothed_y, iters, nfixed, status, max_udiff, 60);
+  return check_launch("fi_tps_solve_mp");
+}

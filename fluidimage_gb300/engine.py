@@ -197,9 +197,30 @@ class TpsOutput:
     w_offsets: object = None
     weights: object = None
     singular: object = None
+    mp_status: object = None
     iters: object = None
     nfixed: object = None
     max_udiff: object = None
+
+
+#: phi(k / 4) for k < PHI_TABLE_SIZE covers distances up to ~1024 px on the
+#: half-integer lattice (32 MiB per device); larger distances use log() directly.
+PHI_TABLE_SIZE = 1 << 22
+#: largest subdomain handled by the mixed-precision solver (shared-memory bound)
+MP_MAX_MEMBERS = 800
+_PHI_TABLES = {}
+
+
+def phi_table(device):
+    """The per-device table of the TPS kernel values (built on first use)."""
+    torch = _torch()
+    key = (device.type, device.index if device.index is not None else torch.cuda.current_device())
+    if key not in _PHI_TABLES:
+        table = torch.empty(PHI_TABLE_SIZE, dtype=torch.float64, device=device)
+        L.check(L.load().fi_tps_phi_table(L.ptr(table), PHI_TABLE_SIZE, L.stream_handle()),
+                "fi_tps_phi_table")
+        _PHI_TABLES[key] = table
+    return _PHI_TABLES[key]
 
 
 def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
@@ -263,19 +284,33 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     singular = torch.empty(nsub, **i32)
     max_udiff = torch.empty(2 * nsub, **f64)
     use_thr = threshold is not None
+    thr = float(threshold) if use_thr else 0.0
+    table = phi_table(dev)
+    status = torch.ones(nsub, **i32)
+    if int(ch.max()) <= MP_MAX_MEMBERS:
+        work64 = torch.empty(int(msz.sum()), dtype=torch.float64, device=dev)
+        matrices32 = torch.empty(int(msz.sum()), dtype=torch.float32, device=dev)
+        with _timed("fi_tps_solve_mp"):
+            L.check(lib.fi_tps_solve_mp(
+                L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
+                L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d), L.ptr(matrices),
+                L.ptr(work64), L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, thr, int(use_thr),
+                L.ptr(woff_d), L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
+                L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), s), "fi_tps_solve_mp")
+    # FP64 LU for the subdomains the mixed-precision solver flagged (or all of them)
     with _timed("fi_tps_solve"):
       L.check(lib.fi_tps_solve(L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux),
                              L.ptr(uy), L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d),
-                             L.ptr(matrices), L.ptr(pivots),
-                             float(threshold) if use_thr else 0.0, int(use_thr), L.ptr(woff_d),
+                             L.ptr(matrices), L.ptr(pivots), thr, int(use_thr), L.ptr(woff_d),
                              L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
-                             L.ptr(nfixed), L.ptr(singular), L.ptr(max_udiff), s),
+                             L.ptr(nfixed), L.ptr(singular), L.ptr(max_udiff), L.ptr(status), s),
             "fi_tps_solve")
     out = TpsOutput(
         out_x=torch.empty(npts, **f64), out_y=torch.empty(npts, **f64),
         rx=torch.empty(npts, **i32), ry=torch.empty(npts, **i32), selection=sel,
         num_centers=nv, nb_subdom=nsub, counts=ch, w_offsets=woff, weights=weights,
         singular=singular, iters=iters, nfixed=nfixed, max_udiff=max_udiff,
+        mp_status=status,
     )
     if want_smooth:
         out.smooth_x = torch.empty(nv, **f64)
@@ -292,7 +327,8 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                    L.ptr(woff_d), L.ptr(weights), L.ptr(px), L.ptr(py), npts,
                                    L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),
                                    L.ptr(partx), L.ptr(party), L.ptr(out.out_x),
-                                   L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry), s),
+                                   L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry),
+                                   L.ptr(table), PHI_TABLE_SIZE, s),
             "fi_tps_interpolate")
     return out
 

@@ -242,7 +242,8 @@ int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, con
  * n_i+3 ints at offsets[i] + 3 i; weights: 2 (n_i+3) doubles at w_offsets[i]
  * (x then y); smoothed_x/y: n_i doubles at offsets[i].  iters, nfixed,
  * max_udiff: [2 * nb_subdom] (x, y); singular: [nb_subdom] (1 = zero pivot,
- * where upstream raises LinAlgError).
+ * where upstream raises LinAlgError).  When only_failed is not NULL, subdomains
+ * with only_failed[i] == 0 are skipped (already solved by fi_tps_solve_mp).
  */
 int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
                  const double* cy, const float* ux, const float* uy, const int32_t* counts,
@@ -250,7 +251,35 @@ int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members, const 
                  double* matrices, int32_t* pivots, double threshold, int use_threshold,
                  const int64_t* w_offsets, double* weights, double* smoothed_x,
                  double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* singular,
-                 double* max_udiff, void* stream);
+                 double* max_udiff, const int32_t* only_failed, void* stream);
+
+/*
+ * Table of phi(k / 4) = (k/4) log(k/4) / 2 for k < count (float64): the TPS kernel
+ * values on the half-integer lattice of PIV vector positions
+ * (compute_tps_matrix, thin_plate_spline.py:136-145).  Built once per device.
+ */
+int fi_tps_phi_table(double* table, int64_t count, void* stream);
+
+/*
+ * Mixed-precision TPS solve (same inputs and outputs as fi_tps_solve): null-space
+ * form B z = Q2^T u with B = Q2^T (K + lam I) Q2 (projected in FP64) factorised
+ * in FP32 (blocked Cholesky) and refined with FP64 residuals to ~1e-11 relative
+ * (K from the phi table); the outlier iterations of
+ * compute_tps_weights_iter (thin_plate_spline_subdom.py:236-280) warm-start from
+ * the previous solution.  matrices and work64: (n_i+3)^2 doubles each at
+ * mat_offsets[i] (K + lam I, and its projected copy); matrices32: (n_i+3)^2 floats
+ * at mat_offsets[i] (the FP32 Cholesky factor).  status[i] = 0 when
+ * solved, 1 when the subdomain must go through fi_tps_solve (pass status as its
+ * only_failed argument): rank-deficient P, Cholesky breakdown or no convergence.
+ */
+int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
+                    const double* cy, const float* ux, const float* uy, const int32_t* counts,
+                    const int64_t* offsets, const int32_t* indices, const int64_t* mat_offsets,
+                    double* matrices, double* work64, float* matrices32, const double* phi_table,
+                    int64_t table_size, double threshold, int use_threshold,
+                    const int64_t* w_offsets, double* weights, double* smoothed_x,
+                    double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
+                    double* max_udiff, void* stream);
 
 /*
  * Smoothed values at the centres, blended over the subdomains that contain them
@@ -276,7 +305,8 @@ int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        const double* py, int npts, const int32_t* ncounts,
                        const int64_t* noffsets, const int32_t* nindices, const double* ncoefs,
                        double* partx, double* party, double* out_x, double* out_y,
-                       int32_t* out_rx, int32_t* out_ry, void* stream);
+                       int32_t* out_rx, int32_t* out_ry, const double* phi_table,
+                       int64_t table_size, void* stream);
 
 #ifdef __cplusplus
 }
