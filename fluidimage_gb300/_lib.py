@@ -82,7 +82,8 @@ _SIGNATURES = {
         C.c_int,
         [P, P, P, P, C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, P, P, P],
     ),
-    "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P]),
+    "fi_tps_lattice": (C.c_int, [P, P, C.c_int, P, P, P]),
+    "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P]),
     "fi_tps_solve": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, C.c_double, C.c_int, P, P, P, P,
@@ -91,14 +92,14 @@ _SIGNATURES = {
     "fi_tps_phi_table": (C.c_int, [P, C.c_int64, P]),
     "fi_tps_solve_mp": (
         C.c_int,
-        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, C.c_double,
+        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P, C.c_double,
          C.c_int, P, P, P, P, P, P, P, P, P],
     ),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
     "fi_tps_interpolate": (
         C.c_int,
         [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,
-         P, P, P, P, P, C.c_int64, P],
+         P, P, P, P, P, C.c_int64, P, P, P],
     ),
 }
 

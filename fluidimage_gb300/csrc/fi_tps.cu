@@ -207,32 +207,53 @@ __global__ void __launch_bounds__(1024)
   *plan = p;
 }
 
+__global__ void k_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
+                              int32_t* on_lattice) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npts) return;
+  const double X = 2.0 * px[i], Y = 2.0 * py[i];
+  const bool ok = X == rint(X) && Y == rint(Y) && fabs(X) < 1073741824.0 &&
+                  fabs(Y) < 1073741824.0;
+  xy2[2 * i] = ok ? (int32_t)X : 0;
+  xy2[2 * i + 1] = ok ? (int32_t)Y : 0;
+  if (!ok) atomicAnd(on_lattice, 0);
+}
+
+__global__ void k_set_int(int32_t* p, int32_t v) { *p = v; }
+
 // Ordered membership of points in subdomain blockIdx.x; mode 0 counts, mode 1 fills.
 __global__ void __launch_bounds__(512)
     k_tps_members(const fi_tps_plan* plan_ptr, const double* px, const double* py, int npts,
                   int mode, int32_t* counts, const int64_t* offsets, int32_t* indices,
-                  double* coefs) {
+                  double* coefs, const int32_t* xy2, const int32_t* on_lattice) {
   __shared__ int warp_tot[33];
   const fi_tps_plan p = *plan_ptr;
   const int i = blockIdx.x;
   const int iy = i / p.nb_subdomx, ix = i % p.nb_subdomx;
   const Limits L = subdom_limits(p, ix, iy);
+  // on the lattice, X = 2x is an integer: x >= l <=> X >= ceil(2l), x < l <=> X < ceil(2l)
+  const bool lat = xy2 != nullptr && on_lattice != nullptr && *on_lattice != 0;
+  const double kmax = 2147483647.0;
+  const int X0 = (int)fmin(ceil(2.0 * L.lminx), kmax), X1 = (int)fmin(ceil(2.0 * L.lmaxx), kmax);
+  const int Y0 = (int)fmin(ceil(2.0 * L.lminy), kmax), Y1 = (int)fmin(ceil(2.0 * L.lmaxy), kmax);
   int base = 0;
   const int64_t off = (mode == 1) ? offsets[i] : 0;
   for (int c0 = 0; c0 < npts; c0 += blockDim.x) {
     const int q = c0 + threadIdx.x;
     bool in = false;
-    double x = 0.0, y = 0.0;
     if (q < npts) {
-      x = px[q];
-      y = py[q];
-      in = inside(L, x, y);
+      if (lat) {
+        const int X = xy2[2 * q], Y = xy2[2 * q + 1];
+        in = X >= X0 && X < X1 && Y >= Y0 && Y < Y1;
+      } else {
+        in = inside(L, px[q], py[q]);
+      }
     }
     int total;
     const int pos = base + block_scan_flag(in, warp_tot, &total);
     if (in && mode == 1) {
       indices[off + pos] = q;
-      coefs[off + pos] = coef_norm(L, x, y);
+      coefs[off + pos] = coef_norm(L, px[q], py[q]);
     }
     base += total;
   }
@@ -495,7 +516,8 @@ __global__ void __launch_bounds__(256)
                const int64_t* w_off, const double* weights, const double* cx, const double* cy,
                const int32_t* ncounts, const int64_t* noffsets, const int32_t* nindices,
                const double* ncoefs, const double* px, const double* py, double* partx,
-               double* party, const double* table, int64_t tsize) {
+               double* party, const double* table, int64_t tsize, const int32_t* cxy2,
+               const int32_t* c_on_lattice) {
   extern __shared__ double sh[];
   const int sd = blockIdx.y;
   const int N = counts[sd], n = N + 3, M = ncounts[sd];
@@ -505,12 +527,16 @@ __global__ void __launch_bounds__(256)
   double* scy = sh + N;
   double* swx = sh + 2 * N;
   double* swy = sh + 2 * N + n;
+  int2* sxy2 = reinterpret_cast<int2*>(swy + n);  // lattice coordinates of the centres
+  __shared__ int s_lat;
   const int64_t off = offsets[sd];
   const double* w = weights + w_off[sd];
+  if (threadIdx.x == 0) s_lat = (cxy2 != nullptr && c_on_lattice != nullptr) ? *c_on_lattice : 0;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const int a = indices[off + j];
     scx[j] = cx[a];
     scy[j] = cy[a];
+    if (cxy2 != nullptr) sxy2[j] = make_int2(cxy2[2 * a], cxy2[2 * a + 1]);
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     swx[j] = w[j];
@@ -522,10 +548,25 @@ __global__ void __launch_bounds__(256)
   const int q = nindices[noff + k];
   const double x = px[q], y = py[q];
   double vx = 0.0, vy = 0.0;
-  for (int j = 0; j < N; ++j) {
-    const double f = tps_phi_tab(scx[j], scy[j], x, y, table, tsize);
-    vx = fma(swx[j], f, vx);
-    vy = fma(swy[j], f, vy);
+  const double X2 = 2.0 * x, Y2 = 2.0 * y;
+  const bool qlat = s_lat && table != nullptr && X2 == rint(X2) && Y2 == rint(Y2) &&
+                    fabs(X2) < 1073741824.0 && fabs(Y2) < 1073741824.0;
+  if (qlat) {  // 4 r^2 in integer arithmetic, table lookup
+    const int QX = (int)X2, QY = (int)Y2;
+    for (int j = 0; j < N; ++j) {
+      const int2 c = sxy2[j];
+      const int64_t dx = (int64_t)(QX - c.x), dy = (int64_t)(QY - c.y);
+      const int64_t kq = dy * dy + dx * dx;
+      const double f = (kq < tsize) ? __ldg(table + kq) : tps_phi(scx[j], scy[j], x, y);
+      vx = fma(swx[j], f, vx);
+      vy = fma(swy[j], f, vy);
+    }
+  } else {
+    for (int j = 0; j < N; ++j) {
+      const double f = tps_phi_tab(scx[j], scy[j], x, y, table, tsize);
+      vx = fma(swx[j], f, vx);
+      vy = fma(swy[j], f, vy);
+    }
   }
   vx = fma(swx[N + 2], x, fma(swx[N + 1], y, __dadd_rn(vx, swx[N])));
   vy = fma(swy[N + 2], x, fma(swy[N + 1], y, __dadd_rn(vy, swy[N])));
@@ -588,15 +629,25 @@ extern "C" int fi_tps_plan_make(const float* xs, const float* ys, const float* d
   return check_launch("fi_tps_plan_make");
 }
 
+extern "C" int fi_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
+                              int32_t* on_lattice, void* stream) {
+  FI_REQUIRE(px && py && xy2 && on_lattice && npts > 0, "fi_tps_lattice: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  k_set_int<<<1, 1, 0, s>>>(on_lattice, 1);
+  k_tps_lattice<<<(npts + 255) / 256, 256, 0, s>>>(px, py, npts, xy2, on_lattice);
+  return check_launch("fi_tps_lattice", 2);
+}
+
 extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px,
                               const double* py, int npts, int mode, int32_t* counts,
                               const int64_t* offsets, int32_t* indices, double* coefs,
-                              void* stream) {
+                              const int32_t* xy2, const int32_t* on_lattice, void* stream) {
   FI_REQUIRE(plan && px && py && nb_subdom > 0 && npts > 0, "fi_tps_members: bad arguments");
   FI_REQUIRE(mode == 0 ? counts != nullptr : (offsets && indices && coefs),
              "fi_tps_members: missing outputs");
   k_tps_members<<<nb_subdom, 512, 0, (cudaStream_t)stream>>>(plan, px, py, npts, mode, counts,
-                                                            offsets, indices, coefs);
+                                                            offsets, indices, coefs, xy2,
+                                                            on_lattice);
   return check_launch("fi_tps_members");
 }
 
@@ -653,6 +704,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                                   const int32_t* nindices, const double* ncoefs, double* partx,
                                   double* party, double* out_x, double* out_y, int32_t* out_rx,
                                   int32_t* out_ry, const double* phi_table, int64_t table_size,
+                                  const int32_t* cxy2, const int32_t* c_on_lattice,
                                   void* stream) {
   FI_REQUIRE(plan && cx && cy && counts && offsets && indices && w_offsets && weights && px &&
                  py && ncounts && noffsets && nindices && ncoefs && partx && party && out_x &&
@@ -660,7 +712,8 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
              "fi_tps_interpolate: null pointer");
   FI_REQUIRE(nb_subdom > 0 && npts > 0, "fi_tps_interpolate: bad sizes");
   cudaStream_t s = (cudaStream_t)stream;
-  const size_t smem = (size_t)(4 * max_members + 6) * sizeof(double);
+  const size_t smem = (size_t)(4 * max_members + 6) * sizeof(double) +
+                      (size_t)max_members * sizeof(int2);
   FI_REQUIRE(smem <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
              max_members);
   static size_t attr = 0;
@@ -674,7 +727,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
     dim3 grid((max_new_members + threads - 1) / threads, nb_subdom);
     k_tps_eval<<<grid, threads, smem, s>>>(counts, offsets, indices, w_offsets, weights, cx, cy,
                                            ncounts, noffsets, nindices, ncoefs, px, py, partx,
-                                           party, phi_table, table_size);
+                                           party, phi_table, table_size, cxy2, c_on_lattice);
     add_launches(1);
   }
   const int threads = 256;

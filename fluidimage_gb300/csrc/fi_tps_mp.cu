@@ -116,7 +116,7 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
   return v;
 }
 
-constexpr int MP_THREADS = 512;
+constexpr int MP_THREADS = 256;
 
 // t = u - A w for two right-hand sides; A (n x n, symmetric, column-major) in FP64.
 __device__ void residual2(const double* A, int n, const double* wx, const double* wy,
@@ -358,8 +358,9 @@ __global__ void __launch_bounds__(MP_THREADS)
     k_tps_solve_mp(const fi_tps_plan* plan_ptr, const double* cx, const double* cy,
                    const float* ux, const float* uy, const int32_t* counts,
                    const int64_t* offsets, const int32_t* indices, const int64_t* mat_off,
-                   double* matrices, double* work64, float* matrices32, const double* phi_table,
-                   int64_t table_size, double threshold, int use_threshold,
+                   double* matrices, float* matrices32, const double* phi_table,
+                   int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
+                   double threshold, int use_threshold,
                    const int64_t* w_off, double* weights, double* smoothed_x,
                    double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
                    double* max_udiff, int max_refine) {
@@ -396,24 +397,37 @@ __global__ void __launch_bounds__(MP_THREADS)
 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
   const double* A64 = matrices + mat_off[sd];  // N x N, K + lam I (kept for residuals)
-  double* W64 = work64 + mat_off[sd];          // N x N, projected copy
-  float* B = matrices32 + mat_off[sd];         // N x N float
+  float* B = matrices32 + mat_off[sd];         // N x N float (lower triangle of B22 used)
+  __shared__ int s_lat;
+  int2* cxy = reinterpret_cast<int2*>(panel);  // lattice coordinates (panel is free here)
 
+  if (threadIdx.x == 0)
+    s_lat = (cxy2 != nullptr && c_on_lattice != nullptr && phi_table != nullptr) ? *c_on_lattice : 0;
   for (int i = threadIdx.x; i < N; i += MP_THREADS) {
     const int a = idx[i];
     xc[i] = cx[a];
     yc[i] = cy[a];
+    if (cxy2 != nullptr) cxy[i] = make_int2(cxy2[2 * a], cxy2[2 * a + 1]);
   }
   __syncthreads();
-  // ---- A = K + lam I in FP64 (column-major), and the copy that gets projected
+  // ---- A = K + lam I in FP64 (column-major); on the lattice, 4 r^2 in integers
   for (int c = wid; c < N; c += nw) {
     const double bx = xc[c], by = yc[c];
+    const int2 cb = cxy[c];
     double* col = matrices + mat_off[sd] + (int64_t)c * N;
-    double* colw = W64 + (int64_t)c * N;
     for (int r = lane; r < N; r += 32) {
-      const double v = (r == c) ? lam : phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
+      double v;
+      if (r == c) {
+        v = lam;
+      } else if (s_lat) {
+        const int2 ca = cxy[r];
+        const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
+        const int64_t kq = dy * dy + dx * dx;
+        v = (kq < table_size) ? __ldg(phi_table + kq) : phi_pair(xc[r], yc[r], bx, by, nullptr, 0);
+      } else {
+        v = phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
+      }
       col[r] = v;
-      colw[r] = v;
     }
   }
   // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
@@ -474,39 +488,115 @@ __global__ void __launch_bounds__(MP_THREADS)
     if (!rank_ok) return;
   }
   __syncthreads();
-  // ---- Q^T A Q in FP64 (three two-sided reflections on the copy W64): the
-  // projection cancels the large affine part of K, so it needs FP64; only the
-  // projected block B22 (norm ~ its condition number times lam) is rounded to FP32.
-  for (int k = 0; k < 3; ++k) {
-    const double* v = V + (int64_t)k * N;
-    const double tau = s_tau[k];
-    for (int c = wid; c < N; c += nw) {  // p = A v (A symmetric: row c = column c)
-      const double* col = W64 + (int64_t)c * N;
-      double acc = 0.0;
-      for (int r = k + lane; r < N; r += 32) acc = fma(col[r], v[r], acc);
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) tx[c] = acc;
+  // ---- B22 = (Q^T A Q)[3:, 3:] with Q = H0 H1 H2 = I - V T V^T (compact WY):
+  // Q^T A Q = A - Z V^T - V Z^T, Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.
+  // FP64 (the projection cancels the large affine part of K); only the lower
+  // triangle of B22 is formed, directly in FP32.
+  {
+    __shared__ double s_T[9], s_M[9], s_G[9];
+    double* Y0 = tx;
+    double* Y1 = ty;
+    double* Y2 = wx;
+    double* Z0 = wy;
+    double* Z1 = zx;
+    double* Z2 = zy;
+    const double* V0 = V;
+    const double* V1 = V + N;
+    const double* V2 = V + 2 * (int64_t)N;
+    for (int c = wid; c < N; c += nw) {  // Y = A V (A symmetric: row c = column c)
+      const double* col = A64 + (int64_t)c * N;
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+      for (int r = lane; r < N; r += 32) {
+        const double a = col[r];
+        a0 = fma(a, V0[r], a0);
+        a1 = fma(a, V1[r], a1);
+        a2 = fma(a, V2[r], a2);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
+      if (lane == 0) {
+        Y0[c] = a0;
+        Y1[c] = a1;
+        Y2[c] = a2;
+      }
     }
     __syncthreads();
-    double vp = 0.0;
-    for (int i = k + threadIdx.x; i < N; i += MP_THREADS) vp += v[i] * tx[i];
-    vp = bsum<MP_THREADS>(vp, sh);
-    const double beta = 0.5 * tau * tau * vp;
-    for (int i = threadIdx.x; i < N; i += MP_THREADS) ty[i] = tau * tx[i] - beta * v[i];
+    // V^T V (upper) and V^T Y (full), block sums
+    const double* Vk[3] = {V0, V1, V2};
+    const double* Yk[3] = {Y0, Y1, Y2};
+    double vtv[3], vty[9];
+    for (int a = 0; a < 3; ++a) {
+      vtv[a] = 0.0;
+      for (int b = 0; b < 3; ++b) vty[3 * a + b] = 0.0;
+    }
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+      vtv[0] += V0[i] * V1[i];
+      vtv[1] += V0[i] * V2[i];
+      vtv[2] += V1[i] * V2[i];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) vty[3 * a + b] += Vk[a][i] * Yk[b][i];
+    }
+    for (int a = 0; a < 3; ++a) vtv[a] = bsum<MP_THREADS>(vtv[a], sh);
+    for (int a = 0; a < 9; ++a) vty[a] = bsum<MP_THREADS>(vty[a], sh);
+    if (threadIdx.x == 0) {
+      double T[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      T[0] = s_tau[0];
+      T[4] = s_tau[1];
+      T[8] = s_tau[2];
+      T[1] = -s_tau[1] * T[0] * vtv[0];                      // T[0][1]
+      T[2] = -s_tau[2] * (T[0] * vtv[1] + T[1] * vtv[2]);    // T[0][2]
+      T[5] = -s_tau[2] * (T[4] * vtv[2]);                    // T[1][2]
+      double G[9];  // (V^T Y) T
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc += vty[3 * a + j] * T[3 * j + b];
+          G[3 * a + b] = acc;
+        }
+      for (int a = 0; a < 3; ++a)  // M = T^T G
+        for (int b = 0; b < 3; ++b) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc += T[3 * j + a] * G[3 * j + b];
+          s_M[3 * a + b] = acc;
+        }
+      for (int a = 0; a < 9; ++a) {
+        s_T[a] = T[a];
+        s_G[a] = G[a];
+      }
+    }
     __syncthreads();
-    for (int c = wid; c < N; c += nw) {  // A -= v w^T + w v^T
-      double* col = W64 + (int64_t)c * N;
-      const double vc = v[c], wc = ty[c];
-      for (int r = lane; r < N; r += 32) col[r] -= fma(v[r], wc, ty[r] * vc);
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) {  // Z = Y T - V M / 2
+      const double y[3] = {Y0[i], Y1[i], Y2[i]};
+      const double v[3] = {V0[i], V1[i], V2[i]};
+      double z[3];
+      for (int k = 0; k < 3; ++k) {
+        double acc = 0.0;
+        for (int j = 0; j < 3; ++j) acc += y[j] * s_T[3 * j + k] - 0.5 * v[j] * s_M[3 * j + k];
+        z[k] = acc;
+      }
+      Z0[i] = z[0];
+      Z1[i] = z[1];
+      Z2[i] = z[2];
+    }
+    __syncthreads();
+    for (int c = 3 + wid; c < N; c += nw) {  // lower triangle of B22, rows r >= c
+      const double* col = A64 + (int64_t)c * N;
+      float* colb = B + (int64_t)c * N;
+      const double vc0 = V0[c], vc1 = V1[c], vc2 = V2[c];
+      const double zc0 = Z0[c], zc1 = Z1[c], zc2 = Z2[c];
+      for (int r = c + lane; r < N; r += 32) {
+        double v = col[r];
+        v -= Z0[r] * vc0 + V0[r] * zc0;
+        v -= Z1[r] * vc1 + V1[r] * zc1;
+        v -= Z2[r] * vc2 + V2[r] * zc2;
+        colb[r] = (float)v;
+      }
     }
     __syncthreads();
   }
-  for (int c = wid; c < N; c += nw) {  // B = float(Q^T A Q), lower triangle of B22 used
-    const double* col = W64 + (int64_t)c * N;
-    float* colb = B + (int64_t)c * N;
-    for (int r = c + lane; r < N; r += 32) colb[r] = (float)col[r];
-  }
-  __syncthreads();
   // ---- FP32 Cholesky of B22 = B[3:, 3:]
   float* B22 = B + 3 + 3 * (int64_t)N;
   if (!chol_factor(B22, m, N, panel, &s_flag)) return;
@@ -681,14 +771,14 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                const double* cx, const double* cy, const float* ux,
                                const float* uy, const int32_t* counts, const int64_t* offsets,
                                const int32_t* indices, const int64_t* mat_offsets,
-                               double* matrices, double* work64, float* matrices32,
-                               const double* phi_table,
-                               int64_t table_size, double threshold, int use_threshold,
+                               double* matrices, float* matrices32, const double* phi_table,
+                               int64_t table_size, const int32_t* cxy2,
+                               const int32_t* c_on_lattice, double threshold, int use_threshold,
                                const int64_t* w_offsets, double* weights, double* smoothed_x,
                                double* smoothed_y, int32_t* iters, int32_t* nfixed,
                                int32_t* status, double* max_udiff, void* stream) {
   FI_REQUIRE(plan && cx && cy && ux && uy && counts && offsets && indices && mat_offsets &&
-                 matrices && work64 && matrices32 && w_offsets && weights && smoothed_x &&
+                 matrices && matrices32 && w_offsets && weights && smoothed_x &&
                  smoothed_y &&
                  iters && nfixed && status && max_udiff,
              "fi_tps_solve_mp: null pointer");
@@ -705,8 +795,8 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
     attr = smem;
   }
   k_tps_solve_mp<<<nb_subdom, MP_THREADS, smem, (cudaStream_t)stream>>>(
-      plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, work64, matrices32,
-      phi_table, table_size, threshold, use_threshold, w_offsets, weights, smoothed_x,
+      plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
+      phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights, smoothed_x,
       smoothed_y, iters, nfixed, status, max_udiff, 60);
   return check_launch("fi_tps_solve_mp");
 }

@@ -223,9 +223,22 @@ def phi_table(device):
     return _PHI_TABLES[key]
 
 
+def lattice_coords(px, py, npts, stream=None):
+    """Integer (2x, 2y) coordinates and the all-on-lattice flag (device tensors)."""
+    torch = _torch()
+    xy2 = torch.empty(2 * npts, dtype=torch.int32, device=px.device)
+    flag = torch.empty(1, dtype=torch.int32, device=px.device)
+    L.check(L.load().fi_tps_lattice(L.ptr(px), L.ptr(py), npts, L.ptr(xy2), L.ptr(flag),
+                                    L.stream_handle(stream)), "fi_tps_lattice")
+    return xy2, flag
+
+
 def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
-            threshold, want_smooth, stream):
-    """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548)."""
+            threshold, want_smooth, stream, p_lattice=None):
+    """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548).
+
+    ``p_lattice``: ``lattice_coords`` of the new positions (computed if None).
+    """
     torch = _torch()
     lib = L.load()
     dev = xs.device
@@ -249,12 +262,15 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     if hdr.status != 0:
         raise ValueError("TPS subdomain layout is degenerate (all vectors on one line)")
     nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
+    cxy2, clat = lattice_coords(cx, cy, nv, stream)
+    pxy2, plat = p_lattice if p_lattice is not None else lattice_coords(px, py, npts, stream)
     counts = torch.empty(nsub, **i32)
     ncounts = torch.empty(nsub, **i32)
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 0, L.ptr(counts),
-                               None, None, None, s), "fi_tps_members")
+                               None, None, None, L.ptr(cxy2), L.ptr(clat), s), "fi_tps_members")
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 0,
-                               L.ptr(ncounts), None, None, None, s), "fi_tps_members")
+                               L.ptr(ncounts), None, None, None, L.ptr(pxy2), L.ptr(plat), s),
+            "fi_tps_members")
     both = torch.cat([counts, ncounts]).cpu().numpy().astype(np.int64)
     ch, nch = both[:nsub], both[nsub:]
     off = np.concatenate([[0], np.cumsum(ch)[:-1]]).astype(np.int64)
@@ -271,9 +287,11 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     nidx = torch.empty(max(ntot, 1), **i32)
     ncoefs = torch.empty(max(ntot, 1), **f64)
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 1, None,
-                               L.ptr(off_d), L.ptr(idx), L.ptr(coefs), s), "fi_tps_members")
+                               L.ptr(off_d), L.ptr(idx), L.ptr(coefs), L.ptr(cxy2), L.ptr(clat),
+                               s), "fi_tps_members")
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 1, None,
-                               L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), s), "fi_tps_members")
+                               L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), L.ptr(pxy2),
+                               L.ptr(plat), s), "fi_tps_members")
     matrices = torch.empty(int(msz.sum()), **f64)
     pivots = torch.empty(tot + 3 * nsub, **i32)
     weights = torch.empty(int(wsz.sum()), **f64)
@@ -288,13 +306,13 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     table = phi_table(dev)
     status = torch.ones(nsub, **i32)
     if int(ch.max()) <= MP_MAX_MEMBERS:
-        work64 = torch.empty(int(msz.sum()), dtype=torch.float64, device=dev)
         matrices32 = torch.empty(int(msz.sum()), dtype=torch.float32, device=dev)
         with _timed("fi_tps_solve_mp"):
             L.check(lib.fi_tps_solve_mp(
                 L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
                 L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d), L.ptr(matrices),
-                L.ptr(work64), L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, thr, int(use_thr),
+                L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
+                thr, int(use_thr),
                 L.ptr(woff_d), L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
                 L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), s), "fi_tps_solve_mp")
     # FP64 LU for the subdomains the mixed-precision solver flagged (or all of them)
@@ -328,7 +346,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                    L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),
                                    L.ptr(partx), L.ptr(party), L.ptr(out.out_x),
                                    L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry),
-                                   L.ptr(table), PHI_TABLE_SIZE, s),
+                                   L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat), s),
             "fi_tps_interpolate")
     return out
 
@@ -412,6 +430,11 @@ class PIVPipeline:
             lay.dev["py"] = torch.as_tensor(lay.gy.astype(np.float64), device=self.device)
             lay.dev["mask"] = (None if mask is None else
                                torch.as_tensor(mask.astype(np.uint8), device=self.device))
+            xy2 = np.empty(2 * lay.nvec, dtype=np.int32)
+            xy2[0::2] = 2 * lay.gx
+            xy2[1::2] = 2 * lay.gy
+            lay.dev["lattice"] = (torch.as_tensor(xy2, device=self.device),
+                                  torch.ones(1, dtype=torch.int32, device=self.device))
             self.layouts.append(lay)
         self.im_min = torch.empty(2, dtype=torch.float32, device=self.device)
 
@@ -438,7 +461,7 @@ class PIVPipeline:
                 prev.tps_next = run_tps(
                     prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
                     lay.dev["px"], lay.dev["py"], lay.nvec, mp.subdom_size, mp.smoothing_coef,
-                    mp.threshold_tps, False, stream)
+                    mp.threshold_tps, False, stream, p_lattice=lay.dev["lattice"])
                 dxin, dyin = prev.tps_next.rx, prev.tps_next.ry
             cur = self._run_pass(lay, im0, im1, dxin, dyin, dt, s)
             self._run_fix(cur, fx, s)
@@ -450,7 +473,8 @@ class PIVPipeline:
             prev.tps_final = run_tps(
                 prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
                 prev.layout.dev["px"], prev.layout.dev["py"], prev.layout.nvec,
-                mp.subdom_size, mp.smoothing_coef, mp.threshold_tps, True, stream)
+                mp.subdom_size, mp.smoothing_coef, mp.threshold_tps, True, stream,
+                p_lattice=prev.layout.dev["lattice"])
         except InterpError as e:
             print("Warning: InterpError at the end of the last piv pass:", e)
         return outs

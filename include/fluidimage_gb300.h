@@ -224,14 +224,26 @@ int fi_tps_plan_make(const float* xs, const float* ys, const float* dx, const fl
                      float* ux, float* uy, int32_t* selection, void* stream);
 
 /*
+ * Half-integer lattice coordinates of npts points: xy2[2i] = 2 px[i],
+ * xy2[2i+1] = 2 py[i] as int32, and *on_lattice (device int) = 1 when every point
+ * has integral 2x, 2y with |2x|, |2y| < 2^30 (PIV vector positions always do:
+ * grid points and midpoints of integer window shifts), else 0.
+ */
+int fi_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
+                   int32_t* on_lattice, void* stream);
+
+/*
  * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
  * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
  * counts), the point indices and their norm coefficients
- * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).
+ * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 and
+ * on_lattice from fi_tps_lattice (both nullable) the limit tests are exact integer
+ * comparisons on the lattice.
  */
 int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
                    int npts, int mode, int32_t* counts, const int64_t* offsets,
-                   int32_t* indices, double* coefs, void* stream);
+                   int32_t* indices, double* coefs, const int32_t* xy2,
+                   const int32_t* on_lattice, void* stream);
 
 /*
  * Per subdomain: build [[K + smoothing I, P], [P^T, 0]] (compute_tps_weights,
@@ -266,17 +278,20 @@ int fi_tps_phi_table(double* table, int64_t count, void* stream);
  * in FP32 (blocked Cholesky) and refined with FP64 residuals to ~1e-11 relative
  * (K from the phi table); the outlier iterations of
  * compute_tps_weights_iter (thin_plate_spline_subdom.py:236-280) warm-start from
- * the previous solution.  matrices and work64: (n_i+3)^2 doubles each at
- * mat_offsets[i] (K + lam I, and its projected copy); matrices32: (n_i+3)^2 floats
- * at mat_offsets[i] (the FP32 Cholesky factor).  status[i] = 0 when
+ * the previous solution.  matrices: (n_i+3)^2 doubles at mat_offsets[i]
+ * (K + lam I); matrices32: (n_i+3)^2 floats at mat_offsets[i] (the FP32 Cholesky
+ * factor of the projected system, formed with the compact WY form of Q).
+ * cxy2/c_on_lattice (nullable, fi_tps_lattice of the centres) give integer table
+ * indices.  status[i] = 0 when
  * solved, 1 when the subdomain must go through fi_tps_solve (pass status as its
  * only_failed argument): rank-deficient P, Cholesky breakdown or no convergence.
  */
 int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
                     const double* cy, const float* ux, const float* uy, const int32_t* counts,
                     const int64_t* offsets, const int32_t* indices, const int64_t* mat_offsets,
-                    double* matrices, double* work64, float* matrices32, const double* phi_table,
-                    int64_t table_size, double threshold, int use_threshold,
+                    double* matrices, float* matrices32, const double* phi_table,
+                    int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
+                    double threshold, int use_threshold,
                     const int64_t* w_offsets, double* weights, double* smoothed_x,
                     double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
                     double* max_udiff, void* stream);
@@ -296,7 +311,8 @@ int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, const double*
  * out_rx/out_ry = round-half-even to int32 (the window shifts of the next pass,
  * works/piv/singlepass.py:752-753).  ncounts/noffsets/nindices/ncoefs: membership
  * of the new positions (fi_tps_members); partx/party: scratch of the same size
- * as nindices.
+ * as nindices.  cxy2/c_on_lattice (nullable, from fi_tps_lattice on the centres)
+ * enable integer 4 r^2 table indices.
  */
 int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        int max_new_members, const double* cx, const double* cy,
@@ -306,7 +322,8 @@ int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        const int64_t* noffsets, const int32_t* nindices, const double* ncoefs,
                        double* partx, double* party, double* out_x, double* out_y,
                        int32_t* out_rx, int32_t* out_ry, const double* phi_table,
-                       int64_t table_size, void* stream);
+                       int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
+                       void* stream);
 
 #ifdef __cplusplus
 }
