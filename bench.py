@@ -305,6 +305,7 @@ def run_gpu(args):
                                   if t is not None)),
         "tps_lu_fallbacks": int(sum(int(t.mp_status.sum().item()) for pd in outs
                                     for t in (pd.tps_next, pd.tps_final) if t is not None)),
+        "tps_outer_iterations": _iter_stats(outs),
         "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kern.items()},
         "roofline": roof,
         "clocks": clk,
@@ -314,6 +315,18 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _iter_stats(outs):
+    """Outlier-replacement solves per subdomain and component, per TPS call."""
+    stats = []
+    for pd in outs:
+        for t in (pd.tps_next, pd.tps_final):
+            if t is not None:
+                it = t.iters.cpu().numpy()
+                stats.append({"subdomains": t.nb_subdom, "mean": round(float(it.mean()), 2),
+                              "max": int(it.max())})
+    return stats
 
 
 def _result_bytes(res):

@@ -12,7 +12,8 @@
 // to FP32 and factorised there (blocked Cholesky, ~N^3/6 flops), and the solution
 // is refined with FP64 residuals t = u - (K + lam I) w (2 N^2 FP64 flops per step
 // for both components, a few steps).  Refinement stops when the correction is below
-// 1e-13 of the solution, or stagnates below 1e-9; a subdomain that does not
+// 1e-10 of the solution (the error then is ~1e-15 relative after the FP32 solve's
+// ~1e-5 contraction), or stagnates below 1e-9; a subdomain that does not
 // converge (or whose P has rank < 3, or whose Cholesky meets a non-positive pivot)
 // is flagged and re-solved by the FP64 LU kernel (k_tps_solve).
 //
@@ -124,12 +125,26 @@ __device__ void residual2(const double* A, int n, const double* wx, const double
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
   for (int c = wid; c < n; c += nw) {
     const double* col = A + (int64_t)c * n;  // row c = column c
-    double ax = 0.0, ay = 0.0;
-    for (int r = lane; r < n; r += 32) {
+    double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+    int r = lane;
+    for (; r + 96 < n; r += 128) {  // four independent loads in flight per lane
+      const double a0 = col[r], a1 = col[r + 32], a2 = col[r + 64], a3 = col[r + 96];
+      ax = fma(a0, wx[r], ax);
+      ay = fma(a0, wy[r], ay);
+      bx = fma(a1, wx[r + 32], bx);
+      by = fma(a1, wy[r + 32], by);
+      ax = fma(a2, wx[r + 64], ax);
+      ay = fma(a2, wy[r + 64], ay);
+      bx = fma(a3, wx[r + 96], bx);
+      by = fma(a3, wy[r + 96], by);
+    }
+    for (; r < n; r += 32) {
       const double a = col[r];
       ax = fma(a, wx[r], ax);
       ay = fma(a, wy[r], ay);
     }
+    ax += bx;
+    ay += by;
     for (int o = 16; o > 0; o >>= 1) {
       ax += __shfl_xor_sync(0xffffffffu, ax, o);
       ay += __shfl_xor_sync(0xffffffffu, ay, o);
@@ -260,101 +275,117 @@ __device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry,
   }
 }
 
-// Blocked right-looking Cholesky (lower) of the m x m matrix B (column-major, ld).
-// Returns false on a non-positive pivot.
-__device__ bool chol_factor(float* B, int m, int ld, float* panel, int* s_flag) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Tiles of 32 x 32 held in registers, one row per lane (a[c] = element (r, c) of
+// the tile, r = lane); rows/columns beyond m read as the identity.
+__device__ __forceinline__ void tile_load(const float* B, int m, int ld, int ti, int tj,
+                                          float (&a)[32], int lane) {
+  const int r = 32 * ti + lane;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const int col = 32 * tj + c;
+    a[c] = (r < m && col < m) ? B[(int64_t)col * ld + r] : ((r == col) ? 1.f : 0.f);
+  }
+}
+__device__ __forceinline__ void tile_store(float* B, int m, int ld, int ti, int tj,
+                                           const float (&a)[32], int lane, bool lower_only) {
+  const int r = 32 * ti + lane;
+  if (r >= m) return;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const int col = 32 * tj + c;
+    if (col < m && (!lower_only || c <= lane)) B[(int64_t)col * ld + r] = a[c];
+  }
+}
+
+// Right-looking tiled Cholesky (lower) of the m x m matrix B (column-major, ld), in
+// place.  Per tile column k: one warp factorises the diagonal tile in registers
+// (shuffles), warps solve the tiles below (one row per lane, L_kk broadcast from
+// shared memory), then update the trailing tile pairs (register accumulators,
+// the second factor transposed in shared memory and read as broadcasts).
+// scratch: (1 + warps) * 32 * 33 floats.  Returns false on a non-positive pivot.
+__device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+  const unsigned full = 0xffffffffu;
+  const int T = (m + 31) / 32;
+  float* Lkk = scratch;                       // 32 x 33
+  float* Lt = scratch + 32 * 33 * (1 + wid);  // per warp, 32 x 33 (transposed tile)
   if (threadIdx.x == 0) *s_flag = 0;
-  for (int J = 0; J < m; J += NB) {
-    const int jb = min(NB, m - J);
-    const int rows = m - J;
-    for (int e = threadIdx.x; e < rows * jb; e += MP_THREADS) {
-      const int r = e % rows, c = e / rows;
-      panel[r * PLD + c] = B[(int64_t)(J + c) * ld + J + r];
-    }
-    __syncthreads();
-    // diagonal block by warp 0 (lane = row)
-    if (wid == 0) {
-      for (int k = 0; k < jb; ++k) {
-        float dkk = panel[k * PLD + k];
-        if (!(dkk > 0.f)) {
-          if (lane == 0) *s_flag = 1;
-          dkk = 1.f;
+  __syncthreads();
+  for (int k = 0; k < T; ++k) {
+    if (wid == 0) {  // POTRF of tile (k, k)
+      float a[32];
+      tile_load(B, m, ld, k, k, a, lane);
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        float djj = __shfl_sync(full, a[j], j);
+        if (!(djj > 0.f)) {
+          bad = true;
+          djj = 1.f;
         }
-        const float d = sqrtf(dkk);
-        if (lane == k) panel[k * PLD + k] = d;
-        __syncwarp();
-        if (lane > k && lane < jb) panel[lane * PLD + k] /= d;
-        __syncwarp();
-        if (lane > k && lane < jb) {
-          const float lk = panel[lane * PLD + k];
-          for (int c = k + 1; c <= lane; ++c) panel[lane * PLD + c] -= lk * panel[c * PLD + k];
-        }
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    // rows below the diagonal block: L21 = A21 L11^-T (one row per thread)
-    for (int r = jb + threadIdx.x; r < rows; r += MP_THREADS) {
-      float* pr = panel + r * PLD;
-      for (int k = 0; k < jb; ++k) {
-        float v = pr[k];
-        for (int c = 0; c < k; ++c) v -= pr[c] * panel[k * PLD + c];
-        pr[k] = v / panel[k * PLD + k];
-      }
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < rows * jb; e += MP_THREADS) {
-      const int r = e % rows, c = e / rows;
-      if (r >= c) B[(int64_t)(J + c) * ld + J + r] = panel[r * PLD + c];
-    }
-    // trailing update of the lower triangle: B22 -= L21 L21^T, 4x4 tiles
-    const int t0 = J + jb, tn = m - t0;
-    if (tn > 0) {
-      const int nt = (tn + 3) / 4;
-      const int ntiles = nt * (nt + 1) / 2;
-      for (int tile = threadIdx.x; tile < ntiles; tile += MP_THREADS) {
-        // tile -> (ti, tj) with tj <= ti
-        int ti = (int)((sqrtf(8.f * tile + 1.f) - 1.f) * 0.5f);
-        while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
-        while (ti * (ti + 1) / 2 > tile) --ti;
-        const int tj = tile - ti * (ti + 1) / 2;
-        float acc[4][4] = {};
-        const int rb = jb + 4 * ti, cb = jb + 4 * tj;
-        for (int k = 0; k < jb; ++k) {
-          float a[4], b[4];
+        const float sq = sqrtf(djj);
+        const float lrj = (lane > j) ? a[j] / sq : ((lane == j) ? sq : 0.f);
+        if (lane >= j) a[j] = lrj;
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            a[q] = (rb + q < rows) ? panel[(rb + q) * PLD + k] : 0.f;
-            b[q] = (cb + q < rows) ? panel[(cb + q) * PLD + k] : 0.f;
-          }
-#pragma unroll
-          for (int p = 0; p < 4; ++p)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a[p], b[q], acc[p][q]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int c = t0 + 4 * tj + q;
-          if (c >= m) continue;
-          float* col = B + (int64_t)c * ld;
-#pragma unroll
-          for (int p = 0; p < 4; ++p) {
-            const int r = t0 + 4 * ti + p;
-            if (r < m && r >= c) col[r] -= acc[p][q];
-          }
+        for (int c = j + 1; c < 32; ++c) {
+          const float lcj = __shfl_sync(full, lrj, c);
+          if (lane >= c) a[c] = fmaf(-lrj, lcj, a[c]);
         }
       }
+      if (bad && lane == 0) *s_flag = 1;
+      tile_store(B, m, ld, k, k, a, lane, true);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) Lkk[lane * 33 + c] = (c <= lane) ? a[c] : 0.f;
     }
     __syncthreads();
-    (void)lane;
+    // TRSM: tiles (i, k), i > k: X L_kk^T = A_ik, row by row in each lane
+    for (int i = k + 1 + wid; i < T; i += nw) {
+      float b[32];
+      tile_load(B, m, ld, i, k, b, lane);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        float v = b[j];
+#pragma unroll
+        for (int c = 0; c < j; ++c) v = fmaf(-b[c], Lkk[j * 33 + c], v);
+        b[j] = v / Lkk[j * 33 + j];
+      }
+      tile_store(B, m, ld, i, k, b, lane, false);
+    }
+    __syncthreads();
+    // trailing update: tiles (i, j), k < j <= i
+    const int n = T - k - 1;
+    const int npairs = n * (n + 1) / 2;
+    for (int pidx = wid; pidx < npairs; pidx += nw) {
+      int ii = (int)((sqrtf(8.f * pidx + 1.f) - 1.f) * 0.5f);
+      while ((ii + 1) * (ii + 2) / 2 <= pidx) ++ii;
+      while (ii * (ii + 1) / 2 > pidx) --ii;
+      const int jj = pidx - ii * (ii + 1) / 2;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      float l[32];
+      tile_load(B, m, ld, j, k, l, lane);  // L_jk rows -> transposed in shared memory
+#pragma unroll
+      for (int t = 0; t < 32; ++t) Lt[t * 33 + lane] = l[t];
+      __syncwarp();
+      if (i != j) tile_load(B, m, ld, i, k, l, lane);  // L_ik rows
+      float acc[32];
+      tile_load(B, m, ld, i, j, acc, lane);
+#pragma unroll
+      for (int t = 0; t < 32; ++t) {
+        const float lr = l[t];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] = fmaf(-lr, Lt[t * 33 + c], acc[c]);
+      }
+      tile_store(B, m, ld, i, j, acc, lane, i == j);
+      __syncwarp();
+    }
+    __syncthreads();
   }
   return *s_flag == 0;
 }
 
 // One block per subdomain.  Status per subdomain: 0 solved here, 1 needs the FP64
 // LU fallback (rank-deficient P, Cholesky breakdown or no convergence).
-__global__ void __launch_bounds__(MP_THREADS)
+__global__ void __launch_bounds__(MP_THREADS, 2)
     k_tps_solve_mp(const fi_tps_plan* plan_ptr, const double* cx, const double* cy,
                    const float* ux, const float* uy, const int32_t* counts,
                    const int64_t* offsets, const int32_t* indices, const int64_t* mat_off,
@@ -393,7 +424,7 @@ __global__ void __launch_bounds__(MP_THREADS)
   float* vy = vx + N;
   float* rx = vy + N;                             // m correction (float)
   float* ry = rx + N;
-  float* panel = ry + N;                          // N * PLD
+  float* panel = ry + N;  // Cholesky / solve scratch: (1 + warps) * 32 * 33 floats
 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
   const double* A64 = matrices + mat_off[sd];  // N x N, K + lam I (kept for residuals)
@@ -410,26 +441,6 @@ __global__ void __launch_bounds__(MP_THREADS)
     if (cxy2 != nullptr) cxy[i] = make_int2(cxy2[2 * a], cxy2[2 * a + 1]);
   }
   __syncthreads();
-  // ---- A = K + lam I in FP64 (column-major); on the lattice, 4 r^2 in integers
-  for (int c = wid; c < N; c += nw) {
-    const double bx = xc[c], by = yc[c];
-    const int2 cb = cxy[c];
-    double* col = matrices + mat_off[sd] + (int64_t)c * N;
-    for (int r = lane; r < N; r += 32) {
-      double v;
-      if (r == c) {
-        v = lam;
-      } else if (s_lat) {
-        const int2 ca = cxy[r];
-        const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
-        const int64_t kq = dy * dy + dx * dx;
-        v = (kq < table_size) ? __ldg(phi_table + kq) : phi_pair(xc[r], yc[r], bx, by, nullptr, 0);
-      } else {
-        v = phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
-      }
-      col[r] = v;
-    }
-  }
   // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
   {
     double* P0 = tx;  // scratch columns
@@ -488,29 +499,37 @@ __global__ void __launch_bounds__(MP_THREADS)
     if (!rank_ok) return;
   }
   __syncthreads();
-  // ---- B22 = (Q^T A Q)[3:, 3:] with Q = H0 H1 H2 = I - V T V^T (compact WY):
-  // Q^T A Q = A - Z V^T - V Z^T, Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.
-  // FP64 (the projection cancels the large affine part of K); only the lower
-  // triangle of B22 is formed, directly in FP32.
+  // ---- A = K + lam I in FP64 (column-major; on the lattice 4 r^2 in integers),
+  // fused with Y = A V for the projection (A symmetric: row c = column c)
+  double* Y0 = tx;
+  double* Y1 = ty;
+  double* Y2 = wx;
   {
-    __shared__ double s_T[9], s_M[9], s_G[9];
-    double* Y0 = tx;
-    double* Y1 = ty;
-    double* Y2 = wx;
-    double* Z0 = wy;
-    double* Z1 = zx;
-    double* Z2 = zy;
     const double* V0 = V;
     const double* V1 = V + N;
     const double* V2 = V + 2 * (int64_t)N;
-    for (int c = wid; c < N; c += nw) {  // Y = A V (A symmetric: row c = column c)
-      const double* col = A64 + (int64_t)c * N;
+    for (int c = wid; c < N; c += nw) {
+      const double bx = xc[c], by = yc[c];
+      const int2 cb = cxy[c];
+      double* col = matrices + mat_off[sd] + (int64_t)c * N;
       double a0 = 0.0, a1 = 0.0, a2 = 0.0;
       for (int r = lane; r < N; r += 32) {
-        const double a = col[r];
-        a0 = fma(a, V0[r], a0);
-        a1 = fma(a, V1[r], a1);
-        a2 = fma(a, V2[r], a2);
+        double v;
+        if (r == c) {
+          v = lam;
+        } else if (s_lat) {
+          const int2 ca = cxy[r];
+          const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
+          const int64_t kq = dy * dy + dx * dx;
+          v = (kq < table_size) ? __ldg(phi_table + kq)
+                                : phi_pair(xc[r], yc[r], bx, by, nullptr, 0);
+        } else {
+          v = phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
+        }
+        col[r] = v;
+        a0 = fma(v, V0[r], a0);
+        a1 = fma(v, V1[r], a1);
+        a2 = fma(v, V2[r], a2);
       }
       for (int o = 16; o > 0; o >>= 1) {
         a0 += __shfl_xor_sync(0xffffffffu, a0, o);
@@ -523,7 +542,20 @@ __global__ void __launch_bounds__(MP_THREADS)
         Y2[c] = a2;
       }
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  // ---- B22 = (Q^T A Q)[3:, 3:] with Q = H0 H1 H2 = I - V T V^T (compact WY):
+  // Q^T A Q = A - Z V^T - V Z^T, Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.
+  // FP64 (the projection cancels the large affine part of K); only the lower
+  // triangle of B22 is formed, directly in FP32.
+  {
+    __shared__ double s_T[9], s_M[9], s_G[9];
+    double* Z0 = wy;
+    double* Z1 = zx;
+    double* Z2 = zy;
+    const double* V0 = V;
+    const double* V1 = V + N;
+    const double* V2 = V + 2 * (int64_t)N;
     // V^T V (upper) and V^T Y (full), block sums
     const double* Vk[3] = {V0, V1, V2};
     const double* Yk[3] = {Y0, Y1, Y2};
@@ -611,6 +643,7 @@ __global__ void __launch_bounds__(MP_THREADS)
   int count[2] = {1, 1}, fixed[2] = {0, 0};
   bool done[2] = {false, false};
   bool converged_all = true;
+  bool first_solve = true;
   while (true) {
     // refine z for the current values
     bool conv = false;
@@ -622,8 +655,16 @@ __global__ void __launch_bounds__(MP_THREADS)
         wy[i] = (i < 3) ? 0.0 : zy[i - 3];
       }
       __syncthreads();
-      apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
-      residual2(A64, N, wx, wy, vx, vy, tx, ty);
+      if (it == 0 && first_solve) {  // z = 0: t = u
+        for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+          tx[i] = (double)vx[i];
+          ty[i] = (double)vy[i];
+        }
+        __syncthreads();
+      } else {
+        apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
+        residual2(A64, N, wx, wy, vx, vy, tx, ty);
+      }
       // rho = (Q^T t)[3:]
       apply_reflectors2<false>(V, s_tau, N, tx, ty, sh);
       for (int i = threadIdx.x; i < m; i += MP_THREADS) {
@@ -642,7 +683,7 @@ __global__ void __launch_bounds__(MP_THREADS)
       }
       dmax = bmax<MP_THREADS>(dmax, sh);
       zmax = bmax<MP_THREADS>(zmax, sh);
-      if (dmax <= 1e-13 * zmax || dmax == 0.0) {
+      if (dmax <= 1e-10 * zmax || dmax == 0.0) {  // next step would be at the FP64 floor
         conv = true;
         break;
       }
@@ -652,6 +693,7 @@ __global__ void __launch_bounds__(MP_THREADS)
       }
       prev = dmax;
     }
+    first_solve = false;
     if (!conv) {
       converged_all = false;
       break;
@@ -784,8 +826,10 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
              "fi_tps_solve_mp: null pointer");
   FI_REQUIRE(nb_subdom > 0, "fi_tps_solve_mp: no subdomain");
   const int N = max_members > 4 ? max_members : 4;
+  const size_t scratch = (size_t)(1 + MP_THREADS / 32) * 32 * 33 * sizeof(float);
+  const size_t lat = (size_t)N * sizeof(int2);
   const size_t smem = (size_t)N * 11 * sizeof(double) + (size_t)N * 4 * sizeof(float) +
-                      (size_t)N * PLD * sizeof(float) + 64;
+                      (scratch > lat ? scratch : lat) + 64;
   FI_REQUIRE(smem <= 220 * 1024, "fi_tps_solve_mp: subdomain of %d vectors too large",
              max_members);
   static size_t attr = 0;
