@@ -156,8 +156,6 @@ __device__ void residual2(const double* A, int n, const double* wx, const double
   }
   __syncthreads();
 }
-constexpr int NB = 32;     // Cholesky panel width
-constexpr int PLD = NB + 1;
 
 // Apply H_k = I - tau_k v_k v_k^T (k in order) to the two vectors x, y (length n).
 template <bool REVERSE>
@@ -182,93 +180,114 @@ __device__ void apply_reflectors2(const double* V, const double* tau, int n, dou
 }
 
 // Solve (L L^T) x = r in place for two right-hand sides (float), L lower m x m,
-// column-major with leading dimension ld; blocks of NB columns.
-__device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry, float* diag) {
+// column-major with leading dimension ld, by tiles of 32: the diagonal tile in one
+// warp (shuffles), the off-diagonal tiles by all warps (rows in registers for the
+// forward sweep, transposed shared-memory tiles for the backward sweep).
+// scratch: (1 + warps) * 32 * 33 floats.
+__device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry,
+                            float* scratch) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
-  // forward: L y = r
-  for (int J = 0; J < m; J += NB) {
-    const int jb = min(NB, m - J);
-    for (int e = threadIdx.x; e < jb * jb; e += MP_THREADS) {
-      const int r = e % jb, c = e / jb;
-      diag[r * PLD + c] = (c <= r) ? L[(int64_t)(J + c) * ld + J + r] : 0.f;
-    }
-    __syncthreads();
+  const unsigned full = 0xffffffffu;
+  const int T = (m + 31) / 32;
+  float* part = scratch;                       // [warp][64] partial sums (backward)
+  float* Lt = scratch + 32 * 33 * (1 + wid);   // per warp transposed tile
+  // ---- forward: L y = r
+  for (int k = 0; k < T; ++k) {
+    const int r0 = 32 * k;
     if (wid == 0) {
-      float vx = lane < jb ? rx[J + lane] : 0.f, vy = lane < jb ? ry[J + lane] : 0.f;
-      for (int k = 0; k < jb; ++k) {
-        const float d = diag[k * PLD + k];
-        const float xk = __shfl_sync(0xffffffffu, vx, k) / d;
-        const float yk = __shfl_sync(0xffffffffu, vy, k) / d;
-        if (lane == k) {
-          vx = xk;
-          vy = yk;
-        } else if (lane > k && lane < jb) {
-          const float l = diag[lane * PLD + k];
-          vx -= l * xk;
-          vy -= l * yk;
+      float Lrow[32];  // row (r0 + lane) of the diagonal tile
+      const int r = r0 + lane;
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        Lrow[c] = (r < m && r0 + c < m) ? L[(int64_t)(r0 + c) * ld + r] : ((c == lane) ? 1.f : 0.f);
+      float vx = (r < m) ? rx[r] : 0.f, vy = (r < m) ? ry[r] : 0.f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const float d = __shfl_sync(full, Lrow[j], j);
+        const float xj = __shfl_sync(full, vx, j) / d;
+        const float yj = __shfl_sync(full, vy, j) / d;
+        if (lane == j) {
+          vx = xj;
+          vy = yj;
+        } else if (lane > j) {
+          vx = fmaf(-Lrow[j], xj, vx);
+          vy = fmaf(-Lrow[j], yj, vy);
         }
       }
-      if (lane < jb) {
-        rx[J + lane] = vx;
-        ry[J + lane] = vy;
+      if (r < m) {
+        rx[r] = vx;
+        ry[r] = vy;
       }
     }
     __syncthreads();
-    for (int r = J + jb + threadIdx.x; r < m; r += MP_THREADS) {
-      float ax = 0.f, ay = 0.f;
-      for (int c = 0; c < jb; ++c) {
-        const float l = L[(int64_t)(J + c) * ld + r];
-        ax += l * rx[J + c];
-        ay += l * ry[J + c];
+    for (int i = k + 1 + wid; i < T; i += nw) {  // r_i -= L_ik y_k
+      const int r = 32 * i + lane;
+      if (r < m) {
+        float sx = 0.f, sy = 0.f;
+#pragma unroll 8
+        for (int c = 0; c < 32; ++c) {
+          if (r0 + c < m) {
+            const float l = L[(int64_t)(r0 + c) * ld + r];
+            sx = fmaf(l, rx[r0 + c], sx);
+            sy = fmaf(l, ry[r0 + c], sy);
+          }
+        }
+        rx[r] -= sx;
+        ry[r] -= sy;
       }
-      rx[r] -= ax;
-      ry[r] -= ay;
     }
     __syncthreads();
   }
-  // backward: L^T x = y
-  for (int J = ((m - 1) / NB) * NB; J >= 0; J -= NB) {
-    const int jb = min(NB, m - J);
-    // y[J:J+jb] -= L[J+jb:m, J:J+jb]^T x[J+jb:m]
-    for (int c = wid; c < jb; c += nw) {
-      const float* col = L + (int64_t)(J + c) * ld;
-      float ax = 0.f, ay = 0.f;
-      for (int r = J + jb + lane; r < m; r += 32) {
-        ax += col[r] * rx[r];
-        ay += col[r] * ry[r];
+  // ---- backward: L^T x = y
+  for (int k = T - 1; k >= 0; --k) {
+    const int c0 = 32 * k;
+    float px = 0.f, py = 0.f;  // lane t: partial of sum_{i>k} sum_r L_ik[r][t] x_i[r]
+    for (int i = k + 1 + wid; i < T; i += nw) {
+      const int r = 32 * i + lane;
+#pragma unroll
+      for (int t = 0; t < 32; ++t)
+        Lt[t * 33 + lane] = (r < m && c0 + t < m) ? L[(int64_t)(c0 + t) * ld + r] : 0.f;
+      __syncwarp();
+#pragma unroll 8
+      for (int rr = 0; rr < 32; ++rr) {
+        const int ri = 32 * i + rr;
+        const float xv = (ri < m) ? rx[ri] : 0.f, yv = (ri < m) ? ry[ri] : 0.f;
+        const float l = Lt[lane * 33 + rr];
+        px = fmaf(l, xv, px);
+        py = fmaf(l, yv, py);
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-      }
-      if (lane == 0) {
-        rx[J + c] -= ax;
-        ry[J + c] -= ay;
-      }
+      __syncwarp();
     }
-    for (int e = threadIdx.x; e < jb * jb; e += MP_THREADS) {
-      const int r = e % jb, c = e / jb;
-      diag[r * PLD + c] = (c <= r) ? L[(int64_t)(J + c) * ld + J + r] : 0.f;
-    }
+    part[wid * 64 + lane] = px;
+    part[wid * 64 + 32 + lane] = py;
     __syncthreads();
     if (wid == 0) {
-      float vx = lane < jb ? rx[J + lane] : 0.f, vy = lane < jb ? ry[J + lane] : 0.f;
-      for (int k = jb - 1; k >= 0; --k) {
-        const float d = diag[k * PLD + k];
-        const float xk = __shfl_sync(0xffffffffu, vx, k) / d;
-        const float yk = __shfl_sync(0xffffffffu, vy, k) / d;
-        if (lane == k) {
-          vx = xk;
-          vy = yk;
-        } else if (lane < k) {
-          const float l = diag[k * PLD + lane];
-          vx -= l * xk;
-          vy -= l * yk;
+      const int t = c0 + lane;
+      float vx = (t < m) ? rx[t] : 0.f, vy = (t < m) ? ry[t] : 0.f;
+      for (int w = 0; w < nw; ++w) {
+        vx -= part[w * 64 + lane];
+        vy -= part[w * 64 + 32 + lane];
+      }
+      float Lcol[32];  // column (c0 + lane) of the diagonal tile: Lcol[j] = L[c0 + j][c0 + lane]
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        Lcol[j] = (t < m && c0 + j < m) ? L[(int64_t)t * ld + c0 + j] : ((j == lane) ? 1.f : 0.f);
+#pragma unroll
+      for (int j = 31; j >= 0; --j) {
+        const float d = __shfl_sync(full, Lcol[j], j);
+        const float xj = __shfl_sync(full, vx, j) / d;
+        const float yj = __shfl_sync(full, vy, j) / d;
+        if (lane == j) {
+          vx = xj;
+          vy = yj;
+        } else if (lane < j) {
+          vx = fmaf(-Lcol[j], xj, vx);
+          vy = fmaf(-Lcol[j], yj, vy);
         }
       }
-      if (lane < jb) {
-        rx[J + lane] = vx;
-        ry[J + lane] = vy;
+      if (t < m) {
+        rx[t] = vx;
+        ry[t] = vy;
       }
     }
     __syncthreads();
@@ -549,7 +568,7 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
   // FP64 (the projection cancels the large affine part of K); only the lower
   // triangle of B22 is formed, directly in FP32.
   {
-    __shared__ double s_T[9], s_M[9], s_G[9];
+    __shared__ double s_T[9], s_M[9];
     double* Z0 = wy;
     double* Z1 = zx;
     double* Z2 = zy;
@@ -594,10 +613,7 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
           for (int j = 0; j < 3; ++j) acc += T[3 * j + a] * G[3 * j + b];
           s_M[3 * a + b] = acc;
         }
-      for (int a = 0; a < 9; ++a) {
-        s_T[a] = T[a];
-        s_G[a] = G[a];
-      }
+      for (int a = 0; a < 9; ++a) s_T[a] = T[a];
     }
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += MP_THREADS) {  // Z = Y T - V M / 2
@@ -683,13 +699,22 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
       }
       dmax = bmax<MP_THREADS>(dmax, sh);
       zmax = bmax<MP_THREADS>(zmax, sh);
-      if (dmax <= 1e-10 * zmax || dmax == 0.0) {  // next step would be at the FP64 floor
+      if (dmax == 0.0) {
         conv = true;
         break;
       }
-      if (it >= 2 && dmax > 0.5 * prev) {  // at the FP64 residual floor
-        conv = dmax <= 1e-9 * zmax;
-        break;
+      if (it >= 1) {
+        // contraction of the FP32-preconditioned refinement, estimated from the last
+        // two corrections; the remaining error is about contraction * dmax
+        const double rho = dmax / prev;
+        if (rho < 0.1 && rho * dmax <= 1e-13 * zmax) {
+          conv = true;
+          break;
+        }
+        if (it >= 2 && rho > 0.5) {  // at the FP64 residual floor
+          conv = dmax <= 1e-9 * zmax;
+          break;
+        }
       }
       prev = dmax;
     }
