@@ -318,14 +318,20 @@ def run_gpu(args):
 
 
 def _iter_stats(outs):
-    """Outlier-replacement solves per subdomain and component, per TPS call."""
+    """Outlier-replacement solves per subdomain and component (and refinement sweeps
+    of the mixed-precision solver), per TPS call."""
     stats = []
     for pd in outs:
         for t in (pd.tps_next, pd.tps_final):
             if t is not None:
                 it = t.iters.cpu().numpy()
-                stats.append({"subdomains": t.nb_subdom, "mean": round(float(it.mean()), 2),
-                              "max": int(it.max())})
+                st = {"subdomains": t.nb_subdom, "mean": round(float(it.mean()), 2),
+                      "max": int(it.max())}
+                if t.mp_sweeps is not None:
+                    sw = t.mp_sweeps.cpu().numpy()
+                    st["refine_sweeps_mean"] = round(float(sw.mean()), 2)
+                    st["refine_sweeps_max"] = int(sw.max())
+                stats.append(st)
     return stats
 
 
@@ -342,22 +348,25 @@ def roofline(dominant, outs, work, peaks, peak_kind, steps):
     """Roofline of the dominant library entry point (algorithmic work per launch)."""
     name, stats = dominant
     avg_s = stats["avg_ms"] / 1e3
-    if name == "fi_tps_solve":
-        # FP64 LU of (N+3)^2 systems: 2/3 (N+3)^3 flops per subdomain; bound by the
-        # FP64 pipe (no measured FP64 peak: nominal 1.25 TFLOP/s)
+    if name in ("fi_tps_solve", "fi_tps_solve_mp"):
+        # The reference solves each subdomain system with FP64 LU (gesv), once per
+        # component and outlier iteration: 2/3 (N+3)^3 flops each.  Bound: the FP64
+        # pipe (MEASURED_PEAKS.json has no FP64 figure: nominal 1.25 TFLOP/s).
         flops = 0.0
         nlaunch = 0
         for pd in outs:
             for tps in (pd.tps_next, pd.tps_final):
                 if tps is not None:
                     n = tps.counts.astype(np.float64) + 3
-                    flops += float((2.0 / 3.0 * n**3).sum())
+                    it = tps.iters.cpu().numpy().reshape(-1, 2).sum(axis=1)
+                    flops += float((2.0 / 3.0 * n**3 * it).sum())
                     nlaunch += 1
         per_launch = flops / max(nlaunch, 1)
         achieved = per_launch / avg_s / 1e12
         peak = 1.25
         return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "work": "reference-equivalent FP64 LU flops, sum 2/3 (N+3)^3 per solve",
                 "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
                 "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
     # correlation / other: HBM bound by the unique image bytes + outputs

@@ -93,7 +93,7 @@ _SIGNATURES = {
     "fi_tps_solve_mp": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P, C.c_double,
-         C.c_int, P, P, P, P, P, P, P, P, P],
+         C.c_int, P, P, P, P, P, P, P, P, P, P],
     ),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
     "fi_tps_interpolate": (

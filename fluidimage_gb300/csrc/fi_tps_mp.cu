@@ -118,52 +118,126 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 }
 
 constexpr int MP_THREADS = 256;
+constexpr int MP_WARPS = MP_THREADS / 32;
+constexpr int TS = 36;  // row stride (floats) of the 32 x 32 shared tiles: float4-aligned rows
 
-// t = u - A w for two right-hand sides; A (n x n, symmetric, column-major) in FP64.
-__device__ void residual2(const double* A, int n, const double* wx, const double* wy,
-                          const float* ux, const float* uy, double* tx, double* ty) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
-  for (int c = wid; c < n; c += nw) {
-    const double* col = A + (int64_t)c * n;  // row c = column c
-    double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
-    int r = lane;
-    for (; r + 96 < n; r += 128) {  // four independent loads in flight per lane
-      const double a0 = col[r], a1 = col[r + 32], a2 = col[r + 64], a3 = col[r + 96];
-      ax = fma(a0, wx[r], ax);
-      ay = fma(a0, wy[r], ay);
-      bx = fma(a1, wx[r + 32], bx);
-      by = fma(a1, wy[r + 32], by);
-      ax = fma(a2, wx[r + 64], ax);
-      ay = fma(a2, wy[r + 64], ay);
-      bx = fma(a3, wx[r + 96], bx);
-      by = fma(a3, wy[r + 96], by);
+// ------------------------------------------------------------------ double-float
+// Values as unevaluated pairs hi + lo of floats (about 48 significant bits).  The
+// error-free transformations use the _rn intrinsics so that no FMA contraction can
+// merge a product into the following sum.
+__device__ __forceinline__ float2 df_split(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+// (a.x + a.y) + (b.x + b.y), renormalised
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  const float lo = __fadd_rn(__fadd_rn(a.y, b.y), err);
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+
+// (sh, sl) += b * z (the lo * lo term, 2^-48 relative, is dropped)
+__device__ __forceinline__ void df_mac(float2 b, float2 z, float& sh, float& sl) {
+  const float p = __fmul_rn(b.x, z.x);
+  float e = __fmaf_rn(b.x, z.x, -p);
+  e = __fmaf_rn(b.x, z.y, e);
+  e = __fmaf_rn(b.y, z.x, e);
+  const float t = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+  sh = t;
+}
+
+// rho = g - B z for two right-hand sides, in double-float; B (m x m, symmetric, both
+// triangles, column-major, leading dimension ld) holds (hi, lo) pairs.  Each warp
+// takes four columns at a time (one row per lane), then reduce-scatters its eight
+// sums over the warp.  rho is rounded to float.
+__device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const float2* zx,
+                             const float2* zy, const float2* gx, const float2* gy, float* rx,
+                             float* ry) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  for (int c0 = 4 * wid; c0 < m; c0 += 4 * MP_WARPS) {
+    float h[8], l[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h[k] = l[k] = 0.f;
+    const float2* col = B + (int64_t)c0 * ld;
+    const int nc = min(4, m - c0);
+#pragma unroll 2
+    for (int r = lane; r < m; r += 32) {
+      const float2 a = zx[r], b = zy[r];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float2 v = (q < nc) ? col[(int64_t)q * ld + r] : make_float2(0.f, 0.f);
+        df_mac(v, a, h[q], l[q]);
+        df_mac(v, b, h[4 + q], l[4 + q]);
+      }
     }
-    for (; r < n; r += 32) {
-      const double a = col[r];
-      ax = fma(a, wx[r], ax);
-      ay = fma(a, wy[r], ay);
+    // reduce-scatter: lane ends with value 4 b4 + 2 b3 + b2 (b_k = bit k of lane)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool up = lane & 16;
+      const float sh_ = up ? h[k] : h[k + 4], sl_ = up ? l[k] : l[k + 4];
+      const float2 keep = up ? make_float2(h[k + 4], l[k + 4]) : make_float2(h[k], l[k]);
+      const float2 got = make_float2(__shfl_xor_sync(full, sh_, 16), __shfl_xor_sync(full, sl_, 16));
+      const float2 s = df_add(keep, got);
+      h[k] = s.x;
+      l[k] = s.y;
     }
-    ax += bx;
-    ay += by;
-    for (int o = 16; o > 0; o >>= 1) {
-      ax += __shfl_xor_sync(0xffffffffu, ax, o);
-      ay += __shfl_xor_sync(0xffffffffu, ay, o);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const bool up = lane & 8;
+      const float sh_ = up ? h[k] : h[k + 2], sl_ = up ? l[k] : l[k + 2];
+      const float2 keep = up ? make_float2(h[k + 2], l[k + 2]) : make_float2(h[k], l[k]);
+      const float2 got = make_float2(__shfl_xor_sync(full, sh_, 8), __shfl_xor_sync(full, sl_, 8));
+      const float2 s = df_add(keep, got);
+      h[k] = s.x;
+      l[k] = s.y;
     }
-    if (lane == 0) {
-      tx[c] = (double)ux[c] - ax;
-      ty[c] = (double)uy[c] - ay;
+    {
+      const bool up = lane & 4;
+      const float sh_ = up ? h[0] : h[1], sl_ = up ? l[0] : l[1];
+      const float2 keep = up ? make_float2(h[1], l[1]) : make_float2(h[0], l[0]);
+      const float2 got = make_float2(__shfl_xor_sync(full, sh_, 4), __shfl_xor_sync(full, sl_, 4));
+      const float2 s = df_add(keep, got);
+      h[0] = s.x;
+      l[0] = s.y;
+    }
+#pragma unroll
+    for (int o = 2; o > 0; o >>= 1) {
+      const float2 got = make_float2(__shfl_xor_sync(full, h[0], o), __shfl_xor_sync(full, l[0], o));
+      const float2 s = df_add(make_float2(h[0], l[0]), got);
+      h[0] = s.x;
+      l[0] = s.y;
+    }
+    if ((lane & 3) == 0) {
+      const int idx = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+      const int c = c0 + (idx & 3);
+      if (c < m) {
+        const float2 g = (idx >> 2) ? gy[c] : gx[c];
+        const float2 d = df_add(g, make_float2(-h[0], -l[0]));
+        ((idx >> 2) ? ry : rx)[c] = __fadd_rn(d.x, d.y);
+      }
     }
   }
   __syncthreads();
 }
 
-// Apply H_k = I - tau_k v_k v_k^T (k in order) to the two vectors x, y (length n).
+// Apply H_k = I - tau_k v_k v_k^T (k in order) to the two vectors x, y (length n);
+// v_k is row k of V (row stride vstride).
 template <bool REVERSE>
-__device__ void apply_reflectors2(const double* V, const double* tau, int n, double* x,
-                                  double* y, double* sh) {
+__device__ void apply_reflectors2(const double* V, int vstride, const double* tau, int n,
+                                  double* x, double* y, double* sh) {
   for (int kk = 0; kk < 3; ++kk) {
     const int k = REVERSE ? 2 - kk : kk;
-    const double* v = V + (int64_t)k * n;
+    const double* v = V + (int64_t)k * vstride;
     double2 d = make_double2(0.0, 0.0);
     for (int i = threadIdx.x; i < n; i += MP_THREADS) {
       d.x += v[i] * x[i];
@@ -179,58 +253,64 @@ __device__ void apply_reflectors2(const double* V, const double* tau, int n, dou
   }
 }
 
-// Solve (L L^T) x = r in place for two right-hand sides (float), L lower m x m,
-// column-major with leading dimension ld, by tiles of 32: the diagonal tile in one
-// warp (shuffles), the off-diagonal tiles by all warps (rows in registers for the
-// forward sweep, transposed shared-memory tiles for the backward sweep).
-// scratch: (1 + warps) * 32 * 33 floats.
-__device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry,
-                            float* scratch) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+// Solve (L L^T) x = r in place for two right-hand sides (float).  L: lower m x m,
+// column-major, leading dimension ld (a multiple of 4, 16-byte aligned base); only
+// its lower triangle is read.  rx, ry: shared, 16-byte aligned, zero from m up to a
+// multiple of 32.  By tiles of 32: the diagonal tile in one warp (shuffles, rows or
+// columns of L in registers), the off-diagonal tiles by all warps with coalesced
+// (forward) or contiguous float4 (backward) loads and float4 broadcasts of x.
+// part: 64 * warps floats.
+__device__ void chol_solve2(const float* __restrict__ L, int m, int ld, float* rx, float* ry,
+                            float* part) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   const int T = (m + 31) / 32;
-  float* part = scratch;                       // [warp][64] partial sums (backward)
-  float* Lt = scratch + 32 * 33 * (1 + wid);   // per warp transposed tile
   // ---- forward: L y = r
   for (int k = 0; k < T; ++k) {
     const int r0 = 32 * k;
     if (wid == 0) {
-      float Lrow[32];  // row (r0 + lane) of the diagonal tile
       const int r = r0 + lane;
+      float Lrow[32];  // row r of the diagonal tile (entries right of the diagonal unused)
 #pragma unroll
-      for (int c = 0; c < 32; ++c)
-        Lrow[c] = (r < m && r0 + c < m) ? L[(int64_t)(r0 + c) * ld + r] : ((c == lane) ? 1.f : 0.f);
-      float vx = (r < m) ? rx[r] : 0.f, vy = (r < m) ? ry[r] : 0.f;
+      for (int c = 0; c < 32; ++c) Lrow[c] = (r < m && r0 + c < m) ? L[(int64_t)(r0 + c) * ld + r] : 0.f;
+      const float inv = (r < m) ? 1.f / L[(int64_t)r * ld + r] : 1.f;
+      float vx = rx[r], vy = ry[r];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const float d = __shfl_sync(full, Lrow[j], j);
-        const float xj = __shfl_sync(full, vx, j) / d;
-        const float yj = __shfl_sync(full, vy, j) / d;
         if (lane == j) {
-          vx = xj;
-          vy = yj;
-        } else if (lane > j) {
+          vx *= inv;
+          vy *= inv;
+        }
+        const float xj = __shfl_sync(full, vx, j), yj = __shfl_sync(full, vy, j);
+        if (lane > j) {
           vx = fmaf(-Lrow[j], xj, vx);
           vy = fmaf(-Lrow[j], yj, vy);
         }
       }
-      if (r < m) {
-        rx[r] = vx;
-        ry[r] = vy;
-      }
+      rx[r] = vx;
+      ry[r] = vy;
     }
     __syncthreads();
-    for (int i = k + 1 + wid; i < T; i += nw) {  // r_i -= L_ik y_k
+    // r_i -= L_ik y_k for the tiles i > k (their rows are below m only in full tiles k)
+    for (int i = k + 1 + wid; i < T; i += MP_WARPS) {
       const int r = 32 * i + lane;
       if (r < m) {
         float sx = 0.f, sy = 0.f;
-#pragma unroll 8
-        for (int c = 0; c < 32; ++c) {
-          if (r0 + c < m) {
-            const float l = L[(int64_t)(r0 + c) * ld + r];
-            sx = fmaf(l, rx[r0 + c], sx);
-            sy = fmaf(l, ry[r0 + c], sy);
-          }
+        const float* Lc = L + (int64_t)r0 * ld + r;
+#pragma unroll
+        for (int c4 = 0; c4 < 8; ++c4) {
+          const float4 yx = *reinterpret_cast<const float4*>(rx + r0 + 4 * c4);
+          const float4 yy = *reinterpret_cast<const float4*>(ry + r0 + 4 * c4);
+          const float l0 = Lc[(int64_t)(4 * c4) * ld], l1 = Lc[(int64_t)(4 * c4 + 1) * ld];
+          const float l2 = Lc[(int64_t)(4 * c4 + 2) * ld], l3 = Lc[(int64_t)(4 * c4 + 3) * ld];
+          sx = fmaf(l0, yx.x, sx);
+          sy = fmaf(l0, yy.x, sy);
+          sx = fmaf(l1, yx.y, sx);
+          sy = fmaf(l1, yy.y, sy);
+          sx = fmaf(l2, yx.z, sx);
+          sy = fmaf(l2, yy.z, sy);
+          sx = fmaf(l3, yx.w, sx);
+          sy = fmaf(l3, yy.w, sy);
         }
         rx[r] -= sx;
         ry[r] -= sy;
@@ -241,54 +321,67 @@ __device__ void chol_solve2(const float* L, int m, int ld, float* rx, float* ry,
   // ---- backward: L^T x = y
   for (int k = T - 1; k >= 0; --k) {
     const int c0 = 32 * k;
-    float px = 0.f, py = 0.f;  // lane t: partial of sum_{i>k} sum_r L_ik[r][t] x_i[r]
-    for (int i = k + 1 + wid; i < T; i += nw) {
-      const int r = 32 * i + lane;
+    const int t = c0 + lane;  // this lane's column
+    float px = 0.f, py = 0.f;
+    for (int i = k + 1 + wid; i < T; i += MP_WARPS) {  // column t is below m here
+      const float* Lc = L + (int64_t)t * ld + 32 * i;
 #pragma unroll
-      for (int t = 0; t < 32; ++t)
-        Lt[t * 33 + lane] = (r < m && c0 + t < m) ? L[(int64_t)(c0 + t) * ld + r] : 0.f;
-      __syncwarp();
-#pragma unroll 8
-      for (int rr = 0; rr < 32; ++rr) {
-        const int ri = 32 * i + rr;
-        const float xv = (ri < m) ? rx[ri] : 0.f, yv = (ri < m) ? ry[ri] : 0.f;
-        const float l = Lt[lane * 33 + rr];
-        px = fmaf(l, xv, px);
-        py = fmaf(l, yv, py);
+      for (int q = 0; q < 8; ++q) {
+        const int row = 32 * i + 4 * q;
+        float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row < ld) lv = *reinterpret_cast<const float4*>(Lc + 4 * q);
+        if (row + 0 >= m) lv.x = 0.f;
+        if (row + 1 >= m) lv.y = 0.f;
+        if (row + 2 >= m) lv.z = 0.f;
+        if (row + 3 >= m) lv.w = 0.f;
+        const float4 xv = *reinterpret_cast<const float4*>(rx + row);
+        const float4 yv = *reinterpret_cast<const float4*>(ry + row);
+        px = fmaf(lv.x, xv.x, px);
+        py = fmaf(lv.x, yv.x, py);
+        px = fmaf(lv.y, xv.y, px);
+        py = fmaf(lv.y, yv.y, py);
+        px = fmaf(lv.z, xv.z, px);
+        py = fmaf(lv.z, yv.z, py);
+        px = fmaf(lv.w, xv.w, px);
+        py = fmaf(lv.w, yv.w, py);
       }
-      __syncwarp();
     }
     part[wid * 64 + lane] = px;
     part[wid * 64 + 32 + lane] = py;
     __syncthreads();
     if (wid == 0) {
-      const int t = c0 + lane;
-      float vx = (t < m) ? rx[t] : 0.f, vy = (t < m) ? ry[t] : 0.f;
-      for (int w = 0; w < nw; ++w) {
+      float vx = rx[t], vy = ry[t];
+#pragma unroll
+      for (int w = 0; w < MP_WARPS; ++w) {
         vx -= part[w * 64 + lane];
         vy -= part[w * 64 + 32 + lane];
       }
-      float Lcol[32];  // column (c0 + lane) of the diagonal tile: Lcol[j] = L[c0 + j][c0 + lane]
+      float Lcol[32];  // Lcol[j] = L[c0 + j][t] (column t of the diagonal tile)
 #pragma unroll
-      for (int j = 0; j < 32; ++j)
-        Lcol[j] = (t < m && c0 + j < m) ? L[(int64_t)t * ld + c0 + j] : ((j == lane) ? 1.f : 0.f);
+      for (int q = 0; q < 8; ++q) {
+        const int row = c0 + 4 * q;
+        float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t < m && row < ld) lv = *reinterpret_cast<const float4*>(L + (int64_t)t * ld + row);
+        Lcol[4 * q] = (row < m) ? lv.x : 0.f;
+        Lcol[4 * q + 1] = (row + 1 < m) ? lv.y : 0.f;
+        Lcol[4 * q + 2] = (row + 2 < m) ? lv.z : 0.f;
+        Lcol[4 * q + 3] = (row + 3 < m) ? lv.w : 0.f;
+      }
+      const float inv = (t < m) ? 1.f / L[(int64_t)t * ld + t] : 1.f;
 #pragma unroll
       for (int j = 31; j >= 0; --j) {
-        const float d = __shfl_sync(full, Lcol[j], j);
-        const float xj = __shfl_sync(full, vx, j) / d;
-        const float yj = __shfl_sync(full, vy, j) / d;
         if (lane == j) {
-          vx = xj;
-          vy = yj;
-        } else if (lane < j) {
+          vx *= inv;
+          vy *= inv;
+        }
+        const float xj = __shfl_sync(full, vx, j), yj = __shfl_sync(full, vy, j);
+        if (lane < j) {
           vx = fmaf(-Lcol[j], xj, vx);
           vy = fmaf(-Lcol[j], yj, vy);
         }
       }
-      if (t < m) {
-        rx[t] = vx;
-        ry[t] = vy;
-      }
+      rx[t] = vx;
+      ry[t] = vy;
     }
     __syncthreads();
   }
@@ -317,17 +410,18 @@ __device__ __forceinline__ void tile_store(float* B, int m, int ld, int ti, int 
 }
 
 // Right-looking tiled Cholesky (lower) of the m x m matrix B (column-major, ld), in
-// place.  Per tile column k: one warp factorises the diagonal tile in registers
-// (shuffles), warps solve the tiles below (one row per lane, L_kk broadcast from
-// shared memory), then update the trailing tile pairs (register accumulators,
-// the second factor transposed in shared memory and read as broadcasts).
-// scratch: (1 + warps) * 32 * 33 floats.  Returns false on a non-positive pivot.
+// place (lower triangle).  Per tile column k: one warp factorises the diagonal tile
+// in registers (shuffles), warps solve the tiles below (one row per lane, rows of
+// L_kk read as float4 broadcasts), then update the trailing tile pairs (register
+// accumulators, the second factor transposed in shared memory, float4 broadcasts).
+// scratch: (1 + warps) * 32 * TS floats, 16-byte aligned.  False on a non-positive
+// pivot.
 __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   const int T = (m + 31) / 32;
-  float* Lkk = scratch;                       // 32 x 33
-  float* Lt = scratch + 32 * 33 * (1 + wid);  // per warp, 32 x 33 (transposed tile)
+  float* Lkk = scratch;                     // row j: L_kk[j][c] for c < j (0 elsewhere), [32] = 1 / L_jj
+  float* Lt = scratch + 32 * TS * (1 + wid);  // per warp, transposed tile
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
   for (int k = 0; k < T; ++k) {
@@ -335,6 +429,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       float a[32];
       tile_load(B, m, ld, k, k, a, lane);
       bool bad = false;
+      float dg = 1.f;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         float djj = __shfl_sync(full, a[j], j);
@@ -343,6 +438,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
           djj = 1.f;
         }
         const float sq = sqrtf(djj);
+        if (lane == j) dg = sq;
         const float lrj = (lane > j) ? a[j] / sq : ((lane == j) ? sq : 0.f);
         if (lane >= j) a[j] = lrj;
 #pragma unroll
@@ -354,19 +450,26 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       if (bad && lane == 0) *s_flag = 1;
       tile_store(B, m, ld, k, k, a, lane, true);
 #pragma unroll
-      for (int c = 0; c < 32; ++c) Lkk[lane * 33 + c] = (c <= lane) ? a[c] : 0.f;
+      for (int c = 0; c < 32; ++c) Lkk[lane * TS + c] = (c < lane) ? a[c] : 0.f;
+      Lkk[lane * TS + 32] = 1.f / dg;
     }
     __syncthreads();
     // TRSM: tiles (i, k), i > k: X L_kk^T = A_ik, row by row in each lane
-    for (int i = k + 1 + wid; i < T; i += nw) {
+    for (int i = k + 1 + wid; i < T; i += MP_WARPS) {
       float b[32];
       tile_load(B, m, ld, i, k, b, lane);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         float v = b[j];
 #pragma unroll
-        for (int c = 0; c < j; ++c) v = fmaf(-b[c], Lkk[j * 33 + c], v);
-        b[j] = v / Lkk[j * 33 + j];
+        for (int c4 = 0; c4 < (j + 3) / 4; ++c4) {  // entries c >= j of row j are 0
+          const float4 q = *reinterpret_cast<const float4*>(Lkk + j * TS + 4 * c4);
+          v = fmaf(-b[4 * c4], q.x, v);
+          v = fmaf(-b[4 * c4 + 1], q.y, v);
+          v = fmaf(-b[4 * c4 + 2], q.z, v);
+          v = fmaf(-b[4 * c4 + 3], q.w, v);
+        }
+        b[j] = v * Lkk[j * TS + 32];
       }
       tile_store(B, m, ld, i, k, b, lane, false);
     }
@@ -374,7 +477,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
     // trailing update: tiles (i, j), k < j <= i
     const int n = T - k - 1;
     const int npairs = n * (n + 1) / 2;
-    for (int pidx = wid; pidx < npairs; pidx += nw) {
+    for (int pidx = wid; pidx < npairs; pidx += MP_WARPS) {
       int ii = (int)((sqrtf(8.f * pidx + 1.f) - 1.f) * 0.5f);
       while ((ii + 1) * (ii + 2) / 2 <= pidx) ++ii;
       while (ii * (ii + 1) / 2 > pidx) --ii;
@@ -383,7 +486,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       float l[32];
       tile_load(B, m, ld, j, k, l, lane);  // L_jk rows -> transposed in shared memory
 #pragma unroll
-      for (int t = 0; t < 32; ++t) Lt[t * 33 + lane] = l[t];
+      for (int t = 0; t < 32; ++t) Lt[t * TS + lane] = l[t];
       __syncwarp();
       if (i != j) tile_load(B, m, ld, i, k, l, lane);  // L_ik rows
       float acc[32];
@@ -392,7 +495,13 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       for (int t = 0; t < 32; ++t) {
         const float lr = l[t];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) acc[c] = fmaf(-lr, Lt[t * 33 + c], acc[c]);
+        for (int c4 = 0; c4 < 8; ++c4) {
+          const float4 q = *reinterpret_cast<const float4*>(Lt + t * TS + 4 * c4);
+          acc[4 * c4] = fmaf(-lr, q.x, acc[4 * c4]);
+          acc[4 * c4 + 1] = fmaf(-lr, q.y, acc[4 * c4 + 1]);
+          acc[4 * c4 + 2] = fmaf(-lr, q.z, acc[4 * c4 + 2]);
+          acc[4 * c4 + 3] = fmaf(-lr, q.w, acc[4 * c4 + 3]);
+        }
       }
       tile_store(B, m, ld, i, j, acc, lane, i == j);
       __syncwarp();
@@ -402,23 +511,49 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
   return *s_flag == 0;
 }
 
+// Shared-memory layout of k_tps_solve_mp for subdomains of at most n centres.
+struct MpLayout {
+  int np;        // n rounded up to 32
+  size_t d_off;  // doubles: V 3n, xc n, yc n, Y/C 3n, W 4n
+  size_t f2_off; // float2: zx, zy, gx, gy (np each)
+  size_t f_off;  // float: vx, vy, rx, ry (np each)
+  size_t i2_off; // int2: lattice coordinates (np)
+  size_t p_off;  // panel: (1 + warps) * 32 * TS floats
+  size_t bytes;
+  __host__ __device__ explicit MpLayout(int n) {
+    np = (n + 31) & ~31;
+    d_off = 0;
+    f2_off = d_off + (size_t)12 * n * sizeof(double);
+    f_off = f2_off + (size_t)4 * np * sizeof(float2);
+    i2_off = f_off + (size_t)4 * np * sizeof(float);
+    p_off = i2_off + (size_t)np * sizeof(int2);
+    bytes = p_off + (size_t)(1 + MP_WARPS) * 32 * TS * sizeof(float);
+  }
+};
+
 // One block per subdomain.  Status per subdomain: 0 solved here, 1 needs the FP64
 // LU fallback (rank-deficient P, Cholesky breakdown or no convergence).
+//
+// Buffers per subdomain (offset mat_off, a multiple of 4 elements): matrices holds
+// B22 = (Q^T A Q)[3:, 3:] as (hi, lo) float pairs, both triangles, leading
+// dimension mp = m rounded up to 4; matrices32 holds its FP32 Cholesky factor (lower
+// triangle, same layout).
 __global__ void __launch_bounds__(MP_THREADS, 2)
     k_tps_solve_mp(const fi_tps_plan* plan_ptr, const double* cx, const double* cy,
                    const float* ux, const float* uy, const int32_t* counts,
                    const int64_t* offsets, const int32_t* indices, const int64_t* mat_off,
                    double* matrices, float* matrices32, const double* phi_table,
                    int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
-                   double threshold, int use_threshold,
-                   const int64_t* w_off, double* weights, double* smoothed_x,
-                   double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
-                   double* max_udiff, int max_refine) {
+                   double threshold, int use_threshold, const int64_t* w_off, double* weights,
+                   double* smoothed_x, double* smoothed_y, int32_t* iters, int32_t* nfixed,
+                   int32_t* status, double* max_udiff, int32_t* sweeps, int max_refine,
+                   int n_layout) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sh[80];
   __shared__ double s_tau[3];
   __shared__ double s_R[9];
-  __shared__ int s_flag, s_bad[2];
+  __shared__ double s_q1[6];
+  __shared__ int s_flag, s_bad[2], s_lat;
   const fi_tps_plan p = *plan_ptr;
   const int sd = blockIdx.x;
   const int N = counts[sd];
@@ -428,28 +563,29 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
   const double lam = p.smoothing;
   if (threadIdx.x == 0) status[sd] = 1;
   if (m < 1) return;  // fewer than 4 centres: FP64 LU path
+  const int mp = (m + 3) & ~3;
 
-  // shared layout (doubles first)
-  double* V = reinterpret_cast<double*>(smraw);  // 3 N
-  double* xc = V + 3 * N;                         // N
-  double* yc = xc + N;                            // N
-  double* wx = yc + N;                            // N  (weights w, then scratch)
-  double* wy = wx + N;
-  double* tx = wy + N;                            // N  (residual / projections)
-  double* ty = tx + N;
-  double* zx = ty + N;                            // m (+3 padding)
-  double* zy = zx + N;
-  float* vx = reinterpret_cast<float*>(zy + N);  // N current values (float32)
-  float* vy = vx + N;
-  float* rx = vy + N;                             // m correction (float)
-  float* ry = rx + N;
-  float* panel = ry + N;  // Cholesky / solve scratch: (1 + warps) * 32 * 33 floats
+  const MpLayout lay(n_layout);
+  const int n = n_layout;
+  double* V = reinterpret_cast<double*>(smraw + lay.d_off);  // 3 n (rows k: v_k)
+  double* xc = V + 3 * n;
+  double* yc = xc + n;
+  double* YC = yc + n;  // Y = A V (3 n), then C = (Q^T A Q)[0:3, 3:] (3 n)
+  double* W = YC + 3 * n;  // 4 n: QR scratch, Z, then t / w
+  float2* zx2 = reinterpret_cast<float2*>(smraw + lay.f2_off);
+  float2* zy2 = zx2 + lay.np;
+  float2* gx2 = zy2 + lay.np;
+  float2* gy2 = gx2 + lay.np;
+  float* vx = reinterpret_cast<float*>(smraw + lay.f_off);
+  float* vy = vx + lay.np;
+  float* rx = vy + lay.np;
+  float* ry = rx + lay.np;
+  int2* cxy = reinterpret_cast<int2*>(smraw + lay.i2_off);
+  float* panel = reinterpret_cast<float*>(smraw + lay.p_off);
 
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = MP_THREADS / 32;
-  const double* A64 = matrices + mat_off[sd];  // N x N, K + lam I (kept for residuals)
-  float* B = matrices32 + mat_off[sd];         // N x N float (lower triangle of B22 used)
-  __shared__ int s_lat;
-  int2* cxy = reinterpret_cast<int2*>(panel);  // lattice coordinates (panel is free here)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2* B2 = reinterpret_cast<float2*>(matrices + mat_off[sd]);
+  float* L32 = matrices32 + mat_off[sd];
 
   if (threadIdx.x == 0)
     s_lat = (cxy2 != nullptr && c_on_lattice != nullptr && phi_table != nullptr) ? *c_on_lattice : 0;
@@ -460,11 +596,25 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
     if (cxy2 != nullptr) cxy[i] = make_int2(cxy2[2 * a], cxy2[2 * a + 1]);
   }
   __syncthreads();
+  const bool lat = s_lat != 0;
+  // A = K + lam I, entry (r, c); on the lattice 4 r^2 is an integer table index
+  auto a_entry = [&](int r, int c) -> double {
+    if (r == c) return lam;
+    if (lat) {
+      const int2 ca = cxy[r], cb = cxy[c];
+      const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
+      const int64_t kq = dy * dy + dx * dx;
+      if (kq < table_size) return __ldg(phi_table + kq);
+      return phi_pair(xc[r], yc[r], xc[c], yc[c], nullptr, 0);
+    }
+    return phi_pair(xc[r], yc[r], xc[c], yc[c], phi_table, table_size);
+  };
+
   // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
   {
-    double* P0 = tx;  // scratch columns
-    double* P1 = ty;
-    double* P2 = wx;
+    double* P0 = W;  // scratch columns
+    double* P1 = W + n;
+    double* P2 = W + 2 * n;
     for (int i = threadIdx.x; i < N; i += MP_THREADS) {
       P0[i] = 1.0;
       P1[i] = yc[i];
@@ -485,7 +635,7 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
         break;
       }
       const double alpha = (x0 >= 0.0) ? -nrm : nrm;
-      double* v = V + (int64_t)k * N;
+      double* v = V + (int64_t)k * n;
       for (int i = threadIdx.x; i < N; i += MP_THREADS) v[i] = (i < k) ? 0.0 : x[i];
       __syncthreads();
       if (threadIdx.x == 0) v[k] = x0 - alpha;
@@ -517,65 +667,41 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
     __syncthreads();
     if (!rank_ok) return;
   }
-  __syncthreads();
-  // ---- A = K + lam I in FP64 (column-major; on the lattice 4 r^2 in integers),
-  // fused with Y = A V for the projection (A symmetric: row c = column c)
-  double* Y0 = tx;
-  double* Y1 = ty;
-  double* Y2 = wx;
-  {
-    const double* V0 = V;
-    const double* V1 = V + N;
-    const double* V2 = V + 2 * (int64_t)N;
-    for (int c = wid; c < N; c += nw) {
-      const double bx = xc[c], by = yc[c];
-      const int2 cb = cxy[c];
-      double* col = matrices + mat_off[sd] + (int64_t)c * N;
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-      for (int r = lane; r < N; r += 32) {
-        double v;
-        if (r == c) {
-          v = lam;
-        } else if (s_lat) {
-          const int2 ca = cxy[r];
-          const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
-          const int64_t kq = dy * dy + dx * dx;
-          v = (kq < table_size) ? __ldg(phi_table + kq)
-                                : phi_pair(xc[r], yc[r], bx, by, nullptr, 0);
-        } else {
-          v = phi_pair(xc[r], yc[r], bx, by, phi_table, table_size);
-        }
-        col[r] = v;
-        a0 = fma(v, V0[r], a0);
-        a1 = fma(v, V1[r], a1);
-        a2 = fma(v, V2[r], a2);
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-      }
-      if (lane == 0) {
-        Y0[c] = a0;
-        Y1[c] = a1;
-        Y2[c] = a2;
-      }
+  const double* V0 = V;
+  const double* V1 = V + n;
+  const double* V2 = V + 2 * n;
+  double* Y0 = YC;
+  double* Y1 = YC + n;
+  double* Y2 = YC + 2 * n;
+  // ---- Y = A V (FP64; A symmetric: row c = column c)
+  for (int c = wid; c < N; c += MP_WARPS) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int r = lane; r < N; r += 32) {
+      const double v = a_entry(r, c);
+      a0 = fma(v, V0[r], a0);
+      a1 = fma(v, V1[r], a1);
+      a2 = fma(v, V2[r], a2);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) {
+      Y0[c] = a0;
+      Y1[c] = a1;
+      Y2[c] = a2;
     }
   }
   __syncthreads();
-  // ---- B22 = (Q^T A Q)[3:, 3:] with Q = H0 H1 H2 = I - V T V^T (compact WY):
-  // Q^T A Q = A - Z V^T - V Z^T, Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.
-  // FP64 (the projection cancels the large affine part of K); only the lower
-  // triangle of B22 is formed, directly in FP32.
+  // ---- Q^T A Q = A - Z V^T - V Z^T (compact WY, Q = H0 H1 H2 = I - V T V^T),
+  // Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.  FP64: the projection cancels the
+  // large affine part of K.
+  double* Z0 = W;
+  double* Z1 = W + n;
+  double* Z2 = W + 2 * n;
   {
     __shared__ double s_T[9], s_M[9];
-    double* Z0 = wy;
-    double* Z1 = zx;
-    double* Z2 = zy;
-    const double* V0 = V;
-    const double* V1 = V + N;
-    const double* V2 = V + 2 * (int64_t)N;
-    // V^T V (upper) and V^T Y (full), block sums
     const double* Vk[3] = {V0, V1, V2};
     const double* Yk[3] = {Y0, Y1, Y2};
     double vtv[3], vty[9];
@@ -630,72 +756,115 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
       Z2[i] = z[2];
     }
     __syncthreads();
-    for (int c = 3 + wid; c < N; c += nw) {  // lower triangle of B22, rows r >= c
-      const double* col = A64 + (int64_t)c * N;
-      float* colb = B + (int64_t)c * N;
-      const double vc0 = V0[c], vc1 = V1[c], vc2 = V2[c];
-      const double zc0 = Z0[c], zc1 = Z1[c], zc2 = Z2[c];
-      for (int r = c + lane; r < N; r += 32) {
-        double v = col[r];
-        v -= Z0[r] * vc0 + V0[r] * zc0;
-        v -= Z1[r] * vc1 + V1[r] * zc1;
-        v -= Z2[r] * vc2 + V2[r] * zc2;
-        colb[r] = (float)v;
+  }
+  auto proj = [&](int r, int c) -> double {  // (Q^T A Q)[r][c], global indices
+    double v = a_entry(r, c);
+    v -= Z0[r] * V0[c] + V0[r] * Z0[c];
+    v -= Z1[r] * V1[c] + V1[r] * Z1[c];
+    v -= Z2[r] * V2[c] + V2[r] * Z2[c];
+    return v;
+  };
+  // C[k][c] = (Q^T A Q)[k][c + 3], k < 3 (Y is no longer needed)
+  double* C = YC;
+  for (int i = threadIdx.x; i < 3 * m; i += MP_THREADS) {
+    const int k = i / m, c = i - k * m;
+    C[k * n + c] = proj(k, c + 3);
+  }
+  // B22 by 32 x 32 tiles (I >= J), half a tile (16 columns) at a time: the lower
+  // entries are written by columns, then mirrored through a per-warp shared tile.
+  {
+    float2* S = reinterpret_cast<float2*>(panel) + wid * 16 * 33;
+    const int T = (m + 31) / 32;
+    const int npairs = T * (T + 1) / 2;
+    for (int pidx = wid; pidx < npairs; pidx += MP_WARPS) {
+      int I = (int)((sqrtf(8.f * pidx + 1.f) - 1.f) * 0.5f);
+      while ((I + 1) * (I + 2) / 2 <= pidx) ++I;
+      while (I * (I + 1) / 2 > pidx) --I;
+      const int J = pidx - I * (I + 1) / 2;
+      const int r = 32 * I + lane;
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+          const int c = 32 * J + 16 * h + q;
+          if (r < m && c < m && r >= c) {
+            const float2 s = df_split(proj(r + 3, c + 3));
+            B2[(int64_t)c * mp + r] = s;
+            L32[(int64_t)c * mp + r] = s.x;
+            S[q * 33 + lane] = s;
+          }
+        }
+        __syncwarp();
+#pragma unroll 4
+        for (int st = 0; st < 16; ++st) {
+          const int rr = 2 * st + (lane >> 4), qq = lane & 15;
+          const int r2 = 32 * I + rr, c2 = 32 * J + 16 * h + qq;
+          if (r2 < m && c2 < m && r2 > c2) B2[(int64_t)r2 * mp + c2] = S[qq * 33 + rr];
+        }
+        __syncwarp();
       }
     }
-    __syncthreads();
   }
-  // ---- FP32 Cholesky of B22 = B[3:, 3:]
-  float* B22 = B + 3 + 3 * (int64_t)N;
-  if (!chol_factor(B22, m, N, panel, &s_flag)) return;
+  __syncthreads();
+  // ---- FP32 Cholesky of B22
+  if (!chol_factor(L32, m, mp, panel, &s_flag)) return;
 
   // ---- outlier iterations with refined solves (x and y in lockstep)
-  for (int r = threadIdx.x; r < N; r += MP_THREADS) {
-    vx[r] = ux[idx[r]];
-    vy[r] = uy[idx[r]];
+  double* tx = W;
+  double* ty = W + n;
+  double* wx = W + 2 * n;
+  double* wy = W + 3 * n;
+  for (int r = threadIdx.x; r < lay.np; r += MP_THREADS) {
+    vx[r] = (r < N) ? ux[idx[r]] : 0.f;
+    vy[r] = (r < N) ? uy[idx[r]] : 0.f;
+    zx2[r] = zy2[r] = make_float2(0.f, 0.f);
+    rx[r] = ry[r] = 0.f;
   }
-  for (int r = threadIdx.x; r < N; r += MP_THREADS) zx[r] = zy[r] = 0.0;
   __syncthreads();
   int count[2] = {1, 1}, fixed[2] = {0, 0};
   bool done[2] = {false, false};
   bool converged_all = true;
-  bool first_solve = true;
+  bool z_zero = true;
+  int nsweeps = 0;
   while (true) {
-    // refine z for the current values
+    // g = Q^T u: rows 3.. as double-float for the refinement, rows 0..2 for a
+    for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+      tx[i] = (double)vx[i];
+      ty[i] = (double)vy[i];
+    }
+    __syncthreads();
+    apply_reflectors2<false>(V, n, s_tau, N, tx, ty, sh);
+    for (int i = threadIdx.x; i < m; i += MP_THREADS) {
+      gx2[i] = df_split(tx[i + 3]);
+      gy2[i] = df_split(ty[i + 3]);
+    }
+    if (threadIdx.x < 3) {
+      s_q1[threadIdx.x] = tx[threadIdx.x];
+      s_q1[3 + threadIdx.x] = ty[threadIdx.x];
+    }
+    __syncthreads();
+    // refine z (B z = g): FP32 Cholesky solves, double-float residuals
     bool conv = false;
     double prev = INFINITY;
     for (int it = 0; it < max_refine; ++it) {
-      // w = Q [0; z]
-      for (int i = threadIdx.x; i < N; i += MP_THREADS) {
-        wx[i] = (i < 3) ? 0.0 : zx[i - 3];
-        wy[i] = (i < 3) ? 0.0 : zy[i - 3];
-      }
-      __syncthreads();
-      if (it == 0 && first_solve) {  // z = 0: t = u
-        for (int i = threadIdx.x; i < N; i += MP_THREADS) {
-          tx[i] = (double)vx[i];
-          ty[i] = (double)vy[i];
+      if (z_zero) {  // z = 0: rho = g
+        for (int i = threadIdx.x; i < m; i += MP_THREADS) {
+          rx[i] = __fadd_rn(gx2[i].x, gx2[i].y);
+          ry[i] = __fadd_rn(gy2[i].x, gy2[i].y);
         }
         __syncthreads();
+        z_zero = false;
       } else {
-        apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
-        residual2(A64, N, wx, wy, vx, vy, tx, ty);
+        residual_df2(B2, m, mp, zx2, zy2, gx2, gy2, rx, ry);
       }
-      // rho = (Q^T t)[3:]
-      apply_reflectors2<false>(V, s_tau, N, tx, ty, sh);
-      for (int i = threadIdx.x; i < m; i += MP_THREADS) {
-        rx[i] = (float)tx[i + 3];
-        ry[i] = (float)ty[i + 3];
-      }
-      __syncthreads();
-      chol_solve2(B22, m, N, rx, ry, panel);
+      chol_solve2(L32, m, mp, rx, ry, panel);
+      ++nsweeps;
       double dmax = 0.0, zmax = 0.0;
       for (int i = threadIdx.x; i < m; i += MP_THREADS) {
-        if (!done[0]) zx[i] += (double)rx[i];
-        if (!done[1]) zy[i] += (double)ry[i];
+        if (!done[0]) zx2[i] = df_add(zx2[i], make_float2(rx[i], 0.f));
+        if (!done[1]) zy2[i] = df_add(zy2[i], make_float2(ry[i], 0.f));
         dmax = fmax(dmax, fmax(done[0] ? 0.0 : fabs((double)rx[i]),
                                done[1] ? 0.0 : fabs((double)ry[i])));
-        zmax = fmax(zmax, fmax(fabs(zx[i]), fabs(zy[i])));
+        zmax = fmax(zmax, fmax(fabs((double)zx2[i].x), fabs((double)zy2[i].x)));
       }
       dmax = bmax<MP_THREADS>(dmax, sh);
       zmax = bmax<MP_THREADS>(zmax, sh);
@@ -711,37 +880,48 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
           conv = true;
           break;
         }
-        if (it >= 2 && rho > 0.5) {  // at the FP64 residual floor
+        if (it >= 2 && rho > 0.5) {  // at the residual floor
           conv = dmax <= 1e-9 * zmax;
           break;
         }
       }
       prev = dmax;
     }
-    first_solve = false;
     if (!conv) {
       converged_all = false;
       break;
     }
-    // final w, s = A w is in t before projection: recompute t = u - A w for a
-    for (int i = threadIdx.x; i < N; i += MP_THREADS) {
-      wx[i] = (i < 3) ? 0.0 : zx[i - 3];
-      wy[i] = (i < 3) ? 0.0 : zy[i - 3];
-    }
-    __syncthreads();
-    apply_reflectors2<true>(V, s_tau, N, wx, wy, sh);
-    residual2(A64, N, wx, wy, vx, vy, tx, ty);
-    // a = R^-1 (Q1^T (u - A w))
-    apply_reflectors2<false>(V, s_tau, N, tx, ty, sh);
+    // a = R^-1 (Q1^T u - C z) (R upper triangular); w = Q [0; z]
     double ax3[3], ay3[3];
-    for (int k = 2; k >= 0; --k) {
-      double sxk = tx[k], syk = ty[k];
-      for (int j = k + 1; j < 3; ++j) {
-        sxk -= s_R[k * 3 + j] * ax3[j];
-        syk -= s_R[k * 3 + j] * ay3[j];
+    {
+      double c6[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = threadIdx.x; i < m; i += MP_THREADS) {
+        const double zxv = df_to_double(zx2[i]), zyv = df_to_double(zy2[i]);
+        for (int k = 0; k < 3; ++k) {
+          c6[k] = fma(C[k * n + i], zxv, c6[k]);
+          c6[3 + k] = fma(C[k * n + i], zyv, c6[3 + k]);
+        }
       }
-      ax3[k] = sxk / s_R[k * 3 + k];
-      ay3[k] = syk / s_R[k * 3 + k];
+      for (int k = 0; k < 3; ++k) {
+        const double2 s2 = bsum2<MP_THREADS>(make_double2(c6[k], c6[3 + k]), sh);
+        c6[k] = s2.x;
+        c6[3 + k] = s2.y;
+      }
+      for (int k = 2; k >= 0; --k) {
+        double sxk = s_q1[k] - c6[k], syk = s_q1[3 + k] - c6[3 + k];
+        for (int j = k + 1; j < 3; ++j) {
+          sxk -= s_R[k * 3 + j] * ax3[j];
+          syk -= s_R[k * 3 + j] * ay3[j];
+        }
+        ax3[k] = sxk / s_R[k * 3 + k];
+        ay3[k] = syk / s_R[k * 3 + k];
+      }
+      for (int i = threadIdx.x; i < N; i += MP_THREADS) {
+        wx[i] = (i < 3) ? 0.0 : df_to_double(zx2[i - 3]);
+        wy[i] = (i < 3) ? 0.0 : df_to_double(zy2[i - 3]);
+      }
+      __syncthreads();
+      apply_reflectors2<true>(V, n, s_tau, N, wx, wy, sh);
     }
     // smoothed = u - lam w; outlier test (compute_tps_weights_iter, subdom.py:236-280)
     if (threadIdx.x == 0) s_bad[0] = s_bad[1] = 0;
@@ -814,6 +994,7 @@ __global__ void __launch_bounds__(MP_THREADS, 2)
     __syncthreads();
     if (done[0] && done[1]) break;
   }
+  if (threadIdx.x == 0 && sweeps != nullptr) sweeps[sd] = nsweeps;
   if (!converged_all) return;
   if (threadIdx.x == 0) {
     iters[2 * sd] = count[0];
@@ -843,18 +1024,19 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                const int32_t* c_on_lattice, double threshold, int use_threshold,
                                const int64_t* w_offsets, double* weights, double* smoothed_x,
                                double* smoothed_y, int32_t* iters, int32_t* nfixed,
-                               int32_t* status, double* max_udiff, void* stream) {
+                               int32_t* status, double* max_udiff, int32_t* sweeps,
+                               void* stream) {
   FI_REQUIRE(plan && cx && cy && ux && uy && counts && offsets && indices && mat_offsets &&
                  matrices && matrices32 && w_offsets && weights && smoothed_x &&
                  smoothed_y &&
                  iters && nfixed && status && max_udiff,
              "fi_tps_solve_mp: null pointer");
   FI_REQUIRE(nb_subdom > 0, "fi_tps_solve_mp: no subdomain");
+  FI_REQUIRE(((uintptr_t)matrices & 15) == 0 && ((uintptr_t)matrices32 & 15) == 0,
+             "fi_tps_solve_mp: matrices must be 16-byte aligned");
   const int N = max_members > 4 ? max_members : 4;
-  const size_t scratch = (size_t)(1 + MP_THREADS / 32) * 32 * 33 * sizeof(float);
-  const size_t lat = (size_t)N * sizeof(int2);
-  const size_t smem = (size_t)N * 11 * sizeof(double) + (size_t)N * 4 * sizeof(float) +
-                      (scratch > lat ? scratch : lat) + 64;
+  const MpLayout lay(N);
+  const size_t smem = lay.bytes;
   FI_REQUIRE(smem <= 220 * 1024, "fi_tps_solve_mp: subdomain of %d vectors too large",
              max_members);
   static size_t attr = 0;
@@ -865,7 +1047,7 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
   }
   k_tps_solve_mp<<<nb_subdom, MP_THREADS, smem, (cudaStream_t)stream>>>(
       plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
-      phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights, smoothed_x,
-      smoothed_y, iters, nfixed, status, max_udiff, 60);
+      phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights,
+      smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, 60, N);
   return check_launch("fi_tps_solve_mp");
 }

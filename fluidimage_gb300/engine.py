@@ -200,6 +200,7 @@ class TpsOutput:
     mp_status: object = None
     iters: object = None
     nfixed: object = None
+    mp_sweeps: object = None
     max_udiff: object = None
 
 
@@ -275,7 +276,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     ch, nch = both[:nsub], both[nsub:]
     off = np.concatenate([[0], np.cumsum(ch)[:-1]]).astype(np.int64)
     noff = np.concatenate([[0], np.cumsum(nch)[:-1]]).astype(np.int64)
-    msz = (ch + 3) ** 2
+    msz = ((ch + 3) ** 2 + 3) // 4 * 4  # offsets stay multiples of 4 (16-byte aligned)
     moff = np.concatenate([[0], np.cumsum(msz)[:-1]]).astype(np.int64)
     wsz = 2 * (ch + 3)
     woff = np.concatenate([[0], np.cumsum(wsz)[:-1]]).astype(np.int64)
@@ -305,6 +306,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     thr = float(threshold) if use_thr else 0.0
     table = phi_table(dev)
     status = torch.ones(nsub, **i32)
+    sweeps = torch.zeros(nsub, **i32)
     if int(ch.max()) <= MP_MAX_MEMBERS:
         matrices32 = torch.empty(int(msz.sum()), dtype=torch.float32, device=dev)
         with _timed("fi_tps_solve_mp"):
@@ -314,7 +316,8 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                 L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
                 thr, int(use_thr),
                 L.ptr(woff_d), L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
-                L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), s), "fi_tps_solve_mp")
+                L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), L.ptr(sweeps), s),
+                "fi_tps_solve_mp")
     # FP64 LU for the subdomains the mixed-precision solver flagged (or all of them)
     with _timed("fi_tps_solve"):
       L.check(lib.fi_tps_solve(L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux),
@@ -328,7 +331,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
         rx=torch.empty(npts, **i32), ry=torch.empty(npts, **i32), selection=sel,
         num_centers=nv, nb_subdom=nsub, counts=ch, w_offsets=woff, weights=weights,
         singular=singular, iters=iters, nfixed=nfixed, max_udiff=max_udiff,
-        mp_status=status,
+        mp_status=status, mp_sweeps=sweeps,
     )
     if want_smooth:
         out.smooth_x = torch.empty(nv, **f64)

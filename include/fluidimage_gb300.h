@@ -274,17 +274,19 @@ int fi_tps_phi_table(double* table, int64_t count, void* stream);
 
 /*
  * Mixed-precision TPS solve (same inputs and outputs as fi_tps_solve): null-space
- * form B z = Q2^T u with B = Q2^T (K + lam I) Q2 (projected in FP64) factorised
- * in FP32 (blocked Cholesky) and refined with FP64 residuals to ~1e-11 relative
- * (K from the phi table); the outlier iterations of
- * compute_tps_weights_iter (thin_plate_spline_subdom.py:236-280) warm-start from
- * the previous solution.  matrices: (n_i+3)^2 doubles at mat_offsets[i]
- * (K + lam I); matrices32: (n_i+3)^2 floats at mat_offsets[i] (the FP32 Cholesky
- * factor of the projected system, formed with the compact WY form of Q).
- * cxy2/c_on_lattice (nullable, fi_tps_lattice of the centres) give integer table
- * indices.  status[i] = 0 when
- * solved, 1 when the subdomain must go through fi_tps_solve (pass status as its
- * only_failed argument): rank-deficient P, Cholesky breakdown or no convergence.
+ * form B z = Q2^T u with B = Q2^T (K + lam I) Q2 (P = Q R, Householder; B projected
+ * in FP64 with the compact WY form of Q), factorised in FP32 (blocked Cholesky) and
+ * refined with double-float (pairs of floats) residuals g - B z; the affine part is
+ * a = R^-1 (Q1^T u - Q1^T A Q2 z).  K comes from the phi table.  The outlier
+ * iterations of compute_tps_weights_iter (thin_plate_spline_subdom.py:236-280)
+ * warm-start from the previous solution.  mat_offsets[i] must be multiples of 4 and
+ * both matrix buffers 16-byte aligned: matrices holds (n_i+3)^2 doubles at
+ * mat_offsets[i] (B as float pairs), matrices32 (n_i+3)^2 floats (its Cholesky
+ * factor).  cxy2/c_on_lattice (nullable, fi_tps_lattice of the centres) give
+ * integer table indices.  status[i] = 0 when solved, 1 when the subdomain must go
+ * through fi_tps_solve (pass status as its only_failed argument): rank-deficient P,
+ * Cholesky breakdown or no convergence.  sweeps (nullable, [nb_subdom]): refinement
+ * sweeps (one FP32 solve each) per subdomain.
  */
 int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
                     const double* cy, const float* ux, const float* uy, const int32_t* counts,
@@ -294,7 +296,7 @@ int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, con
                     double threshold, int use_threshold,
                     const int64_t* w_offsets, double* weights, double* smoothed_x,
                     double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
-                    double* max_udiff, void* stream);
+                    double* max_udiff, int32_t* sweeps, void* stream);
 
 /*
  * Smoothed values at the centres, blended over the subdomains that contain them
