@@ -131,38 +131,50 @@ __device__ __forceinline__ double block_reduce_d(double v, double* sh, bool is_m
   return v;
 }
 
+// Compaction of the valid vectors (no NaN component) in index order, limits and
+// subdomain layout; one block over tiles of 1024 consecutive vectors, the loads of
+// eight tiles issued before their block scans.
 __global__ void __launch_bounds__(1024)
     k_tps_plan(const float* xs, const float* ys, const float* dx, const float* dy, int nvec,
                int subdom_size, double smoothing_coef, double pct, fi_tps_plan* plan, double* cx,
                double* cy, float* ux, float* uy, int32_t* sel) {
+  constexpr int R = 8;
   __shared__ int warp_tot[33];
   __shared__ double red[33];
   double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
   int base = 0;
-  for (int c0 = 0; c0 < nvec; c0 += blockDim.x) {
-    const int i = c0 + threadIdx.x;
-    bool ok = false;
-    float vx = 0.f, vy = 0.f;
-    if (i < nvec) {
-      vx = dx[i];
-      vy = dy[i];
-      ok = !(isnan(vx) || isnan(vy));
+  for (int c0 = 0; c0 < nvec; c0 += R * 1024) {
+    float vx[R], vy[R], px[R], py[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = c0 + r * 1024 + threadIdx.x;
+      const bool in = i < nvec;
+      vx[r] = in ? dx[i] : NAN;
+      vy[r] = in ? dy[i] : NAN;
+      px[r] = in ? xs[i] : 0.f;
+      py[r] = in ? ys[i] : 0.f;
     }
-    int total;
-    const int pos = base + block_scan_flag(ok, warp_tot, &total);
-    if (ok) {
-      const double x = (double)xs[i], y = (double)ys[i];
-      cx[pos] = x;
-      cy[pos] = y;
-      ux[pos] = vx;
-      uy[pos] = vy;
-      if (sel) sel[pos] = i;
-      xmin = fmin(xmin, x);
-      xmax = fmax(xmax, x);
-      ymin = fmin(ymin, y);
-      ymax = fmax(ymax, y);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (c0 + r * 1024 >= nvec) break;  // uniform over the block
+      const int i = c0 + r * 1024 + threadIdx.x;
+      const bool ok = !(isnan(vx[r]) || isnan(vy[r]));
+      int total;
+      const int pos = base + block_scan_flag(ok, warp_tot, &total);
+      if (ok) {
+        const double x = (double)px[r], y = (double)py[r];
+        cx[pos] = x;
+        cy[pos] = y;
+        ux[pos] = vx[r];
+        uy[pos] = vy[r];
+        if (sel) sel[pos] = i;
+        xmin = fmin(xmin, x);
+        xmax = fmax(xmax, x);
+        ymin = fmin(ymin, y);
+        ymax = fmax(ymax, y);
+      }
+      base += total;
     }
-    base += total;
   }
   xmin = block_reduce_d(xmin, red, false);
   xmax = block_reduce_d(xmax, red, true);
@@ -221,12 +233,51 @@ __global__ void k_tps_lattice(const double* px, const double* py, int npts, int3
 
 __global__ void k_set_int(int32_t* p, int32_t v) { *p = v; }
 
+// Index over the points by tiles of YB_TILE: tile_pmax[j] = max of y over tiles
+// 0..j, tile_smin[j] = min over tiles j..end.  Both are monotone, so a y band
+// [lo, hi) can only hold points of tiles [first j with tile_pmax[j] >= lo, first j
+// with tile_smin[j] >= hi).
+constexpr int YB_TILE = 256;
+__global__ void __launch_bounds__(YB_TILE) k_y_tiles(const double* py, int n, double* tmax,
+                                                      double* tmin) {
+  __shared__ double red[33];
+  const int i = blockIdx.x * YB_TILE + threadIdx.x;
+  const double y = (i < n) ? py[i] : NAN;
+  const double mx = block_reduce_d(isnan(y) ? -INFINITY : y, red, true);
+  const double mn = block_reduce_d(isnan(y) ? INFINITY : y, red, false);
+  if (threadIdx.x == 0) {
+    tmax[blockIdx.x] = mx;
+    tmin[blockIdx.x] = mn;
+  }
+}
+
+// In place: running max forward, running min backward (one thread; tiles are few).
+__global__ void k_y_tiles_scan(int ntiles, double* tmax, double* tmin) {
+  if (threadIdx.x != 0) return;
+  for (int j = 1; j < ntiles; ++j) tmax[j] = fmax(tmax[j], tmax[j - 1]);
+  for (int j = ntiles - 2; j >= 0; --j) tmin[j] = fmin(tmin[j], tmin[j + 1]);
+}
+
+// First index q in [0, n) with a[q] >= v for a non-decreasing a (n if none).
+__device__ __forceinline__ int lower_bound_ge(const double* a, int n, double v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] >= v) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
 // Ordered membership of points in subdomain blockIdx.x; mode 0 counts, mode 1 fills.
+// With the tile index y_pmax / y_smin of py (k_y_tiles) only the tiles that can hold
+// the subdomain's y band are scanned.
 __global__ void __launch_bounds__(512)
     k_tps_members(const fi_tps_plan* plan_ptr, const double* px, const double* py, int npts,
                   int mode, int32_t* counts, const int64_t* offsets, int32_t* indices,
-                  double* coefs, const int32_t* xy2, const int32_t* on_lattice) {
+                  double* coefs, const int32_t* xy2, const int32_t* on_lattice,
+                  const double* y_pmax, const double* y_smin) {
   __shared__ int warp_tot[33];
+  __shared__ int s_range[2];
   const fi_tps_plan p = *plan_ptr;
   const int i = blockIdx.x;
   const int iy = i / p.nb_subdomx, ix = i % p.nb_subdomx;
@@ -236,12 +287,24 @@ __global__ void __launch_bounds__(512)
   const double kmax = 2147483647.0;
   const int X0 = (int)fmin(ceil(2.0 * L.lminx), kmax), X1 = (int)fmin(ceil(2.0 * L.lmaxx), kmax);
   const int Y0 = (int)fmin(ceil(2.0 * L.lminy), kmax), Y1 = (int)fmin(ceil(2.0 * L.lmaxy), kmax);
+  if (threadIdx.x == 0) {
+    int q0 = 0, q1 = npts;
+    if (y_pmax != nullptr && y_smin != nullptr) {
+      const int nt = (npts + YB_TILE - 1) / YB_TILE;
+      q0 = min(npts, YB_TILE * lower_bound_ge(y_pmax, nt, L.lminy));
+      q1 = max(q0, min(npts, YB_TILE * lower_bound_ge(y_smin, nt, L.lmaxy)));
+    }
+    s_range[0] = q0;
+    s_range[1] = q1;
+  }
+  __syncthreads();
+  const int qb = s_range[0], qe = s_range[1];
   int base = 0;
   const int64_t off = (mode == 1) ? offsets[i] : 0;
-  for (int c0 = 0; c0 < npts; c0 += blockDim.x) {
+  for (int c0 = qb; c0 < qe; c0 += blockDim.x) {
     const int q = c0 + threadIdx.x;
     bool in = false;
-    if (q < npts) {
+    if (q < qe) {
       if (lat) {
         const int X = xy2[2 * q], Y = xy2[2 * q + 1];
         in = X >= X0 && X < X1 && Y >= Y0 && Y < Y1;
@@ -638,16 +701,26 @@ extern "C" int fi_tps_lattice(const double* px, const double* py, int npts, int3
   return check_launch("fi_tps_lattice", 2);
 }
 
+extern "C" int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, double* y_smin,
+                               void* stream) {
+  FI_REQUIRE(py && y_pmax && y_smin && npts > 0, "fi_tps_y_bounds: bad arguments");
+  const int nt = (npts + YB_TILE - 1) / YB_TILE;
+  k_y_tiles<<<nt, YB_TILE, 0, (cudaStream_t)stream>>>(py, npts, y_pmax, y_smin);
+  k_y_tiles_scan<<<1, 32, 0, (cudaStream_t)stream>>>(nt, y_pmax, y_smin);
+  return check_launch("fi_tps_y_bounds", 2);
+}
+
 extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px,
                               const double* py, int npts, int mode, int32_t* counts,
                               const int64_t* offsets, int32_t* indices, double* coefs,
-                              const int32_t* xy2, const int32_t* on_lattice, void* stream) {
+                              const int32_t* xy2, const int32_t* on_lattice,
+                              const double* y_pmax, const double* y_smin, void* stream) {
   FI_REQUIRE(plan && px && py && nb_subdom > 0 && npts > 0, "fi_tps_members: bad arguments");
   FI_REQUIRE(mode == 0 ? counts != nullptr : (offsets && indices && coefs),
              "fi_tps_members: missing outputs");
   k_tps_members<<<nb_subdom, 512, 0, (cudaStream_t)stream>>>(plan, px, py, npts, mode, counts,
                                                             offsets, indices, coefs, xy2,
-                                                            on_lattice);
+                                                            on_lattice, y_pmax, y_smin);
   return check_launch("fi_tps_members");
 }
 

@@ -234,6 +234,16 @@ def lattice_coords(px, py, npts, stream=None):
     return xy2, flag
 
 
+def y_bounds(py, npts, stream=None):
+    """Prefix max / suffix min of py (fi_tps_y_bounds): index ranges for the
+    membership scans."""
+    torch = _torch()
+    out = torch.empty(2 * max(npts, 1), dtype=torch.float64, device=py.device)
+    L.check(L.load().fi_tps_y_bounds(L.ptr(py), npts, L.ptr(out), L.ptr(out[npts:]),
+                                     L.stream_handle(stream)), "fi_tps_y_bounds")
+    return out[:npts], out[npts:]
+
+
 def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
             threshold, want_smooth, stream, p_lattice=None):
     """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548).
@@ -265,13 +275,16 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
     cxy2, clat = lattice_coords(cx, cy, nv, stream)
     pxy2, plat = p_lattice if p_lattice is not None else lattice_coords(px, py, npts, stream)
+    cb0, cb1 = y_bounds(cy, nv, stream)
+    pb0, pb1 = y_bounds(py, npts, stream)
     counts = torch.empty(nsub, **i32)
     ncounts = torch.empty(nsub, **i32)
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 0, L.ptr(counts),
-                               None, None, None, L.ptr(cxy2), L.ptr(clat), s), "fi_tps_members")
+                               None, None, None, L.ptr(cxy2), L.ptr(clat), L.ptr(cb0),
+                               L.ptr(cb1), s), "fi_tps_members")
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 0,
-                               L.ptr(ncounts), None, None, None, L.ptr(pxy2), L.ptr(plat), s),
-            "fi_tps_members")
+                               L.ptr(ncounts), None, None, None, L.ptr(pxy2), L.ptr(plat),
+                               L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
     both = torch.cat([counts, ncounts]).cpu().numpy().astype(np.int64)
     ch, nch = both[:nsub], both[nsub:]
     off = np.concatenate([[0], np.cumsum(ch)[:-1]]).astype(np.int64)
@@ -289,10 +302,10 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     ncoefs = torch.empty(max(ntot, 1), **f64)
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 1, None,
                                L.ptr(off_d), L.ptr(idx), L.ptr(coefs), L.ptr(cxy2), L.ptr(clat),
-                               s), "fi_tps_members")
+                               L.ptr(cb0), L.ptr(cb1), s), "fi_tps_members")
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 1, None,
                                L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), L.ptr(pxy2),
-                               L.ptr(plat), s), "fi_tps_members")
+                               L.ptr(plat), L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
     matrices = torch.empty(int(msz.sum()), **f64)
     pivots = torch.empty(tot + 3 * nsub, **i32)
     weights = torch.empty(int(wsz.sum()), **f64)

@@ -233,17 +233,30 @@ int fi_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
                    int32_t* on_lattice, void* stream);
 
 /*
+ * Index over the points for fi_tps_members, by tiles of 256 consecutive points:
+ * y_pmax[j] = max of py over tiles 0..j, y_smin[j] = min over tiles j..end
+ * (ceil(npts / 256) doubles each).  Both are monotone, so the scan for a
+ * subdomain's y band covers only the tiles that can hold members (exact for any
+ * point order; a narrow band for row-ordered PIV grids).  No reference counterpart:
+ * an index that replaces the all-points scan of np.where in
+ * ThinPlateSplineSubdom (thin_plate_spline_subdom.py:107, 179).
+ */
+int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, double* y_smin, void* stream);
+
+/*
  * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
  * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
  * counts), the point indices and their norm coefficients
  * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 and
  * on_lattice from fi_tps_lattice (both nullable) the limit tests are exact integer
- * comparisons on the lattice.
+ * comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
+ * restrict the scan to the tiles that can hold members.
  */
 int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
                    int npts, int mode, int32_t* counts, const int64_t* offsets,
                    int32_t* indices, double* coefs, const int32_t* xy2,
-                   const int32_t* on_lattice, void* stream);
+                   const int32_t* on_lattice, const double* y_pmax, const double* y_smin,
+                   void* stream);
 
 /*
  * Per subdomain: build [[K + smoothing I, P], [P^T, 0]] (compute_tps_weights,

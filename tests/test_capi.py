@@ -65,7 +65,7 @@ def test_invalid_arguments_are_rejected_on_the_host(lib):
     assert lib.fi_images_min(None, None, 0, 10, None, None) == -1
     with pytest.raises(_lib.CudaLibError, match="bad arguments"):
         _lib.check(lib.fi_tps_members(None, 0, None, None, 0, 0, None, None, None, None, None,
-                                      None, None))
+                                      None, None, None, None))
 
 
 def test_version(lib):

@@ -185,3 +185,67 @@ def test_correl_plugin_per_window():
             tied = np.count_nonzero(norm_crop < 1e-5) >= 2
             tol = 5e-2 if tied else TOL_PX_TYPICAL
             np.testing.assert_allclose([sdx, sdy], z[tag + "_subpix"], atol=tol)
+
+
+@pytest.mark.parametrize("order", ["rows", "shuffled"])
+def test_members_index_range_matches_full_scan(order):
+    """fi_tps_members restricted by fi_tps_y_bounds gives the same ordered members as
+    the scan over every point, for row-ordered and for shuffled points (on and off
+    the half-integer lattice)."""
+    import ctypes as C
+
+    import torch
+
+    from fluidimage_gb300 import _lib as L, engine
+
+    lib = L.load()
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(5)
+    ny, nx = 70, 90
+    ys, xs = np.meshgrid(np.arange(ny) * 8.0 + 4.0, np.arange(nx) * 8.0 + 4.0, indexing="ij")
+    xs = (xs + rng.integers(0, 2, xs.shape) * 0.5).ravel()
+    ys = (ys + rng.integers(0, 2, ys.shape) * 0.5).ravel()
+    if order == "shuffled":
+        perm = rng.permutation(xs.size)
+        xs, ys = xs[perm], ys[perm]
+    dx = rng.normal(0, 1, xs.size).astype(np.float32)
+    dy = rng.normal(0, 1, xs.size).astype(np.float32)
+    dx[rng.random(xs.size) < 0.05] = np.nan
+    f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)  # noqa: E731
+    tx, ty, tdx, tdy = f32(xs), f32(ys), f32(dx), f32(dy)
+    n = xs.size
+    plan = torch.empty(C.sizeof(L.TpsPlan), dtype=torch.uint8, device=dev)
+    cx = torch.empty(n, dtype=torch.float64, device=dev)
+    cy = torch.empty(n, dtype=torch.float64, device=dev)
+    ux = torch.empty(n, dtype=torch.float32, device=dev)
+    uy = torch.empty(n, dtype=torch.float32, device=dev)
+    sel = torch.empty(n, dtype=torch.int32, device=dev)
+    L.check(lib.fi_tps_plan_make(L.ptr(tx), L.ptr(ty), L.ptr(tdx), L.ptr(tdy), n, 200, 0.5, 20.0,
+                                 L.ptr(plan), L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
+                                 L.ptr(sel), None), "plan")
+    hdr = L.TpsPlan.from_buffer_copy(plan.cpu().numpy().tobytes())
+    nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
+    assert nsub > 20
+    for lattice in (True, False):
+        xy2, flag = engine.lattice_coords(cx, cy, nv) if lattice else (None, None)
+        b0, b1 = engine.y_bounds(cy, nv)
+        res = []
+        for bounded in (False, True):
+            cnt = torch.empty(nsub, dtype=torch.int32, device=dev)
+            args = (L.ptr(xy2), L.ptr(flag)) if lattice else (None, None)
+            bargs = (L.ptr(b0), L.ptr(b1)) if bounded else (None, None)
+            L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 0, L.ptr(cnt),
+                                       None, None, None, *args, *bargs, None), "count")
+            ch = cnt.cpu().numpy().astype(np.int64)
+            off = torch.from_numpy(np.concatenate([[0], np.cumsum(ch)[:-1]])).to(dev)
+            idx = torch.empty(int(ch.sum()), dtype=torch.int32, device=dev)
+            coefs = torch.empty(int(ch.sum()), dtype=torch.float64, device=dev)
+            L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 1, None,
+                                       L.ptr(off), L.ptr(idx), L.ptr(coefs), *args, *bargs, None),
+                    "fill")
+            torch.cuda.synchronize()
+            res.append((ch, idx.cpu().numpy(), coefs.cpu().numpy()))
+        np.testing.assert_array_equal(res[0][0], res[1][0])
+        np.testing.assert_array_equal(res[0][1], res[1][1])
+        np.testing.assert_array_equal(res[0][2], res[1][2])
+        assert res[0][0].sum() > nv  # buffers overlap: points in several subdomains
