@@ -30,6 +30,7 @@ ERR_NAN = 2
 ERR_WRONG_SUBPIX = 3
 ERR_BAD_CROP = 4
 ERR_ALL_NAN = 5
+ERR_CLOSE_BOUNDARY = 6
 
 ERROR_STRINGS = {
     ERR_BOUNDARY: "Correlation peak touching boundary.",
@@ -37,6 +38,7 @@ ERROR_STRINGS = {
     ERR_WRONG_SUBPIX: "wrong subpix",
     ERR_BAD_CROP: "Bad im_crop shape.",
     ERR_ALL_NAN: "Correlation plane without any finite value.",
+    ERR_CLOSE_BOUNDARY: "close boundary",
 }
 
 _F32_1EM8 = np.float32(1e-8)
@@ -290,7 +292,7 @@ def _correl_max(planes, i0, i1, norms):
 # a10: second-chance search — correl.py:226-275 and CorrelFFTBase :561-568
 # ----------------------------------------------------------------------------------
 def displacements_from_correl(planes, norms, shape_crop, displacement_max=None,
-                              particle_radius=3):
+                              particle_radius=3, nb_peaks=1):
     """Batched ``compute_displacements_from_correl`` for the FFT correlation classes.
 
     ``planes`` is modified in place exactly like the upstream per-window call: when
@@ -327,7 +329,47 @@ def displacements_from_correl(planes, norms, shape_crop, displacement_max=None,
         err[retry] = err2
     dx = ix0 - i1
     dy = iy0 - i0
-    return dx, dy, cmax, err, i0, i1
+    if nb_peaks <= 1:
+        return dx, dy, cmax, err, i0, i1
+    other = secondary_peaks(work, norms, err, i0, i1, shape_crop, box0, box1, nb_peaks,
+                            particle_radius)
+    return dx, dy, cmax, err, i0, i1, other
+
+
+def secondary_peaks(work, norms, err, i0, i1, shape_crop, box0, box1, nb_peaks,
+                    particle_radius=3):
+    """Other peaks of ``compute_displacements_from_correl`` (correl.py:250-273).
+
+    For each window whose search did not raise, NaN boxes of ``particle_radius``
+    around the last peak found (on a copy of the searched plane, which holds the
+    displacement mask and the second-chance box) and a new search, up to
+    ``nb_peaks - 1`` times, stopping at the first search that raises.  Returns a
+    list with None for the windows whose search raised, else a list of
+    ``(dx, dy, correl_max)`` (integers, float32).  A plane without any finite value
+    left stops the search (upstream's assert in nan_indices_max).
+    """
+    nvec, n0, n1 = work.shape
+    iy0, ix0 = indices_no_displacement(shape_crop)
+    r = particle_radius
+    out = [None] * nvec
+    for k in range(nvec):
+        if err[k] != 0:
+            continue
+        c = work[k].copy()
+        a0, a1 = int(i0[k]), int(i1[k])
+        peaks = []
+        for _ in range(nb_peaks - 1):
+            sy, ey = _slice_bounds(a0 - r, a0 + r + 1, n0)
+            sx, ex = _slice_bounds(a1 - r, a1 + r + 1, n1)
+            c[int(sy):int(ey), int(sx):int(ex)] = np.nan
+            j0, j1, e = nan_indices_max(c[None], box0, box1)
+            if e[0] != 0:
+                break
+            a0, a1 = int(j0[0]), int(j1[0])
+            cm = _correl_max(c[None], j0, j1, norms[k:k + 1])[0]
+            peaks.append((ix0 - a1, iy0 - a0, cm))
+        out[k] = peaks
+    return out
 
 
 # ----------------------------------------------------------------------------------
@@ -408,12 +450,74 @@ def subpix_2d_gaussian2(planes, i0, i1, shape_crop):
     return dx, dy, wrong
 
 
+SUBPIX_METHODS = ("2d_gaussian", "2d_gaussian2", "centroid", "no_subpix")
+
+
+def subpix_setup(nsubpix):
+    """``SubPix.prepare_subpix`` (subpix.py:86-105): half width, centroid grids and the
+    pseudo-inverse used by '2d_gaussian'."""
+    n = 1 if nsubpix is None else int(nsubpix)
+    xs = np.arange(-n, n + 1, dtype=float)
+    X, Y = np.meshgrid(xs, xs)
+    Xr, Yr = X.ravel(), Y.ravel()
+    M = np.reshape(np.concatenate((Xr**2, Yr**2, Xr, Yr, np.ones(Xr.size))), (5, Xr.size)).T
+    return n, X, Y, np.linalg.pinv(M)
+
+
+def subpix_one(plane, i0, i1, shape_crop, method, nsubpix=None):
+    """``apply_subpix`` / ``SubPix.compute_subpix`` on one plane (correl.py:277-281,
+    subpix.py:107-218), any method.  Returns ``(dx, dy, err)``; on an error
+    (ERR_WRONG_SUBPIX, ERR_CLOSE_BOUNDARY) the integer displacement."""
+    n, X, Y, Minv = subpix_setup(nsubpix)
+    iy0, ix0 = indices_no_displacement(shape_crop)
+    ny, nx = plane.shape
+
+    def run(meth):
+        if i0 - n < 0 or i0 + n + 1 > ny or i1 - n < 0 or i1 + n + 1 > nx:
+            return None, ERR_CLOSE_BOUNDARY
+        with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+            if meth == "2d_gaussian":
+                crop = plane[i0 - n:i0 + n + 1, i1 - n:i1 + n + 1]
+                cmap = crop.ravel().copy()
+                cmap[cmap <= 0.0] = 1e-6
+                coef = np.dot(Minv, np.log(cmap))
+                if coef[0] > 0 or coef[1] > 0:
+                    return run("centroid")
+                sigmax = 1 / np.sqrt(-2 * coef[0])
+                sigmay = 1 / np.sqrt(-2 * coef[1])
+                deplx = coef[2] * sigmax**2
+                deply = coef[3] * sigmay**2
+                if np.isnan(deplx) or np.isnan(deply):
+                    return run("centroid")
+            elif meth == "2d_gaussian2":
+                gx, gy = _gaussian2(plane[None, i0 - 1:i0 + 2, i1 - 1:i1 + 2])
+                deplx, deply = gx[0], gy[0]
+            elif meth == "centroid":
+                crop = plane[i0 - n:i0 + n + 1, i1 - n:i1 + n + 1]
+                s = np.sum(crop)
+                deplx = np.sum(X * crop) / s
+                deply = np.sum(Y * crop) / s
+            else:
+                deplx = deply = 0.0
+            if deplx**2 + deply**2 > 2 * (0.5 + n) ** 2:
+                if meth == "2d_gaussian2":
+                    return run("centroid")
+                return None, ERR_WRONG_SUBPIX
+        return (deplx + i1, deply + i0), 0
+
+    res, err = run(method)
+    if err:
+        return float(ix0 - i1), float(iy0 - i0), err
+    return ix0 - res[0], iy0 - res[1], 0
+
+
 # ----------------------------------------------------------------------------------
 # a12 / a15: one PIV pass — singlepass.py:262-361 and :733-785
 # ----------------------------------------------------------------------------------
 def piv_pass(im0, im1, shape_crop, overlap, *, grid=None, dxin=None, dyin=None,
              apply_subpix=True, displacement_max=None, particle_radius=3,
-             dtype_complex=np.complex64, keep_planes=False):
+             dtype_complex=np.complex64, keep_planes=False, method_subpix="2d_gaussian2",
+             nsubpix=None, nb_peaks_to_search=1):
     """One pass.  Returns a namespace with the ``HeavyPIVResults`` fields."""
     shape_crop = tuple(int(n) for n in shape_crop)
     if grid is None:
@@ -438,22 +542,35 @@ def piv_pass(im0, im1, shape_crop, overlap, *, grid=None, dxin=None, dyin=None,
     correls_max = np.full(nvec, np.nan, dtype=np.float32)
     err = np.full(nvec, ERR_BAD_CROP, dtype=np.uint8)
     planes_all = None
+    secondary = [None] * nvec
 
     iv = np.nonzero(valid)[0]
     if iv.size:
         planes, norms = correl_fft(w0[iv], w1[iv], dtype_complex)
-        dx, dy, cmax, e, i0, i1 = displacements_from_correl(
-            planes, norms, shape_crop, dmax, particle_radius
+        out = displacements_from_correl(
+            planes, norms, shape_crop, dmax, particle_radius, nb_peaks_to_search
         )
+        dx, dy, cmax, e, i0, i1 = out[:6]
+        if nb_peaks_to_search > 1:
+            for j, k in enumerate(iv):
+                secondary[k] = out[6][j]
         fdx = dx.astype(np.float32)
         fdy = dy.astype(np.float32)
         ok = e == 0
         if apply_subpix and ok.any():
             k = np.nonzero(ok)[0]
-            sdx, sdy, wrong = subpix_2d_gaussian2(planes[k], i0[k], i1[k], shape_crop)
-            fdx[k] = sdx
-            fdy[k] = sdy
-            e[k[wrong]] = ERR_WRONG_SUBPIX
+            if method_subpix == "2d_gaussian2":
+                sdx, sdy, wrong = subpix_2d_gaussian2(planes[k], i0[k], i1[k], shape_crop)
+                fdx[k] = sdx
+                fdy[k] = sdy
+                e[k[wrong]] = ERR_WRONG_SUBPIX
+            else:
+                for kk in k:
+                    a, b, ee = subpix_one(planes[kk], int(i0[kk]), int(i1[kk]), shape_crop,
+                                          method_subpix, nsubpix)
+                    fdx[kk] = a
+                    fdy[kk] = b
+                    e[kk] = ee
         deltaxs[iv] = fdx
         deltays[iv] = fdy
         correls_max[iv] = cmax
@@ -470,7 +587,8 @@ def piv_pass(im0, im1, shape_crop, overlap, *, grid=None, dxin=None, dyin=None,
         deltaxs=deltaxs, deltays=deltays, xs=xs, ys=ys, correls_max=correls_max,
         errors=errors, err=err, ixvecs=ixvecs, iyvecs=iyvecs, ixvecs_grid=gx,
         iyvecs_grid=gy, planes=planes_all, shape_crop=shape_crop,
-        deltaxs_input=dxin, deltays_input=dyin,
+        deltaxs_input=dxin, deltays_input=dyin, secondary_peaks=secondary,
+        nb_peaks_to_search=nb_peaks_to_search, method_subpix=method_subpix, nsubpix=nsubpix,
     )
 
 
@@ -552,7 +670,12 @@ def mean_neighbors_xy(deltaxs, deltays, ny, nx):
 
 
 def fix(result, correl_min=0.2, threshold_diff_neighbour=10, displacement_max=None):
-    """``WorkFIX.calcul`` without secondary peaks (fix.py:66-133); in place."""
+    """``WorkFIX.calcul`` (fix.py:66-243); in place.
+
+    With ``result.nb_peaks_to_search >= 2`` the secondary peaks replace a vector when
+    one lies closer to the neighbour mean (fix.py:135-236); this needs the planes
+    (``result.planes``) for the subpixel fit of the chosen peak.
+    """
     deltaxs = result.deltaxs
     deltays = result.deltays
     errors = result.errors
@@ -581,6 +704,7 @@ def fix(result, correl_min=0.2, threshold_diff_neighbour=10, displacement_max=No
         with np.errstate(invalid="ignore"):
             inds = ((deltaxs**2 + deltays**2) > displacement_max**2).nonzero()[0]
         put_to_nan(inds, "delta2 < displacement_max2")
+    d2 = mx = my = None
     if threshold_diff_neighbour is not None:
         ny, nx = len(result.iyvecs), len(result.ixvecs)
         mx, my = mean_neighbors_xy(deltaxs, deltays, ny, nx)
@@ -592,6 +716,62 @@ def fix(result, correl_min=0.2, threshold_diff_neighbour=10, displacement_max=No
             errors[ivec] += f" (diff = {math.sqrt(d2[ivec]):.2f})"
         result.deltaxs_wrong = wrong_x
         result.deltays_wrong = wrong_y
+    if getattr(result, "nb_peaks_to_search", 1) < 2:
+        return result
+    # secondary peaks (fix.py:135-236)
+    ratio = np.float32(0.6)
+    cmin32 = np.float32(correl_min)
+    replaced = {}
+    for ivec, other in enumerate(result.secondary_peaks):
+        if not other:
+            continue
+        correl0 = result.correls_max[ivec]
+        if result.deltaxs_input is not None:
+            dxi = int(result.deltaxs_input[ivec])
+            dyi = int(result.deltays_input[ivec])
+        else:
+            dxi = dyi = 0
+        good = []
+        with np.errstate(invalid="ignore", divide="ignore"):
+            for dx, dy, corr in other:
+                if np.float32(corr) / correl0 > ratio and np.float32(corr) > cmin32:
+                    good.append((int(dx) + dxi, int(dy) + dyi, np.float32(corr)))
+        if not good:
+            continue
+        if d2 is None:
+            raise NameError("name 'differences2' is not defined")
+        dn = np.empty(len(good) + 1)
+        dn[0] = math.sqrt(d2[ivec]) if not np.isnan(d2[ivec]) else np.nan
+        for i, (dx, dy, corr) in enumerate(good):
+            dn[i + 1] = np.sqrt((float(mx[ivec]) - dx) ** 2 + (float(my[ivec]) - dy) ** 2)
+        am = int(np.argmin(dn))
+        if am == 0:
+            continue
+        dx, dy, corr = good[am - 1]
+        if threshold_diff_neighbour is not None and dn[am] > threshold_diff_neighbour:
+            continue
+        if displacement_max and dx**2 + dy**2 > displacement_max:
+            continue
+        iy0, ix0 = indices_no_displacement(result.shape_crop)
+        # upstream's peak indices are Python ints on the first pass and int32 after
+        # (deltaxs_input is an int32 array): the subpixel sums are then float64
+        cast = int if result.deltaxs_input is None else np.int32
+        sdx, sdy, e = subpix_one(result.planes[ivec], cast(iy0 - (dy - dyi)),
+                                 cast(ix0 - (dx - dxi)), result.shape_crop,
+                                 result.method_subpix, result.nsubpix)
+        if e:
+            continue
+        ndx, ndy = sdx + dxi, sdy + dyi
+        old = (wrong_x.get(ivec, deltaxs[ivec]), wrong_y.get(ivec, deltays[ivec]),
+               result.correls_max[ivec])
+        replaced[ivec] = old
+        deltaxs[ivec] = ndx
+        deltays[ivec] = ndy
+        result.correls_max[ivec] = corr
+        if ivec in errors:
+            del wrong_x[ivec], wrong_y[ivec], errors[ivec]
+    if replaced:
+        result.replaced_vectors = replaced
     return result
 
 
@@ -862,13 +1042,18 @@ def multipass(im0, im1, params, dtype_complex=np.complex64, keep_planes=False):
     grids = [make_grid(im0.shape, s, p0.grid.overlap) for s in shapes]
     results = []
     prev = None
+    nb_peaks = int(getattr(p0, "nb_peaks_to_search", 1))
+    extra = dict(method_subpix=getattr(p0, "method_subpix", "2d_gaussian2"),
+                 nsubpix=getattr(p0, "nsubpix", None), nb_peaks_to_search=nb_peaks)
+    keep = keep_planes or nb_peaks > 1
     for ip, shape in enumerate(shapes):
         subpix = ip == mp.number - 1
         if ip == 0:
             res = piv_pass(im0, im1, shape, p0.grid.overlap, grid=grids[ip],
                            apply_subpix=subpix, displacement_max=p0.displacement_max,
                            particle_radius=p0.particle_radius,
-                           dtype_complex=dtype_complex, keep_planes=keep_planes)
+                           dtype_complex=dtype_complex, keep_planes=keep,
+                           **extra)
         else:
             apply_interp(prev, grids[ip], mp)
             dxin = np.round(prev.deltaxs_approx).astype("int32")
@@ -877,7 +1062,7 @@ def multipass(im0, im1, params, dtype_complex=np.complex64, keep_planes=False):
                            dxin=dxin, dyin=dyin, apply_subpix=subpix,
                            displacement_max=p0.displacement_max,
                            particle_radius=p0.particle_radius,
-                           dtype_complex=dtype_complex, keep_planes=keep_planes)
+                           dtype_complex=dtype_complex, keep_planes=keep, **extra)
         fix(res, fx.correl_min, fx.threshold_diff_neighbour, fx.displacement_max)
         results.append(res)
         prev = res

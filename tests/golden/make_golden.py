@@ -82,6 +82,21 @@ def run_workpiv(name, im0, im1, settings, keep_planes=False):
         for key in ("deltaxs_wrong", "deltays_wrong"):
             if hasattr(r, key):
                 _encode_dict(f"p{ip}_{key}", getattr(r, key), out)
+        sec = getattr(r, "secondary_peaks", None)
+        if sec is not None and any(o is not None for o in sec):
+            counts = np.array([-1 if o is None else len(o) for o in sec], dtype=np.int64)
+            flat = [p for o in sec if o for p in o]
+            out[f"p{ip}_secondary_counts"] = counts
+            out[f"p{ip}_secondary_peaks"] = np.array(
+                [[float(a), float(b), float(c)] for a, b, c in flat], dtype=np.float64
+            ).reshape(-1, 3)
+        rep = getattr(r, "replaced_vectors", None)
+        if rep is not None:
+            keys = np.array(sorted(rep), dtype=np.int64)
+            out[f"p{ip}_replaced_keys"] = keys
+            out[f"p{ip}_replaced_vals"] = np.array(
+                [[float(v) for v in rep[int(k)]] for k in keys], dtype=np.float64
+            ).reshape(-1, 3)
         if keep_planes:
             n0, n1 = work_piv.shape_crop_im0
             planes = np.full((len(r.correls), n0, n1), np.nan, dtype=np.float32)
@@ -202,6 +217,43 @@ def case_griddata():
     })
 
 
+def case_secondary_peaks():
+    """nb_peaks_to_search=3 with WorkFIX secondary-peak replacement, two passes with
+    TPS (16 -> 8 px windows), an Oseen vortex and a band of strong image noise in
+    im1 (spurious main peaks, the true peak second)."""
+    model = synthetic.ParticleModel(density=0.05, noise=4.0, dtype="uint8")
+    field = synthetic.oseen_vortex((160, 192), d_max=5.0, rc=40.0)
+    im0, im1 = synthetic.make_pair((160, 192), field, model, seed=6000)
+    rng = np.random.default_rng(1)
+    band = im1[40:100].astype(np.float64) + rng.normal(0.0, 120.0, im1[40:100].shape)
+    im1[40:100] = np.clip(np.round(band), 0, 255).astype(np.uint8)
+    run_workpiv("secondary_peaks_two_pass", im0, im1, {
+        "piv0.shape_crop_im0": 16, "piv0.grid.overlap": 0.5,
+        "piv0.nb_peaks_to_search": 3,
+        "multipass.number": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 100, "multipass.smoothing_coef": 2.0,
+        "fix.threshold_diff_neighbour": 2.5, "fix.correl_min": 0.1,
+        "fix.displacement_max": 9,
+    }, keep_planes=True)
+
+
+def case_subpix_methods():
+    """The other subpixel methods in one pass each: '2d_gaussian', 'centroid' with
+    nsubpix=2 (close-boundary errors near the plane edges), 'no_subpix'."""
+    model = synthetic.ParticleModel(density=0.05, noise=3.0, dtype="uint8")
+    field = synthetic.oseen_vortex((128, 160), d_max=6.0, rc=40.0)
+    im0, im1 = synthetic.make_pair((128, 160), field, model, seed=7000)
+    for tag, method, nsub in (("gaussian", "2d_gaussian", None),
+                              ("centroid2", "centroid", 2),
+                              ("none", "no_subpix", None)):
+        run_workpiv(f"subpix_{tag}_single", im0, im1, {
+            "piv0.shape_crop_im0": 16, "piv0.grid.overlap": 0.5,
+            "piv0.method_subpix": method, "piv0.nsubpix": nsub,
+            "multipass.number": 1, "multipass.use_tps": False,
+            "fix.threshold_diff_neighbour": None,
+        }, keep_planes=True)
+
+
 CASES = {
     "correl_window": case_correl_window,
     "single_pass_c1": case_single_pass_c1,
@@ -209,6 +261,8 @@ CASES = {
     "dmax_two_pass": case_dmax,
     "edges_single_pass": case_edges,
     "griddata_two_pass": case_griddata,
+    "secondary_peaks_two_pass": case_secondary_peaks,
+    "subpix_methods": case_subpix_methods,
 }
 
 if __name__ == "__main__":

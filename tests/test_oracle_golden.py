@@ -138,3 +138,31 @@ def test_fft_energy_parseval():
     np.testing.assert_allclose(norms, (wc.astype(np.float64) ** 2).sum(axis=(1, 2)),
                                rtol=5e-5)
     np.testing.assert_allclose(planes.max(axis=(1, 2)) / norms, 1.0, rtol=5e-5)
+
+
+def test_secondary_peaks_and_replacements_bit_exact(golden_run):
+    """nb_peaks_to_search >= 2: the other peaks of every window and the vectors
+    WorkFIX replaced by one of them (with their old values)."""
+    z, results = golden_run
+    for ip, r in enumerate(results):
+        if f"p{ip}_secondary_counts" in z.files:
+            counts = np.array([-1 if o is None else len(o) for o in r.secondary_peaks])
+            _eq(counts, z[f"p{ip}_secondary_counts"])
+            flat = [p for o in r.secondary_peaks if o for p in o]
+            _eq(np.array(flat, dtype=np.float64).reshape(-1, 3), z[f"p{ip}_secondary_peaks"])
+        if f"p{ip}_replaced_keys" in z.files:
+            rep = getattr(r, "replaced_vectors", {})
+            _eq(sorted(rep), z[f"p{ip}_replaced_keys"])
+            _eq([[float(v) for v in rep[k]] for k in sorted(rep)], z[f"p{ip}_replaced_vals"])
+        else:
+            assert not getattr(r, "replaced_vectors", {})
+
+
+def test_new_fixtures_exercise_the_options():
+    """The secondary-peak fixture replaces vectors in both passes; the subpixel
+    fixtures hit close-boundary and wrong-subpix errors."""
+    z = goldens.load("secondary_peaks_two_pass")
+    assert z["p0_replaced_keys"].size > 0 and z["p1_replaced_keys"].size > 0
+    z = goldens.load("subpix_centroid2_single")
+    vals = [str(v) for v in z["p0_errors_vals"]]
+    assert "close boundary" in vals and "wrong subpix" in vals
