@@ -20,14 +20,22 @@ VEC_PEAK_NAN = 2
 VEC_WRONG_SUBPIX = 3
 VEC_BAD_CROP = 4
 VEC_ALL_NAN = 5
+VEC_CLOSE_BOUNDARY = 6
 
 FLAG_NEAR_TIE = 1
 FLAG_SUBPIX_TIE = 2
+FLAG_SECONDARY_TIE = 4
 
 FIX_CORREL_MIN = 1
 FIX_DISPLACEMENT = 2
 FIX_NEIGHBOUR = 4
+FIX_REPLACED = 8
 FIX_STATIC_MAX_VECTORS = 262144
+
+SUBPIX_METHODS = {"2d_gaussian2": 0, "2d_gaussian": 1, "centroid": 2, "no_subpix": 3}
+MAX_NSUBPIX = 4
+MAX_PEAKS = 4
+PEAK_FIELDS = 5
 
 P = C.c_void_p
 
@@ -41,6 +49,8 @@ class PivPassArgs(C.Structure):
         ("box_i1_stop", C.c_int), ("particle_radius", C.c_int), ("apply_subpix", C.c_int),
         ("deltaxs", P), ("deltays", P), ("correls_max", P), ("errors", P), ("xs", P),
         ("ys", P), ("norms", P), ("planes", P), ("flags", P),
+        ("subpix_method", C.c_int), ("nsubpix", C.c_int), ("subpix_minv", P),
+        ("nb_peaks", C.c_int), ("peaks_count", P), ("peaks", P), ("peaks_err", P),
     ]
 
 
@@ -50,6 +60,10 @@ class FixArgs(C.Structure):
         ("errors", P), ("correl_min", C.c_float), ("use_displacement_max", C.c_int),
         ("displacement_max", C.c_float), ("use_threshold", C.c_int), ("threshold", C.c_float),
         ("deltaxs_out", P), ("deltays_out", P), ("fix_flags", P), ("diff2", P), ("work", P),
+        ("nb_peaks", C.c_int), ("peaks_count", P), ("peaks", P), ("peaks_err", P),
+        ("dxin", P), ("dyin", P),
+        ("threshold64", C.c_double), ("displacement_max64", C.c_double),
+        ("correls_max_out", P), ("replaced", P),
     ]
 
 

@@ -187,7 +187,7 @@ __device__ __forceinline__ Peak gpeak(Peak p, int g, double* red) {
   return p;
 }
 
-// Rectangle of virtual NaNs written by the second-chance search.
+// Rectangle of virtual NaNs (numpy slice semantics, possibly empty).
 struct NanBox {
   int r0, r1, c0, c1;
   __device__ __forceinline__ bool has(int i0, int i1) const {
@@ -195,8 +195,32 @@ struct NanBox {
   }
 };
 
+// The NaN boxes written by the peak searches: the second-chance box, then one box
+// per secondary search (on upstream's copy of the plane).
+struct NanBoxes {
+  NanBox b[FI_MAX_PEAKS];
+  int n;
+  __device__ __forceinline__ bool has(int i0, int i1) const {
+    bool h = false;
+#pragma unroll
+    for (int k = 0; k < FI_MAX_PEAKS; ++k) h |= (k < n) && b[k].has(i0, i1);
+    return h;
+  }
+  __device__ __forceinline__ void add(int i0, int i1, int radius, int N) {
+    int r0, r1, c0, c1;
+    slice_bounds(i0 - radius, i0 + radius + 1, N, &r0, &r1);
+    slice_bounds(i1 - radius, i1 + radius + 1, N, &c0, &c1);
+    if (!(r1 > r0 && c1 > c0) || n >= FI_MAX_PEAKS) return;
+    const NanBox nb{r0, r1, c0, c1};
+#pragma unroll
+    for (int k = 0; k < FI_MAX_PEAKS; ++k)  // static indices keep the boxes in registers
+      if (k == n) b[k] = nb;
+    ++n;
+  }
+};
+
 template <int N>
-__device__ __forceinline__ bool excluded(const float* PL, const uint8_t* mask, const NanBox& nb,
+__device__ __forceinline__ bool excluded(const float* PL, const uint8_t* mask, const NanBoxes& nb,
                                          int i0, int i1) {
   if (mask && __ldg(mask + i0 * N + i1)) return true;
   if (nb.has(i0, i1)) return true;
@@ -224,7 +248,7 @@ struct SearchBox {
 // nan_indices_max + _compute_indices_max on the group's plane (correl.py:88-164).
 template <int N>
 __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchBox& box,
-                             const NanBox& nb, double norm, int t, int g, double* red) {
+                             const NanBoxes& nb, double norm, int t, int g, double* red) {
   using C = Cfg<N>;
   Peak p{-INFINITY, -1, -INFINITY};
   if (t < N && t >= box.i1s && t < box.i1e) {
@@ -268,10 +292,10 @@ __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchB
 }
 
 // compute_subpix_2d_gaussian2 (subpix.py:16-61) in float32 with the upstream
-// operation order, then the centroid fallback of SubPix.compute_subpix
-// (subpix.py:184-216).  Returns 0 or FI_VEC_WRONG_SUBPIX; (dx, dy) displacement.
-__device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix0, int iy0,
-                                     float* dxo, float* dyo, bool* min_tie) {
+// operation order.  False when |depl|^2 > 4.5 (upstream then falls back to the
+// centroid).
+__device__ bool gauss2_depl(const float (&c)[9], float* deplx_o, float* deply_o,
+                            bool* min_tie) {
   float n[9];
   float cmin = c[0];
 #pragma unroll
@@ -313,8 +337,18 @@ __device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix
       __fdiv_rn(__fsub_rn(__fmul_rn(c11, c01), __fmul_rn(__fmul_rn(2.f, c10), c02)), den);
   const float deply =
       __fdiv_rn(__fsub_rn(__fmul_rn(c11, c10), __fmul_rn(__fmul_rn(2.f, c01), c20)), den);
+  *deplx_o = deplx;
+  *deply_o = deply;
   const float r2 = __fadd_rn(__fmul_rn(deplx, deplx), __fmul_rn(deply, deply));
-  if (!(r2 > 4.5f)) {
+  return !(r2 > 4.5f);
+}
+
+// '2d_gaussian2' with the centroid fallback on a 3x3 crop (subpix.py:184-216).
+// Returns 0 or FI_VEC_WRONG_SUBPIX; (dx, dy) displacement.
+__device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix0, int iy0,
+                                     float* dxo, float* dyo, bool* min_tie) {
+  float deplx, deply;
+  if (gauss2_depl(c, &deplx, &deply, min_tie)) {
     *dxo = __fsub_rn((float)ix0, __fadd_rn(deplx, (float)i1));
     *dyo = __fsub_rn((float)iy0, __fadd_rn(deply, (float)i0));
     return FI_VEC_OK;
@@ -343,26 +377,107 @@ __device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix
   return FI_VEC_OK;
 }
 
-template <int N>
-__device__ int subpix_gaussian2(const float* PL, int i0, int i1, float* dxo, float* dyo) {
-  float c[9];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = 0; b < 3; ++b) c[3 * a + b] = PL[(i0 - 1 + a) * Cfg<N>::LDP + (i1 - 1 + b)];
+// Subpixel fit with any method (SubPix.compute_subpix, subpix.py:107-218) at the
+// peak (i0, i1) of the plane; cbox: values inside read as NaN (the second-chance
+// box that upstream writes into the caller's plane).  Outputs the displacement as
+// upstream computes it with Python-int peak indices (d32: float32 for
+// '2d_gaussian2', else the float64 value rounded) and with int32 indices (d64:
+// float64, the '2d_gaussian2' offset promoted).  Returns 0, FI_VEC_WRONG_SUBPIX or
+// FI_VEC_CLOSE_BOUNDARY (then the integer displacement).
+struct SubpixOut {
+  float dx32, dy32;
+  double dx64, dy64;
   bool tie;
-  return subpix_gaussian2_vals(c, i0, i1, N / 2 - 1, N / 2 - 1, dxo, dyo, &tie);
-}
+};
 
 template <int N>
-__device__ int subpix_gaussian2_tie(const float* PL, int i0, int i1, float* dxo, float* dyo,
-                                    bool* tie) {
-  float c[9];
+__device__ int subpix_any(const float* PL, int i0, int i1, int method, int nsub,
+                          const double* minv, const NanBox& cbox, SubpixOut* o) {
+  const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
+  const int n = (method == FI_SUBPIX_GAUSSIAN2) ? 1 : nsub;
+  o->tie = false;
+  auto integer = [&](int err) {
+    o->dx32 = (float)(ix0 - i1);
+    o->dy32 = (float)(iy0 - i0);
+    o->dx64 = (double)(ix0 - i1);
+    o->dy64 = (double)(iy0 - i0);
+    return err;
+  };
+  if (i0 - n < 0 || i0 + n + 1 > N || i1 - n < 0 || i1 + n + 1 > N)
+    return integer(FI_VEC_CLOSE_BOUNDARY);
+  auto val = [&](int r, int c) -> float {
+    return cbox.has(r, c) ? NAN : PL[r * Cfg<N>::LDP + c];
+  };
+  auto from_offsets = [&](double deplx, double deply) {  // float64 offsets
+    o->dx64 = __dsub_rn((double)ix0, __dadd_rn(deplx, (double)i1));
+    o->dy64 = __dsub_rn((double)iy0, __dadd_rn(deply, (double)i0));
+    o->dx32 = (float)o->dx64;
+    o->dy32 = (float)o->dy64;
+  };
+  const double lim = 2.0 * (0.5 + n) * (0.5 + n);
+  int m = method;
+  if (m == FI_SUBPIX_GAUSSIAN2) {
+    float c[9];
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) c[3 * a + b] = PL[(i0 - 1 + a) * Cfg<N>::LDP + (i1 - 1 + b)];
-  return subpix_gaussian2_vals(c, i0, i1, N / 2 - 1, N / 2 - 1, dxo, dyo, tie);
+      for (int b = 0; b < 3; ++b) c[3 * a + b] = val(i0 - 1 + a, i1 - 1 + b);
+    float deplx, deply;
+    if (gauss2_depl(c, &deplx, &deply, &o->tie)) {
+      o->dx32 = __fsub_rn((float)ix0, __fadd_rn(deplx, (float)i1));
+      o->dy32 = __fsub_rn((float)iy0, __fadd_rn(deply, (float)i0));
+      o->dx64 = __dsub_rn((double)ix0, __dadd_rn((double)deplx, (double)i1));
+      o->dy64 = __dsub_rn((double)iy0, __dadd_rn((double)deply, (double)i0));
+      return FI_VEC_OK;
+    }
+    m = FI_SUBPIX_CENTROID;
+  }
+  if (m == FI_SUBPIX_GAUSSIAN) {
+    // coef = pinv(M) . log(crop), float32 logs of the crop with values <= 0 at 1e-6
+    const int w = 2 * n + 1, K = w * w;
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    for (int j = 0; j < K; ++j) {
+      float v = val(i0 - n + j / w, i1 - n + j % w);
+      if (v <= 0.0f) v = 1e-6f;
+      const double l = (double)logf(v);
+      c0 = fma(__ldg(minv + j), l, c0);
+      c1 = fma(__ldg(minv + K + j), l, c1);
+      c2 = fma(__ldg(minv + 2 * K + j), l, c2);
+      c3 = fma(__ldg(minv + 3 * K + j), l, c3);
+    }
+    if (c0 > 0.0 || c1 > 0.0) {
+      m = FI_SUBPIX_CENTROID;
+    } else {
+      const double sx = 1.0 / sqrt(-2.0 * c0), sy = 1.0 / sqrt(-2.0 * c1);
+      const double deplx = c2 * (sx * sx), deply = c3 * (sy * sy);
+      if (isnan(deplx) || isnan(deply)) {
+        m = FI_SUBPIX_CENTROID;
+      } else {
+        if (deplx * deplx + deply * deply > lim) return integer(FI_VEC_WRONG_SUBPIX);
+        from_offsets(deplx, deply);
+        return FI_VEC_OK;
+      }
+    }
+  }
+  if (m == FI_SUBPIX_CENTROID) {
+    const int w = 2 * n + 1;
+    float s = 0.f;
+    double mx = 0.0, my = 0.0;
+    for (int a = 0; a < w; ++a)
+      for (int b = 0; b < w; ++b) {
+        const float v = val(i0 - n + a, i1 - n + b);
+        s = __fadd_rn(s, v);
+        mx = __dadd_rn(mx, __dmul_rn((double)(b - n), (double)v));
+        my = __dadd_rn(my, __dmul_rn((double)(a - n), (double)v));
+      }
+    const double cx = __ddiv_rn(mx, (double)s), cy = __ddiv_rn(my, (double)s);
+    if (__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)) > lim)
+      return integer(FI_VEC_WRONG_SUBPIX);
+    from_offsets(cx, cy);
+    return FI_VEC_OK;
+  }
+  from_offsets(0.0, 0.0);  // 'no_subpix'
+  return FI_VEC_OK;
 }
 
 // SubPix.compute_subpix at given peak indices on planes in global memory
@@ -398,6 +513,20 @@ struct PeakArgs {
   SearchBox box;
   int radius;
   int apply_subpix;
+  int subpix_method;
+  int nsubpix;
+  const double* minv;
+  int nb_peaks;
+};
+
+// Where the secondary peaks of one window go (fi_piv_pass outputs).
+struct SecondaryOut {
+  int32_t* count;   // [nvec]
+  float* peaks;     // [nvec][nb_peaks-1][FI_PEAK_FIELDS]
+  uint8_t* err;     // [nvec][nb_peaks-1]
+  int w;
+  bool has_in;      // pass >= 1: integer input shift (int32 upstream)
+  int dinx, diny;
 };
 
 struct VecResult {
@@ -406,27 +535,27 @@ struct VecResult {
   int i0, i1;
   bool tie;        // near-tie of the two largest plane values (either attempt)
   bool subpix_tie; // tied minimum in the 3x3 subpixel crop
+  bool sec_tie;    // near-tie in a secondary search
   NanBox nb;
 };
 
 template <int N>
 __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double norm, int t,
-                                     int g, double* red) {
+                                     int g, double* red, const SecondaryOut* so) {
   const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
-  NanBox nb{0, 0, 0, 0};
-  PeakOut p1 = find_peak<N>(PL, pa.mask, pa.box, nb, norm, t, g, red);
+  NanBoxes boxes;
+  boxes.n = 0;
+  PeakOut p1 = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
   VecResult r;
   r.tie = p1.tie;
   r.subpix_tie = false;
-  r.nb = nb;
+  r.sec_tie = false;
+  r.nb = NanBox{0, 0, 0, 0};
   PeakOut fin = p1;
   if (p1.err == FI_VEC_PEAK_BOUNDARY || p1.err == FI_VEC_PEAK_NAN) {
-    int r0, r1, c0, c1;
-    slice_bounds(p1.i0 - pa.radius, p1.i0 + pa.radius + 1, N, &r0, &r1);
-    slice_bounds(p1.i1 - pa.radius, p1.i1 + pa.radius + 1, N, &c0, &c1);
-    if (r1 > r0 && c1 > c0) nb = NanBox{r0, r1, c0, c1};
-    r.nb = nb;
-    PeakOut p2 = find_peak<N>(PL, pa.mask, pa.box, nb, norm, t, g, red);
+    boxes.add(p1.i0, p1.i1, pa.radius, N);
+    if (boxes.n) r.nb = boxes.b[0];
+    PeakOut p2 = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
     r.tie = r.tie || p2.tie;
     if (p2.err == FI_VEC_OK) {
       fin = p2;
@@ -441,19 +570,51 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
   r.cmax = fin.cmax;
   if (fin.err == FI_VEC_ALL_NAN) {
     r.dx = r.dy = NAN;
-    return r;
+  } else {
+    r.dx = (float)(ix0 - fin.i1);
+    r.dy = (float)(iy0 - fin.i0);
   }
-  r.dx = (float)(ix0 - fin.i1);
-  r.dy = (float)(iy0 - fin.i0);
-  if (fin.err == FI_VEC_OK && pa.apply_subpix) {
-    if (t == 0) {
-      float sx, sy;
-      bool stie;
-      const int e = subpix_gaussian2_tie<N>(PL, fin.i0, fin.i1, &sx, &sy, &stie);
-      r.subpix_tie = stie;
-      r.err = e;
-      r.dx = sx;
-      r.dy = sy;
+  // upstream's caller plane holds the second-chance box unless the displacement
+  // mask made the search work on a copy (CorrelFFTBase, correl.py:561-568)
+  const NanBox cbox = (pa.mask == nullptr) ? r.nb : NanBox{0, 0, 0, 0};
+  if (fin.err == FI_VEC_OK && pa.apply_subpix && t == 0) {
+    SubpixOut sp;
+    r.err = subpix_any<N>(PL, fin.i0, fin.i1, pa.subpix_method, pa.nsubpix, pa.minv, cbox, &sp);
+    r.subpix_tie = sp.tie;
+    r.dx = sp.dx32;
+    r.dy = sp.dy32;
+  }
+  // other peaks (correl.py:250-273): NaN box around the last peak, search again
+  if (so != nullptr && pa.nb_peaks > 1) {
+    if (fin.err != FI_VEC_OK) {
+      if (t == 0) so->count[so->w] = -1;
+    } else {
+      int a0 = fin.i0, a1 = fin.i1, cnt = 0;
+      const int K = pa.nb_peaks - 1;
+      for (int k = 0; k < K; ++k) {
+        boxes.add(a0, a1, pa.radius, N);
+        const PeakOut q = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
+        r.sec_tie = r.sec_tie || q.tie;
+        if (q.err != FI_VEC_OK) break;
+        a0 = q.i0;
+        a1 = q.i1;
+        if (t == 0) {
+          SubpixOut sp;
+          const int e = subpix_any<N>(PL, a0, a1, pa.subpix_method, pa.nsubpix, pa.minv, cbox,
+                                      &sp);
+          float* o = so->peaks + ((int64_t)so->w * K + k) * FI_PEAK_FIELDS;
+          o[0] = (float)(ix0 - a1);
+          o[1] = (float)(iy0 - a0);
+          o[2] = q.cmax;
+          // the replacement value of WorkFIX (fix.py:205-211): upstream adds the
+          // int32 input shift to the float64 fit, or keeps the first-pass value
+          o[3] = so->has_in ? (float)__dadd_rn(sp.dx64, (double)so->dinx) : sp.dx32;
+          o[4] = so->has_in ? (float)__dadd_rn(sp.dy64, (double)so->diny) : sp.dy32;
+          so->err[(int64_t)so->w * K + k] = (uint8_t)e;
+        }
+        ++cnt;
+      }
+      if (t == 0) so->count[so->w] = cnt;
     }
   }
   return r;
@@ -669,7 +830,13 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
     pa.box = SearchBox{a.box_i0_start, a.box_i0_stop, a.box_i1_start, a.box_i1_stop};
     pa.radius = a.particle_radius;
     pa.apply_subpix = a.apply_subpix;
-    res = peak_and_subpix<N>(PL, pa, norm, t, g, red);
+    pa.subpix_method = a.subpix_method;
+    pa.nsubpix = a.nsubpix;
+    pa.minv = a.subpix_minv;
+    pa.nb_peaks = a.nb_peaks;
+    SecondaryOut so{a.peaks_count, a.peaks, a.peaks_err, w, a.dxin != nullptr, dinx, diny};
+    res = peak_and_subpix<N>(PL, pa, norm, t, g, red, a.nb_peaks > 1 ? &so : nullptr);
+    if (!valid && a.nb_peaks > 1 && t == 0) a.peaks_count[w] = -1;
   }
 
   // ---- outputs ----
@@ -701,7 +868,8 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
       a.errors[w] = (uint8_t)err;
       if (a.flags)
         a.flags[w] = valid ? (uint8_t)((res.tie ? FI_FLAG_NEAR_TIE : 0) |
-                                       (res.subpix_tie ? FI_FLAG_SUBPIX_TIE : 0))
+                                       (res.subpix_tie ? FI_FLAG_SUBPIX_TIE : 0) |
+                                       (res.sec_tie ? FI_FLAG_SECONDARY_TIE : 0))
                            : (uint8_t)0;
       if (!FROM_WINDOWS) {
         a.xs[w] = (float)((double)(ixs0 + ixs1) * 0.5);
@@ -728,7 +896,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
   if (t < N)
     for (int i0 = 0; i0 < N; ++i0) PL[i0 * C::LDP + t] = in[i0 * N + t];
   gsync<C::G>(g);
-  VecResult r = peak_and_subpix<N>(PL, pa, norms[w], t, g, red);
+  VecResult r = peak_and_subpix<N>(PL, pa, norms[w], t, g, red, nullptr);
   if (pa.mask == nullptr && t < N && (r.nb.r1 > r.nb.r0))
     for (int i0 = 0; i0 < N; ++i0)
       if (r.nb.has(i0, t)) in[i0 * N + t] = NAN;
@@ -866,6 +1034,17 @@ extern "C" int fi_piv_pass(const fi_piv_pass_args* args, void* stream) {
   FI_REQUIRE(a.box_i0_start >= 0 && a.box_i0_stop <= a.n && a.box_i1_start >= 0 &&
                  a.box_i1_stop <= a.n,
              "fi_piv_pass: bad search box");
+  FI_REQUIRE(a.subpix_method >= FI_SUBPIX_GAUSSIAN2 && a.subpix_method <= FI_SUBPIX_NONE,
+             "fi_piv_pass: bad subpix_method %d", a.subpix_method);
+  FI_REQUIRE(a.subpix_method == FI_SUBPIX_GAUSSIAN2 ||
+                 (a.nsubpix >= 1 && a.nsubpix <= FI_MAX_NSUBPIX),
+             "fi_piv_pass: nsubpix %d out of 1..%d", a.nsubpix, FI_MAX_NSUBPIX);
+  FI_REQUIRE(a.subpix_method != FI_SUBPIX_GAUSSIAN || a.subpix_minv,
+             "fi_piv_pass: '2d_gaussian' needs subpix_minv");
+  FI_REQUIRE(a.nb_peaks <= FI_MAX_PEAKS, "fi_piv_pass: nb_peaks %d > %d", a.nb_peaks,
+             FI_MAX_PEAKS);
+  FI_REQUIRE(a.nb_peaks <= 1 || (a.peaks_count && a.peaks && a.peaks_err),
+             "fi_piv_pass: secondary peaks need peaks_count, peaks and peaks_err");
   const int64_t nvec64 = (int64_t)a.nx * a.ny;
   FI_REQUIRE(nvec64 < (1ll << 31), "fi_piv_pass: too many vectors");
   const int nvec = (int)nvec64;

@@ -1,9 +1,10 @@
-// False-vector removal of one pass: WorkFIX.calcul (works/piv/fix.py:66-133) with
+// False-vector removal of one pass: WorkFIX.calcul (works/piv/fix.py:66-243) with
 // the NaN-aware 8-neighbour mean mean_neighbors_xy (calcul/mean_neighbors.py:5-155).
 //
 // Stage A (elementwise): vectors with a correlation error, with
 // correls_max < correl_min or with |d|^2 > displacement_max^2 become NaN.
 // Stage B (3x3 stencil on the vector grid): |d - mean8(d)|^2 > threshold^2 -> NaN.
+// Stage C (nb_peaks > 1): replacement by a secondary peak.
 // All arithmetic is float32 in the upstream operation order; comparisons use the
 // float32-rounded thresholds (numpy 2 scalar promotion).
 #include <mutex>
@@ -146,6 +147,76 @@ __global__ void k_fix_b(fi_fix_args a, const float* ix, const float* iy, float t
   a.deltays_out[i] = oy;
 }
 
+// Stage C (fix.py:135-236): a vector whose secondary peaks (correl ratio > 0.6,
+// correl > correl_min, integer displacement + input shift) hold one closer to the
+// neighbour mean of the stage-A field than the vector itself is replaced by that
+// peak's subpixel value, unless its distance exceeds the threshold, its |d|^2
+// exceeds displacement_max (unsquared, as upstream) or its subpixel fit failed.
+// Distances in float64 like upstream; ties keep the first (np.argmin).
+__global__ void k_fix_c(fi_fix_args a, const float* ix, const float* iy) {
+  const int nvec = a.nx * a.ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  const int cnt = a.peaks_count[i];
+  if (cnt <= 0) return;
+  const int K = a.nb_peaks - 1;
+  const float c0 = a.correls_max[i];
+  const float* pk = a.peaks + (int64_t)i * K * FI_PEAK_FIELDS;
+  const int dxi = a.dxin ? a.dxin[i] : 0, dyi = a.dyin ? a.dyin[i] : 0;
+  int good[FI_MAX_PEAKS];
+  int ng = 0;
+  for (int j = 0; j < cnt && j < K; ++j) {
+    const float cm = pk[j * FI_PEAK_FIELDS + 2];
+    if (__fdiv_rn(cm, c0) > 0.6f && cm > a.correl_min) good[ng++] = j;
+  }
+  if (ng == 0) return;
+  const float d2 = a.diff2[i];
+  if (isnan(d2)) return;  // np.argmin picks the NaN distance of the vector itself
+  Grid g{ix, iy, a.ny, a.nx};
+  const int i0 = i / a.nx, i1 = i % a.nx;
+  const float n = nsum<2>(g, i0, i1);
+  const double mx = (double)__fdiv_rn(nsum<0>(g, i0, i1), n);
+  const double my = (double)__fdiv_rn(nsum<1>(g, i0, i1), n);
+  double best = sqrt((double)d2);
+  int am = -1;
+  for (int k = 0; k < ng; ++k) {
+    const int j = good[k];
+    const double ex = mx - (double)((int)pk[j * FI_PEAK_FIELDS] + dxi);
+    const double ey = my - (double)((int)pk[j * FI_PEAK_FIELDS + 1] + dyi);
+    const double dn = sqrt(ex * ex + ey * ey);
+    if (dn < best) {
+      best = dn;
+      am = j;
+    }
+  }
+  if (am < 0) return;
+  if (a.use_threshold && best > a.threshold64) return;
+  const double pdx = (double)((int)pk[am * FI_PEAK_FIELDS] + dxi);
+  const double pdy = (double)((int)pk[am * FI_PEAK_FIELDS + 1] + dyi);
+  if (a.displacement_max64 != 0.0 && pdx * pdx + pdy * pdy > a.displacement_max64) return;
+  if (a.peaks_err[(int64_t)i * K + am] != 0) return;
+  a.replaced[3 * (int64_t)i] = a.deltaxs[i];
+  a.replaced[3 * (int64_t)i + 1] = a.deltays[i];
+  a.replaced[3 * (int64_t)i + 2] = c0;
+  a.deltaxs_out[i] = pk[am * FI_PEAK_FIELDS + 3];
+  a.deltays_out[i] = pk[am * FI_PEAK_FIELDS + 4];
+  a.correls_max_out[i] = pk[am * FI_PEAK_FIELDS + 2];
+  a.fix_flags[i] |= FI_FIX_REPLACED;
+}
+
+// Checks of the secondary-peak inputs; FI_OK when nb_peaks <= 1.
+static int check_secondary(const fi_fix_args& a, const char* who) {
+  if (a.nb_peaks <= 1) return FI_OK;
+  FI_REQUIRE(a.nb_peaks <= FI_MAX_PEAKS, "%s: nb_peaks %d > %d", who, a.nb_peaks, FI_MAX_PEAKS);
+  FI_REQUIRE(a.use_threshold,
+             "%s: secondary peaks need the neighbour test (threshold_diff_neighbour)", who);
+  FI_REQUIRE(a.diff2 && a.peaks_count && a.peaks && a.peaks_err && a.correls_max_out &&
+                 a.replaced,
+             "%s: secondary peaks need diff2, peaks_count, peaks, peaks_err, "
+             "correls_max_out and replaced", who);
+  return FI_OK;
+}
+
 }  // namespace fi
 
 using namespace fi;
@@ -158,6 +229,7 @@ extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
                  a.deltays_out && a.fix_flags,
              "fi_fix: null pointer");
   FI_REQUIRE(!a.use_threshold || a.work, "fi_fix: the neighbour test needs work[2*nvec]");
+  if (check_secondary(a, "fi_fix") != FI_OK) return FI_ERR_INVALID;
   const int nvec = a.nx * a.ny;
   cudaStream_t s = (cudaStream_t)stream;
   const float dmax2 = (float)((double)a.displacement_max * (double)a.displacement_max);
@@ -169,6 +241,10 @@ extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
     k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
     add_launches(1);
+    if (a.nb_peaks > 1) {
+      k_fix_c<<<blocks, threads, 0, s>>>(a, wx, wy);
+      add_launches(1);
+    }
   } else {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
                                        a.deltays_out);
@@ -188,6 +264,7 @@ extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
   FI_REQUIRE(a.deltaxs && a.deltays && a.correls_max && a.errors && a.deltaxs_out &&
                  a.deltays_out && a.fix_flags,
              "fi_fix_static: null pointer");
+  if (check_secondary(a, "fi_fix_static") != FI_OK) return FI_ERR_INVALID;
   float* scratch = nullptr;
   const int rc = fix_scratch_address(&scratch);
   if (rc != FI_OK) return rc;
@@ -204,6 +281,10 @@ extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
     k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
     add_launches(1);
+    if (a.nb_peaks > 1) {
+      k_fix_c<<<blocks, threads, 0, s>>>(a, wx, wy);
+      add_launches(1);
+    }
   } else {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
                                        a.deltays_out);

@@ -369,6 +369,17 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
 
 # --------------------------------------------------------------------------------
 # the pipeline
+def subpix_pinv(nsubpix):
+    """Pseudo-inverse of [X^2, Y^2, X, Y, 1] over the (2 nsubpix + 1)^2 crop, the
+    '2d_gaussian' least-squares operator of SubPix.prepare_subpix
+    (calcul/subpix.py:86-105); float64, row-major 5 x K."""
+    xs = np.arange(-nsubpix, nsubpix + 1, dtype=float)
+    X, Y = np.meshgrid(xs, xs)
+    X, Y = X.ravel(), Y.ravel()
+    M = np.stack([X**2, Y**2, X, Y, np.ones(X.size)], axis=1)
+    return np.ascontiguousarray(np.linalg.pinv(M), dtype=np.float64)
+
+
 # --------------------------------------------------------------------------------
 @dataclass
 class PassDevice:
@@ -389,6 +400,10 @@ class PassDevice:
     planes: object = None
     dxin: object = None
     dyin: object = None
+    peaks_count: object = None  # secondary peaks (nb_peaks_to_search > 1)
+    peaks: object = None
+    peaks_err: object = None
+    replaced: object = None  # [nvec, 3] old dx, dy, correl_max of replaced vectors
     tps_next: Optional[TpsOutput] = None  # interpolation of this pass on the next grid
     tps_final: Optional[TpsOutput] = None
 
@@ -408,10 +423,27 @@ class PIVPipeline:
         self.keep_correls = keep_correls
         self.interp_last = interp_last
         p0, mp = params.piv0, params.multipass
-        if p0.nb_peaks_to_search != 1:
-            raise NotImplementedError("nb_peaks_to_search > 1 is not provided by this backend")
-        if p0.method_subpix != "2d_gaussian2":
-            raise NotImplementedError("method_subpix must be '2d_gaussian2' on this backend")
+        self.nb_peaks = int(p0.nb_peaks_to_search)
+        if not 1 <= self.nb_peaks <= L.MAX_PEAKS:
+            raise NotImplementedError(
+                f"nb_peaks_to_search must be in 1..{L.MAX_PEAKS} on this backend")
+        if self.nb_peaks > 1 and params.fix.threshold_diff_neighbour is None:
+            raise ValueError(
+                "nb_peaks_to_search > 1 needs fix.threshold_diff_neighbour (WorkFIX compares "
+                "the secondary peaks with the neighbour mean, fix.py:168-176)")
+        if p0.method_subpix not in L.SUBPIX_METHODS:
+            raise ValueError(f"method has to be in {list(L.SUBPIX_METHODS)}")
+        if p0.method_subpix == "2d_gaussian2" and p0.nsubpix is not None and p0.nsubpix != 1:
+            raise ValueError(
+                "Subpixel method '2d_gaussian2' doesn't require nsubpix. "
+                "In this case, nsubpix has to be equal to None.")
+        self.subpix_method = L.SUBPIX_METHODS[p0.method_subpix]
+        self.nsubpix = 1 if p0.nsubpix is None else int(p0.nsubpix)
+        if not 1 <= self.nsubpix <= L.MAX_NSUBPIX:
+            raise NotImplementedError(f"nsubpix must be in 1..{L.MAX_NSUBPIX} on this backend")
+        self.subpix_minv = None
+        if p0.method_subpix == "2d_gaussian":
+            self.subpix_minv = torch.as_tensor(subpix_pinv(self.nsubpix), device=self.device)
         if mp.number > 1 and mp.use_tps is not True:
             raise NotImplementedError(
                 "interpolation between passes needs params.multipass.use_tps = True "
@@ -511,6 +543,12 @@ class PIVPipeline:
         )
         if self.keep_correls:
             out.planes = torch.empty(nvec * lay.n * lay.n, **f32)
+        K = self.nb_peaks - 1
+        if K > 0:
+            out.peaks_count = torch.empty(nvec, dtype=torch.int32, device=dev)
+            out.peaks = torch.empty(nvec * K * L.PEAK_FIELDS, **f32)
+            out.peaks_err = torch.empty(nvec * K, **u8)
+            out.replaced = torch.empty(3 * nvec, **f32)
         H, W = self.imshape
         a = L.PivPassArgs()
         a.im0, a.im1, a.dtype, a.height, a.width = L.ptr(im0), L.ptr(im1), dt, H, W
@@ -529,6 +567,11 @@ class PIVPipeline:
         a.norms = None
         a.planes = L.ptr(out.planes)
         a.flags = L.ptr(out.flags)
+        a.subpix_method, a.nsubpix = self.subpix_method, self.nsubpix
+        a.subpix_minv = L.ptr(self.subpix_minv)
+        a.nb_peaks = self.nb_peaks
+        a.peaks_count, a.peaks, a.peaks_err = (L.ptr(out.peaks_count), L.ptr(out.peaks),
+                                               L.ptr(out.peaks_err))
         with _timed("fi_piv_pass"):
             L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
         return out
@@ -550,6 +593,15 @@ class PIVPipeline:
         a.fix_flags, a.diff2 = L.ptr(cur.fix_flags), L.ptr(cur.diff2)
         work = torch.empty(2 * lay.nvec, dtype=torch.float32, device=self.device)
         a.work = L.ptr(work)
+        a.nb_peaks = self.nb_peaks
+        if self.nb_peaks > 1:  # WorkFIX secondary peaks (fix.py:135-236)
+            a.peaks_count, a.peaks, a.peaks_err = (L.ptr(cur.peaks_count), L.ptr(cur.peaks),
+                                                   L.ptr(cur.peaks_err))
+            a.dxin, a.dyin = L.ptr(cur.dxin), L.ptr(cur.dyin)
+            a.threshold64 = float(fx.threshold_diff_neighbour)
+            a.displacement_max64 = float(fx.displacement_max or 0.0)
+            a.correls_max_out = L.ptr(cur.correls_max)
+            a.replaced = L.ptr(cur.replaced)
         with _timed("fi_fix"):
             L.check(lib.fi_fix(C.byref(a), s), "fi_fix")
 
@@ -558,10 +610,12 @@ class PIVPipeline:
 # device -> host results
 # --------------------------------------------------------------------------------
 def error_dict(err, fix_flags, diff2, threshold):
-    """Rebuild ``errors`` of _loop_vectors + WorkFIX (fix.py:66-133) from the codes."""
+    """Rebuild ``errors`` of _loop_vectors + WorkFIX (fix.py:66-236) from the codes."""
     errors = {}
     for i in np.nonzero((err != 0) | (fix_flags != 0))[0]:
         i = int(i)
+        if fix_flags[i] & L.FIX_REPLACED:  # WorkFIX deletes their errors (fix.py:229-234)
+            continue
         s = ERROR_STRINGS.get(int(err[i])) if err[i] else None
         f = int(fix_flags[i])
         for bit, text in ((1, "correl < correl_min"), (2, "delta2 < displacement_max2"),

@@ -15,6 +15,7 @@ import time
 
 import numpy as np
 
+from . import _lib
 from .data_objects import ArrayCouple, HeavyPIVResults, MultipassPIVResults
 from .engine import PIVPipeline, error_dict
 from .errors import InterpError
@@ -204,6 +205,15 @@ class WorkPIV:
                 "deltaxs", "deltays", "fix_flags", "diff2")}
             errors = error_dict(h["errors"], h["fix_flags"], h["diff2"],
                                 fx.threshold_diff_neighbour)
+            secondary = [None] * lay.nvec
+            replaced = {}
+            if pd.peaks_count is not None:
+                secondary = _secondary_peaks(pd, lay.nvec)
+                rep = np.nonzero(h["fix_flags"] & _lib.FIX_REPLACED)[0]
+                if rep.size:
+                    old = pd.replaced.view(lay.nvec, 3)[torch.as_tensor(rep, device=pd.replaced.device)]
+                    for i, (ox, oy, oc) in zip(rep.tolist(), old.cpu().numpy()):
+                        replaced[i] = (ox, oy, oc)
             if lay.index == 0:
                 xs = lay.gx + offx
                 ys = lay.gy + offy
@@ -219,8 +229,10 @@ class WorkPIV:
             r = HeavyPIVResults(
                 h["deltaxs"], h["deltays"], xs, ys, errors, correls_max=h["correls_max"],
                 correls=correls, couple=couple, params=self.params,
-                secondary_peaks=[None] * nvec,
+                secondary_peaks=secondary,
             )
+            if replaced:
+                r.replaced_vectors = replaced
             r.indices_no_displacement = (lay.n // 2 - 1, lay.n // 2 - 1)
             r.displacement_max = lay.displacement_max
             # per-vector near-tie flags (bit 0: top-two plane values within 1e-6
@@ -279,6 +291,20 @@ class WorkPIV:
                 "Singular TPS subdomain system (upstream falls back to griddata, "
                 "which this backend does not provide)"
             )
+
+
+def _secondary_peaks(pd, nvec):
+    """``secondary_peaks`` of _loop_vectors: None where the peak search raised, else
+    the list of (dx, dy, correl_max) of the other peaks (correl.py:250-273)."""
+    counts = pd.peaks_count.cpu().numpy()
+    K = pd.peaks.numel() // (nvec * _lib.PEAK_FIELDS)
+    pk = pd.peaks.view(nvec, K, _lib.PEAK_FIELDS).cpu().numpy()
+    out = [None] * nvec
+    for i in range(nvec):
+        c = int(counts[i])
+        if c >= 0:
+            out[i] = [(int(pk[i, j, 0]), int(pk[i, j, 1]), pk[i, j, 2]) for j in range(c)]
+    return out
 
 
 def _np_dtype(t):

@@ -38,18 +38,30 @@ extern "C" {
 #define FI_VEC_WRONG_SUBPIX 3  /* "wrong subpix" (integer peak kept)     */
 #define FI_VEC_BAD_CROP 4      /* "Bad im_crop shape."                   */
 #define FI_VEC_ALL_NAN 5       /* plane without finite value (upstream asserts) */
-#define FI_VEC_CLOSE_BOUNDARY 6 /* "close boundary" (fi_subpix_at only)   */
+#define FI_VEC_CLOSE_BOUNDARY 6 /* "close boundary" (subpixel crop leaves the plane) */
 
 /* per-vector flag bits written by fi_piv_pass */
 #define FI_FLAG_NEAR_TIE 1   /* top two plane values within 1e-6 relative        */
 #define FI_FLAG_SUBPIX_TIE 2 /* two 3x3 crop values at the minimum (within 1e-5 of
                                 the range): the '2d_gaussian2' 1e-8 floor then
                                 depends on float rounding                         */
+#define FI_FLAG_SECONDARY_TIE 4 /* near-tie in a secondary peak search          */
 
 /* fix flag bits written by fi_fix */
 #define FI_FIX_CORREL_MIN 1     /* "correl < correl_min"        */
 #define FI_FIX_DISPLACEMENT 2   /* "delta2 < displacement_max2" */
 #define FI_FIX_NEIGHBOUR 4      /* "diff neighbour too large"   */
+#define FI_FIX_REPLACED 8       /* replaced by a secondary peak (errors cleared) */
+
+/* Subpixel methods (SubPix.methods, calcul/subpix.py:73) */
+#define FI_SUBPIX_GAUSSIAN2 0   /* '2d_gaussian2' (3 x 3, centroid fallback) */
+#define FI_SUBPIX_GAUSSIAN 1    /* '2d_gaussian' (least squares, nsubpix)    */
+#define FI_SUBPIX_CENTROID 2    /* 'centroid' (nsubpix)                      */
+#define FI_SUBPIX_NONE 3        /* 'no_subpix'                               */
+#define FI_MAX_NSUBPIX 4        /* crops up to 9 x 9                         */
+#define FI_MAX_PEAKS 4          /* nb_peaks_to_search up to 4                */
+#define FI_PEAK_FIELDS 5        /* per secondary peak: dx, dy (integer), correl_max,
+                                   replacement dx, dy (subpixel fit + input shift) */
 
 const char* fi_last_error(void);
 
@@ -97,6 +109,16 @@ typedef struct fi_piv_pass_args {
   double* norms;            /* nullable out [nvec]: sqrt(S0 * S1)             */
   float* planes;            /* nullable out [nvec*n*n], fftshift layout       */
   uint8_t* flags;           /* nullable out [nvec] FI_FLAG_*                  */
+  int subpix_method;        /* FI_SUBPIX_* (params.piv0.method_subpix)        */
+  int nsubpix;              /* crop half width of '2d_gaussian'/'centroid'    */
+  const double* subpix_minv;/* '2d_gaussian': pinv of [X^2, Y^2, X, Y, 1],
+                               5 x (2 nsubpix + 1)^2 row-major, device        */
+  int nb_peaks;             /* params.piv0.nb_peaks_to_search (1..4)          */
+  int32_t* peaks_count;     /* out [nvec] if nb_peaks > 1: secondary peaks
+                               found, -1 where the peak search raised         */
+  float* peaks;             /* out [nvec][nb_peaks-1][FI_PEAK_FIELDS]         */
+  uint8_t* peaks_err;       /* out [nvec][nb_peaks-1]: FI_VEC_* of the subpixel
+                               fit of each secondary peak                     */
 } fi_piv_pass_args;
 
 /*
@@ -166,11 +188,26 @@ typedef struct fi_fix_args {
   uint8_t* fix_flags;          /* out [nvec] FI_FIX_*                          */
   float* diff2;                /* out [nvec]: |d - mean8(d)|^2 (float32)       */
   float* work;                 /* scratch [2*nvec] (floats)                    */
+  /* secondary peaks (fix.py:135-236); nb_peaks > 1 needs use_threshold,
+     diff2 and the outputs below */
+  int nb_peaks;                /* fi_piv_pass nb_peaks (1: no replacement)     */
+  const int32_t* peaks_count;  /* fi_piv_pass outputs                          */
+  const float* peaks;
+  const uint8_t* peaks_err;
+  const int32_t* dxin;         /* nullable: the pass's integer input shifts    */
+  const int32_t* dyin;
+  double threshold64;          /* fix.threshold_diff_neighbour (float64)      */
+  double displacement_max64;   /* fix.displacement_max (0: none)              */
+  float* correls_max_out;      /* out [nvec]: correls_max after replacement (may
+                                  alias correls_max)                          */
+  float* replaced;             /* out [nvec][3]: old dx, dy, correl_max        */
 } fi_fix_args;
 
 /*
- * WorkFIX.calcul without secondary peaks (works/piv/fix.py:66-133) with
- * mean_neighbors_xy (calcul/mean_neighbors.py:128-155).
+ * WorkFIX.calcul (works/piv/fix.py:66-243) with mean_neighbors_xy
+ * (calcul/mean_neighbors.py:128-155): errors, correl_min, displacement_max and
+ * neighbour tests, then (nb_peaks > 1) the replacement of a vector by the
+ * secondary peak closest to the neighbour mean (FI_FIX_REPLACED).
  */
 int fi_fix(const fi_fix_args* args, void* stream);
 

@@ -219,21 +219,26 @@ def case_griddata():
 
 def case_secondary_peaks():
     """nb_peaks_to_search=3 with WorkFIX secondary-peak replacement, two passes with
-    TPS (16 -> 8 px windows), an Oseen vortex and a band of strong image noise in
-    im1 (spurious main peaks, the true peak second)."""
-    model = synthetic.ParticleModel(density=0.05, noise=4.0, dtype="uint8")
-    field = synthetic.oseen_vortex((160, 192), d_max=5.0, rc=40.0)
-    im0, im1 = synthetic.make_pair((160, 192), field, model, seed=6000)
-    rng = np.random.default_rng(1)
-    band = im1[40:100].astype(np.float64) + rng.normal(0.0, 120.0, im1[40:100].shape)
-    im1[40:100] = np.clip(np.round(band), 0, 255).astype(np.uint8)
+    TPS (32 -> 16 px windows): two particle populations moving by (3, 1) and
+    (-4, 2) px share a band of the image, so windows there hold competing peaks.
+    fix.displacement_max = 60 keeps upstream's unsquared check of the replacement
+    (|d|^2 > displacement_max) from rejecting every peak."""
+    shape, band = (192, 256), (60, 130)
+    ma = synthetic.ParticleModel(density=0.05, noise=2.0, dtype="uint8")
+    a0, a1 = synthetic.make_pair(shape, synthetic.uniform_shift(3.0, 1.0), ma, seed=6000)
+    mb = synthetic.ParticleModel(density=0.05, noise=0.0, dtype="uint8")
+    b0, b1 = synthetic.make_pair(shape, synthetic.uniform_shift(-4.0, 2.0), mb, seed=6001)
+    m = np.zeros(shape)
+    m[band[0]:band[1]] = 1.0
+    im0 = np.clip(a0 + m * b0, 0, 255).astype(np.uint8)
+    im1 = np.clip(a1 + m * b1, 0, 255).astype(np.uint8)
     run_workpiv("secondary_peaks_two_pass", im0, im1, {
-        "piv0.shape_crop_im0": 16, "piv0.grid.overlap": 0.5,
+        "piv0.shape_crop_im0": 32, "piv0.grid.overlap": 0.5,
         "piv0.nb_peaks_to_search": 3,
         "multipass.number": 2, "multipass.use_tps": True,
         "multipass.subdom_size": 100, "multipass.smoothing_coef": 2.0,
-        "fix.threshold_diff_neighbour": 2.5, "fix.correl_min": 0.1,
-        "fix.displacement_max": 9,
+        "fix.threshold_diff_neighbour": 3.0, "fix.correl_min": 0.1,
+        "fix.displacement_max": 60,
     }, keep_planes=True)
 
 

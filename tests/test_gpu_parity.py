@@ -113,10 +113,52 @@ def _compare_pass(z, ip, r, report):
             assert got.keys() == want.keys()
             np.testing.assert_allclose([got[k] for k in sorted(got)],
                                        [want[k] for k in sorted(want)], atol=TOL_PX)
+    if f"p{ip}_secondary_counts" in z.files:
+        _compare_secondary(z, ip, r, tie, report)
+
+
+def _compare_secondary(z, ip, r, tie, report):
+    """Secondary peaks (exact integer displacements, correl_max within float32
+    rounding) and the vectors WorkFIX replaced, outside near-ties; a replacement
+    also depends on the neighbours, so vectors next to a near-tie are left out."""
+    counts = z[f"p{ip}_secondary_counts"]
+    flat = z[f"p{ip}_secondary_peaks"]
+    starts = np.concatenate([[0], np.cumsum(np.maximum(counts, 0))])
+    for i, other in enumerate(r.secondary_peaks):
+        if tie[i]:
+            continue
+        assert (other is None) == (counts[i] < 0), i
+        if other is None:
+            continue
+        want = flat[starts[i]:starts[i + 1]]
+        assert len(other) == len(want), (i, other, want)
+        for (dx, dy, cm), (wdx, wdy, wcm) in zip(other, want):
+            assert (dx, dy) == (int(wdx), int(wdy)), (i, other, want)
+            np.testing.assert_allclose(cm, wcm, rtol=2e-5, atol=2e-6)
+    grid = tie.reshape(-1)
+    lay_ny = z[f"p{ip}_iyvecs"].size
+    lay_nx = z[f"p{ip}_ixvecs"].size
+    t2 = grid.reshape(lay_ny, lay_nx)
+    near = np.zeros_like(t2)
+    for a in (-1, 0, 1):
+        for b in (-1, 0, 1):
+            near |= np.roll(np.roll(t2, a, 0), b, 1)
+    near = near.reshape(-1)
+    rep = getattr(r, "replaced_vectors", {})
+    keys = z[f"p{ip}_replaced_keys"] if f"p{ip}_replaced_keys" in z.files else np.zeros(0, int)
+    vals = z[f"p{ip}_replaced_vals"] if f"p{ip}_replaced_keys" in z.files else np.zeros((0, 3))
+    want = {int(k): v for k, v in zip(keys, vals) if not near[int(k)]}
+    got = {k: v for k, v in rep.items() if not near[k]}
+    assert got.keys() == want.keys(), (sorted(got), sorted(want))
+    for k in want:
+        np.testing.assert_allclose(np.asarray(got[k], float), want[k], atol=TOL_PX, rtol=2e-5)
+    report.append({"pass": ip, "replaced": len(rep), "replaced_ref": int(keys.size)})
 
 
 @pytest.mark.parametrize("name", ["single_pass_c1", "multipass_small", "dmax_two_pass",
-                                  "edges_single_pass"])
+                                  "edges_single_pass", "secondary_peaks_two_pass",
+                                  "subpix_gaussian_single", "subpix_centroid2_single",
+                                  "subpix_none_single"])
 def test_workpiv_matches_reference(name):
     z, res = _run(name)
     assert len(res.passes) == int(z["nb_passes"])
