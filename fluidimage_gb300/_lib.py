@@ -87,9 +87,9 @@ _SIGNATURES = {
     "fi_peaks_from_planes": (
         C.c_int,
         [P, P, C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
-         P, P, P, P, P, P, P],
+         C.c_int, C.c_int, P, C.c_int, P, P, P, P, P, P, P, P, P, P],
     ),
-    "fi_subpix_at": (C.c_int, [P, C.c_int, C.c_int, P, P, P, P, P, P]),
+    "fi_subpix_at": (C.c_int, [P, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P]),
     "fi_fix": (C.c_int, [P, P]),
     "fi_fix_static": (C.c_int, [P, P]),
     "fi_tps_plan_make": (

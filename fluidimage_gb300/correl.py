@@ -10,8 +10,10 @@ methods it inherits from ``CorrelFFTBase`` / ``CorrelBase``
 * ``compute_displacements_from_correl(correl, norm) -> (dx, dy, correl_max,
   other_peaks)``, raising ``PIVError`` (``explanation``, ``results``) like
   upstream, including the second-chance search that writes NaNs into the
-  caller's plane when ``displacement_max`` is None;
-* ``apply_subpix(dx, dy, correl)`` ('2d_gaussian2' with centroid fallback);
+  caller's plane when ``displacement_max`` is None, and the other peaks when
+  ``nb_peaks_to_search > 1``;
+* ``apply_subpix(dx, dy, correl)`` (any ``SubPix`` method: '2d_gaussian2' with its
+  centroid fallback, '2d_gaussian', 'centroid', 'no_subpix');
 * ``get_indices_no_displacement()``, ``displacement_max``.
 
 Every computation runs in the CUDA library; the plugin only moves arrays.  It
@@ -54,16 +56,21 @@ class CorrelGB300:
             )
         if im0_shape[0] != im0_shape[1] or im0_shape[0] not in SUPPORTED_WINDOWS:
             raise NotImplementedError(f"window {im0_shape} not supported: square {SUPPORTED_WINDOWS}")
-        if method_subpix != "2d_gaussian2":
-            raise NotImplementedError("method_subpix must be '2d_gaussian2' on this backend")
         if method_subpix == "2d_gaussian2" and nsubpix is not None and nsubpix != 1:
             raise ValueError(
                 "Subpixel method '2d_gaussian2' doesn't require nsubpix. "
                 "In this case, nsubpix has to be equal to None."
             )
-        if nb_peaks_to_search != 1:
-            raise NotImplementedError("nb_peaks_to_search > 1 is not provided by this backend")
+        if method_subpix not in L.SUBPIX_METHODS:
+            raise ValueError(f"method has to be in {list(L.SUBPIX_METHODS)}")
+        self.nsubpix = 1 if nsubpix is None else int(nsubpix)
+        if not 1 <= self.nsubpix <= L.MAX_NSUBPIX:
+            raise NotImplementedError(f"nsubpix must be in 1..{L.MAX_NSUBPIX} on this backend")
+        if not 1 <= int(nb_peaks_to_search) <= L.MAX_PEAKS:
+            raise NotImplementedError(f"nb_peaks_to_search must be in 1..{L.MAX_PEAKS}")
         self.method_subpix = method_subpix
+        self._method = L.SUBPIX_METHODS[method_subpix]
+        self._minv = None
         self.im0_shape = im0_shape
         self.im1_shape = im1_shape
         self.n = im0_shape[0]
@@ -121,10 +128,21 @@ class CorrelGB300:
                                              device=_dev())
         return self._mask_dev
 
+    def _minv_device(self):
+        import torch
+
+        from .engine import subpix_pinv
+
+        if self.method_subpix == "2d_gaussian" and self._minv is None:
+            self._minv = torch.as_tensor(subpix_pinv(self.nsubpix), device=_dev())
+        return self._minv
+
     def peaks_batch(self, planes, norms, apply_subpix=False):
         """Peak search (+ subpixel) of a stack of planes; returns per-plane arrays
-        ``(dx, dy, correl_max, err, i0, i1)``; ``planes`` receives the second-chance
-        NaN boxes like upstream (no displacement_max only)."""
+        ``(dx, dy, correl_max, err, i0, i1, other_peaks)``; ``planes`` receives the
+        second-chance NaN boxes like upstream (no displacement_max only).
+        ``other_peaks`` is None (nb_peaks_to_search == 1) or per plane None (search
+        raised) or a list of ``(dx, dy, correl_max)``."""
         import torch
 
         lib = L.load()
@@ -139,18 +157,34 @@ class CorrelGB300:
         i0 = torch.empty(count, dtype=torch.int32, device=p.device)
         i1 = torch.empty(count, dtype=torch.int32, device=p.device)
         b = self._box
+        nb = int(self.nb_peaks_to_search)
+        K = nb - 1
+        pc = pk = pe = None
+        if K > 0:
+            pc = torch.empty(count, dtype=torch.int32, device=p.device)
+            pk = torch.empty(count * K * L.PEAK_FIELDS, **f32)
+            pe = torch.empty(count * K, dtype=torch.uint8, device=p.device)
         L.check(lib.fi_peaks_from_planes(
             L.ptr(p), L.ptr(nrm), count, self.n, L.ptr(self._mask_device()), b[0], b[1], b[2],
-            b[3], int(self.particle_radius), int(apply_subpix), L.ptr(dx), L.ptr(dy), L.ptr(cm),
-            L.ptr(err), L.ptr(i0), L.ptr(i1), L.stream_handle()), "fi_peaks_from_planes")
+            b[3], int(self.particle_radius), int(apply_subpix), self._method, self.nsubpix,
+            L.ptr(self._minv_device()), nb, L.ptr(dx), L.ptr(dy), L.ptr(cm), L.ptr(err),
+            L.ptr(i0), L.ptr(i1), L.ptr(pc), L.ptr(pk), L.ptr(pe), L.stream_handle()),
+            "fi_peaks_from_planes")
         if isinstance(planes, np.ndarray) and self.where_large_displacement is None:
             planes[...] = p.cpu().numpy().reshape(planes.shape)
+        other = None
+        if K > 0:
+            counts = pc.cpu().numpy()
+            peaks = pk.view(count, K, L.PEAK_FIELDS).cpu().numpy()
+            other = [None if counts[k] < 0 else
+                     [(int(peaks[k, j, 0]), int(peaks[k, j, 1]), peaks[k, j, 2])
+                      for j in range(int(counts[k]))] for k in range(count)]
         return (dx.cpu().numpy(), dy.cpu().numpy(), cm.cpu().numpy(), err.cpu().numpy(),
-                i0.cpu().numpy(), i1.cpu().numpy())
+                i0.cpu().numpy(), i1.cpu().numpy(), other)
 
     def compute_displacements_from_correl(self, correl, norm=1.0):
         """(dx, dy, correl_max, other_peaks) of one plane (correl.py:226-275, 561-568)."""
-        dx, dy, cm, err, i0, i1 = self.peaks_batch(correl, [norm])
+        dx, dy, cm, err, i0, i1, other = self.peaks_batch(correl, [norm])
         cmax = 0.0 if norm == 0 else cm[0]
         e = int(err[0])
         if e == 5:
@@ -159,10 +193,11 @@ class CorrelGB300:
             error = PIVError(explanation=ERROR_STRINGS[e])
             error.results = (int(dx[0]), int(dy[0]), cmax)
             raise error
-        return int(dx[0]), int(dy[0]), cmax, None
+        return int(dx[0]), int(dy[0]), cmax, (None if other is None else other[0])
 
     def apply_subpix(self, dx, dy, correl):
-        """'2d_gaussian2' subpixel displacement (correl.py:277-281, subpix.py:107-218)."""
+        """Subpixel displacement with the plugin's method (correl.py:277-281,
+        subpix.py:107-218)."""
         import torch
 
         lib = L.load()
@@ -173,7 +208,8 @@ class CorrelGB300:
         ox = torch.empty(1, dtype=torch.float32, device=p.device)
         oy = torch.empty(1, dtype=torch.float32, device=p.device)
         err = torch.empty(1, dtype=torch.uint8, device=p.device)
-        L.check(lib.fi_subpix_at(L.ptr(p), 1, self.n, L.ptr(ii0), L.ptr(ii1), L.ptr(ox), L.ptr(oy),
+        L.check(lib.fi_subpix_at(L.ptr(p), 1, self.n, L.ptr(ii0), L.ptr(ii1), self._method,
+                                 self.nsubpix, L.ptr(self._minv_device()), L.ptr(ox), L.ptr(oy),
                                  L.ptr(err), L.stream_handle()), "fi_subpix_at")
         e = int(err.item())
         if e:

@@ -390,8 +390,7 @@ struct SubpixOut {
   bool tie;
 };
 
-template <int N>
-__device__ int subpix_any(const float* PL, int i0, int i1, int method, int nsub,
+__device__ int subpix_any(const float* PL, int ld, int N, int i0, int i1, int method, int nsub,
                           const double* minv, const NanBox& cbox, SubpixOut* o) {
   const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
   const int n = (method == FI_SUBPIX_GAUSSIAN2) ? 1 : nsub;
@@ -405,9 +404,7 @@ __device__ int subpix_any(const float* PL, int i0, int i1, int method, int nsub,
   };
   if (i0 - n < 0 || i0 + n + 1 > N || i1 - n < 0 || i1 + n + 1 > N)
     return integer(FI_VEC_CLOSE_BOUNDARY);
-  auto val = [&](int r, int c) -> float {
-    return cbox.has(r, c) ? NAN : PL[r * Cfg<N>::LDP + c];
-  };
+  auto val = [&](int r, int c) -> float { return cbox.has(r, c) ? NAN : PL[r * ld + c]; };
   auto from_offsets = [&](double deplx, double deply) {  // float64 offsets
     o->dx64 = __dsub_rn((double)ix0, __dadd_rn(deplx, (double)i1));
     o->dy64 = __dsub_rn((double)iy0, __dadd_rn(deply, (double)i0));
@@ -481,29 +478,19 @@ __device__ int subpix_any(const float* PL, int i0, int i1, int method, int nsub,
 }
 
 // SubPix.compute_subpix at given peak indices on planes in global memory
-// (subpix.py:107-218), one thread per plane; "close boundary" when the 3x3
-// crop leaves the plane.
+// (subpix.py:107-218), any method, one thread per plane; "close boundary" when
+// the crop leaves the plane.
 __global__ void k_subpix_at(const float* planes, int count, int n, const int32_t* pi0,
-                            const int32_t* pi1, float* dxs, float* dys, uint8_t* errs) {
+                            const int32_t* pi1, int method, int nsub, const double* minv,
+                            float* dxs, float* dys, uint8_t* errs) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= count) return;
-  const int i0 = pi0[w], i1 = pi1[w];
-  const int ix0 = n / 2 - 1, iy0 = n / 2 - 1;
-  if (i0 - 1 < 0 || i0 + 2 > n || i1 - 1 < 0 || i1 + 2 > n) {
-    dxs[w] = (float)(ix0 - i1);
-    dys[w] = (float)(iy0 - i0);
-    errs[w] = 6;
-    return;
-  }
-  const float* P = planes + (int64_t)w * n * n;
-  float c[9];
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b) c[3 * a + b] = P[(i0 - 1 + a) * n + (i1 - 1 + b)];
-  float dx, dy;
-  bool tie;
-  errs[w] = (uint8_t)subpix_gaussian2_vals(c, i0, i1, ix0, iy0, &dx, &dy, &tie);
-  dxs[w] = dx;
-  dys[w] = dy;
+  SubpixOut sp;
+  const int e = subpix_any(planes + (int64_t)w * n * n, n, n, pi0[w], pi1[w], method, nsub, minv,
+                           NanBox{0, 0, 0, 0}, &sp);
+  errs[w] = (uint8_t)e;
+  dxs[w] = sp.dx32;
+  dys[w] = sp.dy32;
 }
 
 // Peak search with the second chance, then subpixel fit; writes the outputs.
@@ -579,7 +566,8 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
   const NanBox cbox = (pa.mask == nullptr) ? r.nb : NanBox{0, 0, 0, 0};
   if (fin.err == FI_VEC_OK && pa.apply_subpix && t == 0) {
     SubpixOut sp;
-    r.err = subpix_any<N>(PL, fin.i0, fin.i1, pa.subpix_method, pa.nsubpix, pa.minv, cbox, &sp);
+    r.err = subpix_any(PL, Cfg<N>::LDP, N, fin.i0, fin.i1, pa.subpix_method, pa.nsubpix,
+                       pa.minv, cbox, &sp);
     r.subpix_tie = sp.tie;
     r.dx = sp.dx32;
     r.dy = sp.dy32;
@@ -600,8 +588,8 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
         a1 = q.i1;
         if (t == 0) {
           SubpixOut sp;
-          const int e = subpix_any<N>(PL, a0, a1, pa.subpix_method, pa.nsubpix, pa.minv, cbox,
-                                      &sp);
+          const int e = subpix_any(PL, Cfg<N>::LDP, N, a0, a1, pa.subpix_method, pa.nsubpix,
+                                   pa.minv, cbox, &sp);
           float* o = so->peaks + ((int64_t)so->w * K + k) * FI_PEAK_FIELDS;
           o[0] = (float)(ix0 - a1);
           o[1] = (float)(iy0 - a0);
@@ -883,7 +871,8 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::THREADS)
     k_peaks(float* planes, const double* norms, int count, PeakArgs pa, float* dxs, float* dys,
-            float* cmaxs, uint8_t* errs, int32_t* pi0, int32_t* pi1) {
+            float* cmaxs, uint8_t* errs, int32_t* pi0, int32_t* pi1, int32_t* pcount,
+            float* peaks, uint8_t* perr) {
   using C = Cfg<N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int g = threadIdx.x / C::G;
@@ -896,7 +885,8 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
   if (t < N)
     for (int i0 = 0; i0 < N; ++i0) PL[i0 * C::LDP + t] = in[i0 * N + t];
   gsync<C::G>(g);
-  VecResult r = peak_and_subpix<N>(PL, pa, norms[w], t, g, red, nullptr);
+  SecondaryOut so{pcount, peaks, perr, w, false, 0, 0};
+  VecResult r = peak_and_subpix<N>(PL, pa, norms[w], t, g, red, pa.nb_peaks > 1 ? &so : nullptr);
   if (pa.mask == nullptr && t < N && (r.nb.r1 > r.nb.r0))
     for (int i0 = 0; i0 < N; ++i0)
       if (r.nb.has(i0, t)) in[i0 * N + t] = NAN;
@@ -968,7 +958,8 @@ static int launch_pass(const fi_piv_pass_args& a, const float* w0, const float* 
 template <int N>
 static int launch_peaks(float* planes, const double* norms, int count, const PeakArgs& pa,
                         float* dxs, float* dys, float* cm, uint8_t* errs, int32_t* pi0,
-                        int32_t* pi1, cudaStream_t s) {
+                        int32_t* pi1, int32_t* pcount, float* peaks, uint8_t* perr,
+                        cudaStream_t s) {
   using C = Cfg<N>;
   static bool attr_done = false;
   if (!attr_done) {
@@ -978,7 +969,7 @@ static int launch_peaks(float* planes, const double* norms, int count, const Pea
   }
   const int blocks = (count + C::WPB - 1) / C::WPB;
   k_peaks<N><<<blocks, C::THREADS, C::SMEM, s>>>(planes, norms, count, pa, dxs, dys, cm, errs,
-                                                  pi0, pi1);
+                                                  pi0, pi1, pcount, peaks, perr);
   return check_launch("k_peaks");
 }
 
@@ -1079,39 +1070,70 @@ extern "C" int fi_correl_windows(const float* win0, const float* win1, int count
 }
 
 extern "C" int fi_subpix_at(const float* planes, int count, int n, const int32_t* peak_i0,
-                            const int32_t* peak_i1, float* deltaxs, float* deltays,
+                            const int32_t* peak_i1, int subpix_method, int nsubpix,
+                            const double* subpix_minv, float* deltaxs, float* deltays,
                             uint8_t* errors, void* stream) {
   FI_REQUIRE(planes && peak_i0 && peak_i1 && deltaxs && deltays && errors,
              "fi_subpix_at: null pointer");
   FI_REQUIRE(count > 0 && n >= 3, "fi_subpix_at: bad sizes");
+  FI_REQUIRE(subpix_method >= FI_SUBPIX_GAUSSIAN2 && subpix_method <= FI_SUBPIX_NONE,
+             "fi_subpix_at: bad subpix_method %d", subpix_method);
+  FI_REQUIRE(subpix_method == FI_SUBPIX_GAUSSIAN2 || (nsubpix >= 1 && nsubpix <= FI_MAX_NSUBPIX),
+             "fi_subpix_at: nsubpix %d out of 1..%d", nsubpix, FI_MAX_NSUBPIX);
+  FI_REQUIRE(subpix_method != FI_SUBPIX_GAUSSIAN || subpix_minv,
+             "fi_subpix_at: '2d_gaussian' needs subpix_minv");
   k_subpix_at<<<(count + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
-      planes, count, n, peak_i0, peak_i1, deltaxs, deltays, errors);
+      planes, count, n, peak_i0, peak_i1, subpix_method, nsubpix, subpix_minv, deltaxs, deltays,
+      errors);
   return check_launch("fi_subpix_at");
 }
 
 extern "C" int fi_peaks_from_planes(float* planes, const double* norms, int count, int n,
                                     const uint8_t* mask, int box_i0_start, int box_i0_stop,
                                     int box_i1_start, int box_i1_stop, int particle_radius,
-                                    int apply_subpix, float* deltaxs, float* deltays,
-                                    float* correls_max, uint8_t* errors, int32_t* peak_i0,
-                                    int32_t* peak_i1, void* stream) {
+                                    int apply_subpix, int subpix_method, int nsubpix,
+                                    const double* subpix_minv, int nb_peaks, float* deltaxs,
+                                    float* deltays, float* correls_max, uint8_t* errors,
+                                    int32_t* peak_i0, int32_t* peak_i1, int32_t* peaks_count,
+                                    float* peaks, uint8_t* peaks_err, void* stream) {
   FI_REQUIRE(planes && norms && deltaxs && deltays && correls_max && errors,
              "fi_peaks_from_planes: null pointer");
   FI_REQUIRE(supported_n(n), "fi_peaks_from_planes: window size %d not supported", n);
   FI_REQUIRE(count > 0, "fi_peaks_from_planes: no plane");
   FI_REQUIRE(box_i0_start >= 0 && box_i0_stop <= n && box_i1_start >= 0 && box_i1_stop <= n,
              "fi_peaks_from_planes: bad search box");
+  FI_REQUIRE(subpix_method >= FI_SUBPIX_GAUSSIAN2 && subpix_method <= FI_SUBPIX_NONE,
+             "fi_peaks_from_planes: bad subpix_method %d", subpix_method);
+  FI_REQUIRE(subpix_method == FI_SUBPIX_GAUSSIAN2 || (nsubpix >= 1 && nsubpix <= FI_MAX_NSUBPIX),
+             "fi_peaks_from_planes: nsubpix %d out of 1..%d", nsubpix, FI_MAX_NSUBPIX);
+  FI_REQUIRE(subpix_method != FI_SUBPIX_GAUSSIAN || subpix_minv,
+             "fi_peaks_from_planes: '2d_gaussian' needs subpix_minv");
+  FI_REQUIRE(nb_peaks >= 1 && nb_peaks <= FI_MAX_PEAKS, "fi_peaks_from_planes: nb_peaks %d",
+             nb_peaks);
+  FI_REQUIRE(nb_peaks == 1 || (peaks_count && peaks && peaks_err),
+             "fi_peaks_from_planes: secondary peaks need peaks_count, peaks and peaks_err");
   PeakArgs pa;
   pa.mask = mask;
   pa.box = SearchBox{box_i0_start, box_i0_stop, box_i1_start, box_i1_stop};
   pa.radius = particle_radius;
   pa.apply_subpix = apply_subpix;
+  pa.subpix_method = subpix_method;
+  pa.nsubpix = nsubpix;
+  pa.minv = subpix_minv;
+  pa.nb_peaks = nb_peaks;
   cudaStream_t s = (cudaStream_t)stream;
+#define FI_PEAKS_CASE(NN)                                                                     \
+  case NN:                                                                                   \
+    return launch_peaks<NN>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, \
+                            peak_i0, peak_i1, peaks_count, peaks, peaks_err, s);
   switch (n) {
-    case 16: return launch_peaks<16>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, peak_i0, peak_i1, s);
-    case 24: return launch_peaks<24>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, peak_i0, peak_i1, s);
-    case 32: return launch_peaks<32>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, peak_i0, peak_i1, s);
-    case 48: return launch_peaks<48>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, peak_i0, peak_i1, s);
-    default: return launch_peaks<64>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, peak_i0, peak_i1, s);
+    FI_PEAKS_CASE(16)
+    FI_PEAKS_CASE(24)
+    FI_PEAKS_CASE(32)
+    FI_PEAKS_CASE(48)
+    default:
+      return launch_peaks<64>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors,
+                              peak_i0, peak_i1, peaks_count, peaks, peaks_err, s);
   }
+#undef FI_PEAKS_CASE
 }

@@ -151,24 +151,29 @@ int fi_correl_windows(const float* win0, const float* win1, int count, int n,
  * (calcul/correl.py:561-568, 226-275) and CorrelBase.apply_subpix
  * (calcul/correl.py:277-281).  When mask is NULL the second-chance NaN box is
  * written into `planes` in place, as upstream does.  Outputs as fi_piv_pass
- * (integer displacements when apply_subpix == 0), plus the peak indices.
+ * (integer displacements when apply_subpix == 0), plus the peak indices; with
+ * nb_peaks > 1 the other peaks (correl.py:250-273) go to peaks_count / peaks /
+ * peaks_err as in fi_piv_pass_args (replacement fields without input shift).
  */
 int fi_peaks_from_planes(float* planes, const double* norms, int count, int n,
                          const uint8_t* mask, int box_i0_start, int box_i0_stop,
                          int box_i1_start, int box_i1_stop, int particle_radius,
-                         int apply_subpix, float* deltaxs, float* deltays,
-                         float* correls_max, uint8_t* errors, int32_t* peak_i0,
-                         int32_t* peak_i1, void* stream);
+                         int apply_subpix, int subpix_method, int nsubpix,
+                         const double* subpix_minv, int nb_peaks, float* deltaxs,
+                         float* deltays, float* correls_max, uint8_t* errors,
+                         int32_t* peak_i0, int32_t* peak_i1, int32_t* peaks_count,
+                         float* peaks, uint8_t* peaks_err, void* stream);
 
 /*
- * '2d_gaussian2' subpixel fit (with its centroid fallback) at given peak indices
- * (peak_i0 = row, peak_i1 = column) on planes in device memory: the
+ * Subpixel fit (FI_SUBPIX_*, nsubpix, subpix_minv as in fi_piv_pass_args) at given
+ * peak indices (peak_i0 = row, peak_i1 = column) on planes in device memory: the
  * CorrelBase.apply_subpix / SubPix.compute_subpix pair (calcul/correl.py:277-281,
  * calcul/subpix.py:107-218).  Writes displacements and FI_VEC_* codes
  * (FI_VEC_WRONG_SUBPIX, FI_VEC_CLOSE_BOUNDARY keep the integer displacement).
  */
 int fi_subpix_at(const float* planes, int count, int n, const int32_t* peak_i0,
-                 const int32_t* peak_i1, float* deltaxs, float* deltays, uint8_t* errors,
+                 const int32_t* peak_i1, int subpix_method, int nsubpix,
+                 const double* subpix_minv, float* deltaxs, float* deltays, uint8_t* errors,
                  void* stream);
 
 /* Arguments of the false-vector removal of one pass. */

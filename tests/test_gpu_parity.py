@@ -291,3 +291,64 @@ def test_members_index_range_matches_full_scan(order):
         np.testing.assert_array_equal(res[0][1], res[1][1])
         np.testing.assert_array_equal(res[0][2], res[1][2])
         assert res[0][0].sum() > nv  # buffers overlap: points in several subdomains
+
+
+@pytest.mark.parametrize("name", ["secondary_peaks_two_pass", "subpix_gaussian_single",
+                                  "subpix_centroid2_single", "subpix_none_single"])
+def test_correl_plugin_loop_vectors(name):
+    """The per-window plugin driven like upstream's _loop_vectors on the first pass
+    of a fixture (subpixel method, nsubpix, other peaks), against the oracle's pass
+    (itself bit-exact to the fixture): same errors, other peaks and displacements."""
+    from fluidimage_gb300 import CorrelGB300, PIVError
+    from oracle import piv as O
+
+    z = goldens.load(name)
+    p = goldens.params_namespace(z)
+    n = int(z["p0_shape_crop"][0])
+    shape = (n, n)
+    ref = O.piv_pass(z["im0"], z["im1"], shape, p.piv0.grid.overlap,
+                     displacement_max=p.piv0.displacement_max, keep_planes=True,
+                     method_subpix=p.piv0.method_subpix, nsubpix=p.piv0.nsubpix,
+                     nb_peaks_to_search=p.piv0.nb_peaks_to_search)
+    gx, gy = ref.ixvecs_grid, ref.iyvecs_grid
+    im0pad, im1pad, npad = O.pad_images(z["im0"], z["im1"], shape)
+    _, _, ix0p, iy0p, ix1p, iy1p = O.positions_first_pass(gx, gy, npad)
+    w0, v0 = O.crop_windows(im0pad, ix0p, iy0p, shape)
+    w1, v1 = O.crop_windows(im1pad, ix1p, iy1p, shape)
+    c = CorrelGB300(shape, shape, method_subpix=p.piv0.method_subpix, nsubpix=p.piv0.nsubpix,
+                    displacement_max=p.piv0.displacement_max,
+                    particle_radius=p.piv0.particle_radius,
+                    nb_peaks_to_search=p.piv0.nb_peaks_to_search)
+    checked = 0
+    for k in range(0, gx.size, 2):
+        if not (v0[k] and v1[k]):
+            continue
+        plane, norm = c(w0[k], w1[k])
+        top = np.sort(plane[np.isfinite(plane)].ravel())[-2:]
+        if top[1] - top[0] <= 1e-6 * abs(top[1]):  # near-tie: the peak depends on rounding
+            continue
+        try:
+            dx, dy, cmax, other = c.compute_displacements_from_correl(plane, norm)
+        except PIVError as e:
+            assert ref.err[k] in (O.ERR_BOUNDARY, O.ERR_NAN), (k, e.explanation)
+            assert ref.secondary_peaks[k] is None
+            continue
+        want = ref.secondary_peaks[k]
+        if p.piv0.nb_peaks_to_search > 1:
+            assert len(other) == len(want), (k, other, want)
+            for (a, b, cm), (wa, wb, wcm) in zip(other, want):
+                assert (a, b) == (int(wa), int(wb))
+                np.testing.assert_allclose(cm, wcm, rtol=2e-5, atol=2e-6)
+        else:
+            assert other is None
+        try:
+            sdx, sdy = c.apply_subpix(dx, dy, plane)
+            got_err = 0
+        except PIVError as e:
+            got_err = {"wrong subpix": O.ERR_WRONG_SUBPIX,
+                       "close boundary": O.ERR_CLOSE_BOUNDARY}[e.explanation]
+            sdx, sdy = float(dx), float(dy)
+        assert got_err == ref.err[k], k
+        np.testing.assert_allclose([sdx, sdy], [ref.deltaxs[k], ref.deltays[k]], atol=TOL_PX)
+        checked += 1
+    assert checked > 20
