@@ -251,11 +251,42 @@ __global__ void __launch_bounds__(YB_TILE) k_y_tiles(const double* py, int n, do
   }
 }
 
-// In place: running max forward, running min backward (one thread; tiles are few).
-__global__ void k_y_tiles_scan(int ntiles, double* tmax, double* tmin) {
-  if (threadIdx.x != 0) return;
-  for (int j = 1; j < ntiles; ++j) tmax[j] = fmax(tmax[j], tmax[j - 1]);
-  for (int j = ntiles - 2; j >= 0; --j) tmin[j] = fmin(tmin[j], tmin[j + 1]);
+// In place: running max forward, running min backward over the tiles (one block;
+// chunks of 1024 tiles, a Hillis-Steele scan per chunk in shared memory).
+__global__ void __launch_bounds__(1024) k_y_tiles_scan(int ntiles, double* tmax, double* tmin) {
+  __shared__ double a[1024], b[1024];
+  __shared__ double carry[2];
+  const int t = threadIdx.x;
+  if (t == 0) {
+    carry[0] = -INFINITY;
+    carry[1] = INFINITY;
+  }
+  __syncthreads();
+  for (int base = 0; base < ntiles; base += 1024) {
+    const int i = base + t;
+    const int ir = ntiles - 1 - i;  // backward scan reads from the end
+    a[t] = (i < ntiles) ? tmax[i] : -INFINITY;
+    b[t] = (i < ntiles) ? tmin[ir] : INFINITY;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const double va = (t >= o) ? a[t - o] : -INFINITY;
+      const double vb = (t >= o) ? b[t - o] : INFINITY;
+      __syncthreads();
+      a[t] = fmax(a[t], va);
+      b[t] = fmin(b[t], vb);
+      __syncthreads();
+    }
+    if (i < ntiles) {
+      tmax[i] = fmax(a[t], carry[0]);
+      tmin[ir] = fmin(b[t], carry[1]);
+    }
+    __syncthreads();
+    if (t == 0) {
+      carry[0] = fmax(carry[0], a[1023]);
+      carry[1] = fmin(carry[1], b[1023]);
+    }
+    __syncthreads();
+  }
 }
 
 // First index q in [0, n) with a[q] >= v for a non-decreasing a (n if none).
@@ -706,7 +737,7 @@ extern "C" int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, doubl
   FI_REQUIRE(py && y_pmax && y_smin && npts > 0, "fi_tps_y_bounds: bad arguments");
   const int nt = (npts + YB_TILE - 1) / YB_TILE;
   k_y_tiles<<<nt, YB_TILE, 0, (cudaStream_t)stream>>>(py, npts, y_pmax, y_smin);
-  k_y_tiles_scan<<<1, 32, 0, (cudaStream_t)stream>>>(nt, y_pmax, y_smin);
+  k_y_tiles_scan<<<1, 1024, 0, (cudaStream_t)stream>>>(nt, y_pmax, y_smin);
   return check_launch("fi_tps_y_bounds", 2);
 }
 

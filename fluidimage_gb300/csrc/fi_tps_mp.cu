@@ -448,10 +448,17 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
         if (lane == j) dg = sq;
         const float lrj = (lane > j) ? a[j] * rs : ((lane == j) ? sq : 0.f);
         if (lane >= j) a[j] = lrj;
+        // the row update in chunks of 8 shuffles: the fence keeps the compiler from
+        // hoisting all 31 (the row a[] then stays in registers under the cap)
 #pragma unroll
-        for (int c = j + 1; c < 32; ++c) {
-          const float lcj = __shfl_sync(full, lrj, c);
-          if (lane >= c) a[c] = fmaf(-lrj, lcj, a[c]);
+        for (int c0 = (j + 1) & ~7; c0 < 32; c0 += 8) {
+#pragma unroll
+          for (int c = c0; c < c0 + 8; ++c) {
+            if (c <= j) continue;
+            const float lcj = __shfl_sync(full, lrj, c);
+            if (lane >= c) a[c] = fmaf(-lrj, lcj, a[c]);
+          }
+          __syncwarp();
         }
       }
       if (bad && lane == 0) *s_flag = 1;
