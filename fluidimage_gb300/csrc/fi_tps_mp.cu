@@ -484,6 +484,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
           v = fmaf(-b[4 * c4 + 3], q.w, v);
         }
         b[j] = v * Lkk[j * TS + 32];
+        if ((j & 3) == 3) __syncwarp();  // bounds the broadcasts in flight (registers)
       }
       tile_store(B, m, ld, i, k, b, lane, false);
     }
@@ -497,24 +498,38 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       while (ii * (ii + 1) / 2 > pidx) --ii;
       const int jj = pidx - ii * (ii + 1) / 2;
       const int i = k + 1 + ii, j = k + 1 + jj;
-      float l[32];
-      tile_load(B, m, ld, j, k, l, lane);  // L_jk rows -> transposed in shared memory
+      {  // L_jk rows -> transposed in shared memory
+        const int r = 32 * j + lane;
 #pragma unroll
-      for (int t = 0; t < 32; ++t) Lt[t * TS + lane] = l[t];
+        for (int t = 0; t < 32; ++t) {
+          const int col = 32 * k + t;
+          Lt[t * TS + lane] = (r < m && col < m) ? B[(int64_t)col * ld + r] : ((r == col) ? 1.f : 0.f);
+        }
+      }
       __syncwarp();
-      if (i != j) tile_load(B, m, ld, i, k, l, lane);  // L_ik rows
       float acc[32];
       tile_load(B, m, ld, i, j, acc, lane);
+      // acc -= L_ik L_jk^T, the row of L_ik in two halves of 16 (registers)
 #pragma unroll
-      for (int t = 0; t < 32; ++t) {
-        const float lr = l[t];
+      for (int h = 0; h < 2; ++h) {
+        float l[16];
+        const int r = 32 * i + lane;
 #pragma unroll
-        for (int c4 = 0; c4 < 8; ++c4) {
-          const float4 q = *reinterpret_cast<const float4*>(Lt + t * TS + 4 * c4);
-          acc[4 * c4] = fmaf(-lr, q.x, acc[4 * c4]);
-          acc[4 * c4 + 1] = fmaf(-lr, q.y, acc[4 * c4 + 1]);
-          acc[4 * c4 + 2] = fmaf(-lr, q.z, acc[4 * c4 + 2]);
-          acc[4 * c4 + 3] = fmaf(-lr, q.w, acc[4 * c4 + 3]);
+        for (int t = 0; t < 16; ++t) {
+          const int col = 32 * k + 16 * h + t;
+          l[t] = (r < m && col < m) ? B[(int64_t)col * ld + r] : ((r == col) ? 1.f : 0.f);
+        }
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const float lr = l[t];
+#pragma unroll
+          for (int c4 = 0; c4 < 8; ++c4) {
+            const float4 q = *reinterpret_cast<const float4*>(Lt + (16 * h + t) * TS + 4 * c4);
+            acc[4 * c4] = fmaf(-lr, q.x, acc[4 * c4]);
+            acc[4 * c4 + 1] = fmaf(-lr, q.y, acc[4 * c4 + 1]);
+            acc[4 * c4 + 2] = fmaf(-lr, q.z, acc[4 * c4 + 2]);
+            acc[4 * c4 + 3] = fmaf(-lr, q.w, acc[4 * c4 + 3]);
+          }
         }
       }
       tile_store(B, m, ld, i, j, acc, lane, i == j);
