@@ -105,6 +105,7 @@ _SIGNATURES = {
          P, P, P, P, P, P],
     ),
     "fi_tps_phi_table": (C.c_int, [P, C.c_int64, P]),
+    "fi_tps_phi_table2": (C.c_int, [P, C.c_int64, P]),
     "fi_tps_solve_mp": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P, C.c_double,
@@ -114,7 +115,7 @@ _SIGNATURES = {
     "fi_tps_interpolate": (
         C.c_int,
         [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,
-         P, P, P, P, P, C.c_int64, P, P, P],
+         P, P, P, P, P, P, C.c_int64, P, P, P],
     ),
 }
 

@@ -18,6 +18,7 @@
 #include <cmath>
 
 #include "fi_common.cuh"
+#include "fi_df.cuh"
 
 namespace fi {
 
@@ -605,23 +606,30 @@ __global__ void k_tps_blend_centers(const fi_tps_plan* plan_ptr, const double* c
 
 // Interpolation at the new positions of subdomain blockIdx.y:
 // part[k] = coef_k * (sum_j w_j phi(|q_k - c_j|^2) + w_N + w_N+1 y + w_N+2 x).
+// Part of each subdomain's TPS at its new positions: coef * (sum_j w_j phi_j + affine)
+// (interpolate, thin_plate_spline_subdom.py:224-234).  On the lattice with the
+// (hi, lo) table the kernel sum runs in double-float on the FP32 pipe (~1e-14
+// relative per term), else in FP64.
 __global__ void __launch_bounds__(256)
     k_tps_eval(const int32_t* counts, const int64_t* offsets, const int32_t* indices,
                const int64_t* w_off, const double* weights, const double* cx, const double* cy,
                const int32_t* ncounts, const int64_t* noffsets, const int32_t* nindices,
                const double* ncoefs, const double* px, const double* py, double* partx,
-               double* party, const double* table, int64_t tsize, const int32_t* cxy2,
-               const int32_t* c_on_lattice) {
+               double* party, const double* table, const float2* table2, int64_t tsize,
+               const int32_t* cxy2, const int32_t* c_on_lattice, int max_members) {
   extern __shared__ double sh[];
   const int sd = blockIdx.y;
   const int N = counts[sd], n = N + 3, M = ncounts[sd];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (blockIdx.x * blockDim.x >= M) return;
+  const int NM = max_members;
   double* scx = sh;
-  double* scy = sh + N;
-  double* swx = sh + 2 * N;
-  double* swy = sh + 2 * N + n;
-  int2* sxy2 = reinterpret_cast<int2*>(swy + n);  // lattice coordinates of the centres
+  double* scy = sh + NM;
+  double* swx = sh + 2 * NM;
+  double* swy = swx + NM + 3;
+  int2* sxy2 = reinterpret_cast<int2*>(swy + NM + 3);   // lattice coordinates of the centres
+  float2* dwx = reinterpret_cast<float2*>(sxy2 + NM);  // weights as (hi, lo) pairs
+  float2* dwy = dwx + NM;
   __shared__ int s_lat;
   const int64_t off = offsets[sd];
   const double* w = weights + w_off[sd];
@@ -635,6 +643,10 @@ __global__ void __launch_bounds__(256)
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     swx[j] = w[j];
     swy[j] = w[n + j];
+    if (table2 != nullptr && j < N) {
+      dwx[j] = df_split(w[j]);
+      dwy[j] = df_split(w[n + j]);
+    }
   }
   __syncthreads();
   if (k >= M) return;
@@ -645,7 +657,43 @@ __global__ void __launch_bounds__(256)
   const double X2 = 2.0 * x, Y2 = 2.0 * y;
   const bool qlat = s_lat && table != nullptr && X2 == rint(X2) && Y2 == rint(Y2) &&
                     fabs(X2) < 1073741824.0 && fabs(Y2) < 1073741824.0;
-  if (qlat) {  // 4 r^2 in integer arithmetic, table lookup
+  if (qlat && table2 != nullptr) {  // 4 r^2 in integers, double-float sums
+    const int QX = (int)X2, QY = (int)Y2;
+    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+    constexpr int U = 8;  // table loads issued ahead of their use
+    for (int j0 = 0; j0 < N; j0 += U) {
+      float2 f[U];
+      bool far[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        far[u] = false;
+        f[u] = make_float2(0.f, 0.f);
+        if (j < N) {
+          const int2 c = sxy2[j];
+          const int64_t dx = (int64_t)(QX - c.x), dy = (int64_t)(QY - c.y);
+          const int64_t kq = dy * dy + dx * dx;
+          far[u] = kq >= tsize;
+          if (!far[u]) f[u] = __ldg(table2 + kq);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int j = j0 + u;
+        if (j >= N) break;
+        if (far[u]) {  // beyond the table: float64 kernel value
+          const double fd = tps_phi(scx[j], scy[j], x, y);
+          vx = fma(swx[j], fd, vx);
+          vy = fma(swy[j], fd, vy);
+        } else {
+          df_mac(dwx[j], f[u], hx, lx);
+          df_mac(dwy[j], f[u], hy, ly);
+        }
+      }
+    }
+    vx += (double)hx + (double)lx;
+    vy += (double)hy + (double)ly;
+  } else if (qlat) {  // 4 r^2 in integer arithmetic, table lookup
     const int QX = (int)X2, QY = (int)Y2;
     for (int j = 0; j < N; ++j) {
       const int2 c = sxy2[j];
@@ -669,7 +717,6 @@ __global__ void __launch_bounds__(256)
   party[noff + k] = __dmul_rn(c, vy);
 }
 
-// Gather the interpolated values per new position (subdomain order) and round.
 __global__ void k_tps_gather(const fi_tps_plan* plan_ptr, const int32_t* ncounts,
                              const int64_t* noffsets, const int32_t* nindices,
                              const double* ncoefs, const double* partx, const double* party,
@@ -807,7 +854,8 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                                   int npts, const int32_t* ncounts, const int64_t* noffsets,
                                   const int32_t* nindices, const double* ncoefs, double* partx,
                                   double* party, double* out_x, double* out_y, int32_t* out_rx,
-                                  int32_t* out_ry, const double* phi_table, int64_t table_size,
+                                  int32_t* out_ry, const double* phi_table,
+                                  const float* phi_table2, int64_t table_size,
                                   const int32_t* cxy2, const int32_t* c_on_lattice,
                                   void* stream) {
   FI_REQUIRE(plan && cx && cy && counts && offsets && indices && w_offsets && weights && px &&
@@ -817,7 +865,8 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
   FI_REQUIRE(nb_subdom > 0 && npts > 0, "fi_tps_interpolate: bad sizes");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t smem = (size_t)(4 * max_members + 6) * sizeof(double) +
-                      (size_t)max_members * sizeof(int2);
+                      (size_t)max_members * sizeof(int2) +
+                      (size_t)2 * max_members * sizeof(float2);
   FI_REQUIRE(smem <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
              max_members);
   static size_t attr = 0;
@@ -829,9 +878,10 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
   if (max_new_members > 0) {
     const int threads = 256;
     dim3 grid((max_new_members + threads - 1) / threads, nb_subdom);
-    k_tps_eval<<<grid, threads, smem, s>>>(counts, offsets, indices, w_offsets, weights, cx, cy,
-                                           ncounts, noffsets, nindices, ncoefs, px, py, partx,
-                                           party, phi_table, table_size, cxy2, c_on_lattice);
+    k_tps_eval<<<grid, threads, smem, s>>>(
+        counts, offsets, indices, w_offsets, weights, cx, cy, ncounts, noffsets, nindices, ncoefs,
+        px, py, partx, party, phi_table, reinterpret_cast<const float2*>(phi_table2), table_size,
+        cxy2, c_on_lattice, max_members);
     add_launches(1);
   }
   const int threads = 256;

@@ -25,6 +25,7 @@
 #include <cmath>
 
 #include "fi_common.cuh"
+#include "fi_df.cuh"
 
 namespace fi {
 
@@ -51,6 +52,13 @@ __global__ void k_phi_table(double* table, int64_t count) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count;
        k += (int64_t)gridDim.x * blockDim.x)
     table[k] = phi_direct((double)k * 0.25);
+}
+
+// The same values as (hi, lo) float pairs (double-float evaluation).
+__global__ void k_phi_table2(float2* table, int64_t count) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count;
+       k += (int64_t)gridDim.x * blockDim.x)
+    table[k] = df_split(phi_direct((double)k * 0.25));
 }
 
 // ------------------------------------------------------------------ block helpers
@@ -120,40 +128,6 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 }
 
 constexpr int TS = 36;  // row stride (floats) of the 32 x 32 shared tiles: float4-aligned rows
-
-// ------------------------------------------------------------------ double-float
-// Values as unevaluated pairs hi + lo of floats (about 48 significant bits).  The
-// error-free transformations use the _rn intrinsics so that no FMA contraction can
-// merge a product into the following sum.
-__device__ __forceinline__ float2 df_split(double v) {
-  const float hi = __double2float_rn(v);
-  return make_float2(hi, __double2float_rn(v - (double)hi));
-}
-
-__device__ __forceinline__ double df_to_double(float2 a) { return (double)a.x + (double)a.y; }
-
-// (a.x + a.y) + (b.x + b.y), renormalised
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  const float s = __fadd_rn(a.x, b.x);
-  const float bb = __fsub_rn(s, a.x);
-  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
-  const float lo = __fadd_rn(__fadd_rn(a.y, b.y), err);
-  const float hi = __fadd_rn(s, lo);
-  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
-}
-
-// (sh, sl) += b * z (the lo * lo term, 2^-48 relative, is dropped)
-__device__ __forceinline__ void df_mac(float2 b, float2 z, float& sh, float& sl) {
-  const float p = __fmul_rn(b.x, z.x);
-  float e = __fmaf_rn(b.x, z.x, -p);
-  e = __fmaf_rn(b.x, z.y, e);
-  e = __fmaf_rn(b.y, z.x, e);
-  const float t = __fadd_rn(sh, p);
-  const float bb = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb));
-  sl = __fadd_rn(sl, __fadd_rn(err, e));
-  sh = t;
-}
 
 // rho = g - B z for two right-hand sides, in double-float; B (m x m, symmetric, both
 // triangles, column-major, leading dimension ld) holds (hi, lo) pairs.  Each warp
@@ -1045,6 +1019,13 @@ extern "C" int fi_tps_phi_table(double* table, int64_t count, void* stream) {
   FI_REQUIRE(table && count > 0, "fi_tps_phi_table: bad arguments");
   k_phi_table<<<1024, 256, 0, (cudaStream_t)stream>>>(table, count);
   return check_launch("fi_tps_phi_table");
+}
+
+extern "C" int fi_tps_phi_table2(float* table2, int64_t count, void* stream) {
+  FI_REQUIRE(table2 && count > 0 && ((uintptr_t)table2 & 7) == 0,
+             "fi_tps_phi_table2: bad arguments");
+  k_phi_table2<<<1024, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<float2*>(table2), count);
+  return check_launch("fi_tps_phi_table2");
 }
 
 extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members,

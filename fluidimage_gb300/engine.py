@@ -212,14 +212,20 @@ MP_MAX_MEMBERS = 800
 _PHI_TABLES = {}
 
 
-def phi_table(device):
-    """The per-device table of the TPS kernel values (built on first use)."""
+def phi_table(device, pairs=False):
+    """The per-device table of the TPS kernel values, float64 or (hi, lo) float pairs
+    (built on first use)."""
     torch = _torch()
-    key = (device.type, device.index if device.index is not None else torch.cuda.current_device())
+    key = (device.type, device.index if device.index is not None else torch.cuda.current_device(),
+           pairs)
     if key not in _PHI_TABLES:
-        table = torch.empty(PHI_TABLE_SIZE, dtype=torch.float64, device=device)
-        L.check(L.load().fi_tps_phi_table(L.ptr(table), PHI_TABLE_SIZE, L.stream_handle()),
-                "fi_tps_phi_table")
+        if pairs:
+            table = torch.empty(2 * PHI_TABLE_SIZE, dtype=torch.float32, device=device)
+            fn, name = L.load().fi_tps_phi_table2, "fi_tps_phi_table2"
+        else:
+            table = torch.empty(PHI_TABLE_SIZE, dtype=torch.float64, device=device)
+            fn, name = L.load().fi_tps_phi_table, "fi_tps_phi_table"
+        L.check(fn(L.ptr(table), PHI_TABLE_SIZE, L.stream_handle()), name)
         _PHI_TABLES[key] = table
     return _PHI_TABLES[key]
 
@@ -362,7 +368,8 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                    L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),
                                    L.ptr(partx), L.ptr(party), L.ptr(out.out_x),
                                    L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry),
-                                   L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat), s),
+                                   L.ptr(table), L.ptr(phi_table(dev, pairs=True)),
+                                   PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat), s),
             "fi_tps_interpolate")
     return out
 

@@ -328,6 +328,12 @@ int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members, const 
 int fi_tps_phi_table(double* table, int64_t count, void* stream);
 
 /*
+ * The same table as (hi, lo) float pairs (2 * count floats, 8-byte aligned): the
+ * double-float evaluation of fi_tps_interpolate.  No reference counterpart.
+ */
+int fi_tps_phi_table2(float* table2, int64_t count, void* stream);
+
+/*
  * Mixed-precision TPS solve (same inputs and outputs as fi_tps_solve): null-space
  * form B z = Q2^T u with B = Q2^T (K + lam I) Q2 (P = Q R, Householder; B projected
  * in FP64 with the compact WY form of Q), factorised in FP32 (blocked Cholesky) and
@@ -369,7 +375,8 @@ int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, const double*
  * works/piv/singlepass.py:752-753).  ncounts/noffsets/nindices/ncoefs: membership
  * of the new positions (fi_tps_members); partx/party: scratch of the same size
  * as nindices.  cxy2/c_on_lattice (nullable, from fi_tps_lattice on the centres)
- * enable integer 4 r^2 table indices.
+ * enable integer 4 r^2 table indices; with phi_table2 (nullable, fi_tps_phi_table2)
+ * the kernel sums on the lattice run in double-float (~1e-14 relative per term).
  */
 int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        int max_new_members, const double* cx, const double* cy,
@@ -379,8 +386,8 @@ int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        const int64_t* noffsets, const int32_t* nindices, const double* ncoefs,
                        double* partx, double* party, double* out_x, double* out_y,
                        int32_t* out_rx, int32_t* out_ry, const double* phi_table,
-                       int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
-                       void* stream);
+                       const float* phi_table2, int64_t table_size, const int32_t* cxy2,
+                       const int32_t* c_on_lattice, void* stream);
 
 #ifdef __cplusplus
 }
