@@ -43,6 +43,7 @@ METRIC = "PIV vectors/s at <=0.005 px vs FP64; plain FP32 vs batched tensor-core
 UNIT = "vectors/s"
 WORKLOAD = "config2: 2048x2048 uint16 pair, Oseen vortex, 3 passes 64/32/16 px, overlap 0.5, fix thr 2, TPS subdom 200 smoothing 0.5"
 SAMPLE_SHAPE = (512, 512)
+TPS_DRAM_BYTES_PER_SUBDOMAIN = (76.292096e6 + 112.621824e6) / 72
 
 
 def parse_args():
@@ -364,8 +365,16 @@ def roofline(dominant, outs, work, peaks, peak_kind, steps):
         per_launch = flops / max(nlaunch, 1)
         achieved = per_launch / avg_s / 1e12
         peak = 1.25
+        # DRAM bytes per subdomain from one ncu capture of this kernel (72 subdomains
+        # of the same recipe at 1024², profiles/k_tps_solve_mp_config2_1024.md),
+        # scaled by the subdomains of an average launch
+        nsub = sum(t.nb_subdom for pd in outs for t in (pd.tps_next, pd.tps_final)
+                   if t is not None)
+        traffic = TPS_DRAM_BYTES_PER_SUBDOMAIN * nsub / max(nlaunch, 1)
         return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read+write per subdomain (1024^2 capture) "
+                                  "x subdomains per launch",
                 "work": "reference-equivalent FP64 LU flops, sum 2/3 (N+3)^3 per solve",
                 "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
                 "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
