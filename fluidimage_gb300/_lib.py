@@ -37,6 +37,9 @@ MAX_NSUBPIX = 4
 MAX_PEAKS = 4
 PEAK_FIELDS = 5
 
+PRE_U8, PRE_U16, PRE_F32, PRE_F64 = 0, 1, 2, 3
+MODES = {"reflect": 0, "constant": 1, "nearest": 2, "mirror": 3, "wrap": 4}
+
 P = C.c_void_p
 
 
@@ -111,6 +114,16 @@ _SIGNATURES = {
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P, C.c_double,
          C.c_int, P, P, P, P, P, P, P, P, P, P],
     ),
+    "fi_rank_filter": (
+        C.c_int,
+        [P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+         C.c_double, P, P],
+    ),
+    "fi_subtract_weighted": (
+        C.c_int, [P, P, C.c_int, C.c_int64, C.c_double, C.c_int, C.c_int, P, P]),
+    "fi_clamp": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P]),
+    "fi_sq_sum_max": (C.c_int, [P, C.c_int, C.c_int64, P, P, C.c_int, P]),
+    "fi_tanh_rescale": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
     "fi_tps_interpolate": (
         C.c_int,

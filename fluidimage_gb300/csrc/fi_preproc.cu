@@ -1,0 +1,351 @@
+// Image preprocessing on the device: the scipy.ndimage / numpy tools of
+// fluidimage's preprocessing toolbox (works/preproc/_toolbox_py.py:66-155,
+// 189-256, 265-289, 332-355).
+//
+// * rank filters (minimum / maximum / median / percentile) over a box window of a
+//   stack of images (nt, ny, nx), with the boundary modes of scipy.ndimage
+//   ('reflect', 'mirror', 'nearest', 'wrap', 'constant'), window [i - s//2,
+//   i - s//2 + s - 1] along each axis; min and max are separable (one pass per
+//   axis), other ranks select the rank-th smallest window value exactly by a
+//   radix select on order-preserving integer keys (exact for every dtype);
+// * img - weight * filtered with numpy's result type (float64 for integer images
+//   and a float weight, float32 for float32 images, wrapping integer arithmetic for
+//   an integer weight), optionally clamped at 0;
+// * clamping (global_threshold) and the tanh rescaling (rescale_intensity_tanh).
+#include <cstdint>
+#include <cstring>
+
+#include "fi_common.cuh"
+
+namespace fi {
+
+// ------------------------------------------------------------------ element access
+__device__ __forceinline__ double load_d(const void* p, int dtype, int64_t i) {
+  switch (dtype) {
+    case FI_PRE_U8: return (double)static_cast<const uint8_t*>(p)[i];
+    case FI_PRE_U16: return (double)static_cast<const uint16_t*>(p)[i];
+    case FI_PRE_F32: return (double)static_cast<const float*>(p)[i];
+    default: return static_cast<const double*>(p)[i];
+  }
+}
+
+// Order-preserving unsigned key of an element (floats: the sign-magnitude order
+// mapped to unsigned order).  NaN has no place in that order: callers reject
+// images with NaN.
+__device__ __forceinline__ uint64_t key_of(const void* p, int dtype, int64_t i) {
+  switch (dtype) {
+    case FI_PRE_U8: return static_cast<const uint8_t*>(p)[i];
+    case FI_PRE_U16: return static_cast<const uint16_t*>(p)[i];
+    case FI_PRE_F32: {
+      const uint32_t u = __float_as_uint(static_cast<const float*>(p)[i]);
+      return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    }
+    default: {
+      const uint64_t u = (uint64_t)__double_as_longlong(static_cast<const double*>(p)[i]);
+      return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+    }
+  }
+}
+
+__device__ __forceinline__ void store_key(void* p, int dtype, int64_t i, uint64_t k) {
+  switch (dtype) {
+    case FI_PRE_U8: static_cast<uint8_t*>(p)[i] = (uint8_t)k; break;
+    case FI_PRE_U16: static_cast<uint16_t*>(p)[i] = (uint16_t)k; break;
+    case FI_PRE_F32: {
+      const uint32_t u = (uint32_t)k;
+      static_cast<float*>(p)[i] = __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+      break;
+    }
+    default: {
+      const uint64_t u = k;
+      static_cast<double*>(p)[i] = __longlong_as_double(
+          (long long)((u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u));
+    }
+  }
+}
+
+__device__ __forceinline__ int key_bits(int dtype) {
+  return dtype == FI_PRE_U8 ? 8 : dtype == FI_PRE_U16 ? 16 : dtype == FI_PRE_F32 ? 32 : 64;
+}
+
+// scipy.ndimage boundary extension of index i on an axis of length n; -1 means
+// "use cval" (mode 'constant').
+__device__ __forceinline__ int64_t extend(int64_t i, int64_t n, int mode) {
+  if (i >= 0 && i < n) return i;
+  switch (mode) {
+    case FI_MODE_NEAREST: return i < 0 ? 0 : n - 1;
+    case FI_MODE_WRAP: {
+      int64_t r = i % n;
+      return r < 0 ? r + n : r;
+    }
+    case FI_MODE_CONSTANT: return -1;
+    case FI_MODE_MIRROR: {
+      if (n == 1) return 0;
+      const int64_t p = 2 * n - 2;
+      int64_t r = i % p;
+      if (r < 0) r += p;
+      return r < n ? r : p - r;
+    }
+    default: {  // reflect: d c b a | a b c d | d c b a
+      const int64_t p = 2 * n;
+      int64_t r = i % p;
+      if (r < 0) r += p;
+      return r < n ? r : p - 1 - r;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ min / max
+// One axis of a separable minimum or maximum filter over a (nt, ny, nx) stack.
+// Keys compare like the values; cval enters as its key.
+__global__ void k_minmax_axis(const void* in, int in_is_key, const uint64_t* kin, int dtype,
+                              int64_t nt, int64_t ny, int64_t nx, int axis, int size, int mode,
+                              uint64_t ckey, int is_max, uint64_t* kout) {
+  const int64_t total = nt * ny * nx;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = e % nx, y = (e / nx) % ny, t = e / (nx * ny);
+    const int64_t n = axis == 0 ? nt : axis == 1 ? ny : nx;
+    const int64_t pos = axis == 0 ? t : axis == 1 ? y : x;
+    const int64_t stride = axis == 0 ? ny * nx : axis == 1 ? nx : 1;
+    const int64_t base = e - pos * stride;
+    uint64_t best = is_max ? 0ull : ~0ull;
+    const int64_t s0 = pos - size / 2;
+    for (int k = 0; k < size; ++k) {
+      const int64_t j = extend(s0 + k, n, mode);
+      const uint64_t v = (j < 0) ? ckey : (in_is_key ? kin[base + j * stride]
+                                                      : key_of(in, dtype, base + j * stride));
+      best = is_max ? (v > best ? v : best) : (v < best ? v : best);
+    }
+    kout[e] = best;
+  }
+}
+
+__global__ void k_keys_to_values(const uint64_t* k, int dtype, int64_t count, void* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    store_key(out, dtype, e, k[e]);
+}
+
+// ------------------------------------------------------------------ rank select
+// The rank-th smallest value of each box window, by a radix select over the keys
+// (most significant bit first): per bit, count the window values whose key shares
+// the prefix found so far and has a 0 at this bit.
+__global__ void k_rank_select(const void* in, int dtype, int64_t nt, int64_t ny, int64_t nx,
+                              int st, int sy, int sx, int rank, int mode, uint64_t ckey,
+                              void* out) {
+  const int64_t total = nt * ny * nx;
+  const int bits = key_bits(dtype);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = e % nx, y = (e / nx) % ny, t = e / (nx * ny);
+    const int64_t t0 = t - st / 2, y0 = y - sy / 2, x0 = x - sx / 2;
+    uint64_t prefix = 0;
+    int r = rank;
+    for (int b = bits - 1; b >= 0; --b) {
+      const uint64_t hi_mask = (b == 63) ? 0ull : (~0ull << (b + 1));
+      int zeros = 0;
+      for (int a = 0; a < st; ++a) {
+        const int64_t ta = extend(t0 + a, nt, mode);
+        for (int c = 0; c < sy; ++c) {
+          const int64_t yc = extend(y0 + c, ny, mode);
+          for (int d = 0; d < sx; ++d) {
+            const int64_t xd = extend(x0 + d, nx, mode);
+            const uint64_t v = (ta < 0 || yc < 0 || xd < 0)
+                                   ? ckey
+                                   : key_of(in, dtype, (ta * ny + yc) * nx + xd);
+            if ((v & hi_mask) == prefix && !((v >> b) & 1ull)) ++zeros;
+          }
+        }
+      }
+      if (r >= zeros) {
+        r -= zeros;
+        prefix |= (1ull << b);
+      }
+    }
+    store_key(out, dtype, e, prefix);
+  }
+}
+
+// ------------------------------------------------------------------ arithmetic
+// out = img - weight * filt in the numpy result type out_dtype: FI_PRE_F64 /
+// FI_PRE_F32 (float arithmetic; float32 for float32 images), or the image's integer
+// type (an integer weight: wrapping integer arithmetic); clamp: negatives -> 0.
+__global__ void k_subtract_weighted(const void* img, const void* filt, int dtype, int64_t count,
+                                    double weight, int out_dtype, int clamp, void* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (out_dtype == FI_PRE_F64) {
+      // product rounded before the difference, like numpy (no FMA contraction)
+      const double v = __dsub_rn(load_d(img, dtype, e), __dmul_rn(weight, load_d(filt, dtype, e)));
+      static_cast<double*>(out)[e] = (clamp && v < 0.0) ? 0.0 : v;
+    } else if (out_dtype == FI_PRE_F32) {
+      const float w = (float)weight;
+      const float v = __fsub_rn((float)load_d(img, dtype, e),
+                                __fmul_rn(w, (float)load_d(filt, dtype, e)));
+      static_cast<float*>(out)[e] = (clamp && v < 0.f) ? 0.f : v;
+    } else {  // integer weight on an integer image: modular arithmetic of the dtype
+      const int64_t w = (int64_t)weight;
+      const int64_t v = (int64_t)load_d(img, dtype, e) - w * (int64_t)load_d(filt, dtype, e);
+      if (out_dtype == FI_PRE_U8) static_cast<uint8_t*>(out)[e] = (uint8_t)v;
+      else static_cast<uint16_t*>(out)[e] = (uint16_t)v;
+    }
+  }
+}
+
+// global_threshold: img_out[img_out < lo] = lo; img_out[img_out > hi] = hi (the
+// bounds already converted to the image's dtype by the caller).
+__global__ void k_clamp(const void* in, int dtype, int64_t count, double lo, double hi, void* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = load_d(in, dtype, e);
+    const double w = v < lo ? lo : (v > hi ? hi : v);
+    switch (dtype) {
+      case FI_PRE_U8: static_cast<uint8_t*>(out)[e] = (uint8_t)w; break;
+      case FI_PRE_U16: static_cast<uint16_t*>(out)[e] = (uint16_t)w; break;
+      case FI_PRE_F32: static_cast<float*>(out)[e] = (float)w; break;
+      default: static_cast<double*>(out)[e] = w;
+    }
+  }
+}
+
+// Per block: sum of img**2 in the image dtype's arithmetic (integer squares wrap
+// modulo 2^bits like numpy's img**2) accumulated in float64, and max(img).
+__global__ void k_sq_sum_max(const void* in, int dtype, int64_t count, double* part_sum,
+                             double* part_max) {
+  __shared__ double ss[32], sm[32];
+  double s = 0.0, m = -INFINITY;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = load_d(in, dtype, e);
+    double q;
+    if (dtype == FI_PRE_U8) q = (double)(uint8_t)((uint32_t)v * (uint32_t)v);
+    else if (dtype == FI_PRE_U16) q = (double)(uint16_t)((uint32_t)v * (uint32_t)v);
+    else if (dtype == FI_PRE_F32) q = (double)__fmul_rn((float)v, (float)v);
+    else q = v * v;
+    s += q;
+    m = fmax(m, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    ss[wid] = s;
+    sm[wid] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = -INFINITY;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += ss[w];
+      b = fmax(b, sm[w]);
+    }
+    part_sum[blockIdx.x] = a;
+    part_max[blockIdx.x] = b;
+  }
+}
+
+// rescale_intensity_tanh: out = floor(max(img) / max(tanh(img / thr)) * tanh(img / thr))
+// in float64 (tanh is increasing, so max(tanh(img / thr)) = tanh(max(img) / thr)).
+__global__ void k_tanh_rescale(const void* in, int dtype, int64_t count, double thr,
+                               double scale, double* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = floor(scale * tanh(load_d(in, dtype, e) / thr));
+}
+
+static int grid_for(int64_t count) {
+  const int64_t b = (count + 255) / 256;
+  return (int)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
+}
+
+}  // namespace fi
+
+using namespace fi;
+
+extern "C" int fi_rank_filter(const void* in, void* out, int dtype, int nt, int ny, int nx,
+                              int st, int sy, int sx, int rank, int mode, double cval,
+                              void* scratch, void* stream) {
+  FI_REQUIRE(in && out, "fi_rank_filter: null pointer");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_rank_filter: bad dtype %d", dtype);
+  FI_REQUIRE(mode >= FI_MODE_REFLECT && mode <= FI_MODE_WRAP, "fi_rank_filter: bad mode %d",
+             mode);
+  FI_REQUIRE(nt >= 1 && ny >= 1 && nx >= 1 && st >= 1 && sy >= 1 && sx >= 1,
+             "fi_rank_filter: bad sizes");
+  const int64_t wsize = (int64_t)st * sy * sx;
+  FI_REQUIRE(rank >= 0 && rank < wsize, "fi_rank_filter: rank %d not within the window", rank);
+  const int64_t count = (int64_t)nt * ny * nx;
+  cudaStream_t s = (cudaStream_t)stream;
+  // cval as a key of the image's dtype (scipy casts cval to the input type)
+  uint64_t ckey = 0;
+  {
+    double c = cval;
+    switch (dtype) {
+      case FI_PRE_U8: ckey = (uint8_t)(int64_t)c; break;
+      case FI_PRE_U16: ckey = (uint16_t)(int64_t)c; break;
+      case FI_PRE_F32: {
+        float f = (float)c;
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        ckey = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        break;
+      }
+      default: {
+        uint64_t u;
+        memcpy(&u, &c, 8);
+        ckey = (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+      }
+    }
+  }
+  const int g = grid_for(count);
+  if (rank == 0 || rank == wsize - 1) {
+    FI_REQUIRE(scratch, "fi_rank_filter: min/max filters need scratch[2 * count] (uint64)");
+    const int is_max = rank == wsize - 1 && wsize > 1;
+    uint64_t* k0 = static_cast<uint64_t*>(scratch);
+    uint64_t* k1 = k0 + count;
+    k_minmax_axis<<<g, 256, 0, s>>>(in, 0, nullptr, dtype, nt, ny, nx, 2, sx, mode, ckey, is_max, k0);
+    k_minmax_axis<<<g, 256, 0, s>>>(nullptr, 1, k0, dtype, nt, ny, nx, 1, sy, mode, ckey, is_max, k1);
+    k_minmax_axis<<<g, 256, 0, s>>>(nullptr, 1, k1, dtype, nt, ny, nx, 0, st, mode, ckey, is_max, k0);
+    k_keys_to_values<<<g, 256, 0, s>>>(k0, dtype, count, out);
+    return check_launch("fi_rank_filter", 4);
+  }
+  k_rank_select<<<g, 256, 0, s>>>(in, dtype, nt, ny, nx, st, sy, sx, rank, mode, ckey, out);
+  return check_launch("fi_rank_filter");
+}
+
+extern "C" int fi_subtract_weighted(const void* img, const void* filtered, int dtype,
+                                    int64_t count, double weight, int out_dtype, int clamp,
+                                    void* out, void* stream) {
+  FI_REQUIRE(img && filtered && out && count > 0, "fi_subtract_weighted: bad arguments");
+  FI_REQUIRE(out_dtype == FI_PRE_F64 || out_dtype == FI_PRE_F32 ||
+                 (out_dtype == dtype && (dtype == FI_PRE_U8 || dtype == FI_PRE_U16)),
+             "fi_subtract_weighted: bad output dtype %d", out_dtype);
+  k_subtract_weighted<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(
+      img, filtered, dtype, count, weight, out_dtype, clamp, out);
+  return check_launch("fi_subtract_weighted");
+}
+
+extern "C" int fi_clamp(const void* in, int dtype, int64_t count, double lo, double hi, void* out,
+                        void* stream) {
+  FI_REQUIRE(in && out && count > 0, "fi_clamp: bad arguments");
+  k_clamp<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, lo, hi, out);
+  return check_launch("fi_clamp");
+}
+
+extern "C" int fi_sq_sum_max(const void* in, int dtype, int64_t count, double* part_sum,
+                             double* part_max, int nparts, void* stream) {
+  FI_REQUIRE(in && part_sum && part_max && count > 0 && nparts > 0,
+             "fi_sq_sum_max: bad arguments");
+  k_sq_sum_max<<<nparts, 256, 0, (cudaStream_t)stream>>>(in, dtype, count, part_sum, part_max);
+  return check_launch("fi_sq_sum_max");
+}
+
+extern "C" int fi_tanh_rescale(const void* in, int dtype, int64_t count, double threshold,
+                               double scale, double* out, void* stream) {
+  FI_REQUIRE(in && out && count > 0 && threshold != 0.0, "fi_tanh_rescale: bad arguments");
+  k_tanh_rescale<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, threshold,
+                                                                   scale, out);
+  return check_launch("fi_tanh_rescale");
+}

@@ -1,0 +1,403 @@
+"""Image preprocessing on the GPU, with the tools of fluidimage's toolbox.
+
+Mirrors ``fluidimage.works.preproc`` (``WorkPreproc``, ``PreprocToolsPy``;
+works/preproc/__init__.py:62-137, toolbox.py:24-120): the parameter tree
+``params.tools`` (``available_tools``, ``sequence`` and one child per tool with its
+arguments and ``enable``) and ``calcul({"arrays": ..., "names": ...})``.
+
+The tools run in ``libfluidimage_gb300`` on device tensors (uint8, uint16 as int16
+storage, float32, float64), with the arithmetic of the upstream functions in
+works/preproc/_toolbox_py.py:
+
+* ``sliding_minima / sliding_median / sliding_percentile`` (:66-155): a 2-D rank
+  filter per image (scipy.ndimage window and boundary modes), then
+  ``img - weight * filtered`` in numpy's result dtype, negatives set to 0;
+* ``temporal_minima / temporal_median / temporal_percentile`` (:189-256): the rank
+  filter over the stack with ``window_shape`` (nt, ny, nx), no clamping;
+* ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355).
+
+The tools built on scikit-image (``adaptive_threshold``, ``rescale_intensity``,
+``equalize_hist_*``, ``gamma_correction``) and ``sharpen`` keep their parameters
+but raise ``NotImplementedError`` when enabled.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .params import ParamContainer
+
+# Upstream tool signatures (works/preproc/_toolbox_py.py), without ``img``.
+TOOL_DEFAULTS = {
+    "sliding_median": dict(weight=1.0, window_size=30, boundary_condition="reflect"),
+    "sliding_minima": dict(weight=1.0, window_size=30, boundary_condition="reflect"),
+    "sliding_percentile": dict(percentile=10.0, weight=1.0, window_size=30,
+                               boundary_condition="reflect"),
+    "temporal_median": dict(weight=1.0, window_shape=None),
+    "temporal_minima": dict(weight=1.0, window_shape=None),
+    "temporal_percentile": dict(percentile=10.0, weight=1.0, window_shape=None),
+    "global_threshold": dict(minima=0, maxima=None),
+    "adaptive_threshold": dict(window_size=5, offset=0),
+    "rescale_intensity": dict(minima=0.0, maxima=4096),
+    "equalize_hist_global": dict(nbins=256),
+    "equalize_hist_local": dict(radius=10),
+    "equalize_hist_adapt": dict(window_shape=(10, 10), nbins=256),
+    "gamma_correction": dict(gamma=1.0, gain=1.0),
+    "sharpen": dict(sigma1=3.0, sigma2=1.0, alpha=30.0),
+    "rescale_intensity_tanh": dict(threshold=None),
+}
+AVAILABLE_TOOLS = list(TOOL_DEFAULTS)
+
+_DT = {np.dtype(np.uint8): L.PRE_U8, np.dtype(np.uint16): L.PRE_U16,
+       np.dtype(np.float32): L.PRE_F32, np.dtype(np.float64): L.PRE_F64}
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _dtype_of(t):
+    """numpy dtype of the image data of a device tensor (uint16 as int16 storage)."""
+    torch = _torch()
+    return {torch.uint8: np.dtype(np.uint8), torch.int16: np.dtype(np.uint16),
+            torch.float32: np.dtype(np.float32), torch.float64: np.dtype(np.float64)}[t.dtype]
+
+
+def _empty(shape, dtype, device):
+    torch = _torch()
+    td = {np.dtype(np.uint8): torch.uint8, np.dtype(np.uint16): torch.int16,
+          np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}[np.dtype(dtype)]
+    return torch.empty(shape, dtype=td, device=device)
+
+
+def to_device(images, device=None):
+    """Host image(s) -> device tensor (uint16 data kept bit for bit as int16)."""
+    torch = _torch()
+    if isinstance(images, torch.Tensor):
+        return images.to(device or "cuda").contiguous()
+    a = np.ascontiguousarray(images)
+    if a.dtype == np.uint16:
+        a = a.view(np.int16)
+    elif a.dtype not in (np.uint8, np.float32, np.float64):
+        raise TypeError(f"image dtype {a.dtype} not supported (uint8, uint16, float32, float64)")
+    return torch.from_numpy(a).to(device or "cuda")
+
+
+def to_host(t):
+    """Device tensor -> numpy array (int16 storage of uint16 images viewed back)."""
+    a = t.cpu().numpy()
+    return a.view(np.uint16) if a.dtype == np.int16 else a
+
+
+def _as_float64(t):
+    """Values of a device image as float64 (uint16 data from its int16 storage)."""
+    torch = _torch()
+    if t.dtype == torch.int16:
+        return (t.to(torch.int32) & 0xFFFF).to(torch.float64)
+    return t.to(torch.float64)
+
+
+def _per_image(tool):
+    """Upstream's ``iterate_multiple_imgs`` (works/preproc/io.py:46-64): a 2-D image
+    gives the tool's own dtype, a stack is filled image by image into float64."""
+
+    def wrapper(img, *args, **kwargs):
+        if img.dim() == 2:
+            return tool(img, *args, **kwargs)
+        return _as_float64(tool(img, *args, **kwargs))
+
+    wrapper.__name__ = tool.__name__
+    wrapper.__doc__ = tool.__doc__
+    return wrapper
+
+
+def _stack(img):
+    """(nt, ny, nx) view of a 2-D image or a stack."""
+    if img.dim() == 2:
+        return img[None], True
+    if img.dim() == 3:
+        return img, False
+    raise ValueError("images must be 2-D or a 3-D stack")
+
+
+def _rank(size, rank_kind, percentile=None):
+    """scipy.ndimage._rank_filter's rank for a box of ``size`` elements."""
+    if rank_kind == "min":
+        return 0
+    if rank_kind == "median":
+        return size // 2
+    p = float(percentile)
+    if p < 0.0:
+        p += 100.0
+    if p < 0 or p > 100:
+        raise RuntimeError("invalid percentile")
+    return size - 1 if p == 100.0 else int(float(size) * p / 100.0)
+
+
+def rank_filter(img, window, rank_kind, percentile=None, mode="reflect", cval=0.0):
+    """scipy.ndimage minimum_filter / median_filter / percentile_filter of a stack
+    (nt, ny, nx) over the box ``window`` = (st, sy, sx); output in the input dtype."""
+    torch = _torch()
+    lib = L.load()
+    x = img.contiguous()
+    nt, ny, nx = x.shape
+    st, sy, sx = (int(w) for w in window)
+    r = _rank(st * sy * sx, rank_kind, percentile)
+    if mode not in L.MODES:
+        raise RuntimeError(f"boundary mode not supported: {mode}")
+    dt = _DT[_dtype_of(x)]
+    if dt in (L.PRE_F32, L.PRE_F64) and bool(torch.isnan(x).any()):
+        raise ValueError("rank filters of images with NaN are not provided")
+    out = torch.empty_like(x)
+    scratch = None
+    if r in (0, st * sy * sx - 1):
+        scratch = torch.empty(2 * x.numel(), dtype=torch.int64, device=x.device)
+    L.check(lib.fi_rank_filter(L.ptr(x), L.ptr(out), dt, nt, ny, nx, st, sy, sx, r,
+                               L.MODES[mode], float(cval), L.ptr(scratch), L.stream_handle()),
+            "fi_rank_filter")
+    return out
+
+
+def _result_dtype(dtype, weight):
+    """numpy's dtype of ``img - weight * filtered`` (same dtype arrays)."""
+    z = np.zeros(1, dtype=dtype)
+    return (z - weight * z).dtype
+
+
+def _subtract(img, filtered, weight, clamp):
+    lib = L.load()
+    dtype = _dtype_of(img)
+    out_dt = _result_dtype(dtype, weight)
+    if out_dt not in _DT:
+        raise TypeError(f"result dtype {out_dt} not supported")
+    out = _empty(tuple(img.shape), out_dt, img.device)
+    L.check(lib.fi_subtract_weighted(L.ptr(img), L.ptr(filtered), _DT[dtype], img.numel(),
+                                     float(weight), _DT[out_dt], int(clamp), L.ptr(out),
+                                     L.stream_handle()), "fi_subtract_weighted")
+    return out
+
+
+def _window2d(window_size):
+    if isinstance(window_size, (tuple, list)):
+        sy, sx = (int(w) for w in window_size)
+    else:
+        sy = sx = int(window_size)
+    return 1, sy, sx
+
+
+def _sliding(img, weight, window_size, boundary_condition, kind, percentile=None):
+    x, single = _stack(img)
+    f = rank_filter(x, _window2d(window_size), kind, percentile, mode=boundary_condition)
+    out = _subtract(x, f, weight, clamp=True)
+    return out[0] if single else out
+
+
+@_per_image
+def sliding_minima(img, weight=1.0, window_size=30, boundary_condition="reflect"):
+    """img - weight * minimum_filter(img), negatives -> 0 (_toolbox_py.py:129-155)."""
+    return _sliding(img, weight, window_size, boundary_condition, "min")
+
+
+@_per_image
+def sliding_median(img, weight=1.0, window_size=30, boundary_condition="reflect"):
+    """img - weight * median_filter(img), negatives -> 0 (_toolbox_py.py:65-91)."""
+    return _sliding(img, weight, window_size, boundary_condition, "median")
+
+
+@_per_image
+def sliding_percentile(img, percentile=10.0, weight=1.0, window_size=30,
+                       boundary_condition="reflect"):
+    """img - weight * percentile_filter(img), negatives -> 0 (_toolbox_py.py:94-126)."""
+    return _sliding(img, weight, window_size, boundary_condition, "percentile", percentile)
+
+
+def _calcul_windowshape(arr_shape, window_shape):
+    """_toolbox_py.py:163-185."""
+    nb_imgs = arr_shape[0]
+    if len(arr_shape) <= 2 or nb_imgs <= 1:
+        raise ValueError(
+            "Need more than one image to apply temporal filtering (use sliding filter?).")
+    if window_shape is None:
+        window_shape = (nb_imgs, 1, 1)
+    elif isinstance(window_shape, int):
+        window_shape = (window_shape, 1, 1)
+    elif not isinstance(window_shape, (tuple, list)):
+        raise ValueError("window_shape must be a tuple or a list.")
+    elif len(window_shape) == 2:
+        window_shape = (nb_imgs,) + tuple(window_shape)
+    elif window_shape[0] <= 1:
+        raise ValueError("Cannot perform temporal filtering, try spatial filtering.")
+    return tuple(window_shape)
+
+
+def _temporal(img, weight, window_shape, kind, percentile=None):
+    window = _calcul_windowshape(tuple(img.shape), window_shape)
+    f = rank_filter(img, window, kind, percentile)
+    return _subtract(img, f, weight, clamp=False)
+
+
+def temporal_minima(img, weight=1.0, window_shape=None):
+    """img - weight * minimum_filter(img, window_shape) (_toolbox_py.py:239-256)."""
+    return _temporal(img, weight, window_shape, "min")
+
+
+def temporal_median(img, weight=1.0, window_shape=None):
+    """img - weight * median_filter(img, window_shape) (_toolbox_py.py:188-208)."""
+    return _temporal(img, weight, window_shape, "median")
+
+
+def temporal_percentile(img, percentile=10.0, weight=1.0, window_shape=None):
+    """img - weight * percentile_filter(img, window_shape) (_toolbox_py.py:211-236)."""
+    return _temporal(img, weight, window_shape, "percentile", percentile)
+
+
+@_per_image
+def global_threshold(img, minima=0, maxima=None):
+    """Clamp the intensities to [minima, maxima] (_toolbox_py.py:264-289)."""
+    lib = L.load()
+    dtype = _dtype_of(img)
+    if maxima is None:
+        maxima = np.iinfo(dtype).max if dtype.kind in "ui" else 65535
+    out = _empty(tuple(img.shape), dtype, img.device)
+    L.check(lib.fi_clamp(L.ptr(img.contiguous()), _DT[dtype], img.numel(), float(minima),
+                         float(maxima), L.ptr(out), L.stream_handle()), "fi_clamp")
+    return out
+
+
+@_per_image
+def rescale_intensity_tanh(img, threshold=None):
+    """max(img) * tanh(img / threshold) / max(tanh(img / threshold)), floored
+    (_toolbox_py.py:331-355); per image for a stack."""
+    x, single = _stack(img)
+    outs = [_tanh_one(x[i], threshold) for i in range(x.shape[0])]
+    if single:
+        return outs[0]
+    return _torch().stack(outs)
+
+
+def _tanh_one(img, threshold):
+    torch = _torch()
+    lib = L.load()
+    dtype = _dtype_of(img)
+    if dtype == np.float32:
+        raise NotImplementedError("rescale_intensity_tanh of float32 images (upstream works "
+                                  "in float32 there) is not provided")
+    x = img.contiguous()
+    nparts = 152
+    part = torch.empty(2 * nparts, dtype=torch.float64, device=x.device)
+    L.check(lib.fi_sq_sum_max(L.ptr(x), _DT[dtype], x.numel(), L.ptr(part),
+                              L.ptr(part[nparts:]), nparts, L.stream_handle()), "fi_sq_sum_max")
+    host = part.cpu().numpy()
+    vmax = float(host[nparts:].max())
+    if threshold is None:
+        threshold = 2 * math.sqrt(float(host[:nparts].sum()) / x.numel())
+    if threshold == 0:
+        return img
+    scale = vmax / math.tanh(vmax / threshold)
+    out = torch.empty(tuple(x.shape), dtype=torch.float64, device=x.device)
+    L.check(lib.fi_tanh_rescale(L.ptr(x), _DT[dtype], x.numel(), float(threshold), scale,
+                                L.ptr(out), L.stream_handle()), "fi_tanh_rescale")
+    return out
+
+
+def _not_provided(name):
+    def tool(img, **kwargs):
+        raise NotImplementedError(
+            f"preprocessing tool {name!r} is not provided by this backend (upstream builds it "
+            "on scikit-image or chained gaussian filters)")
+
+    tool.__name__ = name
+    return tool
+
+
+TOOLS = {
+    "sliding_median": sliding_median,
+    "sliding_minima": sliding_minima,
+    "sliding_percentile": sliding_percentile,
+    "temporal_median": temporal_median,
+    "temporal_minima": temporal_minima,
+    "temporal_percentile": temporal_percentile,
+    "global_threshold": global_threshold,
+    "rescale_intensity_tanh": rescale_intensity_tanh,
+}
+for _name in AVAILABLE_TOOLS:
+    TOOLS.setdefault(_name, _not_provided(_name))
+
+
+class PreprocToolsGB300:
+    """``PreprocToolsPy`` on the GPU (works/preproc/toolbox.py:24-120)."""
+
+    @classmethod
+    def create_default_params(cls, params):
+        tools = params._set_child("tools", {"available_tools": AVAILABLE_TOOLS,
+                                            "sequence": None})
+        for name in AVAILABLE_TOOLS:
+            attribs = dict(TOOL_DEFAULTS[name])
+            attribs["enable"] = False
+            tools._set_child(name, attribs=attribs)
+        return params
+
+    def __init__(self, params):
+        self.params = params.tools
+
+    def apply(self, img):
+        """Apply the enabled tools, in ``sequence`` order (or the tool list order)."""
+        sequence = self.params.sequence
+        if sequence is None:
+            sequence = self.params.available_tools
+        for name in sequence:
+            p = getattr(self.params, name)
+            if not p.enable:
+                continue
+            kwargs = {k: getattr(p, k) for k in TOOL_DEFAULTS[name]}
+            img = TOOLS[name](img, **kwargs)
+        return img
+
+
+class PreprocResults:
+    """Results of one series: ``data`` maps image names to arrays
+    (data_objects/preproc.py)."""
+
+    def __init__(self, params=None):
+        self.params = params
+        self.data = {}
+
+
+class WorkPreproc:
+    """``WorkPreproc`` on the GPU (works/preproc/__init__.py:62-137)."""
+
+    @classmethod
+    def create_default_params(cls, backend="gb300"):
+        params = ParamContainer(tag="params")
+        params._set_attrib("backend", backend)
+        PreprocToolsGB300.create_default_params(params)
+        return params
+
+    def __init__(self, params=None, device=None):
+        if params is None:
+            params = type(self).create_default_params()
+        self.params = params
+        self.device = device
+        self.tools = PreprocToolsGB300(params)
+
+    def calcul_device(self, images):
+        """Apply the tools to a device stack (nt, ny, nx) or image; returns a tensor."""
+        return self.tools.apply(images)
+
+    def calcul(self, serie):
+        """``serie``: dict with ``arrays`` (a sequence of images) and ``names``."""
+        arrays = serie["arrays"] if isinstance(serie, dict) else serie.get_arrays()
+        names = serie["names"] if isinstance(serie, dict) else serie.names
+        images = to_device(np.array(arrays), self.device)
+        out = to_host(self.calcul_device(images))
+        result = PreprocResults(self.params)
+        result.data.update(dict(zip(names, out)))
+        return result
+
+
+Work = WorkPreproc

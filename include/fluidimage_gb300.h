@@ -389,6 +389,57 @@ int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        const float* phi_table2, int64_t table_size, const int32_t* cxy2,
                        const int32_t* c_on_lattice, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Image preprocessing (works/preproc/_toolbox_py.py)
+ * ------------------------------------------------------------------------- */
+#define FI_PRE_U8 0
+#define FI_PRE_U16 1
+#define FI_PRE_F32 2
+#define FI_PRE_F64 3
+/* scipy.ndimage boundary modes */
+#define FI_MODE_REFLECT 0  /* d c b a | a b c d | d c b a */
+#define FI_MODE_CONSTANT 1 /* k k k k | a b c d | k k k k (cval) */
+#define FI_MODE_NEAREST 2  /* a a a a | a b c d | d d d d */
+#define FI_MODE_MIRROR 3   /* d c b | a b c d | c b a */
+#define FI_MODE_WRAP 4     /* a b c d | a b c d | a b c d */
+
+/*
+ * Rank filter of a stack of nt images ny x nx (FI_PRE_* dtype, C order) over a box
+ * window st x sy x sx, output in the input dtype: the rank-th smallest window value
+ * (scipy.ndimage.rank_filter semantics: window [i - s//2, i - s//2 + s - 1], the
+ * boundary mode and cval); rank 0 / st*sy*sx - 1 are the minimum / maximum filters
+ * (separable; scratch: 2 * nt*ny*nx uint64), other ranks an exact radix select.
+ * Replaces ndi.minimum_filter / median_filter / percentile_filter in sliding_* and
+ * temporal_* (works/preproc/_toolbox_py.py:66-155, 189-256).
+ */
+int fi_rank_filter(const void* in, void* out, int dtype, int nt, int ny, int nx, int st, int sy,
+                   int sx, int rank, int mode, double cval, void* scratch, void* stream);
+
+/*
+ * out = img - weight * filtered in numpy's result dtype out_dtype (FI_PRE_F64,
+ * FI_PRE_F32, or the image's integer dtype for an integer weight: modular
+ * arithmetic), with negatives set to 0 when clamp (sliding_* tools,
+ * _toolbox_py.py:88-91).
+ */
+int fi_subtract_weighted(const void* img, const void* filtered, int dtype, int64_t count,
+                         double weight, int out_dtype, int clamp, void* out, void* stream);
+
+/* global_threshold (_toolbox_py.py:265-289): values below lo set to lo, above hi to hi. */
+int fi_clamp(const void* in, int dtype, int64_t count, double lo, double hi, void* out,
+             void* stream);
+
+/*
+ * Partial sums of img**2 (squares in the image dtype, wrapping for integers as
+ * numpy does) and partial maxima of img, one per block (nparts blocks), for
+ * rescale_intensity_tanh (_toolbox_py.py:332-355).
+ */
+int fi_sq_sum_max(const void* in, int dtype, int64_t count, double* part_sum, double* part_max,
+                  int nparts, void* stream);
+
+/* out = floor(scale * tanh(img / threshold)) in float64 (rescale_intensity_tanh). */
+int fi_tanh_rescale(const void* in, int dtype, int64_t count, double threshold, double scale,
+                    double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -259,6 +259,72 @@ def case_subpix_methods():
         }, keep_planes=True)
 
 
+PREPROC_CASES = [
+    # (name, function, image key, kwargs)
+    ("minima_u8_w7", "sliding_minima", "u8", dict(window_size=7)),
+    ("minima_u8_5x9_nearest", "sliding_minima", "u8", dict(window_size=(5, 9),
+                                                            boundary_condition="nearest")),
+    ("minima_u8_w4_constant", "sliding_minima", "u8", dict(window_size=4, weight=0.7,
+                                                           boundary_condition="constant")),
+    ("median_u8_w5_mirror", "sliding_median", "u8", dict(window_size=5,
+                                                         boundary_condition="mirror")),
+    ("median_u16_w6", "sliding_median", "u16", dict(window_size=6)),
+    ("percentile_u8_w6_wrap", "sliding_percentile", "u8", dict(percentile=10.0, window_size=6,
+                                                               boundary_condition="wrap")),
+    ("minima_f32_w5_half", "sliding_minima", "f32", dict(window_size=5, weight=0.5)),
+    ("minima_u8_int_weight", "sliding_minima", "u8", dict(window_size=3, weight=1)),
+    ("temporal_minima_u8", "temporal_minima", "u8", dict()),
+    ("temporal_median_u16_333", "temporal_median", "u16", dict(window_shape=(3, 3, 3))),
+    ("temporal_percentile_u8_3", "temporal_percentile", "u8", dict(percentile=20.0,
+                                                                   window_shape=3)),
+    ("threshold_u8", "global_threshold", "u8", dict(minima=10, maxima=200)),
+    ("threshold_u16_default", "global_threshold", "u16", dict(minima=50)),
+    ("tanh_u8", "rescale_intensity_tanh", "u8", dict()),
+    ("tanh_u16_thr", "rescale_intensity_tanh", "u16", dict(threshold=900.0)),
+]
+
+
+def case_preproc():
+    """The upstream preprocessing tools (works/preproc/_toolbox_py.py) on stacks of
+    5 small particle images with a background gradient (uint8, uint16, float32)."""
+    import importlib
+    import types
+
+    import fluidimage.works
+
+    # the package __init__ needs image I/O helpers absent here: load the toolbox
+    # module under a bare package entry instead
+    pkg = "fluidimage.works.preproc"
+    if pkg not in sys.modules:
+        mod = types.ModuleType(pkg)
+        mod.__path__ = [str(Path(fluidimage.works.__file__).parent / "preproc")]
+        sys.modules[pkg] = mod
+    tools = importlib.import_module(pkg + "._toolbox_py")
+
+    rng = np.random.default_rng(8000)
+    model8 = synthetic.ParticleModel(density=0.05, noise=3.0, dtype="uint8")
+    shape = (48, 64)
+    frames = []
+    for k in range(5):
+        a, _ = synthetic.make_pair(shape, synthetic.uniform_shift(1.0, 0.5), model8,
+                                   seed=8000 + k)
+        frames.append(a)
+    bg = (np.arange(shape[1])[None, :] * 0.5 + np.arange(shape[0])[:, None] * 0.3)
+    u8 = np.clip(np.array(frames, dtype=np.float64) * 0.6 + bg[None] + 10, 0, 255).astype(np.uint8)
+    u16 = (u8.astype(np.uint16) * 16 + rng.integers(0, 16, u8.shape)).astype(np.uint16)
+    f32 = (u8.astype(np.float32) / 7.0).astype(np.float32)
+    images = {"u8": u8, "u16": u16, "f32": f32}
+    out = {"img_" + k: v for k, v in images.items()}
+    out["numpy_version"] = np.array(np.__version__)
+    for name, fn, key, kwargs in PREPROC_CASES:
+        res = getattr(tools, fn)(img=images[key].copy(), **kwargs)
+        out["out_" + name] = np.asarray(res)
+        out["args_" + name] = np.array(json.dumps({"function": fn, "image": key,
+                                                   "kwargs": kwargs}))
+    np.savez_compressed(HERE / "preproc.npz", **out)
+    print("wrote preproc.npz")
+
+
 CASES = {
     "correl_window": case_correl_window,
     "single_pass_c1": case_single_pass_c1,
@@ -268,6 +334,7 @@ CASES = {
     "griddata_two_pass": case_griddata,
     "secondary_peaks_two_pass": case_secondary_peaks,
     "subpix_methods": case_subpix_methods,
+    "preproc": case_preproc,
 }
 
 if __name__ == "__main__":

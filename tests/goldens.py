@@ -63,4 +63,5 @@ def errors(z, ip, key="errors"):
 
 
 def fixture_names():
-    return sorted(p.stem for p in GOLDEN_DIR.glob("*.npz") if p.stem != "correl_window")
+    return sorted(p.stem for p in GOLDEN_DIR.glob("*.npz")
+                  if p.stem not in ("correl_window", "preproc"))
