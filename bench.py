@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=2048,
                     help="image side (2048 = the config; smaller sizes for profiling)")
+    ap.add_argument("--preproc", action="store_true",
+                    help="time the preprocessing tools instead (second JSON line format)")
     return ap.parse_args()
 
 
@@ -394,9 +396,68 @@ def roofline(dominant, outs, work, peaks, peak_kind, steps):
             "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
 
 
+def run_preproc(args):
+    """Preprocessing tools on 2048^2 uint16 frames of the config-2 images: device
+    throughput (CUDA events, L2 flushed between steps) next to the scipy oracle on
+    a 512^2 crop (one thread)."""
+    import torch
+
+    from fluidimage_gb300 import preproc as P, workloads
+
+    (im0, im1), _ = workloads.config2_images(shape=(args.size, args.size))
+    frames = np.array([im0, im1] * 4)  # 8 frames for the temporal tool
+    dev = torch.device("cuda")
+    t_img = P.to_device(im0, dev)
+    t_stack = P.to_device(frames, dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cases = [
+        ("sliding_minima", dict(window_size=30), t_img, im0),
+        ("sliding_median", dict(window_size=30), t_img, im0),
+        ("temporal_minima", dict(), t_stack, frames),
+    ]
+    out = {"metric": "preprocessing Mpixel/s", "unit": "Mpixel/s", "workload":
+           f"{args.size}x{args.size} uint16 frames of the config-2 pair", "tools": {}}
+    for name, kw, t, host in cases:
+        fn = getattr(P, name)
+        for _ in range(max(args.warmup, 1)):
+            fn(t, **kw)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(t, **kw)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        npx = t.numel()
+        gpu = npx / (statistics.median(ms) / 1e3) / 1e6
+        code = ("import sys, time, json, numpy as np; sys.path.insert(0, %r); "
+                "from oracle import preproc as O; a = np.load(sys.argv[1]); "
+                "t0 = time.perf_counter(); getattr(O, %r)(a, **json.loads(sys.argv[2])); "
+                "print(a.size / (time.perf_counter() - t0) / 1e6)" % (str(ROOT), name))
+        crop = host[..., :512, :512]
+        tmp = ROOT / "gpurun_out" if (ROOT / "gpurun_out").exists() else Path("/tmp")
+        path = tmp / f"_preproc_{name}.npy"
+        np.save(path, np.ascontiguousarray(crop))
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        cpu = float(subprocess.run([sys.executable, "-c", code, str(path), json.dumps(kw)],
+                                   capture_output=True, text=True, env=env,
+                                   check=True).stdout.strip())
+        path.unlink()
+        out["tools"][name] = {"gpu_mpixel_s": gpu, "ms_per_call": statistics.median(ms),
+                              "cpu_baseline_mpixel_s": cpu, "cpu_cores": 1,
+                              "cpu_sample": "512x512 crop, scipy oracle"}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.preproc:
+        run_preproc(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
