@@ -22,6 +22,8 @@
 // K entries come from a table of phi(r^2) = r^2 log(r^2) / 2 indexed by 4 r^2,
 // exact for window centres on the half-integer lattice (the integer window shifts
 // put every PIV vector there); other distances use log() directly.
+#include <cooperative_groups.h>
+
 #include <cmath>
 
 #include "fi_common.cuh"
@@ -560,13 +562,19 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   __shared__ double s_q1[6];
   __shared__ int s_flag, s_bad[2], s_lat;
   const fi_tps_plan p = *plan_ptr;
-  const int sd = blockIdx.x;
+  // a cluster of csize CTAs per subdomain (1 without cluster launch): all of them
+  // factor P and share the FP64 build and projection, rank 0 then solves alone
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int csize = (int)cluster.num_blocks();
+  const int crank = (int)cluster.block_rank();
+  const int sd = blockIdx.x / csize;
   const int N = counts[sd];
   const int m = N - 3;
   const int64_t off = offsets[sd];
   const int32_t* idx = indices + off;
   const double lam = p.smoothing;
-  if (threadIdx.x == 0) status[sd] = 1;
+  if (threadIdx.x == 0 && crank == 0) status[sd] = 1;
   if (m < 1) return;  // fewer than 4 centres: FP64 LU path
   const int mp = (m + 3) & ~3;
 
@@ -678,8 +686,9 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   double* Y0 = YC;
   double* Y1 = YC + n;
   double* Y2 = YC + 2 * n;
-  // ---- Y = A V (FP64; A symmetric: row c = column c)
-  for (int c = wid; c < N; c += NW) {
+  // ---- Y = A V (FP64; A symmetric: row c = column c); the columns are shared by the
+  // cluster's CTAs, each result written into every CTA's Y
+  for (int c = crank * NW + wid; c < N; c += csize * NW) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int r = lane; r < N; r += 32) {
       const double v = a_entry(r, c);
@@ -693,12 +702,15 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
     if (lane == 0) {
-      Y0[c] = a0;
-      Y1[c] = a1;
-      Y2[c] = a2;
+      for (int q = 0; q < csize; ++q) {
+        double* Yq = (q == crank) ? YC : cluster.map_shared_rank(YC, q);
+        Yq[c] = a0;
+        Yq[n + c] = a1;
+        Yq[2 * n + c] = a2;
+      }
     }
   }
-  __syncthreads();
+  cluster.sync();
   // ---- Q^T A Q = A - Z V^T - V Z^T (compact WY, Q = H0 H1 H2 = I - V T V^T),
   // Y = A V, M = T^T (V^T Y) T, Z = Y T - V M / 2.  FP64: the projection cancels the
   // large affine part of K.
@@ -771,9 +783,11 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   };
   // C[k][c] = (Q^T A Q)[k][c + 3], k < 3 (Y is no longer needed)
   double* C = YC;
-  for (int i = threadIdx.x; i < 3 * m; i += NT) {
-    const int k = i / m, c = i - k * m;
-    C[k * n + c] = proj(k, c + 3);
+  if (crank == 0) {
+    for (int i = threadIdx.x; i < 3 * m; i += NT) {
+      const int k = i / m, c = i - k * m;
+      C[k * n + c] = proj(k, c + 3);
+    }
   }
   // B22 by 32 x 32 tiles (I >= J), half a tile (16 columns) at a time: the lower
   // entries are written by columns, then mirrored through a per-warp shared tile.
@@ -781,7 +795,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
     float2* S = reinterpret_cast<float2*>(panel) + wid * 16 * 33;
     const int T = (m + 31) / 32;
     const int npairs = T * (T + 1) / 2;
-    for (int pidx = wid; pidx < npairs; pidx += NW) {
+    for (int pidx = crank * NW + wid; pidx < npairs; pidx += csize * NW) {
       int I = (int)((sqrtf(8.f * pidx + 1.f) - 1.f) * 0.5f);
       while ((I + 1) * (I + 2) / 2 <= pidx) ++I;
       while (I * (I + 1) / 2 > pidx) --I;
@@ -809,7 +823,8 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       }
     }
   }
-  __syncthreads();
+  cluster.sync();  // the cluster's B tiles are in global memory, visible to rank 0
+  if (crank != 0) return;
   // ---- FP32 Cholesky of B22
   if (!chol_factor<NT>(L32, m, mp, panel, &s_flag)) return;
 
@@ -1066,12 +1081,27 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
       FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_solve_mp<256>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  if (wide)
-    k_tps_solve_mp<512><<<nb_subdom, 512, smem, (cudaStream_t)stream>>>(
-        plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
-        phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights,
-        smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, 60, N);
-  else
+  if (wide) {
+    // clusters of S CTAs per subdomain while the subdomains leave SMs idle
+    const int S = (4 * nb_subdom <= nsm) ? 4 : (2 * nb_subdom <= nsm) ? 2 : 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nb_subdom * S));
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FI_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_tps_solve_mp<512>, plan, cx, cy, ux, uy, counts,
+                                   offsets, indices, mat_offsets, matrices, matrices32,
+                                   phi_table, table_size, cxy2, c_on_lattice, threshold,
+                                   use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
+                                   iters, nfixed, status, max_udiff, sweeps, 60, N));
+  } else
     k_tps_solve_mp<256><<<nb_subdom, 256, smem, (cudaStream_t)stream>>>(
         plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
         phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights,
