@@ -190,30 +190,51 @@ class WorkPIV:
 
     # --------------------------------------------------------------------
     def results_to_host(self, outs, couple=None):
-        """Device outputs -> ``MultipassPIVResults`` (upstream attributes and dtypes)."""
-        import torch
+        """Device outputs -> ``MultipassPIVResults`` (upstream attributes and dtypes).
 
-        torch.cuda.current_stream().synchronize()
+        Every array is gathered into one device buffer and copied to pinned host
+        memory at once (one synchronisation)."""
         fx = self.params.fix
         offx, offy = self._xy_offsets()
+        keys = ("deltaxs_raw", "deltays_raw", "correls_max", "errors", "xs", "ys", "flags",
+                "deltaxs", "deltays", "fix_flags", "diff2")
+        want = {}
+        for k, pd in enumerate(outs):
+            for key in keys:
+                want[(k, key)] = getattr(pd, key)
+            if pd.planes is not None:
+                want[(k, "planes")] = pd.planes
+            if pd.dxin is not None:
+                want[(k, "dxin")], want[(k, "dyin")] = pd.dxin, pd.dyin
+            if pd.peaks_count is not None:
+                want[(k, "peaks_count")], want[(k, "peaks")] = pd.peaks_count, pd.peaks
+                want[(k, "replaced")] = pd.replaced
+            for tag in ("tps_next", "tps_final"):
+                tps = getattr(pd, tag)
+                if tps is None:
+                    continue
+                want[(k, tag, "singular")] = tps.singular
+                want[(k, tag, "out_x")], want[(k, tag, "out_y")] = tps.out_x, tps.out_y
+                if tag == "tps_final":
+                    want[(k, tag, "sel")] = tps.selection[: tps.num_centers]
+                    want[(k, tag, "smooth_x")] = tps.smooth_x
+                    want[(k, tag, "smooth_y")] = tps.smooth_y
+        got = dict(zip(want, _fetch(list(want.values()))))
         results = MultipassPIVResults()
         hosts = []
-        for pd in outs:
+        for k, pd in enumerate(outs):
             lay = pd.layout
-            h = {k: getattr(pd, k).cpu().numpy() for k in (
-                "deltaxs_raw", "deltays_raw", "correls_max", "errors", "xs", "ys", "flags",
-                "deltaxs", "deltays", "fix_flags", "diff2")}
+            h = {key: got[(k, key)] for key in keys}
             errors = error_dict(h["errors"], h["fix_flags"], h["diff2"],
                                 fx.threshold_diff_neighbour)
             secondary = [None] * lay.nvec
             replaced = {}
             if pd.peaks_count is not None:
-                secondary = _secondary_peaks(pd, lay.nvec)
-                rep = np.nonzero(h["fix_flags"] & _lib.FIX_REPLACED)[0]
-                if rep.size:
-                    old = pd.replaced.view(lay.nvec, 3)[torch.as_tensor(rep, device=pd.replaced.device)]
-                    for i, (ox, oy, oc) in zip(rep.tolist(), old.cpu().numpy()):
-                        replaced[i] = (ox, oy, oc)
+                secondary = _secondary_peaks(got[(k, "peaks_count")], got[(k, "peaks")],
+                                             lay.nvec)
+                old = got[(k, "replaced")].reshape(lay.nvec, 3)
+                for i in np.nonzero(h["fix_flags"] & _lib.FIX_REPLACED)[0].tolist():
+                    replaced[i] = tuple(old[i])
             if lay.index == 0:
                 xs = lay.gx + offx
                 ys = lay.gy + offy
@@ -222,7 +243,7 @@ class WorkPIV:
                 ys = h["ys"].astype(np.float64) + offy
             nvec = lay.nvec
             if pd.planes is not None:
-                planes = pd.planes.view(nvec, lay.n, lay.n).cpu().numpy()
+                planes = got[(k, "planes")].reshape(nvec, lay.n, lay.n)
                 correls = [None if h["errors"][i] == 4 else planes[i] for i in range(nvec)]
             else:
                 correls = [None] * nvec
@@ -236,48 +257,49 @@ class WorkPIV:
             r.indices_no_displacement = (lay.n // 2 - 1, lay.n // 2 - 1)
             r.displacement_max = lay.displacement_max
             # per-vector near-tie flags (bit 0: top-two plane values within 1e-6
-            # relative; bit 1: tied minimum in the subpixel crop); on these vectors
-            # the upstream result depends on float rounding
+            # relative; bit 1: tied minimum in the subpixel crop; bit 2: near-tie in a
+            # secondary search); on these vectors the upstream result depends on float
+            # rounding
             r.near_tie_flags = h["flags"]
             r.near_ties = int(np.count_nonzero(h["flags"]))
             if fx.threshold_diff_neighbour is not None:
                 r.deltaxs_wrong = {i: h["deltaxs_raw"][i] for i in errors}
                 r.deltays_wrong = {i: h["deltays_raw"][i] for i in errors}
             if pd.dxin is not None:
-                r.deltaxs_input = pd.dxin.cpu().numpy()
-                r.deltays_input = pd.dyin.cpu().numpy()
+                r.deltaxs_input = got[(k, "dxin")]
+                r.deltays_input = got[(k, "dyin")]
             hosts.append((r, h))
             results.append(r)
         for k, pd in enumerate(outs):
             r, h = hosts[k]
             if pd.tps_next is not None:
                 nxt = outs[k + 1].layout
-                self._check_tps(pd.tps_next)
-                r.deltaxs_approx = pd.tps_next.out_x.cpu().numpy()
-                r.deltays_approx = pd.tps_next.out_y.cpu().numpy()
+                self._check_tps(got[(k, "tps_next", "singular")])
+                r.deltaxs_approx = got[(k, "tps_next", "out_x")]
+                r.deltays_approx = got[(k, "tps_next", "out_y")]
                 r.ixvecs_approx = nxt.gx + offx
                 r.iyvecs_approx = nxt.gy + offy
                 r.deltaxs_tps = LazyWeights(pd.tps_next, 0)
                 r.deltays_tps = LazyWeights(pd.tps_next, 1)
             if pd.tps_final is not None:
                 tps = pd.tps_final
-                self._check_tps(tps)
+                self._check_tps(got[(k, "tps_final", "singular")])
                 lay = pd.layout
-                fx_ = tps.out_x.cpu().numpy()
-                fy_ = tps.out_y.cpu().numpy()
+                fx_ = got[(k, "tps_final", "out_x")]
+                fy_ = got[(k, "tps_final", "out_y")]
                 r.ixvecs_final = lay.gx + offx
                 r.iyvecs_final = lay.gy + offy
                 r.deltaxs_final = fx_
                 r.deltays_final = fy_
-                sel = tps.selection[: tps.num_centers].cpu().numpy().astype(np.int64)
+                sel = got[(k, "tps_final", "sel")].astype(np.int64)
                 xs_s = r.ixvecs_final.copy().astype(np.float32)
                 xs_s[sel] = r.xs[sel]
                 ys_s = r.iyvecs_final.copy().astype(np.float32)
                 ys_s[sel] = r.ys[sel]
                 dxs = fx_.copy()
-                dxs[sel] = tps.smooth_x.cpu().numpy()
+                dxs[sel] = got[(k, "tps_final", "smooth_x")]
                 dys = fy_.copy()
-                dys[sel] = tps.smooth_y.cpu().numpy()
+                dys[sel] = got[(k, "tps_final", "smooth_y")]
                 r.xs_smooth, r.ys_smooth = xs_s, ys_s
                 r.deltaxs_smooth, r.deltays_smooth = dxs, dys
                 r.deltaxs_tps = LazyWeights(tps, 0)
@@ -285,20 +307,46 @@ class WorkPIV:
         return results
 
     @staticmethod
-    def _check_tps(tps):
-        if int(tps.singular.sum().item()) != 0:
+    def _check_tps(singular):
+        if int(np.asarray(singular).sum()) != 0:
             raise np.linalg.LinAlgError(
                 "Singular TPS subdomain system (upstream falls back to griddata, "
                 "which this backend does not provide)"
             )
 
 
-def _secondary_peaks(pd, nvec):
+def _fetch(tensors):
+    """Device tensors -> numpy arrays with one copy: the tensors are packed into one
+    device byte buffer (widest elements first, so every array stays aligned) and
+    copied to pinned host memory; the arrays are views of that buffer."""
+    import torch
+
+    np_of = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32,
+             torch.int64: np.int64, torch.uint8: np.uint8, torch.int16: np.int16}
+    order = sorted(range(len(tensors)), key=lambda i: -tensors[i].element_size())
+    flat = [tensors[i].contiguous().view(-1).view(torch.uint8) for i in order]
+    sizes = [f.numel() for f in flat]
+    if not flat:
+        return []
+    buf = torch.cat(flat) if len(flat) > 1 else flat[0]
+    host = torch.empty(buf.numel(), dtype=torch.uint8, pin_memory=True)
+    host.copy_(buf, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    raw = host.numpy()
+    out = [None] * len(tensors)
+    off = 0
+    for i, n in zip(order, sizes):
+        t = tensors[i]
+        out[i] = raw[off:off + n].view(np_of[t.dtype]).reshape(tuple(t.shape))
+        off += n
+    return out
+
+
+def _secondary_peaks(counts, peaks, nvec):
     """``secondary_peaks`` of _loop_vectors: None where the peak search raised, else
     the list of (dx, dy, correl_max) of the other peaks (correl.py:250-273)."""
-    counts = pd.peaks_count.cpu().numpy()
-    K = pd.peaks.numel() // (nvec * _lib.PEAK_FIELDS)
-    pk = pd.peaks.view(nvec, K, _lib.PEAK_FIELDS).cpu().numpy()
+    K = peaks.size // (nvec * _lib.PEAK_FIELDS)
+    pk = peaks.reshape(nvec, K, _lib.PEAK_FIELDS)
     out = [None] * nvec
     for i in range(nvec):
         c = int(counts[i])
