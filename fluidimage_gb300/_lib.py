@@ -101,6 +101,7 @@ _SIGNATURES = {
     ),
     "fi_tps_lattice": (C.c_int, [P, P, C.c_int, P, P, P]),
     "fi_tps_y_bounds": (C.c_int, [P, C.c_int, P, P, P]),
+    "fi_tps_offsets": (C.c_int, [P, P, C.c_int, P, P, P, P, P, P]),
     "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P]),
     "fi_tps_solve": (
         C.c_int,

@@ -290,6 +290,72 @@ __global__ void __launch_bounds__(1024) k_y_tiles_scan(int ntiles, double* tmax,
   }
 }
 
+// Exclusive prefix sum of v over the block of 1024 threads; *total gets the sum.
+__device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t* wsum, int64_t* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) wsum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const int64_t w = wsum[lane];
+    int64_t wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t u = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += u;
+    }
+    wsum[lane] = wi - w;
+    if (lane == 31) wsum[32] = wi;
+  }
+  __syncthreads();
+  const int64_t r = wsum[wid] + incl - v;
+  *total = wsum[32];
+  __syncthreads();
+  return r;
+}
+
+// CSR offsets of the centres' and new positions' membership, offsets of the matrix
+// slots ((n+3)^2 rounded up to 4 elements) and of the weights (2 (n+3)), and the
+// summary [total members, total new members, matrix elements, weight elements,
+// max members, max new members]; one block of 1024 threads.
+__global__ void __launch_bounds__(1024)
+    k_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nsub, int64_t* off,
+                  int64_t* noff, int64_t* moff, int64_t* woff, int64_t* summary) {
+  __shared__ int64_t wsum[33];
+  __shared__ int s_max[2];
+  if (threadIdx.x == 0) s_max[0] = s_max[1] = 0;
+  int64_t carry[4] = {0, 0, 0, 0};
+  __syncthreads();
+  for (int base = 0; base < nsub; base += 1024) {
+    const int i = base + threadIdx.x;
+    const int64_t c = (i < nsub) ? counts[i] : 0;
+    const int64_t nc = (i < nsub) ? ncounts[i] : 0;
+    const int64_t msz = (i < nsub) ? (((c + 3) * (c + 3) + 3) / 4) * 4 : 0;
+    const int64_t wsz = (i < nsub) ? 2 * (c + 3) : 0;
+    if (i < nsub) {
+      atomicMax(&s_max[0], (int)c);
+      atomicMax(&s_max[1], (int)nc);
+    }
+    const int64_t vals[4] = {c, nc, msz, wsz};
+    int64_t* outs[4] = {off, noff, moff, woff};
+    for (int k = 0; k < 4; ++k) {
+      int64_t tot;
+      const int64_t ex = block_scan_i64(vals[k], wsum, &tot);
+      if (i < nsub) outs[k][i] = carry[k] + ex;
+      carry[k] += tot;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 4; ++k) summary[k] = carry[k];
+    summary[4] = s_max[0];
+    summary[5] = s_max[1];
+  }
+}
+
 // First index q in [0, n) with a[q] >= v for a non-decreasing a (n if none).
 __device__ __forceinline__ int lower_bound_ge(const double* a, int n, double v) {
   int lo = 0, hi = n;
@@ -320,6 +386,7 @@ __global__ void __launch_bounds__(512)
   const int X0 = (int)fmin(ceil(2.0 * L.lminx), kmax), X1 = (int)fmin(ceil(2.0 * L.lmaxx), kmax);
   const int Y0 = (int)fmin(ceil(2.0 * L.lminy), kmax), Y1 = (int)fmin(ceil(2.0 * L.lmaxy), kmax);
   if (threadIdx.x == 0) {
+    warp_tot[32] = 0;
     int q0 = 0, q1 = npts;
     if (y_pmax != nullptr && y_smin != nullptr) {
       const int nt = (npts + YB_TILE - 1) / YB_TILE;
@@ -331,6 +398,22 @@ __global__ void __launch_bounds__(512)
   }
   __syncthreads();
   const int qb = s_range[0], qe = s_range[1];
+  if (mode == 0) {  // counts only: per-thread tallies, one block reduction
+    int cnt = 0;
+    for (int q = qb + threadIdx.x; q < qe; q += blockDim.x) {
+      if (lat) {
+        const int X = xy2[2 * q], Y = xy2[2 * q + 1];
+        cnt += (X >= X0 && X < X1 && Y >= Y0 && Y < Y1) ? 1 : 0;
+      } else {
+        cnt += inside(L, px[q], py[q]) ? 1 : 0;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&warp_tot[32], cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) counts[i] = warp_tot[32];
+    return;
+  }
   int base = 0;
   const int64_t off = (mode == 1) ? offsets[i] : 0;
   for (int c0 = qb; c0 < qe; c0 += blockDim.x) {
@@ -786,6 +869,17 @@ extern "C" int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, doubl
   k_y_tiles<<<nt, YB_TILE, 0, (cudaStream_t)stream>>>(py, npts, y_pmax, y_smin);
   k_y_tiles_scan<<<1, 1024, 0, (cudaStream_t)stream>>>(nt, y_pmax, y_smin);
   return check_launch("fi_tps_y_bounds", 2);
+}
+
+extern "C" int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
+                              int64_t* offsets, int64_t* noffsets, int64_t* mat_offsets,
+                              int64_t* w_offsets, int64_t* summary, void* stream) {
+  FI_REQUIRE(counts && ncounts && offsets && noffsets && mat_offsets && w_offsets && summary &&
+                 nb_subdom > 0,
+             "fi_tps_offsets: bad arguments");
+  k_tps_offsets<<<1, 1024, 0, (cudaStream_t)stream>>>(counts, ncounts, nb_subdom, offsets,
+                                                      noffsets, mat_offsets, w_offsets, summary);
+  return check_launch("fi_tps_offsets");
 }
 
 extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px,

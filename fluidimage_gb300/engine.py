@@ -193,8 +193,8 @@ class TpsOutput:
     selection: object = None  # int32 [num_centers]: index of each centre in the pass
     num_centers: int = 0
     nb_subdom: int = 0
-    counts: object = None
-    w_offsets: object = None
+    counts_d: object = None    # int32 [nb_subdom] device: members per subdomain
+    w_offsets_d: object = None  # int64 [nb_subdom] device: weight offsets
     weights: object = None
     singular: object = None
     mp_status: object = None
@@ -202,6 +202,20 @@ class TpsOutput:
     nfixed: object = None
     mp_sweeps: object = None
     max_udiff: object = None
+
+    @property
+    def counts(self):
+        """Members per subdomain (host copy, fetched on first use)."""
+        if not hasattr(self, "_counts"):
+            self._counts = self.counts_d.cpu().numpy().astype(np.int64)
+        return self._counts
+
+    @property
+    def w_offsets(self):
+        """Offsets of the subdomains' weights (host copy, fetched on first use)."""
+        if not hasattr(self, "_woff"):
+            self._woff = self.w_offsets_d.cpu().numpy()
+        return self._woff
 
 
 #: phi(k / 4) for k < PHI_TABLE_SIZE covers distances up to ~1024 px on the
@@ -240,6 +254,16 @@ def lattice_coords(px, py, npts, stream=None):
     return xy2, flag
 
 
+def _readback(t, stream=None):
+    """Small device tensor -> numpy through pinned memory (one synchronisation)."""
+    torch = _torch()
+    host = torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, pin_memory=True)
+    host.copy_(t.contiguous().view(-1).view(torch.uint8), non_blocking=True)
+    (stream or torch.cuda.current_stream()).synchronize()
+    a = host.numpy()
+    return a.view({torch.int64: np.int64, torch.uint8: np.uint8, torch.int32: np.int32}[t.dtype])
+
+
 def y_bounds(py, npts, stream=None):
     """Prefix max / suffix min of py (fi_tps_y_bounds): index ranges for the
     membership scans."""
@@ -273,7 +297,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                      int(subdom_size), float(smoothing_coef), 20.0, L.ptr(plan),
                                      L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy), L.ptr(sel), s),
                 "fi_tps_plan_make")
-    hdr = L.TpsPlan.from_buffer_copy(plan.cpu().numpy().tobytes())
+    hdr = L.TpsPlan.from_buffer_copy(_readback(plan, stream).tobytes())
     if hdr.status == 1:
         raise InterpError("Only nan.")
     if hdr.status != 0:
@@ -291,17 +315,14 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 0,
                                L.ptr(ncounts), None, None, None, L.ptr(pxy2), L.ptr(plat),
                                L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
-    both = torch.cat([counts, ncounts]).cpu().numpy().astype(np.int64)
-    ch, nch = both[:nsub], both[nsub:]
-    off = np.concatenate([[0], np.cumsum(ch)[:-1]]).astype(np.int64)
-    noff = np.concatenate([[0], np.cumsum(nch)[:-1]]).astype(np.int64)
-    msz = ((ch + 3) ** 2 + 3) // 4 * 4  # offsets stay multiples of 4 (16-byte aligned)
-    moff = np.concatenate([[0], np.cumsum(msz)[:-1]]).astype(np.int64)
-    wsz = 2 * (ch + 3)
-    woff = np.concatenate([[0], np.cumsum(wsz)[:-1]]).astype(np.int64)
-    tot, ntot = int(ch.sum()), int(nch.sum())
-    offs = torch.from_numpy(np.concatenate([off, noff, moff, woff])).to(dev, non_blocking=True)
-    off_d, noff_d, moff_d, woff_d = offs[:nsub], offs[nsub:2 * nsub], offs[2 * nsub:3 * nsub], offs[3 * nsub:]
+    # offsets on the device; the host reads back the 6 totals only
+    offs = torch.empty(4 * nsub + 6, dtype=torch.int64, device=dev)
+    off_d, noff_d = offs[:nsub], offs[nsub:2 * nsub]
+    moff_d, woff_d = offs[2 * nsub:3 * nsub], offs[3 * nsub:4 * nsub]
+    L.check(lib.fi_tps_offsets(L.ptr(counts), L.ptr(ncounts), nsub, L.ptr(off_d), L.ptr(noff_d),
+                               L.ptr(moff_d), L.ptr(woff_d), L.ptr(offs[4 * nsub:]), s),
+            "fi_tps_offsets")
+    tot, ntot, msum, wsum, maxc, maxnc = (int(v) for v in _readback(offs[4 * nsub:], stream))
     idx = torch.empty(max(tot, 1), **i32)
     coefs = torch.empty(max(tot, 1), **f64)
     nidx = torch.empty(max(ntot, 1), **i32)
@@ -312,9 +333,9 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 1, None,
                                L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), L.ptr(pxy2),
                                L.ptr(plat), L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
-    matrices = torch.empty(int(msz.sum()), **f64)
+    matrices = torch.empty(msum, **f64)
     pivots = torch.empty(tot + 3 * nsub, **i32)
-    weights = torch.empty(int(wsz.sum()), **f64)
+    weights = torch.empty(wsum, **f64)
     smx = torch.empty(max(tot, 1), **f64)
     smy = torch.empty(max(tot, 1), **f64)
     iters = torch.empty(2 * nsub, **i32)
@@ -326,11 +347,11 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     table = phi_table(dev)
     status = torch.ones(nsub, **i32)
     sweeps = torch.zeros(nsub, **i32)
-    if int(ch.max()) <= MP_MAX_MEMBERS:
-        matrices32 = torch.empty(int(msz.sum()), dtype=torch.float32, device=dev)
+    if maxc <= MP_MAX_MEMBERS:
+        matrices32 = torch.empty(msum, dtype=torch.float32, device=dev)
         with _timed("fi_tps_solve_mp"):
             L.check(lib.fi_tps_solve_mp(
-                L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
+                L.ptr(plan), nsub, maxc, L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
                 L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d), L.ptr(matrices),
                 L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
                 thr, int(use_thr),
@@ -339,7 +360,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                 "fi_tps_solve_mp")
     # FP64 LU for the subdomains the mixed-precision solver flagged (or all of them)
     with _timed("fi_tps_solve"):
-      L.check(lib.fi_tps_solve(L.ptr(plan), nsub, int(ch.max()), L.ptr(cx), L.ptr(cy), L.ptr(ux),
+      L.check(lib.fi_tps_solve(L.ptr(plan), nsub, maxc, L.ptr(cx), L.ptr(cy), L.ptr(ux),
                              L.ptr(uy), L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d),
                              L.ptr(matrices), L.ptr(pivots), thr, int(use_thr), L.ptr(woff_d),
                              L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
@@ -348,7 +369,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     out = TpsOutput(
         out_x=torch.empty(npts, **f64), out_y=torch.empty(npts, **f64),
         rx=torch.empty(npts, **i32), ry=torch.empty(npts, **i32), selection=sel,
-        num_centers=nv, nb_subdom=nsub, counts=ch, w_offsets=woff, weights=weights,
+        num_centers=nv, nb_subdom=nsub, counts_d=counts, w_offsets_d=woff_d, weights=weights,
         singular=singular, iters=iters, nfixed=nfixed, max_udiff=max_udiff,
         mp_status=status, mp_sweeps=sweeps,
     )
@@ -362,7 +383,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     partx = torch.empty(max(ntot, 1), **f64)
     party = torch.empty(max(ntot, 1), **f64)
     with _timed("fi_tps_interpolate"):
-      L.check(lib.fi_tps_interpolate(L.ptr(plan), nsub, int(ch.max()), int(nch.max()), L.ptr(cx),
+      L.check(lib.fi_tps_interpolate(L.ptr(plan), nsub, maxc, maxnc, L.ptr(cx),
                                    L.ptr(cy), L.ptr(counts), L.ptr(off_d), L.ptr(idx),
                                    L.ptr(woff_d), L.ptr(weights), L.ptr(px), L.ptr(py), npts,
                                    L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),

@@ -294,6 +294,18 @@ int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, double* y_smin, 
  * comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
  * restrict the scan to the tiles that can hold members.
  */
+/*
+ * Exclusive prefix sums for the buffers of nb_subdom subdomains from the member
+ * counts of the centres and of the new positions (fi_tps_members mode 0): CSR
+ * offsets of both, matrix slots ((n_i+3)^2 rounded up to 4 elements, as
+ * fi_tps_solve_mp wants) and weights (2 (n_i+3)); summary[6] = total members, total
+ * new members, matrix elements, weight elements, max members, max new members.
+ * No reference counterpart (the host-side bookkeeping of ThinPlateSplineSubdom).
+ */
+int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
+                   int64_t* offsets, int64_t* noffsets, int64_t* mat_offsets,
+                   int64_t* w_offsets, int64_t* summary, void* stream);
+
 int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
                    int npts, int mode, int32_t* counts, const int64_t* offsets,
                    int32_t* indices, double* coefs, const int32_t* xy2,
