@@ -45,6 +45,9 @@ struct Cfg {
   static constexpr int G = (N <= 16) ? 16 : ((N <= 32) ? 32 : 64);  // threads / window
   static constexpr int WPB = (G == 16) ? 16 : ((G == 32) ? 8 : 2);  // windows / block
   static constexpr int THREADS = G * WPB;
+  // resident CTAs per SM asked of the register allocator (16-px windows: 3, i.e.
+  // 24 warps, at <= 85 registers)
+  static constexpr int MIN_BLOCKS = (N <= 16) ? 3 : 1;
   static constexpr int LD = N + 1;   // row stride (float2) of the complex buffer
   static constexpr int LDP = N + 1;  // row stride (float) of the plane
   static constexpr int ZBYTES = N * LD * 8;
@@ -609,7 +612,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
 }
 
 template <int N, bool FROM_WINDOWS>
-__global__ void __launch_bounds__(Cfg<N>::THREADS)
+__global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     k_piv_pass(const fi_piv_pass_args a, const float* __restrict__ win0,
                const float* __restrict__ win1, int nvec, int npad, int do_peaks) {
   using C = Cfg<N>;
@@ -737,18 +740,35 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
     gsum4<C::G>(sums, g, red);
   }
   gminmax4<C::G>(mm, g, red);
-  const double NN = (double)N * (double)N;
-  // a constant window has an exactly zero spectrum (and plane) upstream
-  const bool flat0 = mm[0] == mm[2], flat1 = mm[1] == mm[3];
-  const double S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
-  const double S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
-  const bool flat = flat0 || flat1;
-  const double norm = sqrt(S0 * S1);
-  const float mean0 = (float)(sums[0] / NN), mean1 = (float)(sums[2] / NN);
-  int e0 = 0, e1 = 0;
-  if (S0 > 0.0) frexp(sqrt(S0 / NN), &e0);
-  if (S1 > 0.0) frexp(sqrt(S1 / NN), &e1);
-  const float sc0 = ldexpf(1.0f, -e0), sc1 = ldexpf(1.0f, -e1);
+  // per-window scalars: one thread computes them (FP64 is narrow on this GPU) and
+  // the group reads them back from its scratch
+  if (t == 0) {
+    const double NN = (double)N * (double)N;
+    // a constant window has an exactly zero spectrum (and plane) upstream
+    const bool flat0 = mm[0] == mm[2], flat1 = mm[1] == mm[3];
+    const double S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
+    const double S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
+    int e0 = 0, e1 = 0;
+    if (S0 > 0.0) frexp(sqrt(S0 / NN), &e0);
+    if (S1 > 0.0) frexp(sqrt(S1 / NN), &e1);
+    red[16] = sqrt(S0 * S1);
+    float* rf = reinterpret_cast<float*>(red + 17);
+    rf[0] = (float)(sums[0] / NN);
+    rf[1] = (float)(sums[2] / NN);
+    rf[2] = ldexpf(1.0f, -e0);
+    rf[3] = ldexpf(1.0f, -e1);
+    reinterpret_cast<int*>(red + 19)[0] = (flat0 || flat1) ? 1 : 0;
+    // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1), sc0 sc1 a power of two
+    reinterpret_cast<float*>(red + 20)[0] = (float)(0.25 / (NN * (double)rf[2] * (double)rf[3]));
+  }
+  gsync<C::G>(g);
+  const double norm = red[16];
+  const float mean0 = reinterpret_cast<const float*>(red + 17)[0];
+  const float mean1 = reinterpret_cast<const float*>(red + 17)[1];
+  const float sc0 = reinterpret_cast<const float*>(red + 17)[2];
+  const float sc1 = reinterpret_cast<const float*>(red + 17)[3];
+  const bool flat = reinterpret_cast<const int*>(red + 19)[0] != 0;
+  const float outscale = reinterpret_cast<const float*>(red + 20)[0];
   gsync<C::G>(g);
 
   // ---- forward 2-D FFT of z = x0*sc0 + i*x1*sc1 ----
@@ -803,7 +823,6 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
   }
   gsync<C::G>(g);
   if (t < N) {
-    const float outscale = (float)(0.25 / (NN * (double)sc0 * (double)sc1));
     const int i0 = shift_index<N>(t);
 #pragma unroll
     for (int c = 0; c < N; ++c) PL[i0 * C::LDP + shift_index<N>(c)] = flat ? 0.f : x[c].x * outscale;
