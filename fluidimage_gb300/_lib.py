@@ -112,8 +112,8 @@ _SIGNATURES = {
     "fi_tps_phi_table2": (C.c_int, [P, C.c_int64, P]),
     "fi_tps_solve_mp": (
         C.c_int,
-        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P, C.c_double,
-         C.c_int, P, P, P, P, P, P, P, P, P, P],
+        [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P,
+         C.c_double, C.c_int, P, P, P, P, P, P, P, P, P, P],
     ),
     "fi_rank_filter": (
         C.c_int,

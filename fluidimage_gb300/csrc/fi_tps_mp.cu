@@ -8,10 +8,12 @@
 // w = Q2 z and
 //     B z = g = Q2^T u,   B = Q2^T (K + lam I) Q2   (SPD, cond ~1e4 for lam > 0),
 //     a = R^-1 (Q1^T u - C z),  C = Q1^T (K + lam I) Q2,   smoothed = u - lam w.
-// On this GPU FP32 runs 73x faster than FP64.  B and C are projected once in FP64
-// (compact WY form of Q; the projection cancels the large affine part of K), B is
-// kept as pairs of floats (hi + lo, ~48 bits) and its FP32 rounding is factorised
-// (tiled Cholesky).  z is refined in double-float: rho = g - B z on the FP32 pipe
+// On this GPU FP32 runs 73x faster than FP64.  B and C are projected once with the
+// compact WY form of Q; the projection cancels the large affine part of K, so it
+// needs more than FP32: Y = A V and B are computed in double-float (pairs of floats,
+// error-free products and sums on the FP32 pipe, ~48 bits), the O(n) parts and C in
+// FP64.  B is kept as (hi, lo) pairs and its FP32 rounding is factorised (tiled
+// Cholesky).  z is refined in double-float: rho = g - B z on the FP32 pipe
 // (error-free products and sums), then an FP32 Cholesky solve for the correction.
 // Each sweep contracts the error ~1e3-1e4 times; refinement stops when the
 // predicted remaining error is below 1e-10 of z, or when it stagnates (then it must
@@ -549,8 +551,9 @@ __global__ void __launch_bounds__(NT, 512 / NT)
                    const float* ux, const float* uy, const int32_t* counts,
                    const int64_t* offsets, const int32_t* indices, const int64_t* mat_off,
                    double* matrices, float* matrices32, const double* phi_table,
-                   int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
-                   double threshold, int use_threshold, const int64_t* w_off, double* weights,
+                   const float2* phi_table2, int64_t table_size, const int32_t* cxy2,
+                   const int32_t* c_on_lattice, double threshold, int use_threshold,
+                   const int64_t* w_off, double* weights,
                    double* smoothed_x, double* smoothed_y, int32_t* iters, int32_t* nfixed,
                    int32_t* status, double* max_udiff, int32_t* sweeps, int max_refine,
                    int n_layout) {
@@ -622,6 +625,20 @@ __global__ void __launch_bounds__(NT, 512 / NT)
     }
     return phi_pair(xc[r], yc[r], xc[c], yc[c], phi_table, table_size);
   };
+  // the same entry as a (hi, lo) float pair; ci = lattice coordinates of centre i
+  const float2 lam2 = df_split(lam);
+  auto a_entry_df = [&](int i, int2 ci, int j) -> float2 {
+    if (i == j) return lam2;
+    if (lat) {
+      const int2 cj = cxy[j];
+      const int64_t dx = (int64_t)(ci.x - cj.x), dy = (int64_t)(ci.y - cj.y);
+      const int64_t kq = dy * dy + dx * dx;
+      if (kq < table_size)
+        return phi_table2 != nullptr ? phi_table2[kq] : df_split(__ldg(phi_table + kq));
+      return df_split(phi_pair(xc[i], yc[i], xc[j], yc[j], nullptr, 0));
+    }
+    return df_split(phi_pair(xc[i], yc[i], xc[j], yc[j], phi_table, table_size));
+  };
 
   // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
   {
@@ -686,27 +703,85 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   double* Y0 = YC;
   double* Y1 = YC + n;
   double* Y2 = YC + 2 * n;
-  // ---- Y = A V (FP64; A symmetric: row c = column c); the columns are shared by the
-  // cluster's CTAs, each result written into every CTA's Y
-  for (int c = crank * NW + wid; c < N; c += csize * NW) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int r = lane; r < N; r += 32) {
-      const double v = a_entry(r, c);
-      a0 = fma(v, V0[r], a0);
-      a1 = fma(v, V1[r], a1);
-      a2 = fma(v, V2[r], a2);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-    }
-    if (lane == 0) {
+  // V and Z as (hi, lo) float pairs, [3][np] each: the f2 and f regions (6 np pairs)
+  // are free until the refinement
+  float2* Vd = zx2;
+  float2* Zd = zx2 + 3 * lay.np;
+  const int np = lay.np;
+  for (int i = threadIdx.x; i < np; i += NT) {
+    const bool in = i < N;
+    Vd[i] = in ? df_split(V0[i]) : make_float2(0.f, 0.f);
+    Vd[np + i] = in ? df_split(V1[i]) : make_float2(0.f, 0.f);
+    Vd[2 * np + i] = in ? df_split(V2[i]) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  // ---- Y = A V in double-float on the FP32 pipe.  A is symmetric: lane = column c,
+  // the rows r in chunks (jobs = column block x chunk, a multiple of the warp count
+  // when the scratch allows); the chunks' partial sums are added in a fixed order.
+  // The column blocks are spread over the cluster's CTAs; each Y value is rounded to
+  // double and written into every CTA's Y.
+  {
+    auto write_y = [&](int c, float2 s0, float2 s1, float2 s2) {
+      const double y0 = df_to_double(s0), y1 = df_to_double(s1), y2 = df_to_double(s2);
       for (int q = 0; q < csize; ++q) {
         double* Yq = (q == crank) ? YC : cluster.map_shared_rank(YC, q);
-        Yq[c] = a0;
-        Yq[n + c] = a1;
-        Yq[2 * n + c] = a2;
+        Yq[c] = y0;
+        Yq[n + c] = y1;
+        Yq[2 * n + c] = y2;
+      }
+    };
+    const int ncb = (N + 31) / 32;
+    const int nloc = (crank < ncb) ? (ncb - crank + csize - 1) / csize : 0;
+    int rs = 1;
+    if (nloc > 0) {
+      int a = nloc, b = NW;
+      while (b != 0) {
+        const int t = a % b;
+        a = b;
+        b = t;
+      }
+      rs = NW / a;  // nloc * rs is a multiple of NW
+      const int max_jobs = (int)((size_t)(1 + NW) * 32 * TS * sizeof(float) / (96 * sizeof(float2)));
+      while (rs > 1 && (nloc * rs > max_jobs || 8 * rs > N)) rs >>= 1;
+    }
+    float2* part = reinterpret_cast<float2*>(panel);  // [job][3][32]
+    for (int j = wid; j < nloc * rs; j += NW) {
+      const int l = j / rs, ch = j - l * rs;
+      const int c = 32 * (crank + csize * l) + lane;
+      const int r0 = (int)((int64_t)N * ch / rs), r1 = (int)((int64_t)N * (ch + 1) / rs);
+      float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+      if (c < N) {
+        const int2 cc = cxy[c];
+        for (int r = r0; r < r1; ++r) {
+          const float2 a = a_entry_df(c, cc, r);
+          df_mac(a, Vd[r], h0, l0);
+          df_mac(a, Vd[np + r], h1, l1);
+          df_mac(a, Vd[2 * np + r], h2, l2);
+        }
+      }
+      if (rs == 1) {
+        if (c < N) write_y(c, make_float2(h0, l0), make_float2(h1, l1), make_float2(h2, l2));
+      } else {
+        part[(3 * j + 0) * 32 + lane] = make_float2(h0, l0);
+        part[(3 * j + 1) * 32 + lane] = make_float2(h1, l1);
+        part[(3 * j + 2) * 32 + lane] = make_float2(h2, l2);
+      }
+    }
+    if (rs > 1) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < nloc * 32; t += NT) {
+        const int l = t >> 5, ln = t & 31;
+        const int c = 32 * (crank + csize * l) + ln;
+        if (c >= N) continue;
+        const float2* pj = part + (size_t)3 * 32 * (l * rs);
+        float2 s0 = pj[ln], s1 = pj[32 + ln], s2 = pj[64 + ln];
+        for (int ch = 1; ch < rs; ++ch) {
+          pj += 3 * 32;
+          s0 = df_add(s0, pj[ln]);
+          s1 = df_add(s1, pj[32 + ln]);
+          s2 = df_add(s2, pj[64 + ln]);
+        }
+        write_y(c, s0, s1, s2);
       }
     }
   }
@@ -772,6 +847,13 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       Z1[i] = z[1];
       Z2[i] = z[2];
     }
+    for (int i = N + threadIdx.x; i < np; i += NT) Zd[i] = Zd[np + i] = Zd[2 * np + i] = make_float2(0.f, 0.f);
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += NT) {
+      Zd[i] = df_split(Z0[i]);
+      Zd[np + i] = df_split(Z1[i]);
+      Zd[2 * np + i] = df_split(Z2[i]);
+    }
     __syncthreads();
   }
   auto proj = [&](int r, int c) -> double {  // (Q^T A Q)[r][c], global indices
@@ -801,12 +883,34 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       while (I * (I + 1) / 2 > pidx) --I;
       const int J = pidx - I * (I + 1) / 2;
       const int r = 32 * I + lane;
+      // the row's -Z_k and -V_k pairs and lattice coordinates
+      const int rg = (r < m) ? r + 3 : 3;
+      const int2 cr = cxy[rg];
+      float2 nz[3], nv[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float2 zv = Zd[k * np + rg], vv = Vd[k * np + rg];
+        nz[k] = make_float2(-zv.x, -zv.y);
+        nv[k] = make_float2(-vv.x, -vv.y);
+      }
       for (int h = 0; h < 2; ++h) {
 #pragma unroll 4
         for (int q = 0; q < 16; ++q) {
           const int c = 32 * J + 16 * h + q;
           if (r < m && c < m && r >= c) {
-            const float2 s = df_split(proj(r + 3, c + 3));
+            // A - Z V^T - V Z^T in double-float: entries of A up to ~1e5 cancel to
+            // B entries ~1e2-1e4; the ~2^-48 |A| rounding leaves B within ~1e-11 of
+            // its FP64 value, the interpolated field within ~1e-9 px
+            const int cg_ = c + 3;
+            const float2 a = a_entry_df(rg, cr, cg_);
+            float sh = a.x, sl = a.y;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              df_mac(nz[k], Vd[k * np + cg_], sh, sl);
+              df_mac(nv[k], Zd[k * np + cg_], sh, sl);
+            }
+            const float hi = __fadd_rn(sh, sl);
+            const float2 s = make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
             B2[(int64_t)c * mp + r] = s;
             L32[(int64_t)c * mp + r] = s.x;
             S[q * 33 + lane] = s;
@@ -1048,7 +1152,7 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                const float* uy, const int32_t* counts, const int64_t* offsets,
                                const int32_t* indices, const int64_t* mat_offsets,
                                double* matrices, float* matrices32, const double* phi_table,
-                               int64_t table_size, const int32_t* cxy2,
+                               const float* phi_table2, int64_t table_size, const int32_t* cxy2,
                                const int32_t* c_on_lattice, double threshold, int use_threshold,
                                const int64_t* w_offsets, double* weights, double* smoothed_x,
                                double* smoothed_y, int32_t* iters, int32_t* nfixed,
@@ -1062,6 +1166,7 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
   FI_REQUIRE(nb_subdom > 0, "fi_tps_solve_mp: no subdomain");
   FI_REQUIRE(((uintptr_t)matrices & 15) == 0 && ((uintptr_t)matrices32 & 15) == 0,
              "fi_tps_solve_mp: matrices must be 16-byte aligned");
+  FI_REQUIRE(((uintptr_t)phi_table2 & 7) == 0, "fi_tps_solve_mp: phi_table2 must be 8-byte aligned");
   const int N = max_members > 4 ? max_members : 4;
   // 16 warps per subdomain when the subdomains fit in one wave of blocks (shorter
   // latency per subdomain), else two blocks of 8 warps per SM
@@ -1098,13 +1203,15 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
     cfg.numAttrs = 1;
     FI_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_tps_solve_mp<512>, plan, cx, cy, ux, uy, counts,
                                    offsets, indices, mat_offsets, matrices, matrices32,
-                                   phi_table, table_size, cxy2, c_on_lattice, threshold,
+                                   phi_table, reinterpret_cast<const float2*>(phi_table2),
+                                   table_size, cxy2, c_on_lattice, threshold,
                                    use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
                                    iters, nfixed, status, max_udiff, sweeps, 60, N));
   } else
     k_tps_solve_mp<256><<<nb_subdom, 256, smem, (cudaStream_t)stream>>>(
         plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
-        phi_table, table_size, cxy2, c_on_lattice, threshold, use_threshold, w_offsets, weights,
+        phi_table, reinterpret_cast<const float2*>(phi_table2), table_size, cxy2, c_on_lattice,
+        threshold, use_threshold, w_offsets, weights,
         smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, 60, N);
   return check_launch("fi_tps_solve_mp");
 }

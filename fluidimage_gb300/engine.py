@@ -353,7 +353,8 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
             L.check(lib.fi_tps_solve_mp(
                 L.ptr(plan), nsub, maxc, L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
                 L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d), L.ptr(matrices),
-                L.ptr(matrices32), L.ptr(table), PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
+                L.ptr(matrices32), L.ptr(table), L.ptr(phi_table(dev, pairs=True)),
+                PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
                 thr, int(use_thr),
                 L.ptr(woff_d), L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
                 L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), L.ptr(sweeps), s),

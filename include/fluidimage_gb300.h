@@ -348,7 +348,7 @@ int fi_tps_phi_table2(float* table2, int64_t count, void* stream);
 /*
  * Mixed-precision TPS solve (same inputs and outputs as fi_tps_solve): null-space
  * form B z = Q2^T u with B = Q2^T (K + lam I) Q2 (P = Q R, Householder; B projected
- * in FP64 with the compact WY form of Q), factorised in FP32 (blocked Cholesky) and
+ * in double-float with the compact WY form of Q), factorised in FP32 (blocked Cholesky) and
  * refined with double-float (pairs of floats) residuals g - B z; the affine part is
  * a = R^-1 (Q1^T u - Q1^T A Q2 z).  K comes from the phi table.  The outlier
  * iterations of compute_tps_weights_iter (thin_plate_spline_subdom.py:236-280)
@@ -356,7 +356,8 @@ int fi_tps_phi_table2(float* table2, int64_t count, void* stream);
  * both matrix buffers 16-byte aligned: matrices holds (n_i+3)^2 doubles at
  * mat_offsets[i] (B as float pairs), matrices32 (n_i+3)^2 floats (its Cholesky
  * factor).  cxy2/c_on_lattice (nullable, fi_tps_lattice of the centres) give
- * integer table indices.  status[i] = 0 when solved, 1 when the subdomain must go
+ * integer indices into phi_table and phi_table2 (nullable; fi_tps_phi_table2 of the
+ * same size, the pairs the double-float projection reads).  status[i] = 0 when solved, 1 when the subdomain must go
  * through fi_tps_solve (pass status as its only_failed argument): rank-deficient P,
  * Cholesky breakdown or no convergence.  sweeps (nullable, [nb_subdom]): refinement
  * sweeps (one FP32 solve each) per subdomain.
@@ -365,8 +366,8 @@ int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, con
                     const double* cy, const float* ux, const float* uy, const int32_t* counts,
                     const int64_t* offsets, const int32_t* indices, const int64_t* mat_offsets,
                     double* matrices, float* matrices32, const double* phi_table,
-                    int64_t table_size, const int32_t* cxy2, const int32_t* c_on_lattice,
-                    double threshold, int use_threshold,
+                    const float* phi_table2, int64_t table_size, const int32_t* cxy2,
+                    const int32_t* c_on_lattice, double threshold, int use_threshold,
                     const int64_t* w_offsets, double* weights, double* smoothed_x,
                     double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
                     double* max_udiff, int32_t* sweeps, void* stream);
