@@ -639,6 +639,35 @@ __global__ void __launch_bounds__(NT, 512 / NT)
     }
     return df_split(phi_pair(xc[i], yc[i], xc[j], yc[j], phi_table, table_size));
   };
+  // entries (i, j0 .. j0 + cnt - 1) of A as pairs (0 < cnt <= 8, the rest zero): on the
+  // lattice the eight table loads are issued before any is used (the loads, mostly
+  // L2 hits, bound these phases), the diagonal and far entries patched afterwards
+  auto a_batch_df = [&](int i, int2 ci, int j0, int cnt, float2(&out)[8]) {
+    if (lat && phi_table2 != nullptr) {
+      int64_t kq[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int2 cj = cxy[j0 + min(u, cnt - 1)];
+        const int64_t dx = (int64_t)(ci.x - cj.x), dy = (int64_t)(ci.y - cj.y);
+        kq[u] = dy * dy + dx * dx;
+        out[u] = phi_table2[kq[u] < table_size ? kq[u] : 0];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u;
+        if (u >= cnt)
+          out[u] = make_float2(0.f, 0.f);
+        else if (j == i)
+          out[u] = lam2;
+        else if (kq[u] >= table_size)
+          out[u] = df_split(phi_pair(xc[i], yc[i], xc[j], yc[j], nullptr, 0));
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        out[u] = (u < cnt) ? a_entry_df(i, ci, j0 + u) : make_float2(0.f, 0.f);
+    }
+  };
 
   // ---- Householder QR of P = [1, y, x] (FP64), V rows k hold v_k (zeros above k)
   {
@@ -752,11 +781,19 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
       if (c < N) {
         const int2 cc = cxy[c];
-        for (int r = r0; r < r1; ++r) {
-          const float2 a = a_entry_df(c, cc, r);
-          df_mac(a, Vd[r], h0, l0);
-          df_mac(a, Vd[np + r], h1, l1);
-          df_mac(a, Vd[2 * np + r], h2, l2);
+        for (int rb = r0; rb < r1; rb += 8) {
+          const int cnt = min(8, r1 - rb);
+          float2 a[8];
+          a_batch_df(c, cc, rb, cnt, a);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            if (u < cnt) {
+              const int r = rb + u;
+              df_mac(a[u], Vd[r], h0, l0);
+              df_mac(a[u], Vd[np + r], h1, l1);
+              df_mac(a[u], Vd[2 * np + r], h2, l2);
+            }
+          }
         }
       }
       if (rs == 1) {
@@ -894,26 +931,32 @@ __global__ void __launch_bounds__(NT, 512 / NT)
         nv[k] = make_float2(-vv.x, -vv.y);
       }
       for (int h = 0; h < 2; ++h) {
-#pragma unroll 4
-        for (int q = 0; q < 16; ++q) {
-          const int c = 32 * J + 16 * h + q;
-          if (r < m && c < m && r >= c) {
-            // A - Z V^T - V Z^T in double-float: entries of A up to ~1e5 cancel to
-            // B entries ~1e2-1e4; the ~2^-48 |A| rounding leaves B within ~1e-11 of
-            // its FP64 value, the interpolated field within ~1e-9 px
-            const int cg_ = c + 3;
-            const float2 a = a_entry_df(rg, cr, cg_);
-            float sh = a.x, sl = a.y;
+        for (int qb = 0; qb < 16; qb += 8) {
+          const int c0 = 32 * J + 16 * h + qb;
+          if (c0 >= m) break;
+          const int cnt = min(8, m - c0);
+          float2 a[8];
+          a_batch_df(rg, cr, c0 + 3, cnt, a);
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              df_mac(nz[k], Vd[k * np + cg_], sh, sl);
-              df_mac(nv[k], Zd[k * np + cg_], sh, sl);
+          for (int u = 0; u < 8; ++u) {
+            const int c = c0 + u;
+            if (u < cnt && r < m && r >= c) {
+              // A - Z V^T - V Z^T in double-float: entries of A up to ~1e5 cancel to
+              // B entries ~1e2-1e4; the ~2^-48 |A| rounding leaves B within ~1e-11 of
+              // its FP64 value, the interpolated field within ~1e-9 px
+              const int cg_ = c + 3;
+              float sh = a[u].x, sl = a[u].y;
+#pragma unroll
+              for (int k = 0; k < 3; ++k) {
+                df_mac(nz[k], Vd[k * np + cg_], sh, sl);
+                df_mac(nv[k], Zd[k * np + cg_], sh, sl);
+              }
+              const float hi = __fadd_rn(sh, sl);
+              const float2 sv = make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
+              B2[(int64_t)c * mp + r] = sv;
+              L32[(int64_t)c * mp + r] = sv.x;
+              S[(qb + u) * 33 + lane] = sv;
             }
-            const float hi = __fadd_rn(sh, sl);
-            const float2 s = make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
-            B2[(int64_t)c * mp + r] = s;
-            L32[(int64_t)c * mp + r] = s.x;
-            S[q * 33 + lane] = s;
           }
         }
         __syncwarp();
