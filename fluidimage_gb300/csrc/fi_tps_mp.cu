@@ -391,61 +391,76 @@ __device__ __forceinline__ void tile_store(float* B, int m, int ld, int ti, int 
   }
 }
 
+// POTRF of one 32 x 32 tile held in registers (a[c] = element (lane, c)): writes the
+// factor's lower triangle to tile (k, k) of B, its rows (zero right of the diagonal)
+// and 1 / L_jj (column 32) to Lkk; sets *s_flag on a non-positive pivot.
+__device__ __forceinline__ void potrf_tile(float (&a)[32], float* B, int m, int ld, int k,
+                                           float* Lkk, int lane, int* s_flag) {
+  const unsigned full = 0xffffffffu;
+  bool bad = false;
+  float dg = 1.f;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    float djj = __shfl_sync(full, a[j], j);
+    if (!(djj > 0.f)) {
+      bad = true;
+      djj = 1.f;
+    }
+    const float rs = rsqrtf(djj);  // FP32 factor: refinement absorbs its rounding
+    const float sq = djj * rs;
+    if (lane == j) dg = sq;
+    const float lrj = (lane > j) ? a[j] * rs : ((lane == j) ? sq : 0.f);
+    if (lane >= j) a[j] = lrj;
+    // the row update in chunks of 8 shuffles: the fence keeps the compiler from
+    // hoisting all 31 (the row a[] then stays in registers under the cap)
+#pragma unroll
+    for (int c0 = (j + 1) & ~7; c0 < 32; c0 += 8) {
+#pragma unroll
+      for (int c = c0; c < c0 + 8; ++c) {
+        if (c <= j) continue;
+        const float lcj = __shfl_sync(full, lrj, c);
+        if (lane >= c) a[c] = fmaf(-lrj, lcj, a[c]);
+      }
+      __syncwarp();
+    }
+  }
+  if (bad && lane == 0) *s_flag = 1;
+  tile_store(B, m, ld, k, k, a, lane, true);
+#pragma unroll
+  for (int c = 0; c < 32; ++c) Lkk[lane * TS + c] = (c < lane) ? a[c] : 0.f;
+  Lkk[lane * TS + 32] = 1.f / dg;
+}
+
 // Right-looking tiled Cholesky (lower) of the m x m matrix B (column-major, ld), in
-// place (lower triangle).  Per tile column k: one warp factorises the diagonal tile
-// in registers (shuffles), warps solve the tiles below (one row per lane, rows of
-// L_kk read as float4 broadcasts), then update the trailing tile pairs (register
-// accumulators, the second factor transposed in shared memory, float4 broadcasts).
-// scratch: (1 + warps) * 32 * TS floats, 16-byte aligned.  False on a non-positive
+// place (lower triangle).  Per tile column k: warps solve the tiles below the
+// diagonal (one row per lane, rows of L_kk read as float4 broadcasts), then update
+// the trailing tile pairs (register accumulators, packed FP32x2 FMAs, the second
+// factor transposed in shared memory, float4 broadcasts).  Lookahead: warp 0 first
+// updates the next diagonal tile and factorises it in registers (shuffles) while the
+// other warps update the rest; the tiles go to the warps in the order they finish.
+// scratch: (2 + warps) * 32 * TS floats, 16-byte aligned.  False on a non-positive
 // pivot.
 template <int NT>
-__device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag) {
+__device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag,
+                            int* s_next) {
   constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   const int T = (m + 31) / 32;
-  float* Lkk = scratch;                     // row j: L_kk[j][c] for c < j (0 elsewhere), [32] = 1 / L_jj
-  float* Lt = scratch + 32 * TS * (1 + wid);  // per warp, transposed tile
+  // two L_kk buffers (step k reads buffer k & 1 while step k + 1's is written); row
+  // j: L_kk[j][c] for c < j (0 elsewhere), [32] = 1 / L_jj
+  float* Lkk0 = scratch;
+  float* Lt = scratch + 32 * TS * (2 + wid);  // per warp, transposed tile
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
+  if (wid == 0) {
+    float a[32];
+    tile_load(B, m, ld, 0, 0, a, lane);
+    potrf_tile(a, B, m, ld, 0, Lkk0, lane, s_flag);
+  }
+  __syncthreads();
   for (int k = 0; k < T; ++k) {
-    if (wid == 0) {  // POTRF of tile (k, k)
-      float a[32];
-      tile_load(B, m, ld, k, k, a, lane);
-      bool bad = false;
-      float dg = 1.f;
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        float djj = __shfl_sync(full, a[j], j);
-        if (!(djj > 0.f)) {
-          bad = true;
-          djj = 1.f;
-        }
-        const float rs = rsqrtf(djj);  // FP32 factor: refinement absorbs its rounding
-        const float sq = djj * rs;
-        if (lane == j) dg = sq;
-        const float lrj = (lane > j) ? a[j] * rs : ((lane == j) ? sq : 0.f);
-        if (lane >= j) a[j] = lrj;
-        // the row update in chunks of 8 shuffles: the fence keeps the compiler from
-        // hoisting all 31 (the row a[] then stays in registers under the cap)
-#pragma unroll
-        for (int c0 = (j + 1) & ~7; c0 < 32; c0 += 8) {
-#pragma unroll
-          for (int c = c0; c < c0 + 8; ++c) {
-            if (c <= j) continue;
-            const float lcj = __shfl_sync(full, lrj, c);
-            if (lane >= c) a[c] = fmaf(-lrj, lcj, a[c]);
-          }
-          __syncwarp();
-        }
-      }
-      if (bad && lane == 0) *s_flag = 1;
-      tile_store(B, m, ld, k, k, a, lane, true);
-#pragma unroll
-      for (int c = 0; c < 32; ++c) Lkk[lane * TS + c] = (c < lane) ? a[c] : 0.f;
-      Lkk[lane * TS + 32] = 1.f / dg;
-    }
-    __syncthreads();
+    const float* Lkk = Lkk0 + (k & 1) * 32 * TS;
     // TRSM: tiles (i, k), i > k: X L_kk^T = A_ik, row by row in each lane
     for (int i = k + 1 + wid; i < T; i += NW) {
       float b[32];
@@ -466,11 +481,14 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       }
       tile_store(B, m, ld, i, k, b, lane, false);
     }
+    if (threadIdx.x == 0) *s_next = NW;
     __syncthreads();
-    // trailing update: tiles (i, j), k < j <= i
+    if (k + 1 >= T) break;
+    // trailing update: tiles (i, j), k < j <= i; pair 0 is tile (k + 1, k + 1)
     const int n = T - k - 1;
     const int npairs = n * (n + 1) / 2;
-    for (int pidx = wid; pidx < npairs; pidx += NW) {
+    int pidx = wid;
+    while (pidx < npairs) {
       int ii = (int)((sqrtf(8.f * pidx + 1.f) - 1.f) * 0.5f);
       while ((ii + 1) * (ii + 2) / 2 <= pidx) ++ii;
       while (ii * (ii + 1) / 2 > pidx) --ii;
@@ -499,19 +517,29 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
         }
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
-          const float lr = l[t];
+          const float2 lr = make_float2(-l[t], -l[t]);
 #pragma unroll
           for (int c4 = 0; c4 < 8; ++c4) {
             const float4 q = *reinterpret_cast<const float4*>(Lt + (16 * h + t) * TS + 4 * c4);
-            acc[4 * c4] = fmaf(-lr, q.x, acc[4 * c4]);
-            acc[4 * c4 + 1] = fmaf(-lr, q.y, acc[4 * c4 + 1]);
-            acc[4 * c4 + 2] = fmaf(-lr, q.z, acc[4 * c4 + 2]);
-            acc[4 * c4 + 3] = fmaf(-lr, q.w, acc[4 * c4 + 3]);
+            float2 a01 = make_float2(acc[4 * c4], acc[4 * c4 + 1]);
+            float2 a23 = make_float2(acc[4 * c4 + 2], acc[4 * c4 + 3]);
+            a01 = __ffma2_rn(lr, make_float2(q.x, q.y), a01);
+            a23 = __ffma2_rn(lr, make_float2(q.z, q.w), a23);
+            acc[4 * c4] = a01.x;
+            acc[4 * c4 + 1] = a01.y;
+            acc[4 * c4 + 2] = a23.x;
+            acc[4 * c4 + 3] = a23.y;
           }
         }
       }
-      tile_store(B, m, ld, i, j, acc, lane, i == j);
+      if (pidx == 0)
+        potrf_tile(acc, B, m, ld, k + 1, Lkk0 + ((k + 1) & 1) * 32 * TS, lane, s_flag);
+      else
+        tile_store(B, m, ld, i, j, acc, lane, i == j);
       __syncwarp();
+      int nxt = 0;
+      if (lane == 0) nxt = atomicAdd(s_next, 1);
+      pidx = __shfl_sync(full, nxt, 0);
     }
     __syncthreads();
   }
@@ -525,7 +553,7 @@ struct MpLayout {
   size_t f2_off; // float2: zx, zy, gx, gy (np each)
   size_t f_off;  // float: vx, vy, rx, ry (np each)
   size_t i2_off; // int2: lattice coordinates (np)
-  size_t p_off;  // panel: (1 + warps) * 32 * TS floats
+  size_t p_off;  // panel: (2 + warps) * 32 * TS floats
   size_t bytes;
   __host__ __device__ MpLayout(int n, int warps) {
     np = (n + 31) & ~31;
@@ -534,7 +562,7 @@ struct MpLayout {
     f_off = f2_off + (size_t)4 * np * sizeof(float2);
     i2_off = f_off + (size_t)4 * np * sizeof(float);
     p_off = i2_off + (size_t)np * sizeof(int2);
-    bytes = p_off + (size_t)(1 + warps) * 32 * TS * sizeof(float);
+    bytes = p_off + (size_t)(2 + warps) * 32 * TS * sizeof(float);
   }
 };
 
@@ -563,7 +591,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   __shared__ double s_tau[3];
   __shared__ double s_R[9];
   __shared__ double s_q1[6];
-  __shared__ int s_flag, s_bad[2], s_lat;
+  __shared__ int s_flag, s_next, s_bad[2], s_lat;
   const fi_tps_plan p = *plan_ptr;
   // a cluster of csize CTAs per subdomain (1 without cluster launch): all of them
   // factor P and share the FP64 build and projection, rank 0 then solves alone
@@ -770,7 +798,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
         b = t;
       }
       rs = NW / a;  // nloc * rs is a multiple of NW
-      const int max_jobs = (int)((size_t)(1 + NW) * 32 * TS * sizeof(float) / (96 * sizeof(float2)));
+      const int max_jobs = (int)((size_t)(2 + NW) * 32 * TS * sizeof(float) / (96 * sizeof(float2)));
       while (rs > 1 && (nloc * rs > max_jobs || 8 * rs > N)) rs >>= 1;
     }
     float2* part = reinterpret_cast<float2*>(panel);  // [job][3][32]
@@ -973,7 +1001,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   cluster.sync();  // the cluster's B tiles are in global memory, visible to rank 0
   if (crank != 0) return;
   // ---- FP32 Cholesky of B22
-  if (!chol_factor<NT>(L32, m, mp, panel, &s_flag)) return;
+  if (!chol_factor<NT>(L32, m, mp, panel, &s_flag, &s_next)) return;
 
   // ---- outlier iterations with refined solves (x and y in lockstep)
   double* tx = W;
