@@ -83,6 +83,7 @@ _SIGNATURES = {
     "fi_last_error": (C.c_char_p, []),
     "fi_version": (C.c_char_p, []),
     "fi_abi_sizes": (C.c_int, [P]),
+    "fi_memcpy_d2h": (C.c_int, [P, P, C.c_int64, P]),
     "fi_launch_count": (C.c_longlong, []),
     "fi_images_min": (C.c_int, [P, P, C.c_int, C.c_int64, P, P]),
     "fi_piv_pass": (C.c_int, [P, P]),
@@ -103,6 +104,14 @@ _SIGNATURES = {
     "fi_tps_y_bounds": (C.c_int, [P, C.c_int, P, P, P]),
     "fi_tps_offsets": (C.c_int, [P, P, C.c_int, P, P, P, P, P, P]),
     "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P]),
+    "fi_tps_layout": (
+        C.c_int,
+        [P, C.c_int, P, P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P],
+    ),
+    "fi_tps_members_fill": (
+        C.c_int,
+        [P, C.c_int, P, P, C.c_int, P, P, C.c_int, P, P, P, P, P, P, P, P, P, P, P, P],
+    ),
     "fi_tps_solve": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, C.c_double, C.c_int, P, P, P, P,

@@ -1012,6 +1012,14 @@ extern "C" int fi_abi_sizes(int64_t* out) {
   return FI_OK;
 }
 
+extern "C" int fi_memcpy_d2h(void* host_dst, const void* device_src, int64_t nbytes,
+                             void* stream) {
+  FI_REQUIRE(host_dst && device_src && nbytes >= 0, "fi_memcpy_d2h: bad arguments");
+  FI_CUDA_TRY(cudaMemcpyAsync(host_dst, device_src, (size_t)nbytes, cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
+  return FI_OK;
+}
+
 extern "C" int fi_images_min(const void* im0, const void* im1, int dtype, int64_t count,
                              float* out_min, void* stream) {
   FI_REQUIRE(im0 && im1 && out_min, "fi_images_min: null pointer");

@@ -896,6 +896,56 @@ extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const doub
   return check_launch("fi_tps_members");
 }
 
+extern "C" int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const double* cx,
+                             const double* cy, int num_centers, const double* px,
+                             const double* py, int npts, int p_given, int32_t* cxy2,
+                             int32_t* clat, int32_t* pxy2, int32_t* plat, double* cbounds,
+                             double* pbounds, int32_t* counts, int32_t* ncounts,
+                             int64_t* offsets, void* stream) {
+  FI_REQUIRE(plan && cx && cy && px && py && cxy2 && clat && pxy2 && plat && cbounds &&
+                 pbounds && counts && ncounts && offsets && nb_subdom > 0 &&
+                 num_centers > 0 && npts > 0,
+             "fi_tps_layout: bad arguments");
+  const int ctiles = (num_centers + YB_TILE - 1) / YB_TILE;
+  const int ptiles = (npts + YB_TILE - 1) / YB_TILE;
+  int rc = fi_tps_lattice(cx, cy, num_centers, cxy2, clat, stream);
+  if (rc == FI_OK && !p_given) rc = fi_tps_lattice(px, py, npts, pxy2, plat, stream);
+  if (rc == FI_OK) rc = fi_tps_y_bounds(cy, num_centers, cbounds, cbounds + ctiles, stream);
+  if (rc == FI_OK) rc = fi_tps_y_bounds(py, npts, pbounds, pbounds + ptiles, stream);
+  if (rc == FI_OK)
+    rc = fi_tps_members(plan, nb_subdom, cx, cy, num_centers, 0, counts, nullptr, nullptr,
+                        nullptr, cxy2, clat, cbounds, cbounds + ctiles, stream);
+  if (rc == FI_OK)
+    rc = fi_tps_members(plan, nb_subdom, px, py, npts, 0, ncounts, nullptr, nullptr, nullptr,
+                        pxy2, plat, pbounds, pbounds + ptiles, stream);
+  if (rc == FI_OK)
+    rc = fi_tps_offsets(counts, ncounts, nb_subdom, offsets, offsets + nb_subdom,
+                        offsets + 2 * nb_subdom, offsets + 3 * nb_subdom,
+                        offsets + 4 * nb_subdom, stream);
+  return rc;
+}
+
+extern "C" int fi_tps_members_fill(const fi_tps_plan* plan, int nb_subdom, const double* cx,
+                                   const double* cy, int num_centers, const double* px,
+                                   const double* py, int npts, const int32_t* cxy2,
+                                   const int32_t* clat, const int32_t* pxy2,
+                                   const int32_t* plat, const double* cbounds,
+                                   const double* pbounds, const int64_t* offsets,
+                                   int32_t* indices, double* coefs, int32_t* nindices,
+                                   double* ncoefs, void* stream) {
+  FI_REQUIRE(plan && cx && cy && px && py && cbounds && pbounds && offsets && indices &&
+                 coefs && nindices && ncoefs && nb_subdom > 0 && num_centers > 0 && npts > 0,
+             "fi_tps_members_fill: bad arguments");
+  const int ctiles = (num_centers + YB_TILE - 1) / YB_TILE;
+  const int ptiles = (npts + YB_TILE - 1) / YB_TILE;
+  int rc = fi_tps_members(plan, nb_subdom, cx, cy, num_centers, 1, nullptr, offsets, indices,
+                          coefs, cxy2, clat, cbounds, cbounds + ctiles, stream);
+  if (rc == FI_OK)
+    rc = fi_tps_members(plan, nb_subdom, px, py, npts, 1, nullptr, offsets + nb_subdom,
+                        nindices, ncoefs, pxy2, plat, pbounds, pbounds + ptiles, stream);
+  return rc;
+}
+
 extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members,
                             const double* cx, const double* cy, const float* ux,
                             const float* uy, const int32_t* counts, const int64_t* offsets,

@@ -134,7 +134,8 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 constexpr int TS = 36;  // row stride (floats) of the 32 x 32 shared tiles: float4-aligned rows
 
 // rho = g - B z for two right-hand sides, in double-float; B (m x m, symmetric, both
-// triangles, column-major, leading dimension ld) holds (hi, lo) pairs.  Each warp
+// triangles, column-major, leading dimension ld) holds (hi, lo) pairs, read with the
+// streaming hint (B is twice the FP32 factor, which should stay in L2).  Each warp
 // takes four columns at a time (one row per lane), then reduce-scatters its eight
 // sums over the warp.  rho is rounded to float.
 template <int NT>
@@ -155,7 +156,7 @@ __device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const 
       const float2 a = zx[r], b = zy[r];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const float2 v = (q < nc) ? col[(int64_t)q * ld + r] : make_float2(0.f, 0.f);
+        const float2 v = (q < nc) ? __ldcs(col + (int64_t)q * ld + r) : make_float2(0.f, 0.f);
         df_mac(v, a, h[q], l[q]);
         df_mac(v, b, h[4 + q], l[4 + q]);
       }
@@ -605,7 +606,10 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   const int64_t off = offsets[sd];
   const int32_t* idx = indices + off;
   const double lam = p.smoothing;
-  if (threadIdx.x == 0 && crank == 0) status[sd] = 1;
+  if (threadIdx.x == 0 && crank == 0) {
+    status[sd] = 1;
+    if (sweeps != nullptr) sweeps[sd] = 0;
+  }
   if (m < 1) return;  // fewer than 4 centres: FP64 LU path
   const int mp = (m + 3) & ~3;
 
@@ -981,7 +985,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
               }
               const float hi = __fadd_rn(sh, sl);
               const float2 sv = make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
-              B2[(int64_t)c * mp + r] = sv;
+              __stcs(B2 + (int64_t)c * mp + r, sv);  // streaming: keeps L2 for the factor
               L32[(int64_t)c * mp + r] = sv.x;
               S[(qb + u) * 33 + lane] = sv;
             }
@@ -992,7 +996,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
         for (int st = 0; st < 16; ++st) {
           const int rr = 2 * st + (lane >> 4), qq = lane & 15;
           const int r2 = 32 * I + rr, c2 = 32 * J + 16 * h + qq;
-          if (r2 < m && c2 < m && r2 > c2) B2[(int64_t)r2 * mp + c2] = S[qq * 33 + rr];
+          if (r2 < m && c2 < m && r2 > c2) __stcs(B2 + (int64_t)r2 * mp + c2, S[qq * 33 + rr]);
         }
         __syncwarp();
       }

@@ -254,14 +254,31 @@ def lattice_coords(px, py, npts, stream=None):
     return xy2, flag
 
 
+_PINNED = {}
+
+
+def _readback_raw(addr, nbytes, stream=None):
+    """``nbytes`` at device address ``addr`` -> bytes, through a pinned buffer kept
+    per process (one synchronisation of the stream)."""
+    torch = _torch()
+    buf = _PINNED.get("small")
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(4096, nbytes), dtype=torch.uint8, pin_memory=True)
+        _PINNED["small"] = buf
+    strm = stream or torch.cuda.current_stream()
+    L.check(L.load().fi_memcpy_d2h(buf.data_ptr(), addr, nbytes, strm.cuda_stream),
+            "fi_memcpy_d2h")
+    strm.synchronize()
+    return bytes(buf.numpy()[:nbytes])
+
+
 def _readback(t, stream=None):
     """Small device tensor -> numpy through pinned memory (one synchronisation)."""
     torch = _torch()
-    host = torch.empty(t.numel() * t.element_size(), dtype=torch.uint8, pin_memory=True)
-    host.copy_(t.contiguous().view(-1).view(torch.uint8), non_blocking=True)
-    (stream or torch.cuda.current_stream()).synchronize()
-    a = host.numpy()
-    return a.view({torch.int64: np.int64, torch.uint8: np.uint8, torch.int32: np.int32}[t.dtype])
+    t = t.contiguous()
+    raw = _readback_raw(t.data_ptr(), t.numel() * t.element_size(), stream)
+    return np.frombuffer(raw, dtype={torch.int64: np.int64, torch.uint8: np.uint8,
+                                     torch.int32: np.int32}[t.dtype]).copy()
 
 
 def y_bounds(py, npts, stream=None):
@@ -274,6 +291,30 @@ def y_bounds(py, npts, stream=None):
     return out[:npts], out[npts:]
 
 
+class _Carved:
+    """Buffers carved from one device allocation (one allocator call instead of
+    one per buffer): ``specs`` is a list of (count, torch dtype); each buffer starts
+    on a 16-byte boundary.  ``addr[i]`` is the device address of buffer i (what the
+    library calls take), ``tensor(i)`` a typed view (built only where a tensor is
+    kept)."""
+
+    def __init__(self, device, specs):
+        torch = _torch()
+        self.specs = specs
+        self.offsets, nbytes = [], 0
+        for count, dtype in specs:
+            self.offsets.append(nbytes)
+            nbytes += -(-count * dtype.itemsize // 16) * 16
+        self.buf = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=device)
+        base = self.buf.data_ptr()
+        self.addr = [base + o for o in self.offsets]
+
+    def tensor(self, i):
+        count, dtype = self.specs[i]
+        o = self.offsets[i]
+        return self.buf[o:o + count * dtype.itemsize].view(dtype)
+
+
 def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
             threshold, want_smooth, stream, p_lattice=None):
     """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548).
@@ -284,115 +325,99 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     lib = L.load()
     dev = xs.device
     s = L.stream_handle(stream)
-    f64 = dict(dtype=torch.float64, device=dev)
-    i32 = dict(dtype=torch.int32, device=dev)
-    plan = torch.empty(C.sizeof(L.TpsPlan), dtype=torch.uint8, device=dev)
-    cx = torch.empty(nvec, **f64)
-    cy = torch.empty(nvec, **f64)
-    ux = torch.empty(nvec, dtype=torch.float32, device=dev)
-    uy = torch.empty(nvec, dtype=torch.float32, device=dev)
-    sel = torch.empty(nvec, **i32)
+    u8_, i32_, i64_, f32_, f64_ = (torch.uint8, torch.int32, torch.int64, torch.float32,
+                                   torch.float64)
+    # the plan and the compacted centres; the host needs the plan header first
+    cA = _Carved(dev, [(C.sizeof(L.TpsPlan), u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
+                       (nvec, f32_), (nvec, i32_)])
+    plan, cx, cy, ux, uy, sel = cA.addr
     with _timed("fi_tps_plan_make"):
         L.check(lib.fi_tps_plan_make(L.ptr(xs), L.ptr(ys), L.ptr(dx), L.ptr(dy), nvec,
-                                     int(subdom_size), float(smoothing_coef), 20.0, L.ptr(plan),
-                                     L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy), L.ptr(sel), s),
+                                     int(subdom_size), float(smoothing_coef), 20.0, plan, cx,
+                                     cy, ux, uy, sel, s),
                 "fi_tps_plan_make")
-    hdr = L.TpsPlan.from_buffer_copy(_readback(plan, stream).tobytes())
+    hdr = L.TpsPlan.from_buffer_copy(_readback_raw(plan, C.sizeof(L.TpsPlan), stream))
     if hdr.status == 1:
         raise InterpError("Only nan.")
     if hdr.status != 0:
         raise ValueError("TPS subdomain layout is degenerate (all vectors on one line)")
     nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
-    cxy2, clat = lattice_coords(cx, cy, nv, stream)
-    pxy2, plat = p_lattice if p_lattice is not None else lattice_coords(px, py, npts, stream)
-    cb0, cb1 = y_bounds(cy, nv, stream)
-    pb0, pb1 = y_bounds(py, npts, stream)
-    counts = torch.empty(nsub, **i32)
-    ncounts = torch.empty(nsub, **i32)
-    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 0, L.ptr(counts),
-                               None, None, None, L.ptr(cxy2), L.ptr(clat), L.ptr(cb0),
-                               L.ptr(cb1), s), "fi_tps_members")
-    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 0,
-                               L.ptr(ncounts), None, None, None, L.ptr(pxy2), L.ptr(plat),
-                               L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
-    # offsets on the device; the host reads back the 6 totals only
-    offs = torch.empty(4 * nsub + 6, dtype=torch.int64, device=dev)
-    off_d, noff_d = offs[:nsub], offs[nsub:2 * nsub]
-    moff_d, woff_d = offs[2 * nsub:3 * nsub], offs[3 * nsub:4 * nsub]
-    L.check(lib.fi_tps_offsets(L.ptr(counts), L.ptr(ncounts), nsub, L.ptr(off_d), L.ptr(noff_d),
-                               L.ptr(moff_d), L.ptr(woff_d), L.ptr(offs[4 * nsub:]), s),
-            "fi_tps_offsets")
-    tot, ntot, msum, wsum, maxc, maxnc = (int(v) for v in _readback(offs[4 * nsub:], stream))
-    idx = torch.empty(max(tot, 1), **i32)
-    coefs = torch.empty(max(tot, 1), **f64)
-    nidx = torch.empty(max(ntot, 1), **i32)
-    ncoefs = torch.empty(max(ntot, 1), **f64)
-    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(cx), L.ptr(cy), nv, 1, None,
-                               L.ptr(off_d), L.ptr(idx), L.ptr(coefs), L.ptr(cxy2), L.ptr(clat),
-                               L.ptr(cb0), L.ptr(cb1), s), "fi_tps_members")
-    L.check(lib.fi_tps_members(L.ptr(plan), nsub, L.ptr(px), L.ptr(py), npts, 1, None,
-                               L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs), L.ptr(pxy2),
-                               L.ptr(plat), L.ptr(pb0), L.ptr(pb1), s), "fi_tps_members")
-    matrices = torch.empty(msum, **f64)
-    pivots = torch.empty(tot + 3 * nsub, **i32)
-    weights = torch.empty(wsum, **f64)
-    smx = torch.empty(max(tot, 1), **f64)
-    smy = torch.empty(max(tot, 1), **f64)
-    iters = torch.empty(2 * nsub, **i32)
-    nfixed = torch.empty(2 * nsub, **i32)
-    singular = torch.empty(nsub, **i32)
-    max_udiff = torch.empty(2 * nsub, **f64)
+    ctiles, ptiles = -(-nv // 256), -(-npts // 256)
+    p_given = p_lattice is not None
+    # layout: lattice coordinates, y bounds, member counts, offsets (one call)
+    specs = [(2 * nv, i32_), (1, i32_), (2 * ctiles, f64_), (2 * ptiles, f64_), (nsub, i32_),
+             (nsub, i32_), (4 * nsub + 6, i64_)]
+    if not p_given:
+        specs += [(2 * npts, i32_), (1, i32_)]
+    cB = _Carved(dev, specs)
+    cxy2, clat, cbounds, pbounds, counts, ncounts, offs = cB.addr[:7]
+    pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[7:]
+    L.check(lib.fi_tps_layout(plan, nsub, cx, cy, nv, L.ptr(px), L.ptr(py), npts,
+                              int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds, counts,
+                              ncounts, offs, s),
+            "fi_tps_layout")
+    off_d, noff_d, moff_d, woff_d = (offs + 8 * k * nsub for k in range(4))
+    # the host reads back the 6 totals only
+    tot, ntot, msum, wsum, maxc, maxnc = (
+        int(v) for v in np.frombuffer(_readback_raw(offs + 32 * nsub, 48, stream), np.int64))
+    use_mp = maxc <= MP_MAX_MEMBERS
+    t1, nt1 = max(tot, 1), max(ntot, 1)
+    # scratch of this call (the matrices dominate) apart from the outputs that the
+    # results keep (weights, interpolated fields, per-subdomain statistics)
+    cS = _Carved(dev, [
+        (msum, f64_), (msum if use_mp else 0, f32_), (t1, f64_), (nt1, f64_), (t1, f64_),
+        (t1, f64_), (nt1, f64_), (nt1, f64_), (t1, i32_), (nt1, i32_), (tot + 3 * nsub, i32_)])
+    matrices, matrices32, coefs, ncoefs, smx, smy, partx, party, idx, nidx, pivots = cS.addr
+    cO = _Carved(dev, [
+        (wsum, f64_), (2 * nsub, f64_), (npts, f64_), (npts, f64_),
+        (nv if want_smooth else 0, f64_), (nv if want_smooth else 0, f64_), (2 * nsub, i32_),
+        (2 * nsub, i32_), (nsub, i32_), (nsub, i32_), (nsub, i32_), (npts, i32_), (npts, i32_)])
+    (weights, max_udiff, out_x, out_y, smooth_x, smooth_y, iters, nfixed, singular, status,
+     sweeps, rx, ry) = cO.addr
+    L.check(lib.fi_tps_members_fill(plan, nsub, cx, cy, nv, L.ptr(px), L.ptr(py), npts, cxy2,
+                                    clat, pxy2, plat, cbounds, pbounds, offs, idx, coefs, nidx,
+                                    ncoefs, s),
+            "fi_tps_members_fill")
     use_thr = threshold is not None
     thr = float(threshold) if use_thr else 0.0
-    table = phi_table(dev)
-    status = torch.ones(nsub, **i32)
-    sweeps = torch.zeros(nsub, **i32)
-    if maxc <= MP_MAX_MEMBERS:
-        matrices32 = torch.empty(msum, dtype=torch.float32, device=dev)
+    table = L.ptr(phi_table(dev))
+    table2 = L.ptr(phi_table(dev, pairs=True))
+    if use_mp:  # the solver writes status (1: needs the FP64 LU) and sweeps
         with _timed("fi_tps_solve_mp"):
             L.check(lib.fi_tps_solve_mp(
-                L.ptr(plan), nsub, maxc, L.ptr(cx), L.ptr(cy), L.ptr(ux), L.ptr(uy),
-                L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d), L.ptr(matrices),
-                L.ptr(matrices32), L.ptr(table), L.ptr(phi_table(dev, pairs=True)),
-                PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat),
-                thr, int(use_thr),
-                L.ptr(woff_d), L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
-                L.ptr(nfixed), L.ptr(status), L.ptr(max_udiff), L.ptr(sweeps), s),
+                plan, nsub, maxc, cx, cy, ux, uy, counts, off_d, idx, moff_d, matrices,
+                matrices32, table, table2, PHI_TABLE_SIZE, cxy2, clat, thr, int(use_thr),
+                woff_d, weights, smx, smy, iters, nfixed, status, max_udiff, sweeps, s),
                 "fi_tps_solve_mp")
+    else:
+        cO.tensor(9).fill_(1)
+        cO.tensor(10).zero_()
     # FP64 LU for the subdomains the mixed-precision solver flagged (or all of them)
     with _timed("fi_tps_solve"):
-      L.check(lib.fi_tps_solve(L.ptr(plan), nsub, maxc, L.ptr(cx), L.ptr(cy), L.ptr(ux),
-                             L.ptr(uy), L.ptr(counts), L.ptr(off_d), L.ptr(idx), L.ptr(moff_d),
-                             L.ptr(matrices), L.ptr(pivots), thr, int(use_thr), L.ptr(woff_d),
-                             L.ptr(weights), L.ptr(smx), L.ptr(smy), L.ptr(iters),
-                             L.ptr(nfixed), L.ptr(singular), L.ptr(max_udiff), L.ptr(status), s),
-            "fi_tps_solve")
+        L.check(lib.fi_tps_solve(plan, nsub, maxc, cx, cy, ux, uy, counts, off_d, idx, moff_d,
+                                 matrices, pivots, thr, int(use_thr), woff_d, weights, smx,
+                                 smy, iters, nfixed, singular, max_udiff, status, s),
+                "fi_tps_solve")
+    if want_smooth:
+        L.check(lib.fi_tps_blend_centers(plan, nv, cx, cy, counts, off_d, idx, coefs, smx, smy,
+                                         smooth_x, smooth_y, s),
+                "fi_tps_blend_centers")
+    with _timed("fi_tps_interpolate"):
+        L.check(lib.fi_tps_interpolate(plan, nsub, maxc, maxnc, cx, cy, counts, off_d, idx,
+                                       woff_d, weights, L.ptr(px), L.ptr(py), npts, ncounts,
+                                       noff_d, nidx, ncoefs, partx, party, out_x, out_y, rx, ry,
+                                       table, table2, PHI_TABLE_SIZE, cxy2, clat, s),
+                "fi_tps_interpolate")
+    # tensors for what the caller keeps (built while the GPU works)
     out = TpsOutput(
-        out_x=torch.empty(npts, **f64), out_y=torch.empty(npts, **f64),
-        rx=torch.empty(npts, **i32), ry=torch.empty(npts, **i32), selection=sel,
-        num_centers=nv, nb_subdom=nsub, counts_d=counts, w_offsets_d=woff_d, weights=weights,
-        singular=singular, iters=iters, nfixed=nfixed, max_udiff=max_udiff,
-        mp_status=status, mp_sweeps=sweeps,
+        out_x=cO.tensor(2), out_y=cO.tensor(3), rx=cO.tensor(11), ry=cO.tensor(12),
+        selection=cA.tensor(5), num_centers=nv, nb_subdom=nsub, counts_d=cB.tensor(4),
+        w_offsets_d=cB.tensor(6)[3 * nsub:4 * nsub], weights=cO.tensor(0),
+        singular=cO.tensor(8), iters=cO.tensor(6), nfixed=cO.tensor(7),
+        max_udiff=cO.tensor(1), mp_status=cO.tensor(9), mp_sweeps=cO.tensor(10),
     )
     if want_smooth:
-        out.smooth_x = torch.empty(nv, **f64)
-        out.smooth_y = torch.empty(nv, **f64)
-        L.check(lib.fi_tps_blend_centers(L.ptr(plan), nv, L.ptr(cx), L.ptr(cy), L.ptr(counts),
-                                         L.ptr(off_d), L.ptr(idx), L.ptr(coefs), L.ptr(smx),
-                                         L.ptr(smy), L.ptr(out.smooth_x), L.ptr(out.smooth_y), s),
-                "fi_tps_blend_centers")
-    partx = torch.empty(max(ntot, 1), **f64)
-    party = torch.empty(max(ntot, 1), **f64)
-    with _timed("fi_tps_interpolate"):
-      L.check(lib.fi_tps_interpolate(L.ptr(plan), nsub, maxc, maxnc, L.ptr(cx),
-                                   L.ptr(cy), L.ptr(counts), L.ptr(off_d), L.ptr(idx),
-                                   L.ptr(woff_d), L.ptr(weights), L.ptr(px), L.ptr(py), npts,
-                                   L.ptr(ncounts), L.ptr(noff_d), L.ptr(nidx), L.ptr(ncoefs),
-                                   L.ptr(partx), L.ptr(party), L.ptr(out.out_x),
-                                   L.ptr(out.out_y), L.ptr(out.rx), L.ptr(out.ry),
-                                   L.ptr(table), L.ptr(phi_table(dev, pairs=True)),
-                                   PHI_TABLE_SIZE, L.ptr(cxy2), L.ptr(clat), s),
-            "fi_tps_interpolate")
+        out.smooth_x, out.smooth_y = cO.tensor(4), cO.tensor(5)
     return out
 
 
@@ -640,18 +665,24 @@ class PIVPipeline:
 # --------------------------------------------------------------------------------
 def error_dict(err, fix_flags, diff2, threshold):
     """Rebuild ``errors`` of _loop_vectors + WorkFIX (fix.py:66-236) from the codes."""
+    err = np.asarray(err)
+    fix_flags = np.asarray(fix_flags)
+    # WorkFIX deletes the errors of replaced vectors (fix.py:229-234)
+    sel = np.nonzero(((err != 0) | (fix_flags != 0)) & ((fix_flags & L.FIX_REPLACED) == 0))[0]
+    if sel.size == 0:
+        return {}
+    codes = err[sel].tolist()
+    flags = fix_flags[sel].tolist()
+    diffs = np.sqrt(np.asarray(diff2)[sel].astype(np.float64)).tolist()
+    texts = ((1, "correl < correl_min"), (2, "delta2 < displacement_max2"),
+             (4, "diff neighbour too large"))
     errors = {}
-    for i in np.nonzero((err != 0) | (fix_flags != 0))[0]:
-        i = int(i)
-        if fix_flags[i] & L.FIX_REPLACED:  # WorkFIX deletes their errors (fix.py:229-234)
-            continue
-        s = ERROR_STRINGS.get(int(err[i])) if err[i] else None
-        f = int(fix_flags[i])
-        for bit, text in ((1, "correl < correl_min"), (2, "delta2 < displacement_max2"),
-                          (4, "diff neighbour too large")):
+    for i, e, f, d in zip(sel.tolist(), codes, flags, diffs):
+        s = ERROR_STRINGS.get(e) if e else None
+        for bit, text in texts:
             if f & bit:
                 s = text if s is None else s + " + " + text
         if f & 4:
-            s += f" (diff = {np.sqrt(np.float64(diff2[i])):.2f})"
+            s += f" (diff = {d:.2f})"
         errors[i] = s
     return errors

@@ -263,8 +263,9 @@ class WorkPIV:
             r.near_tie_flags = h["flags"]
             r.near_ties = int(np.count_nonzero(h["flags"]))
             if fx.threshold_diff_neighbour is not None:
-                r.deltaxs_wrong = {i: h["deltaxs_raw"][i] for i in errors}
-                r.deltays_wrong = {i: h["deltays_raw"][i] for i in errors}
+                ierr = np.fromiter(errors, dtype=np.int64, count=len(errors))
+                r.deltaxs_wrong = dict(zip(errors, h["deltaxs_raw"][ierr]))
+                r.deltays_wrong = dict(zip(errors, h["deltays_raw"][ierr]))
             if pd.dxin is not None:
                 r.deltaxs_input = got[(k, "dxin")]
                 r.deltays_input = got[(k, "dyin")]

@@ -75,6 +75,12 @@ long long fi_launch_count(void);
 int fi_abi_sizes(int64_t* out3);
 
 /*
+ * Asynchronous copy of nbytes from device memory to (pinned) host memory on the
+ * stream: the few integers the host reads between the TPS stages.
+ */
+int fi_memcpy_d2h(void* host_dst, const void* device_src, int64_t nbytes, void* stream);
+
+/*
  * Minimum of two images, written as two floats to out_min[0..1] (device).
  * Replaces the "im - im.min()" of BaseWorkPIV._pad_images
  * (works/piv/singlepass.py:196-208).
@@ -286,15 +292,6 @@ int fi_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
 int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, double* y_smin, void* stream);
 
 /*
- * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
- * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
- * counts), the point indices and their norm coefficients
- * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 and
- * on_lattice from fi_tps_lattice (both nullable) the limit tests are exact integer
- * comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
- * restrict the scan to the tiles that can hold members.
- */
-/*
  * Exclusive prefix sums for the buffers of nb_subdom subdomains from the member
  * counts of the centres and of the new positions (fi_tps_members mode 0): CSR
  * offsets of both, matrix slots ((n_i+3)^2 rounded up to 4 elements, as
@@ -306,11 +303,50 @@ int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
                    int64_t* offsets, int64_t* noffsets, int64_t* mat_offsets,
                    int64_t* w_offsets, int64_t* summary, void* stream);
 
+/*
+ * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
+ * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
+ * counts), the point indices and their norm coefficients
+ * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 and
+ * on_lattice from fi_tps_lattice (both nullable) the limit tests are exact integer
+ * comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
+ * restrict the scan to the tiles that can hold members.
+ */
 int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
                    int npts, int mode, int32_t* counts, const int64_t* offsets,
                    int32_t* indices, double* coefs, const int32_t* xy2,
                    const int32_t* on_lattice, const double* y_pmax, const double* y_smin,
                    void* stream);
+
+/*
+ * The layout stages of one TPS interpolation in one call: fi_tps_lattice of the
+ * centres (cx, cy) and, unless p_given, of the new positions (px, py) (else pxy2 /
+ * plat are read); fi_tps_y_bounds of both; the member counts of both
+ * (fi_tps_members mode 0) and fi_tps_offsets.  Buffers: cxy2 [2 num_centers],
+ * pxy2 [2 npts], clat / plat [1], cbounds / pbounds [2 ceil(n / 256)] (y_pmax then
+ * y_smin), counts / ncounts [nb_subdom], offsets [4 nb_subdom + 6] (offsets,
+ * noffsets, mat_offsets, w_offsets, summary).  No reference counterpart (the
+ * bookkeeping of ThinPlateSplineSubdom.__init__ / init_with_new_positions,
+ * thin_plate_spline_subdom.py:25-127, 160-206).
+ */
+int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const double* cx, const double* cy,
+                  int num_centers, const double* px, const double* py, int npts, int p_given,
+                  int32_t* cxy2, int32_t* clat, int32_t* pxy2, int32_t* plat, double* cbounds,
+                  double* pbounds, int32_t* counts, int32_t* ncounts, int64_t* offsets,
+                  void* stream);
+
+/*
+ * Both membership fills (fi_tps_members mode 1) after fi_tps_layout: the centres
+ * into indices / coefs at offsets[0:nb_subdom], the new positions into nindices /
+ * ncoefs at offsets[nb_subdom:2 nb_subdom]; the other buffers as fi_tps_layout
+ * wrote them.
+ */
+int fi_tps_members_fill(const fi_tps_plan* plan, int nb_subdom, const double* cx,
+                        const double* cy, int num_centers, const double* px, const double* py,
+                        int npts, const int32_t* cxy2, const int32_t* clat, const int32_t* pxy2,
+                        const int32_t* plat, const double* cbounds, const double* pbounds,
+                        const int64_t* offsets, int32_t* indices, double* coefs,
+                        int32_t* nindices, double* ncoefs, void* stream);
 
 /*
  * Per subdomain: build [[K + smoothing I, P], [P^T, 0]] (compute_tps_weights,
