@@ -102,11 +102,11 @@ _SIGNATURES = {
     ),
     "fi_tps_lattice": (C.c_int, [P, P, C.c_int, P, P, P]),
     "fi_tps_y_bounds": (C.c_int, [P, C.c_int, P, P, P]),
-    "fi_tps_offsets": (C.c_int, [P, P, C.c_int, P, P, P, P, P, P]),
+    "fi_tps_offsets": (C.c_int, [P, P, C.c_int, P, P, P, P, P, P, P]),
     "fi_tps_members": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P]),
     "fi_tps_layout": (
         C.c_int,
-        [P, C.c_int, P, P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P],
+        [P, C.c_int, P, P, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P],
     ),
     "fi_tps_members_fill": (
         C.c_int,
@@ -122,7 +122,7 @@ _SIGNATURES = {
     "fi_tps_solve_mp": (
         C.c_int,
         [P, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, P, P, P, C.c_int64, P, P,
-         C.c_double, C.c_int, P, P, P, P, P, P, P, P, P, P],
+         C.c_double, C.c_int, P, P, P, P, P, P, P, P, P, P, P],
     ),
     "fi_rank_filter": (
         C.c_int,

@@ -317,13 +317,18 @@ __device__ __forceinline__ int64_t block_scan_i64(int64_t v, int64_t* wsum, int6
   return r;
 }
 
+// subdomain counts up to which fi_tps_offsets ranks the subdomains by size
+constexpr int ORDER_MAX = 8192;
+
 // CSR offsets of the centres' and new positions' membership, offsets of the matrix
-// slots ((n+3)^2 rounded up to 4 elements) and of the weights (2 (n+3)), and the
+// slots ((n+3)^2 rounded up to 4 elements) and of the weights (2 (n+3)), the
 // summary [total members, total new members, matrix elements, weight elements,
-// max members, max new members]; one block of 1024 threads.
+// max members, max new members] and (nullable) the solve order, largest subdomains
+// first; one block of 1024 threads.
 __global__ void __launch_bounds__(1024)
     k_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nsub, int64_t* off,
-                  int64_t* noff, int64_t* moff, int64_t* woff, int64_t* summary) {
+                  int64_t* noff, int64_t* moff, int64_t* woff, int64_t* summary,
+                  int32_t* order) {
   __shared__ int64_t wsum[33];
   __shared__ int s_max[2];
   if (threadIdx.x == 0) s_max[0] = s_max[1] = 0;
@@ -353,6 +358,22 @@ __global__ void __launch_bounds__(1024)
     for (int k = 0; k < 4; ++k) summary[k] = carry[k];
     summary[4] = s_max[0];
     summary[5] = s_max[1];
+  }
+  // solve order: members descending, index ascending among equal counts (stable
+  // rank by counting, O(nsub^2) / 1024 per thread; identity beyond ORDER_MAX)
+  if (order != nullptr) {
+    for (int i = threadIdx.x; i < nsub; i += blockDim.x) {
+      int rank = i;
+      if (nsub <= ORDER_MAX) {
+        const int ci = counts[i];
+        rank = 0;
+        for (int j = 0; j < nsub; ++j) {
+          const int cj = counts[j];
+          rank += (cj > ci) || (cj == ci && j < i);
+        }
+      }
+      order[rank] = i;
+    }
   }
 }
 
@@ -873,12 +894,14 @@ extern "C" int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, doubl
 
 extern "C" int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
                               int64_t* offsets, int64_t* noffsets, int64_t* mat_offsets,
-                              int64_t* w_offsets, int64_t* summary, void* stream) {
+                              int64_t* w_offsets, int64_t* summary, int32_t* order,
+                              void* stream) {
   FI_REQUIRE(counts && ncounts && offsets && noffsets && mat_offsets && w_offsets && summary &&
                  nb_subdom > 0,
              "fi_tps_offsets: bad arguments");
   k_tps_offsets<<<1, 1024, 0, (cudaStream_t)stream>>>(counts, ncounts, nb_subdom, offsets,
-                                                      noffsets, mat_offsets, w_offsets, summary);
+                                                      noffsets, mat_offsets, w_offsets, summary,
+                                                      order);
   return check_launch("fi_tps_offsets");
 }
 
@@ -901,7 +924,7 @@ extern "C" int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const doubl
                              const double* py, int npts, int p_given, int32_t* cxy2,
                              int32_t* clat, int32_t* pxy2, int32_t* plat, double* cbounds,
                              double* pbounds, int32_t* counts, int32_t* ncounts,
-                             int64_t* offsets, void* stream) {
+                             int64_t* offsets, int32_t* order, void* stream) {
   FI_REQUIRE(plan && cx && cy && px && py && cxy2 && clat && pxy2 && plat && cbounds &&
                  pbounds && counts && ncounts && offsets && nb_subdom > 0 &&
                  num_centers > 0 && npts > 0,
@@ -921,7 +944,7 @@ extern "C" int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const doubl
   if (rc == FI_OK)
     rc = fi_tps_offsets(counts, ncounts, nb_subdom, offsets, offsets + nb_subdom,
                         offsets + 2 * nb_subdom, offsets + 3 * nb_subdom,
-                        offsets + 4 * nb_subdom, stream);
+                        offsets + 4 * nb_subdom, order, stream);
   return rc;
 }
 

@@ -584,8 +584,8 @@ __global__ void __launch_bounds__(NT, 512 / NT)
                    const int32_t* c_on_lattice, double threshold, int use_threshold,
                    const int64_t* w_off, double* weights,
                    double* smoothed_x, double* smoothed_y, int32_t* iters, int32_t* nfixed,
-                   int32_t* status, double* max_udiff, int32_t* sweeps, int max_refine,
-                   int n_layout) {
+                   int32_t* status, double* max_udiff, int32_t* sweeps,
+                   const int32_t* order, int max_refine, int n_layout) {
   constexpr int NW = NT / 32;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sh[80];
@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   cg::cluster_group cluster = cg::this_cluster();
   const int csize = (int)cluster.num_blocks();
   const int crank = (int)cluster.block_rank();
-  const int sd = blockIdx.x / csize;
+  const int sd = order != nullptr ? order[blockIdx.x / csize] : (int)(blockIdx.x / csize);
   const int N = counts[sd];
   const int m = N - 3;
   const int64_t off = offsets[sd];
@@ -1232,7 +1232,7 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                const int64_t* w_offsets, double* weights, double* smoothed_x,
                                double* smoothed_y, int32_t* iters, int32_t* nfixed,
                                int32_t* status, double* max_udiff, int32_t* sweeps,
-                               void* stream) {
+                               const int32_t* order, void* stream) {
   FI_REQUIRE(plan && cx && cy && ux && uy && counts && offsets && indices && mat_offsets &&
                  matrices && matrices32 && w_offsets && weights && smoothed_x &&
                  smoothed_y &&
@@ -1281,12 +1281,12 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                    phi_table, reinterpret_cast<const float2*>(phi_table2),
                                    table_size, cxy2, c_on_lattice, threshold,
                                    use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
-                                   iters, nfixed, status, max_udiff, sweeps, 60, N));
+                                   iters, nfixed, status, max_udiff, sweeps, order, 60, N));
   } else
     k_tps_solve_mp<256><<<nb_subdom, 256, smem, (cudaStream_t)stream>>>(
         plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
         phi_table, reinterpret_cast<const float2*>(phi_table2), table_size, cxy2, c_on_lattice,
         threshold, use_threshold, w_offsets, weights,
-        smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, 60, N);
+        smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, order, 60, N);
   return check_launch("fi_tps_solve_mp");
 }

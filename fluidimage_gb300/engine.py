@@ -346,15 +346,15 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     p_given = p_lattice is not None
     # layout: lattice coordinates, y bounds, member counts, offsets (one call)
     specs = [(2 * nv, i32_), (1, i32_), (2 * ctiles, f64_), (2 * ptiles, f64_), (nsub, i32_),
-             (nsub, i32_), (4 * nsub + 6, i64_)]
+             (nsub, i32_), (4 * nsub + 6, i64_), (nsub, i32_)]
     if not p_given:
         specs += [(2 * npts, i32_), (1, i32_)]
     cB = _Carved(dev, specs)
-    cxy2, clat, cbounds, pbounds, counts, ncounts, offs = cB.addr[:7]
-    pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[7:]
+    cxy2, clat, cbounds, pbounds, counts, ncounts, offs, order = cB.addr[:8]
+    pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[8:]
     L.check(lib.fi_tps_layout(plan, nsub, cx, cy, nv, L.ptr(px), L.ptr(py), npts,
                               int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds, counts,
-                              ncounts, offs, s),
+                              ncounts, offs, order, s),
             "fi_tps_layout")
     off_d, noff_d, moff_d, woff_d = (offs + 8 * k * nsub for k in range(4))
     # the host reads back the 6 totals only
@@ -387,7 +387,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
             L.check(lib.fi_tps_solve_mp(
                 plan, nsub, maxc, cx, cy, ux, uy, counts, off_d, idx, moff_d, matrices,
                 matrices32, table, table2, PHI_TABLE_SIZE, cxy2, clat, thr, int(use_thr),
-                woff_d, weights, smx, smy, iters, nfixed, status, max_udiff, sweeps, s),
+                woff_d, weights, smx, smy, iters, nfixed, status, max_udiff, sweeps, order, s),
                 "fi_tps_solve_mp")
     else:
         cO.tensor(9).fill_(1)

@@ -296,12 +296,15 @@ int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, double* y_smin, 
  * counts of the centres and of the new positions (fi_tps_members mode 0): CSR
  * offsets of both, matrix slots ((n_i+3)^2 rounded up to 4 elements, as
  * fi_tps_solve_mp wants) and weights (2 (n_i+3)); summary[6] = total members, total
- * new members, matrix elements, weight elements, max members, max new members.
- * No reference counterpart (the host-side bookkeeping of ThinPlateSplineSubdom).
+ * new members, matrix elements, weight elements, max members, max new members;
+ * order (nullable, [nb_subdom]) = the subdomains by decreasing member count (ties
+ * by index; the identity above 8192 subdomains), the block order of
+ * fi_tps_solve_mp.  No reference counterpart (the host-side bookkeeping of
+ * ThinPlateSplineSubdom).
  */
 int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
                    int64_t* offsets, int64_t* noffsets, int64_t* mat_offsets,
-                   int64_t* w_offsets, int64_t* summary, void* stream);
+                   int64_t* w_offsets, int64_t* summary, int32_t* order, void* stream);
 
 /*
  * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
@@ -325,7 +328,8 @@ int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, con
  * (fi_tps_members mode 0) and fi_tps_offsets.  Buffers: cxy2 [2 num_centers],
  * pxy2 [2 npts], clat / plat [1], cbounds / pbounds [2 ceil(n / 256)] (y_pmax then
  * y_smin), counts / ncounts [nb_subdom], offsets [4 nb_subdom + 6] (offsets,
- * noffsets, mat_offsets, w_offsets, summary).  No reference counterpart (the
+ * noffsets, mat_offsets, w_offsets, summary), order (nullable, [nb_subdom]) as in
+ * fi_tps_offsets.  No reference counterpart (the
  * bookkeeping of ThinPlateSplineSubdom.__init__ / init_with_new_positions,
  * thin_plate_spline_subdom.py:25-127, 160-206).
  */
@@ -333,7 +337,7 @@ int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const double* cx, cons
                   int num_centers, const double* px, const double* py, int npts, int p_given,
                   int32_t* cxy2, int32_t* clat, int32_t* pxy2, int32_t* plat, double* cbounds,
                   double* pbounds, int32_t* counts, int32_t* ncounts, int64_t* offsets,
-                  void* stream);
+                  int32_t* order, void* stream);
 
 /*
  * Both membership fills (fi_tps_members mode 1) after fi_tps_layout: the centres
@@ -396,7 +400,9 @@ int fi_tps_phi_table2(float* table2, int64_t count, void* stream);
  * same size, the pairs the double-float projection reads).  status[i] = 0 when solved, 1 when the subdomain must go
  * through fi_tps_solve (pass status as its only_failed argument): rank-deficient P,
  * Cholesky breakdown or no convergence.  sweeps (nullable, [nb_subdom]): refinement
- * sweeps (one FP32 solve each) per subdomain.
+ * sweeps (one FP32 solve each) per subdomain.  order (nullable, fi_tps_offsets):
+ * the subdomains in the order the blocks take them (largest first shortens the
+ * last wave).
  */
 int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
                     const double* cy, const float* ux, const float* uy, const int32_t* counts,
@@ -406,7 +412,7 @@ int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, con
                     const int32_t* c_on_lattice, double threshold, int use_threshold,
                     const int64_t* w_offsets, double* weights, double* smoothed_x,
                     double* smoothed_y, int32_t* iters, int32_t* nfixed, int32_t* status,
-                    double* max_udiff, int32_t* sweeps, void* stream);
+                    double* max_udiff, int32_t* sweeps, const int32_t* order, void* stream);
 
 /*
  * Smoothed values at the centres, blended over the subdomains that contain them
