@@ -432,15 +432,22 @@ __device__ __forceinline__ void potrf_tile(float (&a)[32], float* B, int m, int 
   Lkk[lane * TS + 32] = 1.f / dg;
 }
 
+// Shared memory of chol_factor for an m x m matrix: two L_kk tiles (rows of TS
+// floats) and the current tile column, transposed (T - 1 tiles of 32 x 32).
+__host__ __device__ inline size_t chol_scratch_bytes(int m) {
+  const int T = (m + 31) / 32;
+  return (size_t)2 * 32 * TS * sizeof(float) + (size_t)(T > 1 ? T - 1 : 0) * 1024 * sizeof(float);
+}
+
 // Right-looking tiled Cholesky (lower) of the m x m matrix B (column-major, ld), in
 // place (lower triangle).  Per tile column k: warps solve the tiles below the
-// diagonal (one row per lane, rows of L_kk read as float4 broadcasts), then update
-// the trailing tile pairs (register accumulators, packed FP32x2 FMAs, the second
-// factor transposed in shared memory, float4 broadcasts).  Lookahead: warp 0 first
-// updates the next diagonal tile and factorises it in registers (shuffles) while the
-// other warps update the rest; the tiles go to the warps in the order they finish.
-// scratch: (2 + warps) * 32 * TS floats, 16-byte aligned.  False on a non-positive
-// pivot.
+// diagonal (one row per lane, rows of L_kk read as float4 broadcasts) and keep them,
+// transposed, in shared memory; then they update the trailing tile pairs (register
+// accumulators, packed FP32x2 FMAs, both factors read from the shared tile column:
+// the update loads only its own tile).  Lookahead: warp 0 first updates the next
+// diagonal tile and factorises it in registers (shuffles) while the other warps
+// update the rest; the tiles go to the warps in the order they finish.
+// scratch: chol_scratch_bytes(m), 16-byte aligned.  False on a non-positive pivot.
 template <int NT>
 __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag,
                             int* s_next) {
@@ -451,7 +458,8 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
   // two L_kk buffers (step k reads buffer k & 1 while step k + 1's is written); row
   // j: L_kk[j][c] for c < j (0 elsewhere), [32] = 1 / L_jj
   float* Lkk0 = scratch;
-  float* Lt = scratch + 32 * TS * (2 + wid);  // per warp, transposed tile
+  // tile column k: tile i > k at P + (i - k - 1) * 1024, element [t * 32 + r] = L_ik[r][t]
+  float* P = scratch + 2 * 32 * TS;
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
   if (wid == 0) {
@@ -481,6 +489,10 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
         if ((j & 3) == 3) __syncwarp();  // bounds the broadcasts in flight (registers)
       }
       tile_store(B, m, ld, i, k, b, lane, false);
+      float* Pi = P + (i - k - 1) * 1024;
+      const bool rin = 32 * i + lane < m;  // rows past m: zero (their updates are unused)
+#pragma unroll
+      for (int t = 0; t < 32; ++t) Pi[t * 32 + lane] = rin ? b[t] : 0.f;
     }
     if (threadIdx.x == 0) *s_next = NW;
     __syncthreads();
@@ -495,49 +507,32 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       while (ii * (ii + 1) / 2 > pidx) --ii;
       const int jj = pidx - ii * (ii + 1) / 2;
       const int i = k + 1 + ii, j = k + 1 + jj;
-      {  // L_jk rows -> transposed in shared memory
-        const int r = 32 * j + lane;
-#pragma unroll
-        for (int t = 0; t < 32; ++t) {
-          const int col = 32 * k + t;
-          Lt[t * TS + lane] = (r < m && col < m) ? B[(int64_t)col * ld + r] : ((r == col) ? 1.f : 0.f);
-        }
-      }
-      __syncwarp();
+      const float* Pi = P + ii * 1024;
+      const float* Pj = P + jj * 1024;
       float acc[32];
       tile_load(B, m, ld, i, j, acc, lane);
-      // acc -= L_ik L_jk^T, the row of L_ik in two halves of 16 (registers)
+      // acc -= L_ik L_jk^T: L_ik[lane][t] and the row t of L_jk^T from shared memory
+#pragma unroll 4
+      for (int t = 0; t < 32; ++t) {
+        const float l = -Pi[t * 32 + lane];
+        const float2 lr = make_float2(l, l);
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        float l[16];
-        const int r = 32 * i + lane;
-#pragma unroll
-        for (int t = 0; t < 16; ++t) {
-          const int col = 32 * k + 16 * h + t;
-          l[t] = (r < m && col < m) ? B[(int64_t)col * ld + r] : ((r == col) ? 1.f : 0.f);
-        }
-#pragma unroll
-        for (int t = 0; t < 16; ++t) {
-          const float2 lr = make_float2(-l[t], -l[t]);
-#pragma unroll
-          for (int c4 = 0; c4 < 8; ++c4) {
-            const float4 q = *reinterpret_cast<const float4*>(Lt + (16 * h + t) * TS + 4 * c4);
-            float2 a01 = make_float2(acc[4 * c4], acc[4 * c4 + 1]);
-            float2 a23 = make_float2(acc[4 * c4 + 2], acc[4 * c4 + 3]);
-            a01 = __ffma2_rn(lr, make_float2(q.x, q.y), a01);
-            a23 = __ffma2_rn(lr, make_float2(q.z, q.w), a23);
-            acc[4 * c4] = a01.x;
-            acc[4 * c4 + 1] = a01.y;
-            acc[4 * c4 + 2] = a23.x;
-            acc[4 * c4 + 3] = a23.y;
-          }
+        for (int c4 = 0; c4 < 8; ++c4) {
+          const float4 q = *reinterpret_cast<const float4*>(Pj + t * 32 + 4 * c4);
+          float2 a01 = make_float2(acc[4 * c4], acc[4 * c4 + 1]);
+          float2 a23 = make_float2(acc[4 * c4 + 2], acc[4 * c4 + 3]);
+          a01 = __ffma2_rn(lr, make_float2(q.x, q.y), a01);
+          a23 = __ffma2_rn(lr, make_float2(q.z, q.w), a23);
+          acc[4 * c4] = a01.x;
+          acc[4 * c4 + 1] = a01.y;
+          acc[4 * c4 + 2] = a23.x;
+          acc[4 * c4 + 3] = a23.y;
         }
       }
       if (pidx == 0)
         potrf_tile(acc, B, m, ld, k + 1, Lkk0 + ((k + 1) & 1) * 32 * TS, lane, s_flag);
       else
         tile_store(B, m, ld, i, j, acc, lane, i == j);
-      __syncwarp();
       int nxt = 0;
       if (lane == 0) nxt = atomicAdd(s_next, 1);
       pidx = __shfl_sync(full, nxt, 0);
@@ -563,7 +558,13 @@ struct MpLayout {
     f_off = f2_off + (size_t)4 * np * sizeof(float2);
     i2_off = f_off + (size_t)4 * np * sizeof(float);
     p_off = i2_off + (size_t)np * sizeof(int2);
-    bytes = p_off + (size_t)(2 + warps) * 32 * TS * sizeof(float);
+    // the panel also holds the projection's per-warp tiles and the solves' partial
+    // sums; the Cholesky scratch starts at f2_off (the f2, f and i2 regions are free
+    // while it runs)
+    size_t pbytes = (size_t)(2 + warps) * 32 * TS * sizeof(float);
+    const size_t chol = chol_scratch_bytes(n);
+    if (f2_off + chol > p_off + pbytes) pbytes = f2_off + chol - p_off;
+    bytes = p_off + pbytes;
   }
 };
 
@@ -1005,7 +1006,9 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   cluster.sync();  // the cluster's B tiles are in global memory, visible to rank 0
   if (crank != 0) return;
   // ---- FP32 Cholesky of B22
-  if (!chol_factor<NT>(L32, m, mp, panel, &s_flag, &s_next)) return;
+  if (!chol_factor<NT>(L32, m, mp, reinterpret_cast<float*>(smraw + lay.f2_off), &s_flag,
+                       &s_next))
+    return;
 
   // ---- outlier iterations with refined solves (x and y in lockstep)
   double* tx = W;

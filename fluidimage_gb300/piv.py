@@ -216,9 +216,21 @@ class WorkPIV:
                 want[(k, tag, "singular")] = tps.singular
                 want[(k, tag, "out_x")], want[(k, tag, "out_y")] = tps.out_x, tps.out_y
                 if tag == "tps_final":
-                    want[(k, tag, "sel")] = tps.selection[: tps.num_centers]
-                    want[(k, tag, "smooth_x")] = tps.smooth_x
-                    want[(k, tag, "smooth_y")] = tps.smooth_y
+                    # the *_smooth fields (singlepass.py:515-529): the grid with the
+                    # selected vectors' values scattered in, built on the device
+                    lay = pd.layout
+                    sel = tps.selection[: tps.num_centers].long()
+                    gx, gy = lay.dev["px"] + offx, lay.dev["py"] + offy
+                    sx = gx if lay.index == 0 else pd.xs.double() + offx
+                    sy = gy if lay.index == 0 else pd.ys.double() + offy
+                    xs_s, ys_s = gx.float(), gy.float()
+                    xs_s[sel] = sx[sel].float()
+                    ys_s[sel] = sy[sel].float()
+                    want[(k, tag, "xs_smooth")], want[(k, tag, "ys_smooth")] = xs_s, ys_s
+                    want[(k, tag, "dx_smooth")] = tps.out_x.clone().index_copy_(
+                        0, sel, tps.smooth_x)
+                    want[(k, tag, "dy_smooth")] = tps.out_y.clone().index_copy_(
+                        0, sel, tps.smooth_y)
         got = dict(zip(want, _fetch(list(want.values()))))
         results = MultipassPIVResults()
         hosts = []
@@ -292,17 +304,10 @@ class WorkPIV:
                 r.iyvecs_final = lay.gy + offy
                 r.deltaxs_final = fx_
                 r.deltays_final = fy_
-                sel = got[(k, "tps_final", "sel")].astype(np.int64)
-                xs_s = r.ixvecs_final.copy().astype(np.float32)
-                xs_s[sel] = r.xs[sel]
-                ys_s = r.iyvecs_final.copy().astype(np.float32)
-                ys_s[sel] = r.ys[sel]
-                dxs = fx_.copy()
-                dxs[sel] = got[(k, "tps_final", "smooth_x")]
-                dys = fy_.copy()
-                dys[sel] = got[(k, "tps_final", "smooth_y")]
-                r.xs_smooth, r.ys_smooth = xs_s, ys_s
-                r.deltaxs_smooth, r.deltays_smooth = dxs, dys
+                r.xs_smooth = got[(k, "tps_final", "xs_smooth")]
+                r.ys_smooth = got[(k, "tps_final", "ys_smooth")]
+                r.deltaxs_smooth = got[(k, "tps_final", "dx_smooth")]
+                r.deltays_smooth = got[(k, "tps_final", "dy_smooth")]
                 r.deltaxs_tps = LazyWeights(tps, 0)
                 r.deltays_tps = LazyWeights(tps, 1)
         return results
