@@ -38,4 +38,24 @@ __device__ __forceinline__ void df_mac(float2 b, float2 z, float& sh, float& sl)
   sh = t;
 }
 
+__device__ __forceinline__ float2 df_neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// Two independent df_mac in the lanes of float2 pairs, with packed FP32x2
+// instructions (each lane rounds exactly as df_mac):
+// (sh.x, sl.x) += b * (zh.x + zl.x) and (sh.y, sl.y) += b * (zh.y + zl.y).
+__device__ __forceinline__ void df_mac_x2(float2 b, float2 zh, float2 zl, float2& sh,
+                                          float2& sl) {
+  const float2 bh = make_float2(b.x, b.x), bl = make_float2(b.y, b.y);
+  const float2 p = __fmul2_rn(bh, zh);
+  float2 e = __ffma2_rn(bh, zh, df_neg2(p));
+  e = __ffma2_rn(bh, zl, e);
+  e = __ffma2_rn(bl, zh, e);
+  const float2 t = __fadd2_rn(sh, p);
+  const float2 bb = __fadd2_rn(t, df_neg2(sh));
+  const float2 err = __fadd2_rn(__fadd2_rn(sh, df_neg2(__fadd2_rn(t, df_neg2(bb)))),
+                                __fadd2_rn(p, df_neg2(bb)));
+  sl = __fadd2_rn(sl, __fadd2_rn(err, e));
+  sh = t;
+}
+
 }  // namespace fi

@@ -146,20 +146,29 @@ __device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   for (int c0 = 4 * wid; c0 < m; c0 += 4 * NW) {
-    float h[8], l[8];
+    // column q: x sums in lane .x, y sums in lane .y of the pairs (packed FP32x2)
+    float2 H[4], Lo[4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) h[k] = l[k] = 0.f;
+    for (int q = 0; q < 4; ++q) H[q] = Lo[q] = make_float2(0.f, 0.f);
     const float2* col = B + (int64_t)c0 * ld;
     const int nc = min(4, m - c0);
 #pragma unroll 2
     for (int r = lane; r < m; r += 32) {
       const float2 a = zx[r], b = zy[r];
+      const float2 zh = make_float2(a.x, b.x), zl = make_float2(a.y, b.y);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const float2 v = (q < nc) ? __ldcs(col + (int64_t)q * ld + r) : make_float2(0.f, 0.f);
-        df_mac(v, a, h[q], l[q]);
-        df_mac(v, b, h[4 + q], l[4 + q]);
+        df_mac_x2(v, zh, zl, H[q], Lo[q]);
       }
+    }
+    float h[8], l[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      h[q] = H[q].x;
+      l[q] = Lo[q].x;
+      h[4 + q] = H[q].y;
+      l[4 + q] = Lo[q].y;
     }
     // reduce-scatter: lane ends with value 4 b4 + 2 b3 + b2 (b_k = bit k of lane)
 #pragma unroll
@@ -811,7 +820,9 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       const int l = j / rs, ch = j - l * rs;
       const int c = 32 * (crank + csize * l) + lane;
       const int r0 = (int)((int64_t)N * ch / rs), r1 = (int)((int64_t)N * (ch + 1) / rs);
-      float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+      // sums of V0 and V1 in the lanes of (h01, l01) (packed FP32x2), V2 in (h2, l2)
+      float2 h01 = make_float2(0.f, 0.f), l01 = make_float2(0.f, 0.f);
+      float h2 = 0.f, l2 = 0.f;
       if (c < N) {
         const int2 cc = cxy[c];
         for (int rb = r0; rb < r1; rb += 8) {
@@ -822,13 +833,14 @@ __global__ void __launch_bounds__(NT, 512 / NT)
           for (int u = 0; u < 8; ++u) {
             if (u < cnt) {
               const int r = rb + u;
-              df_mac(a[u], Vd[r], h0, l0);
-              df_mac(a[u], Vd[np + r], h1, l1);
+              const float2 v0 = Vd[r], v1 = Vd[np + r];
+              df_mac_x2(a[u], make_float2(v0.x, v1.x), make_float2(v0.y, v1.y), h01, l01);
               df_mac(a[u], Vd[2 * np + r], h2, l2);
             }
           }
         }
       }
+      const float h0 = h01.x, l0 = l01.x, h1 = h01.y, l1 = l01.y;
       if (rs == 1) {
         if (c < N) write_y(c, make_float2(h0, l0), make_float2(h1, l1), make_float2(h2, l2));
       } else {
@@ -970,25 +982,39 @@ __global__ void __launch_bounds__(NT, 512 / NT)
           const int cnt = min(8, m - c0);
           float2 a[8];
           a_batch_df(rg, cr, c0 + 3, cnt, a);
+          // A - Z V^T - V Z^T in double-float: entries of A up to ~1e5 cancel to B
+          // entries ~1e2-1e4; the ~2^-48 |A| rounding leaves B within ~1e-11 of its
+          // FP64 value, the interpolated field within ~1e-9 px.  Columns c, c + 1 in
+          // the lanes of float2 pairs (packed FP32x2 instructions).
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < 8; u += 2) {
             const int c = c0 + u;
-            if (u < cnt && r < m && r >= c) {
-              // A - Z V^T - V Z^T in double-float: entries of A up to ~1e5 cancel to
-              // B entries ~1e2-1e4; the ~2^-48 |A| rounding leaves B within ~1e-11 of
-              // its FP64 value, the interpolated field within ~1e-9 px
-              const int cg_ = c + 3;
-              float sh = a[u].x, sl = a[u].y;
+            const bool in0 = u < cnt && r < m && r >= c;
+            const bool in1 = u + 1 < cnt && r < m && r >= c + 1;
+            if (in0 || in1) {
+              const int cg0 = c + 3, cg1 = min(c + 4, N - 1);
+              float2 sh = make_float2(a[u].x, a[u + 1].x), sl = make_float2(a[u].y, a[u + 1].y);
 #pragma unroll
               for (int k = 0; k < 3; ++k) {
-                df_mac(nz[k], Vd[k * np + cg_], sh, sl);
-                df_mac(nv[k], Zd[k * np + cg_], sh, sl);
+                const float2 v0 = Vd[k * np + cg0], v1 = Vd[k * np + cg1];
+                const float2 z0 = Zd[k * np + cg0], z1 = Zd[k * np + cg1];
+                df_mac_x2(nz[k], make_float2(v0.x, v1.x), make_float2(v0.y, v1.y), sh, sl);
+                df_mac_x2(nv[k], make_float2(z0.x, z1.x), make_float2(z0.y, z1.y), sh, sl);
               }
-              const float hi = __fadd_rn(sh, sl);
-              const float2 sv = make_float2(hi, __fsub_rn(sl, __fsub_rn(hi, sh)));
-              __stcs(B2 + (int64_t)c * mp + r, sv);  // streaming: keeps L2 for the factor
-              L32[(int64_t)c * mp + r] = sv.x;
-              S[(qb + u) * 33 + lane] = sv;
+              const float2 hi = __fadd2_rn(sh, sl);
+              const float2 lo = __fadd2_rn(sl, df_neg2(__fadd2_rn(hi, df_neg2(sh))));
+              if (in0) {
+                const float2 sv = make_float2(hi.x, lo.x);
+                __stcs(B2 + (int64_t)c * mp + r, sv);  // streaming: keeps L2 for the factor
+                L32[(int64_t)c * mp + r] = sv.x;
+                S[(qb + u) * 33 + lane] = sv;
+              }
+              if (in1) {
+                const float2 sv = make_float2(hi.y, lo.y);
+                __stcs(B2 + (int64_t)(c + 1) * mp + r, sv);
+                L32[(int64_t)(c + 1) * mp + r] = sv.x;
+                S[(qb + u + 1) * 33 + lane] = sv;
+              }
             }
           }
         }
