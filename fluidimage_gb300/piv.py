@@ -194,7 +194,46 @@ class WorkPIV:
 
         Every array is gathered into one device buffer and copied to pinned host
         memory at once (one synchronisation)."""
-        fx = self.params.fix
+        want = self._device_results(outs)
+        handle = _fetch_start(list(want.values()))
+        return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
+
+    def calcul_series(self, couples):
+        """Results of a series of couples, in order (a generator): the GPU computes
+        couple i while a host thread builds the results of couple i - 1 from their
+        pinned copy, so that the host-side work overlaps the device work (the role of
+        the executors of a PIV topology, topologies/piv.py:143-151, for this work).
+        """
+        import torch
+        from concurrent.futures import ThreadPoolExecutor
+
+        dev = torch.device(self.device or "cuda")
+        pending = None
+        with ThreadPoolExecutor(max_workers=1) as pool:
+            for couple in couples:
+                if isinstance(couple, dict):
+                    couple = ArrayCouple(**couple)
+                if not isinstance(couple, ArrayCouple):
+                    raise ValueError(
+                        f"not isinstance(couple, ArrayCouple), {type(couple) = }")
+                couple.apply_mask(self.params.mask)
+                im0, im1 = couple.get_arrays()
+                outs = self.calcul_device(_to_device(im0, dev), _to_device(im1, dev))
+                want = self._device_results(outs)
+                handle = _fetch_start(list(want.values()))
+                fut = pool.submit(self._results_from_handle, outs, couple, want, handle)
+                if pending is not None:
+                    yield pending.result()
+                pending = fut
+            if pending is not None:
+                yield pending.result()
+
+    def _results_from_handle(self, outs, couple, want, handle):
+        return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
+
+    def _device_results(self, outs):
+        """The device tensors the host results are built from (keyed by pass and
+        name); the *_smooth fields are assembled on the device here."""
         offx, offy = self._xy_offsets()
         keys = ("deltaxs_raw", "deltays_raw", "correls_max", "errors", "xs", "ys", "flags",
                 "deltaxs", "deltays", "fix_flags", "diff2")
@@ -231,7 +270,14 @@ class WorkPIV:
                         0, sel, tps.smooth_x)
                     want[(k, tag, "dy_smooth")] = tps.out_y.clone().index_copy_(
                         0, sel, tps.smooth_y)
-        got = dict(zip(want, _fetch(list(want.values()))))
+        return want
+
+    def _host_results(self, outs, couple, got):
+        """``MultipassPIVResults`` from the host copies ``got`` of ``_device_results``."""
+        fx = self.params.fix
+        offx, offy = self._xy_offsets()
+        keys = ("deltaxs_raw", "deltays_raw", "correls_max", "errors", "xs", "ys", "flags",
+                "deltaxs", "deltays", "fix_flags", "diff2")
         results = MultipassPIVResults()
         hosts = []
         for k, pd in enumerate(outs):
@@ -321,31 +367,49 @@ class WorkPIV:
             )
 
 
-def _fetch(tensors):
-    """Device tensors -> numpy arrays with one copy: the tensors are packed into one
+def _fetch_start(tensors):
+    """Start the copy of device tensors to the host: the tensors are packed into one
     device byte buffer (widest elements first, so every array stays aligned) and
-    copied to pinned host memory; the arrays are views of that buffer."""
+    copied asynchronously to pinned host memory; ``_fetch_finish`` waits for it."""
     import torch
 
-    np_of = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32,
-             torch.int64: np.int64, torch.uint8: np.uint8, torch.int16: np.int16}
     order = sorted(range(len(tensors)), key=lambda i: -tensors[i].element_size())
     flat = [tensors[i].contiguous().view(-1).view(torch.uint8) for i in order]
-    sizes = [f.numel() for f in flat]
     if not flat:
-        return []
+        return None
     buf = torch.cat(flat) if len(flat) > 1 else flat[0]
     host = torch.empty(buf.numel(), dtype=torch.uint8, pin_memory=True)
     host.copy_(buf, non_blocking=True)
-    torch.cuda.current_stream().synchronize()
+    done = torch.cuda.Event()
+    done.record()
+    meta = [(tuple(t.shape), t.dtype) for t in tensors]
+    return host, done, order, [f.numel() for f in flat], meta
+
+
+def _fetch_finish(handle):
+    """numpy views (one per tensor given to ``_fetch_start``) of the pinned buffer,
+    once its copy is complete."""
+    import torch
+
+    if handle is None:
+        return []
+    host, done, order, sizes, meta = handle
+    done.synchronize()
+    np_of = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32,
+             torch.int64: np.int64, torch.uint8: np.uint8, torch.int16: np.int16}
     raw = host.numpy()
-    out = [None] * len(tensors)
+    out = [None] * len(meta)
     off = 0
     for i, n in zip(order, sizes):
-        t = tensors[i]
-        out[i] = raw[off:off + n].view(np_of[t.dtype]).reshape(tuple(t.shape))
+        shape, dtype = meta[i]
+        out[i] = raw[off:off + n].view(np_of[dtype]).reshape(shape)
         off += n
     return out
+
+
+def _fetch(tensors):
+    """Device tensors -> numpy arrays with one copy (views of one pinned buffer)."""
+    return _fetch_finish(_fetch_start(tensors))
 
 
 def _secondary_peaks(counts, peaks, nvec):
