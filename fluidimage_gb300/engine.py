@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -254,17 +255,17 @@ def lattice_coords(px, py, npts, stream=None):
     return xy2, flag
 
 
-_PINNED = {}
+_PINNED = threading.local()
 
 
 def _readback_raw(addr, nbytes, stream=None):
     """``nbytes`` at device address ``addr`` -> bytes, through a pinned buffer kept
-    per process (one synchronisation of the stream)."""
+    per host thread (one synchronisation of the stream)."""
     torch = _torch()
-    buf = _PINNED.get("small")
+    buf = getattr(_PINNED, "small", None)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(4096, nbytes), dtype=torch.uint8, pin_memory=True)
-        _PINNED["small"] = buf
+        _PINNED.small = buf
     strm = stream or torch.cuda.current_stream()
     L.check(L.load().fi_memcpy_d2h(buf.data_ptr(), addr, nbytes, strm.cuda_stream),
             "fi_memcpy_d2h")
@@ -538,7 +539,6 @@ class PIVPipeline:
             lay.dev["lattice"] = (torch.as_tensor(xy2, device=self.device),
                                   torch.ones(1, dtype=torch.int32, device=self.device))
             self.layouts.append(lay)
-        self.im_min = torch.empty(2, dtype=torch.float32, device=self.device)
 
     # ----------------------------------------------------------------------
     def run(self, im0, im1, stream=None) -> List[PassDevice]:
@@ -552,7 +552,9 @@ class PIVPipeline:
         s = L.stream_handle(stream)
         dt = _DTYPES[self.dtype]
         H, W = self.imshape
-        L.check(lib.fi_images_min(L.ptr(im0), L.ptr(im1), dt, H * W, L.ptr(self.im_min), s),
+        im_min = torch.empty(2, dtype=torch.float32, device=self.device)  # per run: runs
+        # on several streams may overlap
+        L.check(lib.fi_images_min(L.ptr(im0), L.ptr(im1), dt, H * W, L.ptr(im_min), s),
                 "fi_images_min")
         mp, fx = self.params.multipass, self.params.fix
         outs: List[PassDevice] = []
@@ -565,7 +567,7 @@ class PIVPipeline:
                     lay.dev["px"], lay.dev["py"], lay.nvec, mp.subdom_size, mp.smoothing_coef,
                     mp.threshold_tps, False, stream, p_lattice=lay.dev["lattice"])
                 dxin, dyin = prev.tps_next.rx, prev.tps_next.ry
-            cur = self._run_pass(lay, im0, im1, dxin, dyin, dt, s)
+            cur = self._run_pass(lay, im0, im1, im_min, dxin, dyin, dt, s)
             self._run_fix(cur, fx, s)
             outs.append(cur)
             prev = cur
@@ -581,7 +583,7 @@ class PIVPipeline:
             print("Warning: InterpError at the end of the last piv pass:", e)
         return outs
 
-    def _run_pass(self, lay, im0, im1, dxin, dyin, dt, s) -> PassDevice:
+    def _run_pass(self, lay, im0, im1, im_min, dxin, dyin, dt, s) -> PassDevice:
         torch = _torch()
         lib = L.load()
         nvec, dev = lay.nvec, self.device
@@ -606,7 +608,7 @@ class PIVPipeline:
         H, W = self.imshape
         a = L.PivPassArgs()
         a.im0, a.im1, a.dtype, a.height, a.width = L.ptr(im0), L.ptr(im1), dt, H, W
-        a.im_min = L.ptr(self.im_min)
+        a.im_min = L.ptr(im_min)
         a.n = lay.n
         a.ixvecs, a.nx = L.ptr(lay.dev["ixvecs"]), lay.ixvecs.size
         a.iyvecs, a.ny = L.ptr(lay.dev["iyvecs"]), lay.iyvecs.size

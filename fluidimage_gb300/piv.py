@@ -198,18 +198,36 @@ class WorkPIV:
         handle = _fetch_start(list(want.values()))
         return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
 
-    def calcul_series(self, couples):
-        """Results of a series of couples, in order (a generator): the GPU computes
-        couple i while a host thread builds the results of couple i - 1 from their
-        pinned copy, so that the host-side work overlaps the device work (the role of
-        the executors of a PIV topology, topologies/piv.py:143-151, for this work).
+    def calcul_series(self, couples, streams=2):
+        """Results of a series of couples, in order (a generator).  ``streams`` couples
+        are in flight at once, each on its own host thread and CUDA stream: the GPU
+        works on one couple's kernels while another couple's host-side steps (the TPS
+        readbacks, the results) run, the role of the executors of a PIV topology
+        (topologies/piv.py:143-151) for this work.
         """
+        import collections
+        import threading
+
         import torch
         from concurrent.futures import ThreadPoolExecutor
 
         dev = torch.device(self.device or "cuda")
-        pending = None
-        with ThreadPoolExecutor(max_workers=1) as pool:
+        local = threading.local()
+
+        def run(couple):
+            if getattr(local, "stream", None) is None:
+                local.stream = torch.cuda.Stream(device=dev)
+            with torch.cuda.stream(local.stream):
+                im0, im1 = couple.get_arrays()
+                outs = self.calcul_device(_to_device(im0, dev), _to_device(im1, dev),
+                                          stream=local.stream)
+                want = self._device_results(outs)
+                handle = _fetch_start(list(want.values()))
+                return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
+
+        nstreams = max(1, int(streams))
+        pending = collections.deque()
+        with ThreadPoolExecutor(max_workers=nstreams) as pool:
             for couple in couples:
                 if isinstance(couple, dict):
                     couple = ArrayCouple(**couple)
@@ -217,19 +235,13 @@ class WorkPIV:
                     raise ValueError(
                         f"not isinstance(couple, ArrayCouple), {type(couple) = }")
                 couple.apply_mask(self.params.mask)
-                im0, im1 = couple.get_arrays()
-                outs = self.calcul_device(_to_device(im0, dev), _to_device(im1, dev))
-                want = self._device_results(outs)
-                handle = _fetch_start(list(want.values()))
-                fut = pool.submit(self._results_from_handle, outs, couple, want, handle)
-                if pending is not None:
-                    yield pending.result()
-                pending = fut
-            if pending is not None:
-                yield pending.result()
-
-    def _results_from_handle(self, outs, couple, want, handle):
-        return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
+                im0, _ = couple.get_arrays()
+                self._pipeline(tuple(im0.shape), _host_dtype(im0))  # built here, once
+                if len(pending) >= nstreams:
+                    yield pending.popleft().result()
+                pending.append(pool.submit(run, couple))
+            while pending:
+                yield pending.popleft().result()
 
     def _device_results(self, outs):
         """The device tensors the host results are built from (keyed by pass and
@@ -423,6 +435,13 @@ def _secondary_peaks(counts, peaks, nvec):
         if c >= 0:
             out[i] = [(int(pk[i, j, 0]), int(pk[i, j, 1]), pk[i, j, 2]) for j in range(c)]
     return out
+
+
+def _host_dtype(a):
+    """Image element type of a host image (numpy array or torch tensor)."""
+    import torch
+
+    return _np_dtype(a) if isinstance(a, torch.Tensor) else np.asarray(a).dtype
 
 
 def _np_dtype(t):
