@@ -746,20 +746,46 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     const double NN = (double)N * (double)N;
     // a constant window has an exactly zero spectrum (and plane) upstream
     const bool flat0 = mm[0] == mm[2], flat1 = mm[1] == mm[3];
-    const double S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
-    const double S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
-    int e0 = 0, e1 = 0;
-    if (S0 > 0.0) frexp(sqrt(S0 / NN), &e0);
-    if (S1 > 0.0) frexp(sqrt(S1 / NN), &e1);
-    red[16] = sqrt(S0 * S1);
     float* rf = reinterpret_cast<float*>(red + 17);
-    rf[0] = (float)(sums[0] / NN);
-    rf[1] = (float)(sums[2] / NN);
+    int e0 = 0, e1 = 0;
+    double S0, S1;
+    if constexpr ((N & (N - 1)) == 0) {
+      // N^2 a power of two: the divisions by N^2 are exact products by 2^-2L, and the
+      // exponent of sqrt(S / N^2) follows from the one of S (frexp(sqrt(m 2^x)) has
+      // exponent (x + 1) >> 1): the same values with a few FP64 instructions (this
+      // thread issues them for the whole window; FP64 is narrow on this GPU)
+      constexpr int L = (N == 16) ? 4 : (N == 32) ? 5 : (N == 64) ? 6 : 3;
+      constexpr double INN = 1.0 / ((double)N * (double)N);
+      S0 = flat0 ? 0.0 : fmax(sums[1] - (sums[0] * sums[0]) * INN, 0.0);
+      S1 = flat1 ? 0.0 : fmax(sums[3] - (sums[2] * sums[2]) * INN, 0.0);
+      int x0 = 0, x1 = 0;
+      if (S0 > 0.0) {
+        frexp(S0, &x0);
+        e0 = (x0 - 2 * L + 1) >> 1;
+      }
+      if (S1 > 0.0) {
+        frexp(S1, &x1);
+        e1 = (x1 - 2 * L + 1) >> 1;
+      }
+      rf[0] = (float)(sums[0] * INN);
+      rf[1] = (float)(sums[2] * INN);
+      // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1) = 2^(e0 + e1 - 2 - 2L)
+      reinterpret_cast<float*>(red + 20)[0] = ldexpf(1.0f, e0 + e1 - 2 - 2 * L);
+    } else {
+      S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
+      S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
+      if (S0 > 0.0) frexp(sqrt(S0 / NN), &e0);
+      if (S1 > 0.0) frexp(sqrt(S1 / NN), &e1);
+      rf[0] = (float)(sums[0] / NN);
+      rf[1] = (float)(sums[2] / NN);
+      // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1), sc0 sc1 a power of two
+      reinterpret_cast<float*>(red + 20)[0] =
+          (float)(0.25 / (NN * (double)ldexpf(1.0f, -e0) * (double)ldexpf(1.0f, -e1)));
+    }
+    red[16] = sqrt(S0 * S1);
     rf[2] = ldexpf(1.0f, -e0);
     rf[3] = ldexpf(1.0f, -e1);
     reinterpret_cast<int*>(red + 19)[0] = (flat0 || flat1) ? 1 : 0;
-    // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1), sc0 sc1 a power of two
-    reinterpret_cast<float*>(red + 20)[0] = (float)(0.25 / (NN * (double)rf[2] * (double)rf[3]));
   }
   gsync<C::G>(g);
   const double norm = red[16];
