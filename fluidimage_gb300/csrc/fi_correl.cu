@@ -892,8 +892,10 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
         err = FI_VEC_BAD_CROP;
       }
       if (a.dxin) {
-        dxo = (float)((double)dxo + (double)dinx);
-        dyo = (float)((double)dyo + (double)diny);
+        // float32 + int32 promotes to float64 upstream, then rounds to float32: the
+        // exact sum rounded once, which is the float sum for |shift| < 2^24
+        dxo = (abs(dinx) < (1 << 24)) ? __fadd_rn(dxo, (float)dinx) : (float)((double)dxo + (double)dinx);
+        dyo = (abs(diny) < (1 << 24)) ? __fadd_rn(dyo, (float)diny) : (float)((double)dyo + (double)diny);
       }
       a.deltaxs[w] = dxo;
       a.deltays[w] = dyo;
@@ -905,8 +907,10 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
                                        (res.sec_tie ? FI_FLAG_SECONDARY_TIE : 0))
                            : (uint8_t)0;
       if (!FROM_WINDOWS) {
-        a.xs[w] = (float)((double)(ixs0 + ixs1) * 0.5);
-        a.ys[w] = (float)((double)(iys0 + iys1) * 0.5);
+        // midpoints: exact in float32 below 2^24
+        const int sx = ixs0 + ixs1, sy = iys0 + iys1;
+        a.xs[w] = (abs(sx) < (1 << 24)) ? __fmul_rn((float)sx, 0.5f) : (float)((double)sx * 0.5);
+        a.ys[w] = (abs(sy) < (1 << 24)) ? __fmul_rn((float)sy, 0.5f) : (float)((double)sy * 0.5);
       }
     }
   }
