@@ -45,7 +45,12 @@ METRIC = "PIV vectors/s at <=0.005 px vs FP64; plain FP32 vs batched tensor-core
 UNIT = "vectors/s"
 WORKLOAD = "config2: 2048x2048 uint16 pair, Oseen vortex, 3 passes 64/32/16 px, overlap 0.5, fix thr 2, TPS subdom 200 smoothing 0.5"
 SAMPLE_SHAPE = (512, 512)
-TPS_DRAM_BYTES_PER_SUBDOMAIN = (76.292096e6 + 112.621824e6) / 72
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tps_solve_mp per subdomain:
+# one CTA of 16 warps per subdomain (launches of at most one subdomain per SM; 72
+# subdomains of the config-2 recipe at 1024^2) and two 8-warp CTAs per SM (the
+# 342-subdomain launch of the 2048^2 workload)
+TPS_DRAM_BYTES_PER_SUBDOMAIN_WIDE = (76.292096e6 + 112.621824e6) / 72
+TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW = (880.266752e6 + 590.642688e6) / 342
 
 
 def parse_args():
@@ -399,16 +404,20 @@ def roofline(dominant, outs, work, peaks, peak_kind, steps):
         per_launch = flops / max(nlaunch, 1)
         achieved = per_launch / avg_s / 1e12
         peak = 1.25
-        # DRAM bytes per subdomain from one ncu capture of this kernel (72 subdomains
-        # of the same recipe at 1024², profiles/k_tps_solve_mp_config2_1024.md),
-        # scaled by the subdomains of an average launch
-        nsub = sum(t.nb_subdom for pd in outs for t in (pd.tps_next, pd.tps_final)
-                   if t is not None)
-        traffic = TPS_DRAM_BYTES_PER_SUBDOMAIN * nsub / max(nlaunch, 1)
+        # DRAM bytes per subdomain from ncu captures of this kernel (one per launch
+        # shape), times the subdomains of each launch, averaged over the launches
+        import torch
+
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        traffic = sum(
+            t.nb_subdom * (TPS_DRAM_BYTES_PER_SUBDOMAIN_WIDE if t.nb_subdom <= nsm
+                           else TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW)
+            for pd in outs for t in (pd.tps_next, pd.tps_final) if t is not None
+        ) / max(nlaunch, 1)
         return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read+write per subdomain (1024^2 capture) "
-                                  "x subdomains per launch",
+                "traffic_source": "ncu dram__bytes_read+write per subdomain (captures of "
+                                  "both launch shapes) x subdomains, per launch",
                 "work": "reference-equivalent FP64 LU flops, sum 2/3 (N+3)^3 per solve",
                 "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
                 "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
