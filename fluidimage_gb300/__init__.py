@@ -5,6 +5,8 @@
   with all windows of a pass in one kernel launch.
 * ``CorrelGB300`` / ``correlation_classes``: the per-window correlation plugin
   (``params.piv0.method_correl = "gb300"``).
+* ``WorkBOS``: background-oriented schlieren (PIV against a reference image kept
+  on the GPU).
 
 Importing the package is cheap: the CUDA library is loaded on first use by
 ``fluidimage_gb300._lib`` and fails loudly when it is missing (no CPU fallback).
@@ -17,8 +19,9 @@ from .data_objects import ArrayCouple, HeavyPIVResults, MultipassPIVResults  # n
 from .errors import InterpError, PIVError  # noqa: E402
 from .params import ParamContainer  # noqa: E402
 from .piv import WorkPIV  # noqa: E402
+from .bos import WorkBOS  # noqa: E402
 
 __all__ = [
-    "WorkPIV", "CorrelGB300", "correlation_classes", "register_upstream", "ArrayCouple",
+    "WorkPIV", "WorkBOS", "CorrelGB300", "correlation_classes", "register_upstream", "ArrayCouple",
     "HeavyPIVResults", "MultipassPIVResults", "PIVError", "InterpError", "ParamContainer",
 ]
