@@ -342,7 +342,7 @@ def run_gpu(args):
                                 "api": "WorkPIV.calcul, one pair per call, L2 flushed before"}},
         "gpu_launches": int(launches),
         "tps_subdomains": int(sum(t.nb_subdom for pd in outs for t in (pd.tps_next, pd.tps_final)
-                                  if t is not None)),
+                                  if t is not None and hasattr(t, "nb_subdom"))),
         "tps_lu_fallbacks": int(sum(int(t.mp_status.sum().item()) for pd in outs
                                     for t in (pd.tps_next, pd.tps_final) if t is not None)),
         "tps_outer_iterations": _iter_stats(outs),

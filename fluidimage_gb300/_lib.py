@@ -40,6 +40,9 @@ PEAK_FIELDS = 5
 PRE_U8, PRE_U16, PRE_F32, PRE_F64 = 0, 1, 2, 3
 MODES = {"reflect": 0, "constant": 1, "nearest": 2, "mirror": 3, "wrap": 4}
 
+GRID_COCIRCULAR = 1
+GRID_NEAREST_TIE = 2
+
 P = C.c_void_p
 
 
@@ -135,6 +138,12 @@ _SIGNATURES = {
     "fi_sq_sum_max": (C.c_int, [P, C.c_int, C.c_int64, P, P, C.c_int, P]),
     "fi_tanh_rescale": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
+    "fi_griddata": (
+        C.c_int,
+        [P, P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, C.c_int, P, P, P, P, P, P, P,
+         P],
+    ),
+    "fi_griddata_scratch_ints": (C.c_int64, [C.c_int, C.c_int]),
     "fi_tps_interpolate": (
         C.c_int,
         [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,

@@ -255,6 +255,20 @@ def lattice_coords(px, py, npts, stream=None):
     return xy2, flag
 
 
+@dataclass
+class GridOutput:
+    """griddata interpolation of a pass on a grid (linear on the Delaunay
+    triangulation, nearest outside the hull; calcul/interpolate/griddata.py:11-27)."""
+
+    out_x: object  # float64 [npts] device
+    out_y: object
+    rx: object     # int32 [npts] device (rounded)
+    ry: object
+    flags: object  # uint8 [npts]: GRID_COCIRCULAR, GRID_NEAREST_TIE
+    num_centers: int = 0
+    selection: object = None
+
+
 _PINNED = threading.local()
 
 
@@ -422,6 +436,47 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     return out
 
 
+def run_griddata(xs, ys, dx, dy, nvec, grid, px, py, npts, stream):
+    """apply_interp with griddata on device (singlepass.py:498-556): the valid
+    vectors of a pass (on its window grid ``grid`` = (ixvecs, iyvecs) device int32,
+    nx, ny) interpolated at (px, py)."""
+    torch = _torch()
+    lib = L.load()
+    dev = xs.device
+    s = L.stream_handle(stream)
+    ixvecs, iyvecs, nx, ny = grid
+    u8_, i32_, f32_, f64_ = torch.uint8, torch.int32, torch.float32, torch.float64
+    cA = _Carved(dev, [(C.sizeof(L.TpsPlan), u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
+                       (nvec, f32_), (nvec, i32_)])
+    plan, cx, cy, ux, uy, sel = cA.addr
+    # the compaction of the valid vectors (the subdomain layout it also computes is
+    # not used)
+    L.check(lib.fi_tps_plan_make(L.ptr(xs), L.ptr(ys), L.ptr(dx), L.ptr(dy), nvec, 200, 1.0,
+                                 20.0, plan, cx, cy, ux, uy, sel, s), "fi_tps_plan_make")
+    nscr = int(lib.fi_griddata_scratch_ints(nx, ny))
+    cO = _Carved(dev, [(npts, f64_), (npts, f64_), (npts, i32_), (npts, i32_), (npts, u8_),
+                       (nscr, i32_), (2, i32_)])
+    out_x, out_y, rx, ry, flags, scratch, status = cO.addr
+    hdr = L.TpsPlan.from_buffer_copy(_readback_raw(plan, C.sizeof(L.TpsPlan), stream))
+    if hdr.status == 1:
+        raise InterpError("Only nan.")
+    if hdr.status != 0:
+        raise ValueError("griddata: the vectors are all on one line (no triangulation)")
+    nv = hdr.num_centers
+    with _timed("fi_griddata"):
+        L.check(lib.fi_griddata(cx, cy, ux, uy, sel, nv, L.ptr(ixvecs), nx, L.ptr(iyvecs), ny,
+                                L.ptr(px), L.ptr(py), npts, scratch, out_x, out_y, rx, ry,
+                                flags, status, s), "fi_griddata")
+    st = int(np.frombuffer(_readback_raw(status, 4, stream), np.int32)[0])
+    if st != 0:
+        raise RuntimeError({1: "griddata: a position is off the half-integer lattice",
+                            2: "griddata: a gap of more than 4 grid steps without vectors",
+                            3: "griddata: bad vector selection"}.get(st, f"griddata: {st}"))
+    return GridOutput(out_x=cO.tensor(0), out_y=cO.tensor(1), rx=cO.tensor(2),
+                      ry=cO.tensor(3), flags=cO.tensor(4), num_centers=nv,
+                      selection=cA.tensor(5))
+
+
 # --------------------------------------------------------------------------------
 # the pipeline
 def subpix_pinv(nsubpix):
@@ -459,8 +514,8 @@ class PassDevice:
     peaks: object = None
     peaks_err: object = None
     replaced: object = None  # [nvec, 3] old dx, dy, correl_max of replaced vectors
-    tps_next: Optional[TpsOutput] = None  # interpolation of this pass on the next grid
-    tps_final: Optional[TpsOutput] = None
+    tps_next: Optional[object] = None  # TpsOutput or GridOutput: this pass on the next grid
+    tps_final: Optional[object] = None  # TpsOutput or GridOutput: on its own grid
 
 
 class PIVPipeline:
@@ -499,15 +554,6 @@ class PIVPipeline:
         self.subpix_minv = None
         if p0.method_subpix == "2d_gaussian":
             self.subpix_minv = torch.as_tensor(subpix_pinv(self.nsubpix), device=self.device)
-        if mp.number > 1 and mp.use_tps is not True:
-            raise NotImplementedError(
-                "interpolation between passes needs params.multipass.use_tps = True "
-                "(the griddata path is not provided by this backend)"
-            )
-        if mp.use_tps is False and interp_last:
-            raise NotImplementedError(
-                "the final griddata interpolation is not provided (use_tps=False); "
-                "pass interp_last=False to skip it")
         shapes = pass_shapes(p0.shape_crop_im0, mp.number, mp.coeff_zoom)
         if p0.shape_crop_im1 is not None:
             s1 = p0.shape_crop_im1
@@ -562,10 +608,17 @@ class PIVPipeline:
         for lay in self.layouts:
             dxin = dyin = None
             if prev is not None:
-                prev.tps_next = run_tps(
-                    prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
-                    lay.dev["px"], lay.dev["py"], lay.nvec, mp.subdom_size, mp.smoothing_coef,
-                    mp.threshold_tps, False, stream, p_lattice=lay.dev["lattice"])
+                if mp.use_tps is True:
+                    prev.tps_next = run_tps(
+                        prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                        lay.dev["px"], lay.dev["py"], lay.nvec, mp.subdom_size,
+                        mp.smoothing_coef, mp.threshold_tps, False, stream,
+                        p_lattice=lay.dev["lattice"])
+                else:  # use_tps False or 'last': griddata between passes
+                    prev.tps_next = run_griddata(
+                        prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                        self._grid(prev.layout), lay.dev["px"], lay.dev["py"], lay.nvec,
+                        stream)
                 dxin, dyin = prev.tps_next.rx, prev.tps_next.ry
             cur = self._run_pass(lay, im0, im1, im_min, dxin, dyin, dt, s)
             self._run_fix(cur, fx, s)
@@ -574,14 +627,24 @@ class PIVPipeline:
         if not self.interp_last:
             return outs
         try:
-            prev.tps_final = run_tps(
-                prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
-                prev.layout.dev["px"], prev.layout.dev["py"], prev.layout.nvec,
-                mp.subdom_size, mp.smoothing_coef, mp.threshold_tps, True, stream,
-                p_lattice=prev.layout.dev["lattice"])
+            if mp.use_tps is True or mp.use_tps == "last":
+                prev.tps_final = run_tps(
+                    prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                    prev.layout.dev["px"], prev.layout.dev["py"], prev.layout.nvec,
+                    mp.subdom_size, mp.smoothing_coef, mp.threshold_tps, True, stream,
+                    p_lattice=prev.layout.dev["lattice"])
+            else:
+                prev.tps_final = run_griddata(
+                    prev.xs, prev.ys, prev.deltaxs, prev.deltays, prev.layout.nvec,
+                    self._grid(prev.layout), prev.layout.dev["px"], prev.layout.dev["py"],
+                    prev.layout.nvec, stream)
         except InterpError as e:
             print("Warning: InterpError at the end of the last piv pass:", e)
         return outs
+
+    @staticmethod
+    def _grid(lay):
+        return lay.dev["ixvecs"], lay.dev["iyvecs"], lay.ixvecs.size, lay.iyvecs.size
 
     def _run_pass(self, lay, im0, im1, im_min, dxin, dyin, dt, s) -> PassDevice:
         torch = _torch()

@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _lib
 from .data_objects import ArrayCouple, HeavyPIVResults, MultipassPIVResults
-from .engine import PIVPipeline, error_dict
+from .engine import GridOutput, PIVPipeline, error_dict
 from .errors import InterpError
 from .params import ParamContainer
 
@@ -264,8 +264,11 @@ class WorkPIV:
                 tps = getattr(pd, tag)
                 if tps is None:
                     continue
-                want[(k, tag, "singular")] = tps.singular
                 want[(k, tag, "out_x")], want[(k, tag, "out_y")] = tps.out_x, tps.out_y
+                if isinstance(tps, GridOutput):
+                    want[(k, tag, "flags")] = tps.flags
+                    continue
+                want[(k, tag, "singular")] = tps.singular
                 if tag == "tps_final":
                     # the *_smooth fields (singlepass.py:515-529): the grid with the
                     # selected vectors' values scattered in, built on the device
@@ -345,23 +348,29 @@ class WorkPIV:
             r, h = hosts[k]
             if pd.tps_next is not None:
                 nxt = outs[k + 1].layout
-                self._check_tps(got[(k, "tps_next", "singular")])
                 r.deltaxs_approx = got[(k, "tps_next", "out_x")]
                 r.deltays_approx = got[(k, "tps_next", "out_y")]
                 r.ixvecs_approx = nxt.gx + offx
                 r.iyvecs_approx = nxt.gy + offy
-                r.deltaxs_tps = LazyWeights(pd.tps_next, 0)
-                r.deltays_tps = LazyWeights(pd.tps_next, 1)
+                if isinstance(pd.tps_next, GridOutput):
+                    # cocircular cells / equidistant nearest vectors (several valid
+                    # triangulations: upstream's result there depends on Qhull)
+                    r.griddata_tie_flags_approx = got[(k, "tps_next", "flags")]
+                else:
+                    self._check_tps(got[(k, "tps_next", "singular")])
+                    r.deltaxs_tps = LazyWeights(pd.tps_next, 0)
+                    r.deltays_tps = LazyWeights(pd.tps_next, 1)
             if pd.tps_final is not None:
                 tps = pd.tps_final
-                self._check_tps(got[(k, "tps_final", "singular")])
                 lay = pd.layout
-                fx_ = got[(k, "tps_final", "out_x")]
-                fy_ = got[(k, "tps_final", "out_y")]
                 r.ixvecs_final = lay.gx + offx
                 r.iyvecs_final = lay.gy + offy
-                r.deltaxs_final = fx_
-                r.deltays_final = fy_
+                r.deltaxs_final = got[(k, "tps_final", "out_x")]
+                r.deltays_final = got[(k, "tps_final", "out_y")]
+                if isinstance(tps, GridOutput):
+                    r.griddata_tie_flags_final = got[(k, "tps_final", "flags")]
+                    continue
+                self._check_tps(got[(k, "tps_final", "singular")])
                 r.xs_smooth = got[(k, "tps_final", "xs_smooth")]
                 r.ys_smooth = got[(k, "tps_final", "ys_smooth")]
                 r.deltaxs_smooth = got[(k, "tps_final", "dx_smooth")]
@@ -374,8 +383,7 @@ class WorkPIV:
     def _check_tps(singular):
         if int(np.asarray(singular).sum()) != 0:
             raise np.linalg.LinAlgError(
-                "Singular TPS subdomain system (upstream falls back to griddata, "
-                "which this backend does not provide)"
+                "Singular TPS subdomain system (upstream then falls back to griddata)"
             )
 
 

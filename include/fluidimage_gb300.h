@@ -415,6 +415,31 @@ int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, con
                     double* max_udiff, int32_t* sweeps, const int32_t* order, void* stream);
 
 /*
+ * griddata of apply_interp (calcul/interpolate/griddata.py:11-27,
+ * works/piv/singlepass.py:498-556): the values (ux, uy) of the num_centers valid
+ * vectors of a pass (cx, cy, selection: the compaction of fi_tps_plan_make;
+ * selection[i] = index of centre i in the pass's nx x ny window grid, whose node
+ * coordinates are ixvecs, iyvecs) interpolated linearly on their Delaunay
+ * triangulation at npts points (px, py), and set to the nearest centre's value
+ * outside the convex hull.  Positions must be half-integers (PIV vector positions
+ * are).  out_x/out_y (float64), rx/ry (nullable, rounded half to even as the next
+ * pass's shifts), flags (nullable, uint8): bit 0 = the point lies in a cell of four
+ * or more cocircular centres (several Delaunay triangulations exist; the triangle
+ * with the smallest centre indices is used), bit 1 = equidistant nearest centres
+ * (the smallest index is used).  scratch: fi_griddata_scratch_ints(nx, ny) int32,
+ * 8-byte aligned.  *status (device int32) = 0, or 1 (a point off the half-integer
+ * lattice), 2 (no certified triangle within 4 grid steps), 3 (bad selection).
+ */
+int fi_griddata(const double* cx, const double* cy, const float* ux, const float* uy,
+                const int32_t* selection, int num_centers, const int32_t* ixvecs, int nx,
+                const int32_t* iyvecs, int ny, const double* px, const double* py, int npts,
+                int32_t* scratch, double* out_x, double* out_y, int32_t* rx, int32_t* ry,
+                uint8_t* flags, int32_t* status, void* stream);
+
+/* Scratch size (int32 elements) of fi_griddata for an nx x ny window grid. */
+int64_t fi_griddata_scratch_ints(int nx, int ny);
+
+/*
  * Smoothed values at the centres, blended over the subdomains that contain them
  * (compute_tps_weights_subdom, thin_plate_spline_subdom.py:128-159).
  */

@@ -48,9 +48,8 @@ def _run(name, **kw):
 
     z = goldens.load(name)
     params = _params(z)
-    interp_last = params.multipass.use_tps is not False
     keep = any(k.endswith("_planes") for k in z.files)
-    work = WorkPIV(params, keep_correls=keep, interp_last=interp_last, **kw)
+    work = WorkPIV(params, keep_correls=keep, **kw)
     res = work.calcul({"arrays": (z["im0"], z["im1"]), "names": ("im0", "im1")})
     torch.cuda.synchronize()
     return z, res
@@ -70,11 +69,21 @@ def _same_errors(got, want, skip=()):
         assert abs(float(gs[1][:-1]) - float(ws[1][:-1])) <= 0.0100001, (k, g, w)
 
 
-def _compare_pass(z, ip, r, report):
-    """Strict comparison outside the flagged near-tie vectors (counted)."""
+def _compare_pass(z, ip, r, report, prev=None):
+    """Strict comparison outside the flagged near-tie vectors (counted).  A vector
+    whose window shift came from an ambiguous griddata point of the previous pass
+    (several Delaunay triangulations; upstream follows Qhull's) and differs from
+    upstream's shift is counted with them."""
     gdx = z[f"p{ip}_deltaxs"]
     gdy = z[f"p{ip}_deltays"]
     tie = r.near_tie_flags != 0
+    amb = getattr(prev, "griddata_tie_flags_approx", None)
+    if amb is not None and f"p{ip}_deltaxs_input" in z.files:
+        moved = ((r.deltaxs_input != z[f"p{ip}_deltaxs_input"])
+                 | (r.deltays_input != z[f"p{ip}_deltays_input"]))
+        assert not (moved & (amb == 0)).any(), "a shift differs at an unambiguous point"
+        tie = tie | moved
+        report.append({"pass": ip, "shifts_from_ambiguous_griddata": int(moved.sum())})
     nt = ~tie
     np.testing.assert_array_equal(np.isnan(r.deltaxs)[nt], np.isnan(gdx)[nt])
     ok = ~np.isnan(gdx) & nt
@@ -88,24 +97,35 @@ def _compare_pass(z, ip, r, report):
     cm = z[f"p{ip}_correls_max"]
     okc = ~np.isnan(cm) & nt
     np.testing.assert_allclose(r.correls_max[okc], cm[okc], rtol=2e-5, atol=2e-6)
-    np.testing.assert_array_equal(np.asarray(r.xs, float), z[f"p{ip}_xs"])
-    np.testing.assert_array_equal(np.asarray(r.ys, float), z[f"p{ip}_ys"])
+    np.testing.assert_array_equal(np.asarray(r.xs, float)[nt], z[f"p{ip}_xs"][nt])
+    np.testing.assert_array_equal(np.asarray(r.ys, float)[nt], z[f"p{ip}_ys"][nt])
     skip = set(np.nonzero(tie)[0].tolist())
     _same_errors(r.errors, goldens.errors(z, ip), skip)
     for key in ("deltaxs_input", "deltays_input"):
         if f"p{ip}_{key}" in z.files:
-            np.testing.assert_array_equal(getattr(r, key), z[f"p{ip}_{key}"])
-    # griddata fields (use_tps=False) are not produced by this backend
-    interp = goldens.params_namespace(z).multipass.use_tps is not False
+            np.testing.assert_array_equal(getattr(r, key)[nt], z[f"p{ip}_{key}"][nt])
+    # interpolated fields; griddata points in cells of cocircular vectors (or with
+    # equidistant nearest vectors) have several valid values (upstream's follows
+    # Qhull's triangulation): they are counted and left out
     for key in ("deltaxs_approx", "deltays_approx", "deltaxs_final", "deltays_final",
                 "deltaxs_smooth", "deltays_smooth"):
-        if f"p{ip}_{key}" in z.files and interp:
-            np.testing.assert_allclose(getattr(r, key), z[f"p{ip}_{key}"], rtol=0, atol=1e-3,
-                                       err_msg=key)
+        if f"p{ip}_{key}" in z.files:
+            got, want = getattr(r, key), z[f"p{ip}_{key}"]
+            flags = getattr(r, "griddata_tie_flags_" + key.split("_")[1], None)
+            sel = np.ones(want.shape, bool) if flags is None else flags == 0
+            if not key.endswith("_approx"):  # on this pass's grid
+                sel &= nt
+            if flags is not None:
+                report.append({"pass": ip, key + "_griddata_ties": int((~sel).sum())})
+            # a window shifted differently (ambiguous griddata) moves its vector: the
+            # TPS of the pass then changes nearby, within the displacement bar
+            atol = 1e-3 if bool(nt.all()) or key.endswith("_approx") else TOL_PX
+            np.testing.assert_allclose(got[sel], want[sel], rtol=0, atol=atol, err_msg=key)
     for key in ("ixvecs_approx", "iyvecs_approx", "ixvecs_final", "iyvecs_final",
                 "xs_smooth", "ys_smooth"):
-        if f"p{ip}_{key}" in z.files and interp:
-            np.testing.assert_array_equal(getattr(r, key), z[f"p{ip}_{key}"], err_msg=key)
+        if f"p{ip}_{key}" in z.files:
+            m = nt if key.endswith("_smooth") else np.ones(z[f"p{ip}_{key}"].shape, bool)
+            np.testing.assert_array_equal(getattr(r, key)[m], z[f"p{ip}_{key}"][m], err_msg=key)
     for key in ("deltaxs_wrong", "deltays_wrong"):
         if f"p{ip}_{key}_keys" in z.files:
             want = {k: v for k, v in goldens.errors(z, ip, key).items() if k not in skip}
@@ -157,14 +177,17 @@ def _compare_secondary(z, ip, r, tie, report):
 
 @pytest.mark.parametrize("name", ["single_pass_c1", "multipass_small", "dmax_two_pass",
                                   "edges_single_pass", "secondary_peaks_two_pass",
+                                  "griddata_two_pass",
                                   "subpix_gaussian_single", "subpix_centroid2_single",
                                   "subpix_none_single"])
 def test_workpiv_matches_reference(name):
     z, res = _run(name)
     assert len(res.passes) == int(z["nb_passes"])
     report = []
+    prev = None
     for ip, r in enumerate(res.passes):
-        _compare_pass(z, ip, r, report)
+        _compare_pass(z, ip, r, report, prev)
+        prev = r
     print(name, report)
 
 
