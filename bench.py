@@ -56,7 +56,7 @@ TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW = (880.266752e6 + 590.642688e6) / 342
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -88,18 +88,28 @@ def _oracle_worker(pair, q):
     q.put(_oracle_sample(pair))
 
 
-def cpu_baseline_single():
+def _oracle_samples(min_seconds):
+    """Oracle multipass on successive 512x512 sample pairs until ``min_seconds`` of
+    work; returns (vectors, seconds, pairs)."""
+    nvec, dt, n = 0, 0.0, 0
+    while dt < min_seconds and n < 200:
+        v, t = _oracle_sample(n)
+        nvec, dt, n = nvec + v, dt + t, n + 1
+    return nvec, dt, n
+
+
+def cpu_baseline_single(min_seconds=10.0):
     env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
     code = ("import sys, json; sys.path.insert(0, %r); import bench; "
-            "print(json.dumps(bench._oracle_sample(0)))" % str(ROOT))
+            "print(json.dumps(bench._oracle_samples(%r)))" % (str(ROOT), float(min_seconds)))
     out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                          timeout=600)
     if out.returncode != 0:
         return None
-    nvec, dt = json.loads(out.stdout.strip().splitlines()[-1])
+    nvec, dt, n = json.loads(out.stdout.strip().splitlines()[-1])
     return {"value": nvec / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"one {SAMPLE_SHAPE[0]}x{SAMPLE_SHAPE[1]} pair of the same workload "
-                      f"({nvec} final vectors, 3 passes + fix + TPS) in {dt:.2f} s, "
+            "sample": f"{n} {SAMPLE_SHAPE[0]}x{SAMPLE_SHAPE[1]} pairs of the same workload "
+                      f"({nvec} final vectors, 3 passes + fix + TPS each) in {dt:.1f} s, "
                       "numpy oracle, 1 thread"}
 
 
@@ -160,21 +170,29 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling every 20 ms; returns once the first sample arrived (the
+        timed region starts after it)."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t_end = time.perf_counter() + 3.0
+        while not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """Summary of the samples read between host times t0 and t1 (all samples
+        when none falls there)."""
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -184,7 +202,10 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        lines = [ln for t, ln in self.lines if t0 is None or t0 <= t <= t1]
+        if not lines:
+            lines = [ln for _, ln in self.lines]
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 7:
                 continue
@@ -247,6 +268,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     launches0 = lib.fi_launch_count()
     clocks.start()
+    t_timed0 = time.perf_counter()
     step_ms = []
     for _ in range(args.steps):
         flush.fill_(1.0)
@@ -261,7 +283,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         step_ms.append(ev0.elapsed_time(ev1))
     torch.cuda.synchronize()
-    clk = clocks.stop()
+    clk = clocks.stop(t_timed0, time.perf_counter())
     launches = lib.fi_launch_count() - launches0
     if dist is not None:
         dist.barrier()
