@@ -36,6 +36,7 @@ struct GdArgs {
   const int32_t* iyvecs;
   int ny;
   const int32_t* nodemap;   // [ny][nx] centre index or -1
+  const int2* cxy;          // doubled centre coordinates (exact: half-integers)
   const int2* hull_left;    // left chain of the hull, increasing Y (doubled coords)
   const int2* hull_right;   // right chain
   const int32_t* hull_n;    // [2]: lengths
@@ -56,9 +57,7 @@ __device__ __forceinline__ long long orient2(long long ax, long long ay, long lo
 }
 
 // doubled coordinates of a centre (exact: positions are half-integers)
-__device__ __forceinline__ int2 centre_xy2(const GdArgs& a, int i) {
-  return make_int2((int)(2.0 * a.cx[i]), (int)(2.0 * a.cy[i]));
-}
+__device__ __forceinline__ int2 centre_xy2(const GdArgs& a, int i) { return a.cxy[i]; }
 
 // largest k with 2 * v[k] <= X2 (-1 if none); v increasing
 __device__ __forceinline__ int floor_index(const int32_t* v, int n, long long X2) {
@@ -117,15 +116,18 @@ __device__ int hull_position(const GdArgs& a, long long X, long long Y, int2* e0
   return res;
 }
 
-__global__ void k_gd_nodemap(const int32_t* sel, int nc, int32_t* nodemap, int nnodes,
-                             int32_t* status) {
+__global__ void k_gd_nodemap(const int32_t* sel, const double* cx, const double* cy, int nc,
+                             int32_t* nodemap, int2* cxy, int nnodes, int32_t* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const int w = sel[i];
-  if (w < 0 || w >= nnodes) {
-    atomicExch(status, 3);
+  const double X = 2.0 * cx[i], Y = 2.0 * cy[i];
+  if (w < 0 || w >= nnodes || X != rint(X) || Y != rint(Y) || fabs(X) > 1e9 || fabs(Y) > 1e9) {
+    atomicExch(status, w < 0 || w >= nnodes ? 3 : 1);
+    cxy[i] = make_int2(0, 0);
     return;
   }
+  cxy[i] = make_int2((int)X, (int)Y);
   nodemap[w] = i;
 }
 
@@ -283,14 +285,16 @@ __device__ __forceinline__ __int128 lifted(const Cand& A, const Cand& B, const C
 
 // incircle(A, B, C, P) > 0 <=> P strictly inside the circle of (A, B, C)
 // (counter-clockwise)
-__device__ __forceinline__ __int128 incircle(const Cand& A, const Cand& B, const Cand& C,
-                                             const Cand& P) {
+// Window coordinates stay below 2^13 (at most 8 grid steps of at most 64 px, doubled),
+// so the terms stay below 2^56: exact in 64-bit integers.
+__device__ __forceinline__ long long incircle(const Cand& A, const Cand& B, const Cand& C,
+                                              const Cand& P) {
   const long long adx = A.dx - P.dx, ady = A.dy - P.dy;
   const long long bdx = B.dx - P.dx, bdy = B.dy - P.dy;
   const long long cdx = C.dx - P.dx, cdy = C.dy - P.dy;
-  return (__int128)(adx * adx + ady * ady) * (bdx * cdy - cdx * bdy) -
-         (__int128)(bdx * bdx + bdy * bdy) * (adx * cdy - cdx * ady) +
-         (__int128)(cdx * cdx + cdy * cdy) * (adx * bdy - bdx * ady);
+  return (adx * adx + ady * ady) * (bdx * cdy - cdx * bdy) -
+         (bdx * bdx + bdy * bdy) * (adx * cdy - cdx * ady) +
+         (cdx * cdx + cdy * cdy) * (adx * bdy - bdx * ady);
 }
 
 __device__ __forceinline__ void sort3(int (&s)[3]) {
@@ -485,13 +489,13 @@ __global__ void __launch_bounds__(128) k_gd_interp(GdArgs a) {
       Cand A = make_cand(a, T[0], X, Y), B = make_cand(a, T[1], X, Y), Cc = make_cand(a, T[2], X, Y);
       orient_ccw(A, B, Cc);
       int inside = -1;
-      __int128 best_det = 0;
+      long long best_det = 0;
       for (int row = r0; row <= r1; ++row)
         for (int col = c0; col <= c1; ++col) {
           const int i = a.nodemap[row * a.nx + col];
           if (i < 0 || i == A.idx || i == B.idx || i == Cc.idx) continue;
           const Cand P = make_cand(a, i, X, Y);
-          const __int128 det = incircle(A, B, Cc, P);
+          const long long det = incircle(A, B, Cc, P);
           if (det > best_det || (det > 0 && det == best_det && i < inside)) {
             best_det = det;
             inside = i;
@@ -533,13 +537,19 @@ __global__ void __launch_bounds__(128) k_gd_interp(GdArgs a) {
     Cand A = make_cand(a, T[0], X, Y), B = make_cand(a, T[1], X, Y), Cc = make_cand(a, T[2], X, Y);
     orient_ccw(A, B, Cc);
     {
-      const double ax = A.dx, ay = A.dy, bx = B.dx, by = B.dy, cx = Cc.dx, cy = Cc.dy;
-      const double d = 2.0 * (ax * (by - cy) + bx * (cy - ay) + cx * (ay - by));
-      const double a2 = ax * ax + ay * ay, b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
-      const double ux = (a2 * (by - cy) + b2 * (cy - ay) + c2 * (ay - by)) / d;
-      const double uy = (a2 * (cx - bx) + b2 * (ax - cx) + c2 * (bx - ax)) / d;
-      const double rad = sqrt((ax - ux) * (ax - ux) + (ay - uy) * (ay - uy)) * (1.0 + 1e-9) + 1e-9;
-      if (!(ux - rad > xlo && ux + rad < xhi && uy - rad > ylo && uy + rad < yhi)) continue;
+      // circumcentre numerators in exact integers, the test in float with a margin
+      // far above its rounding (conservative: a rejected circle only grows the window)
+      const long long ax = A.dx, ay = A.dy, bx = B.dx, by = B.dy, cx = Cc.dx, cy = Cc.dy;
+      const long long dd = 2 * (ax * (by - cy) + bx * (cy - ay) + cx * (ay - by));
+      const long long a2 = ax * ax + ay * ay, b2 = bx * bx + by * by, c2 = cx * cx + cy * cy;
+      const float ux = (float)(a2 * (by - cy) + b2 * (cy - ay) + c2 * (ay - by)) / (float)dd;
+      const float uy = (float)(a2 * (cx - bx) + b2 * (ax - cx) + c2 * (bx - ax)) / (float)dd;
+      const float ex = (float)ax - ux, ey = (float)ay - uy;
+      const float rad = sqrtf(ex * ex + ey * ey);
+      const float mg = 1e-4f * (fabsf(ux) + fabsf(uy) + rad + 1.f);
+      if (!(ux - rad - mg > (float)xlo && ux + rad + mg < (float)xhi &&
+            uy - rad - mg > (float)ylo && uy + rad + mg < (float)yhi))
+        continue;
     }
     // cocircular centres (on the circumcircle): the triangles of that set containing
     // q are all Delaunay; take the smallest sorted index triple, flag the query when
@@ -637,21 +647,23 @@ extern "C" int fi_griddata(const double* cx, const double* cy, const float* ux, 
   const int nnodes = nx * ny;
   FI_REQUIRE(2 * (nx + ny) <= GD_HULL_MAX, "fi_griddata: window grid of %d x %d too large",
              nx, ny);
+  FI_REQUIRE(num_centers <= nnodes, "fi_griddata: more centres than grid nodes");
   int32_t* nodemap = scratch;
-  int2* left = reinterpret_cast<int2*>(scratch + ((nnodes + 1) & ~1));
+  int2* cxy = reinterpret_cast<int2*>(scratch + ((nnodes + 1) & ~1));
+  int2* left = cxy + nnodes;
   int2* right = left + 2 * (nx + ny);
   int32_t* hull_n = reinterpret_cast<int32_t*>(right + 2 * (nx + ny));
-  GdArgs a{cx, cy, ux, uy, num_centers, ixvecs, nx, iyvecs, ny, nodemap, left, right, hull_n,
-           px, py, npts, out_x, out_y, rx, ry, flags, status};
+  GdArgs a{cx, cy, ux, uy, num_centers, ixvecs, nx, iyvecs, ny, nodemap, cxy, left, right,
+           hull_n, px, py, npts, out_x, out_y, rx, ry, flags, status};
   k_gd_fill<<<(nnodes + 255) / 256, 256, 0, s>>>(nodemap, nnodes, -1);
   k_gd_fill<<<1, 32, 0, s>>>(status, 1, 0);
-  k_gd_nodemap<<<(num_centers + 255) / 256, 256, 0, s>>>(selection, num_centers, nodemap,
-                                                         nnodes, status);
+  k_gd_nodemap<<<(num_centers + 255) / 256, 256, 0, s>>>(selection, cx, cy, num_centers,
+                                                         nodemap, cxy, nnodes, status);
   k_gd_hull<<<1, 1024, 0, s>>>(a, left, right, hull_n);
   k_gd_interp<<<(npts + 127) / 128, 128, 0, s>>>(a);
   return check_launch("fi_griddata", 5);
 }
 
 extern "C" int64_t fi_griddata_scratch_ints(int nx, int ny) {
-  return (int64_t)((nx * ny + 1) & ~1) + 8LL * (nx + ny) + 2;
+  return (int64_t)((nx * ny + 1) & ~1) + 2LL * nx * ny + 8LL * (nx + ny) + 2;
 }
