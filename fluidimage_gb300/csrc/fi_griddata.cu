@@ -23,6 +23,7 @@ namespace fi {
 namespace {
 
 constexpr int GD_RMAX = 8;                        // window half-width in grid steps
+                                                  // (then the whole grid)
 constexpr int GD_MAXC = 64;                       // nearest centres of the window kept
 
 struct GdArgs {
@@ -343,10 +344,12 @@ __global__ void __launch_bounds__(128) k_gd_interp(GdArgs a) {
   Cand cand[GD_MAXC];
   uint8_t flag = 0;
   int T[3] = {-1, -1, -1};  // a triangle (centre indices) containing q
-  for (int r = 1; r <= GD_RMAX; ++r) {
-    // nodes of columns [i0 - r + 1, i0 + r] and rows [j0 - r + 1, j0 + r]
-    const int c0 = max(i0 - r + 1, 0), c1 = min(i0 + r, a.nx - 1);
-    const int r0 = max(j0 - r + 1, 0), r1 = min(j0 + r, a.ny - 1);
+  for (int r = 1; r <= GD_RMAX + 1; ++r) {
+    // nodes of columns [i0 - r + 1, i0 + r] and rows [j0 - r + 1, j0 + r]; past
+    // GD_RMAX steps (a large region without vectors) the whole grid
+    const bool all = r > GD_RMAX;
+    const int c0 = all ? 0 : max(i0 - r + 1, 0), c1 = all ? a.nx - 1 : min(i0 + r, a.nx - 1);
+    const int r0 = all ? 0 : max(j0 - r + 1, 0), r1 = all ? a.ny - 1 : min(j0 + r, a.ny - 1);
     int n = 0;
     for (int row = r0; row <= r1; ++row)
       for (int col = c0; col <= c1; ++col) {
@@ -376,10 +379,10 @@ __global__ void __launch_bounds__(128) k_gd_interp(GdArgs a) {
       }
     // exclusive bounds of the region the window covers: a centre of column c has
     // 2 ixvecs[c] <= X2 <= 2 ixvecs[c] + 1
-    const double xlo = (i0 - r >= 0) ? 2.0 * a.ixvecs[i0 - r] + 1.0 - (double)X : -1e300;
-    const double xhi = (i0 + r + 1 < a.nx) ? 2.0 * a.ixvecs[i0 + r + 1] - (double)X : 1e300;
-    const double ylo = (j0 - r >= 0) ? 2.0 * a.iyvecs[j0 - r] + 1.0 - (double)Y : -1e300;
-    const double yhi = (j0 + r + 1 < a.ny) ? 2.0 * a.iyvecs[j0 + r + 1] - (double)Y : 1e300;
+    const double xlo = (!all && i0 - r >= 0) ? 2.0 * a.ixvecs[i0 - r] + 1.0 - (double)X : -1e300;
+    const double xhi = (!all && i0 + r + 1 < a.nx) ? 2.0 * a.ixvecs[i0 + r + 1] - (double)X : 1e300;
+    const double ylo = (!all && j0 - r >= 0) ? 2.0 * a.iyvecs[j0 - r] + 1.0 - (double)Y : -1e300;
+    const double yhi = (!all && j0 + r + 1 < a.ny) ? 2.0 * a.iyvecs[j0 + r + 1] - (double)Y : 1e300;
     if (outside) {
       // nearest centre (ties: smallest index), certified when the nearest distance
       // is below the distance to the uncovered region
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(128) k_gd_interp(GdArgs a) {
     if (a.flags) a.flags[q] = flag;
     return;
   }
-  atomicExch(a.status, 2);  // no certified triangle within GD_RMAX grid steps
+  atomicExch(a.status, 2);  // no certified triangle (cannot happen with the whole grid)
   a.out_x[q] = a.out_y[q] = NAN;
   if (a.rx) a.rx[q] = 0;
   if (a.ry) a.ry[q] = 0;

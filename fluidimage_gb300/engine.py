@@ -470,7 +470,7 @@ def run_griddata(xs, ys, dx, dy, nvec, grid, px, py, npts, stream):
     st = int(np.frombuffer(_readback_raw(status, 4, stream), np.int32)[0])
     if st != 0:
         raise RuntimeError({1: "griddata: a position is off the half-integer lattice",
-                            2: "griddata: a gap of more than 4 grid steps without vectors",
+                            2: "griddata: no Delaunay triangle found",
                             3: "griddata: bad vector selection"}.get(st, f"griddata: {st}"))
     return GridOutput(out_x=cO.tensor(0), out_y=cO.tensor(1), rx=cO.tensor(2),
                       ry=cO.tensor(3), flags=cO.tensor(4), num_centers=nv,

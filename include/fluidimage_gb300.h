@@ -428,7 +428,7 @@ int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, con
  * with the smallest centre indices is used), bit 1 = equidistant nearest centres
  * (the smallest index is used).  scratch: fi_griddata_scratch_ints(nx, ny) int32,
  * 8-byte aligned.  *status (device int32) = 0, or 1 (a point off the half-integer
- * lattice), 2 (no certified triangle within 4 grid steps), 3 (bad selection).
+ * lattice), 2 (no certified triangle: not expected), 3 (bad selection).
  */
 int fi_griddata(const double* cx, const double* cy, const float* ux, const float* uy,
                 const int32_t* selection, int num_centers, const int32_t* ixvecs, int nx,

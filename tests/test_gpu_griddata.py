@@ -81,7 +81,8 @@ def _gpu(ixvecs, iyvecs, cx, cy, sel, vx, vy, qx, qy):
 
 @pytest.mark.parametrize("seed,half,holes,block", [
     (1, True, 0.1, None), (2, True, 0.0, None), (3, False, 0.05, None),
-    (4, True, 0.2, ((5, 11), (7, 14))), (5, False, 0.0, ((0, 4), (0, 5)))])
+    (4, True, 0.2, ((5, 11), (7, 14))), (5, False, 0.0, ((0, 4), (0, 5))),
+    (6, True, 0.05, ((2, 16), (3, 18)))])
 def test_griddata_matches_scipy(seed, half, holes, block):
     ixvecs, iyvecs, cx, cy, sel, vx, vy, qx, qy = _case(seed, half=half, holes=holes,
                                                         hole_block=block)
