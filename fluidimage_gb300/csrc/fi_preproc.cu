@@ -167,6 +167,64 @@ __global__ void k_rank_select(const void* in, int dtype, int64_t nt, int64_t ny,
   }
 }
 
+// The same for 2-D windows (st == 1) of integer and float32 images, by tiles: a
+// block stages its output tile plus the window halo (boundary extension applied
+// once per staged element) as 32-bit keys in shared memory, then each thread runs
+// the radix select over its window there; the select starts at the highest key bit
+// set in the tile (higher bits are zero for every staged value).
+constexpr int RS_TX = 32, RS_TY = 16;
+constexpr int RS_MAX_SMEM = 96 * 1024;
+
+__global__ void __launch_bounds__(RS_TX * RS_TY)
+    k_rank_select_tile(const void* in, int dtype, int64_t ny, int64_t nx, int sy, int sx,
+                       int rank, int mode, uint32_t ckey, void* out) {
+  extern __shared__ uint32_t patch[];
+  __shared__ uint32_t s_or;
+  const int pw = RS_TX + sx - 1, ph = RS_TY + sy - 1;
+  const int64_t t = blockIdx.z;
+  const int64_t x00 = (int64_t)blockIdx.x * RS_TX - sx / 2;
+  const int64_t y00 = (int64_t)blockIdx.y * RS_TY - sy / 2;
+  const int tid = threadIdx.y * RS_TX + threadIdx.x;
+  if (tid == 0) s_or = 0u;
+  __syncthreads();
+  uint32_t acc_or = 0u;
+  for (int e = tid; e < pw * ph; e += RS_TX * RS_TY) {
+    const int py = e / pw, px = e - py * pw;
+    const int64_t yc = extend(y00 + py, ny, mode), xd = extend(x00 + px, nx, mode);
+    const uint32_t v = (yc < 0 || xd < 0) ? ckey
+                                          : (uint32_t)key_of(in, dtype, (t * ny + yc) * nx + xd);
+    patch[e] = v;
+    acc_or |= v;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc_or |= __shfl_xor_sync(0xffffffffu, acc_or, o);
+  if ((tid & 31) == 0) atomicOr(&s_or, acc_or);
+  __syncthreads();
+  const int64_t x = (int64_t)blockIdx.x * RS_TX + threadIdx.x;
+  const int64_t y = (int64_t)blockIdx.y * RS_TY + threadIdx.y;
+  if (x >= nx || y >= ny) return;
+  const uint32_t all = s_or;
+  int top = 31;
+  while (top >= 0 && !((all >> top) & 1u)) --top;
+  uint32_t prefix = 0u;
+  int r = rank;
+  for (int b = top; b >= 0; --b) {
+    const uint32_t hi_mask = (b == 31) ? 0u : (~0u << (b + 1));
+    int zeros = 0;
+    for (int c = 0; c < sy; ++c) {
+      const uint32_t* row = patch + (threadIdx.y + c) * pw + threadIdx.x;
+      for (int d = 0; d < sx; ++d) {
+        const uint32_t v = row[d];
+        zeros += ((v & hi_mask) == prefix && !((v >> b) & 1u)) ? 1 : 0;
+      }
+    }
+    if (r >= zeros) {
+      r -= zeros;
+      prefix |= (1u << b);
+    }
+  }
+  store_key(out, dtype, (t * ny + y) * nx + x, prefix);
+}
+
 // ------------------------------------------------------------------ arithmetic
 // out = img - weight * filt in the numpy result type out_dtype: FI_PRE_F64 /
 // FI_PRE_F32 (float arithmetic; float32 for float32 images), or the image's integer
@@ -310,6 +368,18 @@ extern "C" int fi_rank_filter(const void* in, void* out, int dtype, int nt, int 
     k_minmax_axis<<<g, 256, 0, s>>>(nullptr, 1, k1, dtype, nt, ny, nx, 0, st, mode, ckey, is_max, k0);
     k_keys_to_values<<<g, 256, 0, s>>>(k0, dtype, count, out);
     return check_launch("fi_rank_filter", 4);
+  }
+  const size_t tile_smem = (size_t)(RS_TX + sx - 1) * (RS_TY + sy - 1) * sizeof(uint32_t);
+  if (st == 1 && dtype != FI_PRE_F64 && tile_smem <= RS_MAX_SMEM) {
+    if (tile_smem > 48 * 1024)
+      FI_CUDA_TRY(cudaFuncSetAttribute(k_rank_select_tile,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tile_smem));
+    const dim3 grid((unsigned)((nx + RS_TX - 1) / RS_TX), (unsigned)((ny + RS_TY - 1) / RS_TY),
+                    (unsigned)nt);
+    k_rank_select_tile<<<grid, dim3(RS_TX, RS_TY), tile_smem, s>>>(
+        in, dtype, ny, nx, sy, sx, rank, mode, (uint32_t)ckey, out);
+    return check_launch("fi_rank_filter");
   }
   k_rank_select<<<g, 256, 0, s>>>(in, dtype, nt, ny, nx, st, sy, sx, rank, mode, ckey, out);
   return check_launch("fi_rank_filter");
