@@ -44,6 +44,17 @@ ERROR_STRINGS = {
 _F32_1EM8 = np.float32(1e-8)
 
 
+def _f32_pow2(a):
+    """``x ** 2`` on float32 scalars as numpy evaluates it in the upstream source
+    (subpix.py:57-58, :201): through the C library's ``powf``, which can round a
+    near-tie the other way from ``x * x`` (4.2536864**2 lies 0.49994 ulp above a
+    float32; ``powf`` returns the upper neighbour).  Element by element for that
+    reason; the CUDA kernels use the correctly rounded product."""
+    a = np.asarray(a, dtype=np.float32)
+    return np.fromiter((v ** 2 for v in a.ravel()), dtype=np.float32,
+                       count=a.size).reshape(a.shape)
+
+
 # ----------------------------------------------------------------------------------
 # a1: window grid — works/piv/singlepass.py:108-141 and _init_crop :363-389
 # ----------------------------------------------------------------------------------
@@ -402,7 +413,7 @@ def _gaussian2(crops):
         c11 = c11 / np.float32(4)
         c20 = c20 / np.float32(6)
         c02 = c02 / np.float32(6)
-        den = np.float32(4) * c20 * c02 - c11 * c11
+        den = np.float32(4) * c20 * c02 - _f32_pow2(c11)
         deplx = (c11 * c01 - np.float32(2) * c10 * c02) / den
         deply = (c11 * c10 - np.float32(2) * c01 * c20) / den
     return deplx, deply
@@ -426,7 +437,7 @@ def subpix_2d_gaussian2(planes, i0, i1, shape_crop):
     crops = planes[idx[:, None, None], r, c]
     deplx, deply = _gaussian2(crops)
     with np.errstate(invalid="ignore", over="ignore"):
-        big = (deplx * deplx + deply * deply) > np.float32(4.5)
+        big = (_f32_pow2(deplx) + _f32_pow2(deply)) > np.float32(4.5)
     dx = np.empty(nvec, dtype=np.float32)
     dy = np.empty(nvec, dtype=np.float32)
     wrong = np.zeros(nvec, dtype=bool)

@@ -217,6 +217,20 @@ def case_griddata():
     })
 
 
+def case_griddata_oseen():
+    """Config-2 recipe on a 384x384 uint16 Oseen pair with use_tps=False: griddata
+    between the three passes and at the end (the setting of most upstream examples)."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = synthetic.oseen_vortex((384, 384), d_max=6.0, rc=60.0)
+    im0, im1 = synthetic.make_pair((384, 384), field, model, seed=7000)
+    run_workpiv("griddata_oseen_three_pass", im0, im1, {
+        "piv0.shape_crop_im0": 64, "piv0.grid.overlap": 0.5,
+        "multipass.number": 3, "multipass.coeff_zoom": 2, "multipass.use_tps": False,
+        "fix.threshold_diff_neighbour": 2,
+    })
+
+
 def case_secondary_peaks():
     """nb_peaks_to_search=3 with WorkFIX secondary-peak replacement, two passes with
     TPS (32 -> 16 px windows): two particle populations moving by (3, 1) and
@@ -332,6 +346,7 @@ CASES = {
     "dmax_two_pass": case_dmax,
     "edges_single_pass": case_edges,
     "griddata_two_pass": case_griddata,
+    "griddata_oseen_three_pass": case_griddata_oseen,
     "secondary_peaks_two_pass": case_secondary_peaks,
     "subpix_methods": case_subpix_methods,
     "preproc": case_preproc,

@@ -177,7 +177,7 @@ def _compare_secondary(z, ip, r, tie, report):
 
 @pytest.mark.parametrize("name", ["single_pass_c1", "multipass_small", "dmax_two_pass",
                                   "edges_single_pass", "secondary_peaks_two_pass",
-                                  "griddata_two_pass",
+                                  "griddata_two_pass", "griddata_oseen_three_pass",
                                   "subpix_gaussian_single", "subpix_centroid2_single",
                                   "subpix_none_single"])
 def test_workpiv_matches_reference(name):
