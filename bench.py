@@ -231,6 +231,24 @@ def _peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Element-wise maximum over ranks of per-rank times (the slowest replica sets
+    the job's time); ``values`` unchanged on one process."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_throughput(units_per_rank, world, ms):
+    """Whole-job units/s of ``world`` replicas that each processed
+    ``units_per_rank`` units in ``ms`` (the maximum over ranks)."""
+    return world * units_per_rank / (ms / 1e3)
+
+
 def run_gpu(args):
     import torch
 
@@ -288,11 +306,6 @@ def run_gpu(args):
     if dist is not None:
         dist.barrier()
     ms = statistics.mean(step_ms)
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nvec_final / (ms / 1e3)
 
     # ---- end to end through the public API (pinned host images -> host results)
     h0 = torch.from_numpy(im0.view(np.int16)).pin_memory()
@@ -331,8 +344,13 @@ def run_gpu(args):
         pass
     torch.cuda.synchronize()
     series_ms = 1e3 * (time.perf_counter() - t_start) / n_series
-    e2e_value = world * nvec_final / (series_ms / 1e3)
-    single_value = world * nvec_final / (statistics.mean(single_ms) / 1e3)
+    if dist is not None:
+        dist.barrier()
+    ms, series_ms, single_mean = max_over_ranks(
+        [ms, series_ms, statistics.mean(single_ms)], dist, dev)
+    value = replica_throughput(nvec_final, world, ms)
+    e2e_value = replica_throughput(nvec_final, world, series_ms)
+    single_value = replica_throughput(nvec_final, world, single_mean)
 
     if rank != 0:
         if dist is not None:
@@ -360,7 +378,7 @@ def run_gpu(args):
                 "api": f"WorkPIV.calcul_series over {n_series} pairs, 2 pairs in flight "
                        "(own host thread and CUDA stream each)",
                 "single_call": {"value": single_value, "unit": UNIT,
-                                "ms_per_step": statistics.mean(single_ms),
+                                "ms_per_step": single_mean,
                                 "api": "WorkPIV.calcul, one pair per call, L2 flushed before"}},
         "gpu_launches": int(launches),
         "tps_subdomains": int(sum(t.nb_subdom for pd in outs for t in (pd.tps_next, pd.tps_final)

@@ -69,11 +69,26 @@ def _same_errors(got, want, skip=()):
         assert abs(float(gs[1][:-1]) - float(ws[1][:-1])) <= 0.0100001, (k, g, w)
 
 
+def _griddata_of(r, key):
+    """The oracle's ``griddata`` (scipy, linear then nearest) of the pass's own
+    vectors onto the grid of field ``key`` (``..._approx`` or ``..._final``)."""
+    from oracle import piv as O
+
+    kind = key.split("_")[1]
+    gx = np.asarray(getattr(r, "ixvecs_" + kind))
+    gy = np.asarray(getattr(r, "iyvecs_" + kind))
+    sel = ~(np.isnan(r.deltaxs) | np.isnan(r.deltays))
+    comp = r.deltaxs if key.startswith("deltaxs") else r.deltays
+    centers = np.vstack([np.asarray(r.xs, float)[sel], np.asarray(r.ys, float)[sel]])
+    return O.griddata(centers, np.asarray(comp, np.float64)[sel], np.unique(gx),
+                      np.unique(gy))
+
+
 def _compare_pass(z, ip, r, report, prev=None):
     """Strict comparison outside the flagged near-tie vectors (counted).  A vector
     whose window shift came from an ambiguous griddata point of the previous pass
-    (several Delaunay triangulations; upstream follows Qhull's) and differs from
-    upstream's shift is counted with them."""
+    (several Delaunay triangulations; upstream follows Qhull's), or from a triangle
+    holding such a vector, and differs from upstream's shift is counted with them."""
     gdx = z[f"p{ip}_deltaxs"]
     gdy = z[f"p{ip}_deltays"]
     tie = r.near_tie_flags != 0
@@ -81,7 +96,15 @@ def _compare_pass(z, ip, r, report, prev=None):
     if amb is not None and f"p{ip}_deltaxs_input" in z.files:
         moved = ((r.deltaxs_input != z[f"p{ip}_deltaxs_input"])
                  | (r.deltays_input != z[f"p{ip}_deltays_input"]))
-        assert not (moved & (amb == 0)).any(), "a shift differs at an unambiguous point"
+        odd = moved & (amb == 0)
+        if odd.any():
+            # an unambiguous point whose triangle holds a vector of the previous pass
+            # that differs from upstream's (a near-tie, or itself moved): the shift
+            # must be upstream's rule, round(griddata), applied to the GPU's vectors
+            for comp in ("deltaxs", "deltays"):
+                want = np.round(_griddata_of(prev, comp + "_approx")).astype(np.int32)
+                np.testing.assert_array_equal(getattr(r, comp + "_input")[odd], want[odd],
+                                              err_msg="a shift differs at an unambiguous point")
         tie = tie | moved
         report.append({"pass": ip, "shifts_from_ambiguous_griddata": int(moved.sum())})
     nt = ~tie
@@ -117,6 +140,14 @@ def _compare_pass(z, ip, r, report, prev=None):
                 sel &= nt
             if flags is not None:
                 report.append({"pass": ip, key + "_griddata_ties": int((~sel).sum())})
+            if flags is not None and not bool(nt.all()):
+                # a vector moved by an ambiguous shift (or a near-tie peak) changes
+                # the linear interpolation over its triangles: the GPU field is then
+                # checked against scipy's griddata of the GPU's own vectors
+                want = _griddata_of(r, key)
+                np.testing.assert_allclose(got[sel], want[sel], rtol=0, atol=1e-5,
+                                           err_msg=key)
+                continue
             # a window shifted differently (ambiguous griddata) moves its vector: the
             # TPS of the pass then changes nearby, within the displacement bar
             atol = 1e-3 if bool(nt.all()) or key.endswith("_approx") else TOL_PX
