@@ -152,14 +152,22 @@ __device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const 
     for (int q = 0; q < 4; ++q) H[q] = Lo[q] = make_float2(0.f, 0.f);
     const float2* col = B + (int64_t)c0 * ld;
     const int nc = min(4, m - c0);
+    // two rows per lane and load (16 bytes: twice the bytes in flight per load); ld
+    // is a multiple of 4, so row r + 1 < ld; the padding rows past m are masked
 #pragma unroll 2
-    for (int r = lane; r < m; r += 32) {
-      const float2 a = zx[r], b = zy[r];
-      const float2 zh = make_float2(a.x, b.x), zl = make_float2(a.y, b.y);
+    for (int r = 2 * lane; r < m; r += 64) {
+      const float4 a = *reinterpret_cast<const float4*>(zx + r);
+      const float4 b = *reinterpret_cast<const float4*>(zy + r);
+      const float2 zh0 = make_float2(a.x, b.x), zl0 = make_float2(a.y, b.y);
+      const float2 zh1 = make_float2(a.z, b.z), zl1 = make_float2(a.w, b.w);
+      const bool two = r + 1 < m;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const float2 v = (q < nc) ? __ldcs(col + (int64_t)q * ld + r) : make_float2(0.f, 0.f);
-        df_mac_x2(v, zh, zl, H[q], Lo[q]);
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (q < nc) v = __ldcs(reinterpret_cast<const float4*>(col + (int64_t)q * ld + r));
+        if (!two) v.z = v.w = 0.f;
+        df_mac_x2(make_float2(v.x, v.y), zh0, zl0, H[q], Lo[q]);
+        df_mac_x2(make_float2(v.z, v.w), zh1, zl1, H[q], Lo[q]);
       }
     }
     float h[8], l[8];
@@ -238,142 +246,6 @@ __device__ void apply_reflectors2(const double* V, int vstride, const double* ta
     for (int i = threadIdx.x; i < n; i += NT) {
       x[i] -= cx * v[i];
       y[i] -= cy * v[i];
-    }
-    __syncthreads();
-  }
-}
-
-// Solve (L L^T) x = r in place for two right-hand sides (float).  L: lower m x m,
-// column-major, leading dimension ld (a multiple of 4, 16-byte aligned base); only
-// its lower triangle is read.  rx, ry: shared, 16-byte aligned, zero from m up to a
-// multiple of 32.  By tiles of 32: the diagonal tile in one warp (shuffles, rows or
-// columns of L in registers), the off-diagonal tiles by all warps with coalesced
-// (forward) or contiguous float4 (backward) loads and float4 broadcasts of x.
-// part: 64 * warps floats.
-template <int NT>
-__device__ void chol_solve2(const float* __restrict__ L, int m, int ld, float* rx, float* ry,
-                            float* part) {
-  constexpr int NW = NT / 32;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned full = 0xffffffffu;
-  const int T = (m + 31) / 32;
-  // ---- forward: L y = r
-  for (int k = 0; k < T; ++k) {
-    const int r0 = 32 * k;
-    if (wid == 0) {
-      const int r = r0 + lane;
-      float Lrow[32];  // row r of the diagonal tile (entries right of the diagonal unused)
-#pragma unroll
-      for (int c = 0; c < 32; ++c) Lrow[c] = (r < m && r0 + c < m) ? L[(int64_t)(r0 + c) * ld + r] : 0.f;
-      const float inv = (r < m) ? 1.f / L[(int64_t)r * ld + r] : 1.f;
-      float vx = rx[r], vy = ry[r];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        if (lane == j) {
-          vx *= inv;
-          vy *= inv;
-        }
-        const float xj = __shfl_sync(full, vx, j), yj = __shfl_sync(full, vy, j);
-        if (lane > j) {
-          vx = fmaf(-Lrow[j], xj, vx);
-          vy = fmaf(-Lrow[j], yj, vy);
-        }
-      }
-      rx[r] = vx;
-      ry[r] = vy;
-    }
-    __syncthreads();
-    // r_i -= L_ik y_k for the tiles i > k (their rows are below m only in full tiles k)
-    for (int i = k + 1 + wid; i < T; i += NW) {
-      const int r = 32 * i + lane;
-      if (r < m) {
-        float sx = 0.f, sy = 0.f;
-        const float* Lc = L + (int64_t)r0 * ld + r;
-#pragma unroll
-        for (int c4 = 0; c4 < 8; ++c4) {
-          const float4 yx = *reinterpret_cast<const float4*>(rx + r0 + 4 * c4);
-          const float4 yy = *reinterpret_cast<const float4*>(ry + r0 + 4 * c4);
-          const float l0 = Lc[(int64_t)(4 * c4) * ld], l1 = Lc[(int64_t)(4 * c4 + 1) * ld];
-          const float l2 = Lc[(int64_t)(4 * c4 + 2) * ld], l3 = Lc[(int64_t)(4 * c4 + 3) * ld];
-          sx = fmaf(l0, yx.x, sx);
-          sy = fmaf(l0, yy.x, sy);
-          sx = fmaf(l1, yx.y, sx);
-          sy = fmaf(l1, yy.y, sy);
-          sx = fmaf(l2, yx.z, sx);
-          sy = fmaf(l2, yy.z, sy);
-          sx = fmaf(l3, yx.w, sx);
-          sy = fmaf(l3, yy.w, sy);
-        }
-        rx[r] -= sx;
-        ry[r] -= sy;
-      }
-    }
-    __syncthreads();
-  }
-  // ---- backward: L^T x = y
-  for (int k = T - 1; k >= 0; --k) {
-    const int c0 = 32 * k;
-    const int t = c0 + lane;  // this lane's column
-    float px = 0.f, py = 0.f;
-    for (int i = k + 1 + wid; i < T; i += NW) {  // column t is below m here
-      const float* Lc = L + (int64_t)t * ld + 32 * i;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int row = 32 * i + 4 * q;
-        float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (row < ld) lv = *reinterpret_cast<const float4*>(Lc + 4 * q);
-        if (row + 0 >= m) lv.x = 0.f;
-        if (row + 1 >= m) lv.y = 0.f;
-        if (row + 2 >= m) lv.z = 0.f;
-        if (row + 3 >= m) lv.w = 0.f;
-        const float4 xv = *reinterpret_cast<const float4*>(rx + row);
-        const float4 yv = *reinterpret_cast<const float4*>(ry + row);
-        px = fmaf(lv.x, xv.x, px);
-        py = fmaf(lv.x, yv.x, py);
-        px = fmaf(lv.y, xv.y, px);
-        py = fmaf(lv.y, yv.y, py);
-        px = fmaf(lv.z, xv.z, px);
-        py = fmaf(lv.z, yv.z, py);
-        px = fmaf(lv.w, xv.w, px);
-        py = fmaf(lv.w, yv.w, py);
-      }
-    }
-    part[wid * 64 + lane] = px;
-    part[wid * 64 + 32 + lane] = py;
-    __syncthreads();
-    if (wid == 0) {
-      float vx = rx[t], vy = ry[t];
-#pragma unroll
-      for (int w = 0; w < NW; ++w) {
-        vx -= part[w * 64 + lane];
-        vy -= part[w * 64 + 32 + lane];
-      }
-      float Lcol[32];  // Lcol[j] = L[c0 + j][t] (column t of the diagonal tile)
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int row = c0 + 4 * q;
-        float4 lv = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (t < m && row < ld) lv = *reinterpret_cast<const float4*>(L + (int64_t)t * ld + row);
-        Lcol[4 * q] = (row < m) ? lv.x : 0.f;
-        Lcol[4 * q + 1] = (row + 1 < m) ? lv.y : 0.f;
-        Lcol[4 * q + 2] = (row + 2 < m) ? lv.z : 0.f;
-        Lcol[4 * q + 3] = (row + 3 < m) ? lv.w : 0.f;
-      }
-      const float inv = (t < m) ? 1.f / L[(int64_t)t * ld + t] : 1.f;
-#pragma unroll
-      for (int j = 31; j >= 0; --j) {
-        if (lane == j) {
-          vx *= inv;
-          vy *= inv;
-        }
-        const float xj = __shfl_sync(full, vx, j), yj = __shfl_sync(full, vy, j);
-        if (lane < j) {
-          vx = fmaf(-Lcol[j], xj, vx);
-          vy = fmaf(-Lcol[j], yj, vy);
-        }
-      }
-      rx[t] = vx;
-      ry[t] = vy;
     }
     __syncthreads();
   }
@@ -551,6 +423,203 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
   return *s_flag == 0;
 }
 
+// Inverses of the diagonal tiles of the factor L (lower, column-major, ld), for
+// chol_solve2: tile k's inverse (lower triangular) packed by columns at dinv + 528 k,
+// column c holding rows c..31 from tri_colstart(c).  Reading row i (fixed column,
+// consecutive rows) or column c (rows i >= c: offsets that are triangular numbers
+// apart, distinct modulo 32) is free of bank conflicts.  Rows and columns past m are
+// the identity's.
+__device__ __forceinline__ int tri_colstart(int c) { return 32 * c - (c * (c - 1)) / 2; }
+constexpr int TRI_TILE = 528;  // 32 * 33 / 2
+
+template <int NT>
+__device__ void chol_diag_inverses(const float* __restrict__ L, int m, int ld, float* dinv) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  const int T = (m + 31) / 32;
+  for (int k = wid; k < T; k += NW) {
+    float a[32];  // a[j] = L[32 k + lane][32 k + j] (only j <= lane is read below)
+    tile_load(L, m, ld, k, k, a, lane);
+    float dl = 1.f;  // L[lane][lane] (constant indices keep a[] in registers)
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if (j == lane) dl = a[j];
+    const float rdiag = 1.f / dl;
+    // lane i: row i of X = inv(L_kk), right-looking: row j is final once scaled by
+    // 1 / L_jj, then every later row i takes off L_ij X_j (independent columns: the
+    // dependent chain is 32 steps long, not 528)
+    float x[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) x[c] = (c == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const float rj = __shfl_sync(full, rdiag, j);
+#pragma unroll
+      for (int c = 0; c <= j; ++c) {
+        const float xjc = __shfl_sync(full, x[c], j) * rj;
+        if (lane == j)
+          x[c] = xjc;
+        else if (lane > j)
+          x[c] = fmaf(-a[j], xjc, x[c]);
+      }
+    }
+    float* D = dinv + TRI_TILE * k + lane;
+#pragma unroll
+    for (int c = 0; c < 32; ++c)
+      if (c <= lane) D[tri_colstart(c) - c] = x[c];
+  }
+  __syncthreads();
+}
+
+// Solve (L L^T) x = r in place for two right-hand sides (float).  L: lower m x m,
+// column-major, leading dimension ld (a multiple of 4, 16-byte aligned base); only
+// its lower triangle is read.  rx, ry: shared, 16-byte aligned, zero from m up to a
+// multiple of 32.  dinv: the diagonal tiles' inverses (chol_diag_inverses), so that
+// a diagonal step is a triangular product in one warp instead of a chain of 32
+// dependent shuffles.  By tiles of 32: the off-diagonal tiles by all warps with
+// coalesced (forward) or contiguous float4 (backward) loads, issued before the
+// barrier that publishes the diagonal step (their values do not depend on it), and
+// float4 broadcasts of x.  part: 64 * warps floats.
+template <int NT>
+__device__ void chol_solve2(const float* __restrict__ L, int m, int ld, float* rx, float* ry,
+                            float* part, const float* dinv) {
+  constexpr int NW = NT / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int T = (m + 31) / 32;
+  // ---- forward: L y = r
+  for (int k = 0; k < T; ++k) {
+    const int r0 = 32 * k;
+    // this warp's first off-diagonal tile (k + 1 + wid), loaded ahead
+    const int ia = k + 1 + wid;
+    const int ra = 32 * ia + lane;
+    float la[32];
+    if (ia < T && ra < m) {
+      const float* Lc = L + (int64_t)r0 * ld + ra;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) la[c] = Lc[(int64_t)c * ld];
+    }
+    if (wid == 0) {
+      // y_k = inv(L_kk) r_k: lane i sums row i of the inverse
+      const float* D = dinv + TRI_TILE * k + lane;
+      float vx = 0.f, vy = 0.f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j <= lane) {
+          const float l = D[tri_colstart(j) - j];
+          vx = fmaf(l, rx[r0 + j], vx);
+          vy = fmaf(l, ry[r0 + j], vy);
+        }
+      }
+      __syncwarp();
+      rx[r0 + lane] = vx;
+      ry[r0 + lane] = vy;
+    }
+    __syncthreads();
+    // r_i -= L_ik y_k for the tiles i > k (their rows are below m only in full tiles k)
+    for (int i = ia; i < T; i += NW) {
+      const int r = 32 * i + lane;
+      if (r < m) {
+        if (i != ia) {
+          const float* Lc = L + (int64_t)r0 * ld + r;
+#pragma unroll
+          for (int c = 0; c < 32; ++c) la[c] = Lc[(int64_t)c * ld];
+        }
+        float sx = 0.f, sy = 0.f, sx2 = 0.f, sy2 = 0.f;
+#pragma unroll
+        for (int c4 = 0; c4 < 8; c4 += 2) {
+          const float4 yx = *reinterpret_cast<const float4*>(rx + r0 + 4 * c4);
+          const float4 yy = *reinterpret_cast<const float4*>(ry + r0 + 4 * c4);
+          const float4 yx2 = *reinterpret_cast<const float4*>(rx + r0 + 4 * c4 + 4);
+          const float4 yy2 = *reinterpret_cast<const float4*>(ry + r0 + 4 * c4 + 4);
+          sx = fmaf(la[4 * c4], yx.x, sx);
+          sy = fmaf(la[4 * c4], yy.x, sy);
+          sx = fmaf(la[4 * c4 + 1], yx.y, sx);
+          sy = fmaf(la[4 * c4 + 1], yy.y, sy);
+          sx = fmaf(la[4 * c4 + 2], yx.z, sx);
+          sy = fmaf(la[4 * c4 + 2], yy.z, sy);
+          sx = fmaf(la[4 * c4 + 3], yx.w, sx);
+          sy = fmaf(la[4 * c4 + 3], yy.w, sy);
+          sx2 = fmaf(la[4 * c4 + 4], yx2.x, sx2);
+          sy2 = fmaf(la[4 * c4 + 4], yy2.x, sy2);
+          sx2 = fmaf(la[4 * c4 + 5], yx2.y, sx2);
+          sy2 = fmaf(la[4 * c4 + 5], yy2.y, sy2);
+          sx2 = fmaf(la[4 * c4 + 6], yx2.z, sx2);
+          sy2 = fmaf(la[4 * c4 + 6], yy2.z, sy2);
+          sx2 = fmaf(la[4 * c4 + 7], yx2.w, sx2);
+          sy2 = fmaf(la[4 * c4 + 7], yy2.w, sy2);
+        }
+        rx[r] -= sx + sx2;
+        ry[r] -= sy + sy2;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- backward: L^T x = y
+  for (int k = T - 1; k >= 0; --k) {
+    const int c0 = 32 * k;
+    const int t = c0 + lane;  // this lane's column
+    float px = 0.f, py = 0.f;
+    for (int i = k + 1 + wid; i < T; i += NW) {  // column t is below m here
+      const float* Lc = L + (int64_t)t * ld + 32 * i;
+      float4 lv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int row = 32 * i + 4 * q;
+        lv[q] = (row < ld) ? *reinterpret_cast<const float4*>(Lc + 4 * q)
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row + 0 >= m) lv[q].x = 0.f;
+        if (row + 1 >= m) lv[q].y = 0.f;
+        if (row + 2 >= m) lv[q].z = 0.f;
+        if (row + 3 >= m) lv[q].w = 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int row = 32 * i + 4 * q;
+        const float4 xv = *reinterpret_cast<const float4*>(rx + row);
+        const float4 yv = *reinterpret_cast<const float4*>(ry + row);
+        px = fmaf(lv[q].x, xv.x, px);
+        py = fmaf(lv[q].x, yv.x, py);
+        px = fmaf(lv[q].y, xv.y, px);
+        py = fmaf(lv[q].y, yv.y, py);
+        px = fmaf(lv[q].z, xv.z, px);
+        py = fmaf(lv[q].z, yv.z, py);
+        px = fmaf(lv[q].w, xv.w, px);
+        py = fmaf(lv[q].w, yv.w, py);
+      }
+    }
+    part[wid * 64 + lane] = px;
+    part[wid * 64 + 32 + lane] = py;
+    __syncthreads();
+    if (wid == 0) {
+      float vx = rx[t], vy = ry[t];
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        vx -= part[w * 64 + lane];
+        vy -= part[w * 64 + 32 + lane];
+      }
+      rx[t] = vx;
+      ry[t] = vy;
+      __syncwarp();
+      // x_k = inv(L_kk)^T v_k: lane c sums column c of the inverse (rows i >= c)
+      const float* D = dinv + TRI_TILE * k + tri_colstart(lane) - lane;
+      float sx = 0.f, sy = 0.f;
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        if (i >= lane) {
+          const float l = D[i];
+          sx = fmaf(l, rx[c0 + i], sx);
+          sy = fmaf(l, ry[c0 + i], sy);
+        }
+      }
+      __syncwarp();
+      rx[t] = sx;
+      ry[t] = sy;
+    }
+    __syncthreads();
+  }
+}
+
 // Shared-memory layout of k_tps_solve_mp for subdomains of at most n centres.
 struct MpLayout {
   int np;        // n rounded up to 32
@@ -558,7 +627,7 @@ struct MpLayout {
   size_t f2_off; // float2: zx, zy, gx, gy (np each)
   size_t f_off;  // float: vx, vy, rx, ry (np each)
   size_t i2_off; // int2: lattice coordinates (np)
-  size_t p_off;  // panel: (2 + warps) * 32 * TS floats
+  size_t p_off;  // panel: (2 + warps) * 32 * TS floats at least
   size_t bytes;
   __host__ __device__ MpLayout(int n, int warps) {
     np = (n + 31) & ~31;
@@ -571,6 +640,9 @@ struct MpLayout {
     // sums; the Cholesky scratch starts at f2_off (the f2, f and i2 regions are free
     // while it runs)
     size_t pbytes = (size_t)(2 + warps) * 32 * TS * sizeof(float);
+    // the solves: per-warp partial sums, then the diagonal tiles' inverses
+    const size_t sol = ((size_t)64 * warps + (size_t)((n + 31) / 32) * TRI_TILE) * sizeof(float);
+    if (pbytes < sol) pbytes = sol;
     const size_t chol = chol_scratch_bytes(n);
     if (f2_off + chol > p_off + pbytes) pbytes = f2_off + chol - p_off;
     bytes = p_off + pbytes;
@@ -1036,6 +1108,10 @@ __global__ void __launch_bounds__(NT, 512 / NT)
                        &s_next))
     return;
 
+  // the diagonal tiles' inverses, after the per-warp partial sums of the solves
+  float* dinv = panel + 64 * NW;
+  chol_diag_inverses<NT>(L32, m, mp, dinv);
+
   // ---- outlier iterations with refined solves (x and y in lockstep)
   double* tx = W;
   double* ty = W + n;
@@ -1084,7 +1160,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
       } else {
         residual_df2<NT>(B2, m, mp, zx2, zy2, gx2, gy2, rx, ry);
       }
-      chol_solve2<NT>(L32, m, mp, rx, ry, panel);
+      chol_solve2<NT>(L32, m, mp, rx, ry, panel, dinv);
       ++nsweeps;
       double dmax = 0.0, zmax = 0.0;
       for (int i = threadIdx.x; i < m; i += NT) {
