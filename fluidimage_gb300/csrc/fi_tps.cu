@@ -132,24 +132,61 @@ __device__ __forceinline__ double block_reduce_d(double v, double* sh, bool is_m
   return v;
 }
 
+// float -> double, exact, by the IEEE 754 bit layouts on the integer pipe (normal
+// numbers; zero, subnormals, infinities and NaN through the hardware conversion)
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
 // Compaction of the valid vectors (no NaN component) in index order, limits and
-// subdomain layout; one block over tiles of 1024 consecutive vectors, the loads of
-// eight tiles issued before their block scans.
+// subdomain layout; one block of 32 warps, each over one contiguous segment of the
+// vectors: the warps count their valid vectors, one block scan places the segments,
+// then each warp writes its vectors in order (ballots within the warp), with the
+// loads of four chunks of 32 issued before they are used.
 __global__ void __launch_bounds__(1024)
     k_tps_plan(const float* xs, const float* ys, const float* dx, const float* dy, int nvec,
                int subdom_size, double smoothing_coef, double pct, fi_tps_plan* plan, double* cx,
                double* cy, float* ux, float* uy, int32_t* sel) {
-  constexpr int R = 8;
+  constexpr int R = 4;
   __shared__ int warp_tot[33];
   __shared__ double red[33];
-  double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
-  int base = 0;
-  for (int c0 = 0; c0 < nvec; c0 += R * 1024) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int seg = (((nvec + nw - 1) / nw) + 31) & ~31;
+  const int s0 = min(nvec, wid * seg), s1 = min(nvec, s0 + seg);
+  int cnt = 0;
+#pragma unroll 4
+  for (int i = s0 + lane; i < s1; i += 32) cnt += (isnan(dx[i]) || isnan(dy[i])) ? 0 : 1;
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) warp_tot[wid] = cnt;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = lane < nw ? warp_tot[lane] : 0;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane < nw) warp_tot[lane] = incl - v;
+    if (lane == 31) warp_tot[32] = incl;
+  }
+  __syncthreads();
+  const int base = warp_tot[32];
+  int pos = warp_tot[wid];
+  // limits in float32 (exact: the positions are float32); FP64 is narrow on this GPU
+  // and one block does all the vectors
+  float fxmin = INFINITY, fxmax = -INFINITY, fymin = INFINITY, fymax = -INFINITY;
+  for (int c0 = s0; c0 < s1; c0 += R * 32) {
     float vx[R], vy[R], px[R], py[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int i = c0 + r * 1024 + threadIdx.x;
-      const bool in = i < nvec;
+      const int i = c0 + 32 * r + lane;
+      const bool in = i < s1;
       vx[r] = in ? dx[i] : NAN;
       vy[r] = in ? dy[i] : NAN;
       px[r] = in ? xs[i] : 0.f;
@@ -157,26 +194,25 @@ __global__ void __launch_bounds__(1024)
     }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      if (c0 + r * 1024 >= nvec) break;  // uniform over the block
-      const int i = c0 + r * 1024 + threadIdx.x;
+      const int i = c0 + 32 * r + lane;
       const bool ok = !(isnan(vx[r]) || isnan(vy[r]));
-      int total;
-      const int pos = base + block_scan_flag(ok, warp_tot, &total);
+      const unsigned b = __ballot_sync(0xffffffffu, ok);
       if (ok) {
-        const double x = (double)px[r], y = (double)py[r];
-        cx[pos] = x;
-        cy[pos] = y;
-        ux[pos] = vx[r];
-        uy[pos] = vy[r];
-        if (sel) sel[pos] = i;
-        xmin = fmin(xmin, x);
-        xmax = fmax(xmax, x);
-        ymin = fmin(ymin, y);
-        ymax = fmax(ymax, y);
+        const int at = pos + __popc(b & ((1u << lane) - 1u));
+        cx[at] = f2d_exact(px[r]);
+        cy[at] = f2d_exact(py[r]);
+        ux[at] = vx[r];
+        uy[at] = vy[r];
+        if (sel) sel[at] = i;
+        fxmin = fminf(fxmin, px[r]);
+        fxmax = fmaxf(fxmax, px[r]);
+        fymin = fminf(fymin, py[r]);
+        fymax = fmaxf(fymax, py[r]);
       }
-      base += total;
+      pos += __popc(b);
     }
   }
+  double xmin = fxmin, xmax = fxmax, ymin = fymin, ymax = fymax;
   xmin = block_reduce_d(xmin, red, false);
   xmax = block_reduce_d(xmax, red, true);
   ymin = block_reduce_d(ymin, red, false);
@@ -387,6 +423,34 @@ __device__ __forceinline__ int lower_bound_ge(const double* a, int n, double v) 
   return lo;
 }
 
+// First index q in [0, n) with a[q] >= v for a non-decreasing a (n if none), by one
+// warp: each round probes 32 evenly spaced entries and keeps the part holding the
+// answer (ceil(log32 n) rounds of loads instead of log2 n dependent loads).
+__device__ __forceinline__ int warp_lower_bound_ge(const double* a, int n, double v, int lane) {
+  int lo = 0, hi = n;  // the answer lies in [lo, hi]
+  while (lo < hi) {
+    const int step = (hi - lo + 31) / 32;
+    const int at = lo + (lane + 1) * step - 1;  // last entry of part `lane`
+    const bool ge = at >= hi || a[at] >= v;
+    const unsigned b = __ballot_sync(0xffffffffu, ge);
+    if (b == 0u) return hi;  // every entry of [lo, hi) is below v
+    const int first = __ffs(b) - 1;
+    const int nlo = lo + first * step;
+    hi = min(hi, lo + (first + 1) * step - 1);
+    lo = nlo;
+  }
+  return lo;
+}
+
+// coef_norm with the subdomain's constants c = (xc, yc, dxm^2, dym^2) computed once
+// (the same operations in the same order)
+__device__ __forceinline__ double coef_norm_hoisted(const double* c, double x, double y) {
+  const double ddx = __dsub_rn(x, c[0]), ddy = __dsub_rn(y, c[1]);
+  const double dx2 = __ddiv_rn(__dmul_rn(ddx, ddx), c[2]);
+  const double dy2 = __ddiv_rn(__dmul_rn(ddy, ddy), c[3]);
+  return __dadd_rn(__dmul_rn(__dsub_rn(1.0, dx2), __dsub_rn(1.0, dy2)), 0.001);
+}
+
 // Ordered membership of points in subdomain blockIdx.x; mode 0 counts, mode 1 fills.
 // With the tile index y_pmax / y_smin of py (k_y_tiles) only the tiles that can hold
 // the subdomain's y band are scanned.
@@ -396,28 +460,51 @@ __global__ void __launch_bounds__(512)
                   double* coefs, const int32_t* xy2, const int32_t* on_lattice,
                   const double* y_pmax, const double* y_smin) {
   __shared__ int warp_tot[33];
-  __shared__ int s_range[2];
-  const fi_tps_plan p = *plan_ptr;
+  __shared__ int s_range[2], s_box[4];
+  __shared__ Limits sL;
+  __shared__ double s_cn[4];  // coef_norm's subdomain constants: xc, yc, dxm^2, dym^2
   const int i = blockIdx.x;
-  const int iy = i / p.nb_subdomx, ix = i % p.nb_subdomx;
-  const Limits L = subdom_limits(p, ix, iy);
-  // on the lattice, X = 2x is an integer: x >= l <=> X >= ceil(2l), x < l <=> X < ceil(2l)
-  const bool lat = xy2 != nullptr && on_lattice != nullptr && *on_lattice != 0;
-  const double kmax = 2147483647.0;
-  const int X0 = (int)fmin(ceil(2.0 * L.lminx), kmax), X1 = (int)fmin(ceil(2.0 * L.lmaxx), kmax);
-  const int Y0 = (int)fmin(ceil(2.0 * L.lminy), kmax), Y1 = (int)fmin(ceil(2.0 * L.lmaxy), kmax);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // the subdomain's limits once per block (FP64 is narrow on this GPU)
   if (threadIdx.x == 0) {
+    const fi_tps_plan p = *plan_ptr;
+    const int iy = i / p.nb_subdomx, ix = i % p.nb_subdomx;
+    const Limits L = subdom_limits(p, ix, iy);
+    sL = L;
+    // on the lattice, X = 2x is an integer: x >= l <=> X >= ceil(2l), x < l <=> X < ceil(2l)
+    const double kmax = 2147483647.0;
+    s_box[0] = (int)fmin(ceil(2.0 * L.lminx), kmax);
+    s_box[1] = (int)fmin(ceil(2.0 * L.lmaxx), kmax);
+    s_box[2] = (int)fmin(ceil(2.0 * L.lminy), kmax);
+    s_box[3] = (int)fmin(ceil(2.0 * L.lmaxy), kmax);
+    const double xc = __dmul_rn(0.5, __dadd_rn(L.lminx, L.lmaxx));
+    const double yc = __dmul_rn(0.5, __dadd_rn(L.lminy, L.lmaxy));
+    const double dxm = __dsub_rn(L.lmaxx, xc), dym = __dsub_rn(L.lmaxy, yc);
+    s_cn[0] = xc;
+    s_cn[1] = yc;
+    s_cn[2] = __dmul_rn(dxm, dxm);
+    s_cn[3] = __dmul_rn(dym, dym);
     warp_tot[32] = 0;
+  }
+  __syncthreads();
+  const Limits L = sL;
+  // the scanned band: tiles that can hold the subdomain's y range (32-ary searches
+  // by warp 0 over the non-decreasing tile bounds: two rounds of loads for 8k tiles)
+  if (wid == 0) {
     int q0 = 0, q1 = npts;
     if (y_pmax != nullptr && y_smin != nullptr) {
       const int nt = (npts + YB_TILE - 1) / YB_TILE;
-      q0 = min(npts, YB_TILE * lower_bound_ge(y_pmax, nt, L.lminy));
-      q1 = max(q0, min(npts, YB_TILE * lower_bound_ge(y_smin, nt, L.lmaxy)));
+      q0 = min(npts, YB_TILE * warp_lower_bound_ge(y_pmax, nt, L.lminy, lane));
+      q1 = max(q0, min(npts, YB_TILE * warp_lower_bound_ge(y_smin, nt, L.lmaxy, lane)));
     }
-    s_range[0] = q0;
-    s_range[1] = q1;
+    if (lane == 0) {
+      s_range[0] = q0;
+      s_range[1] = q1;
+    }
   }
+  const bool lat = xy2 != nullptr && on_lattice != nullptr && *on_lattice != 0;
   __syncthreads();
+  const int X0 = s_box[0], X1 = s_box[1], Y0 = s_box[2], Y1 = s_box[3];
   const int qb = s_range[0], qe = s_range[1];
   if (mode == 0) {  // counts only: per-thread tallies, one block reduction
     int cnt = 0;
@@ -435,28 +522,56 @@ __global__ void __launch_bounds__(512)
     if (threadIdx.x == 0) counts[i] = warp_tot[32];
     return;
   }
-  int base = 0;
-  const int64_t off = (mode == 1) ? offsets[i] : 0;
-  for (int c0 = qb; c0 < qe; c0 += blockDim.x) {
-    const int q = c0 + threadIdx.x;
-    bool in = false;
-    if (q < qe) {
-      if (lat) {
-        const int X = xy2[2 * q], Y = xy2[2 * q + 1];
-        in = X >= X0 && X < X1 && Y >= Y0 && Y < Y1;
-      } else {
-        in = inside(L, px[q], py[q]);
-      }
+  // fill: the band in one contiguous segment per warp; the warps count their members,
+  // one block scan places the segments, then each warp writes its members in order
+  // (ballots within the warp: two barriers in all instead of three per 512 points)
+  auto member = [&](int q) -> bool {
+    if (lat) {
+      const int2 XY = reinterpret_cast<const int2*>(xy2)[q];
+      return XY.x >= X0 && XY.x < X1 && XY.y >= Y0 && XY.y < Y1;
     }
-    int total;
-    const int pos = base + block_scan_flag(in, warp_tot, &total);
-    if (in && mode == 1) {
-      indices[off + pos] = q;
-      coefs[off + pos] = coef_norm(L, px[q], py[q]);
+    return inside(L, px[q], py[q]);
+  };
+  const int nw = blockDim.x >> 5;
+  const int seg = (((qe - qb) + nw - 1) / nw + 31) & ~31;
+  const int s0 = min(qe, qb + wid * seg), s1 = min(qe, s0 + seg);
+  int cnt = 0;
+#pragma unroll 4
+  for (int q = s0 + lane; q < s1; q += 32) cnt += member(q) ? 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) warp_tot[wid] = cnt;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = lane < nw ? warp_tot[lane] : 0;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
     }
-    base += total;
+    if (lane < nw) warp_tot[lane] = incl - v;
   }
-  if (threadIdx.x == 0 && mode == 0) counts[i] = base;
+  __syncthreads();
+  int64_t pos = offsets[i] + warp_tot[wid];
+  constexpr int R = 4;  // membership of four chunks of 32 tested (loads issued) first
+  for (int c0 = s0; c0 < s1; c0 += R * 32) {
+    bool in[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int q = c0 + 32 * r + lane;
+      in[r] = q < s1 && member(q);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int q = c0 + 32 * r + lane;
+      const unsigned b = __ballot_sync(0xffffffffu, in[r]);
+      if (in[r]) {
+        const int64_t at = pos + __popc(b & ((1u << lane) - 1u));
+        indices[at] = q;
+        coefs[at] = coef_norm_hoisted(s_cn, px[q], py[q]);
+      }
+      pos += __popc(b);
+    }
+  }
 }
 
 // Block argmax of |col[k..n-1]| with the first index on ties (LAPACK idamax).
@@ -913,6 +1028,7 @@ extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const doub
   FI_REQUIRE(plan && px && py && nb_subdom > 0 && npts > 0, "fi_tps_members: bad arguments");
   FI_REQUIRE(mode == 0 ? counts != nullptr : (offsets && indices && coefs),
              "fi_tps_members: missing outputs");
+  FI_REQUIRE(((uintptr_t)xy2 & 7) == 0, "fi_tps_members: xy2 must be 8-byte aligned");
   k_tps_members<<<nb_subdom, 512, 0, (cudaStream_t)stream>>>(plan, px, py, npts, mode, counts,
                                                             offsets, indices, coefs, xy2,
                                                             on_lattice, y_pmax, y_smin);

@@ -310,9 +310,9 @@ int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nb_subdom,
  * Ordered subdomain membership of npts points (px, py float64).  mode 0 writes
  * counts[nb_subdom]; mode 1 writes, at offsets[i] (exclusive prefix sums of the
  * counts), the point indices and their norm coefficients
- * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 and
- * on_lattice from fi_tps_lattice (both nullable) the limit tests are exact integer
- * comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
+ * (_compute_coef_norm, thin_plate_spline_subdom.py:208-222).  With xy2 (8-byte
+ * aligned) and on_lattice from fi_tps_lattice (both nullable) the limit tests are
+ * exact integer comparisons on the lattice.  y_pmax / y_smin (nullable, fi_tps_y_bounds of py)
  * restrict the scan to the tiles that can hold members.
  */
 int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, const double* py,
