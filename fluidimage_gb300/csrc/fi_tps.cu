@@ -788,25 +788,94 @@ __global__ void __launch_bounds__(512)
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Subdomain bounds along x and y for the blends, computed once per block (FP64 is
+// narrow on this GPU): lo[j] = linspace_j - buffer, hi[j] = linspace_{j+1} + buffer,
+// and on the half-pixel lattice the integers ceil(2 lo), ceil(2 hi) (for X = 2x an
+// integer, x >= l <=> X >= ceil(2l) and x < l <=> X < ceil(2l)).  Both sequences are
+// non-decreasing, so the subdomains holding a point form one range per axis.
+constexpr int BLEND_AXIS_MAX = 512;
+struct AxisBounds {
+  double lo[BLEND_AXIS_MAX], hi[BLEND_AXIS_MAX];
+  int ilo[BLEND_AXIS_MAX], ihi[BLEND_AXIS_MAX];
+  double vmin, vmax, buffer;
+  int nb;
+};
+__device__ __forceinline__ void axis_bound(double vmin, double vmax, int nb, double buffer, int j,
+                                           double& lo, double& hi, int& ilo, int& ihi) {
+  const double kmax = 2147483647.0;
+  lo = __dsub_rn(linspace_at(vmin, vmax, nb + 1, j), buffer);
+  hi = __dadd_rn(linspace_at(vmin, vmax, nb + 1, j + 1), buffer);
+  ilo = (int)fmax(fmin(ceil(2.0 * lo), kmax), -kmax);
+  ihi = (int)fmax(fmin(ceil(2.0 * hi), kmax), -kmax);
+}
+// the tables when nb <= BLEND_AXIS_MAX (else axis_range computes the bounds it reads)
+__device__ void axis_bounds_fill(AxisBounds& b, double vmin, double vmax, int nb, double buffer) {
+  if (threadIdx.x == 0) {
+    b.vmin = vmin;
+    b.vmax = vmax;
+    b.buffer = buffer;
+    b.nb = nb;
+  }
+  if (nb > BLEND_AXIS_MAX) return;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x)
+    axis_bound(vmin, vmax, nb, buffer, j, b.lo[j], b.hi[j], b.ilo[j], b.ihi[j]);
+}
+// [first, last) of the subdomains along one axis holding v (V = 2v when on the lattice)
+__device__ __forceinline__ int2 axis_range(const AxisBounds& b, double v, bool lat, int V) {
+  const int nb = b.nb;
+  const bool tab = nb <= BLEND_AXIS_MAX;
+  auto above = [&](int j) -> bool {  // hi_j > v
+    if (tab) return lat ? (b.ihi[j] > V) : (b.hi[j] > v);
+    double lo, hi;
+    int ilo, ihi;
+    axis_bound(b.vmin, b.vmax, nb, b.buffer, j, lo, hi, ilo, ihi);
+    return lat ? (ihi > V) : (hi > v);
+  };
+  auto starts = [&](int j) -> bool {  // lo_j <= v
+    if (tab) return lat ? (b.ilo[j] <= V) : (b.lo[j] <= v);
+    double lo, hi;
+    int ilo, ihi;
+    axis_bound(b.vmin, b.vmax, nb, b.buffer, j, lo, hi, ilo, ihi);
+    return lat ? (ilo <= V) : (lo <= v);
+  };
+  int lo = 0, hi = nb;  // first j with hi_j > v
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (above(mid)) hi = mid; else lo = mid + 1;
+  }
+  int end = lo;
+  while (end < nb && starts(end)) ++end;
+  return make_int2(lo, end);
+}
+// V = 2v as an integer when v is on the half-pixel lattice
+__device__ __forceinline__ bool on_half_lattice(double v, int& V) {
+  const double t = 2.0 * v;
+  if (!(fabs(t) < 1e9)) return false;
+  V = (int)t;
+  return (double)V == t;
+}
+
 // Smoothed values at the centres: sum over containing subdomains, in order.
 __global__ void k_tps_blend_centers(const fi_tps_plan* plan_ptr, const double* cx,
                                     const double* cy, const int32_t* counts,
                                     const int64_t* offsets, const int32_t* indices,
                                     const double* coefs, const double* smx, const double* smy,
                                     double* outx, double* outy) {
+  __shared__ AxisBounds bx, by;
   const fi_tps_plan p = *plan_ptr;
+  axis_bounds_fill(bx, p.x_min, p.x_max, p.nb_subdomx, p.buffer_x);
+  axis_bounds_fill(by, p.y_min, p.y_max, p.nb_subdomy, p.buffer_y);
+  __syncthreads();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= p.num_centers) return;
   const double x = cx[q], y = cy[q];
-  const double wx = __ddiv_rn(__dsub_rn(p.x_max, p.x_min), (double)p.nb_subdomx);
-  const double wy = __ddiv_rn(__dsub_rn(p.y_max, p.y_min), (double)p.nb_subdomy);
-  const int ixc = (wx > 0) ? (int)floor((x - p.x_min) / wx) : 0;
-  const int iyc = (wy > 0) ? (int)floor((y - p.y_min) / wy) : 0;
+  int X = 0, Y = 0;
+  const bool lat = on_half_lattice(x, X) && on_half_lattice(y, Y);
+  const int2 rx_ = axis_range(bx, x, lat, X);
+  const int2 ry_ = axis_range(by, y, lat, Y);
   double sx = 0.0, sy = 0.0, nrm = 0.0;
-  for (int iy = clampi(iyc - 2, 0, p.nb_subdomy - 1); iy <= clampi(iyc + 2, 0, p.nb_subdomy - 1); ++iy)
-    for (int ix = clampi(ixc - 2, 0, p.nb_subdomx - 1); ix <= clampi(ixc + 2, 0, p.nb_subdomx - 1); ++ix) {
-      const Limits L = subdom_limits(p, ix, iy);
-      if (!inside(L, x, y)) continue;
+  for (int iy = ry_.x; iy < ry_.y; ++iy)
+    for (int ix = rx_.x; ix < rx_.y; ++ix) {
       const int sd = iy * p.nb_subdomx + ix;
       const int64_t off = offsets[sd];
       int lo = 0, hi = counts[sd] - 1;
@@ -941,19 +1010,21 @@ __global__ void k_tps_gather(const fi_tps_plan* plan_ptr, const int32_t* ncounts
                              const double* ncoefs, const double* partx, const double* party,
                              const double* px, const double* py, int npts, double* outx,
                              double* outy, int32_t* rx, int32_t* ry) {
+  __shared__ AxisBounds bx, by;
   const fi_tps_plan p = *plan_ptr;
+  axis_bounds_fill(bx, p.x_min, p.x_max, p.nb_subdomx, p.buffer_x);
+  axis_bounds_fill(by, p.y_min, p.y_max, p.nb_subdomy, p.buffer_y);
+  __syncthreads();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= npts) return;
   const double x = px[q], y = py[q];
-  const double wx = __ddiv_rn(__dsub_rn(p.x_max, p.x_min), (double)p.nb_subdomx);
-  const double wy = __ddiv_rn(__dsub_rn(p.y_max, p.y_min), (double)p.nb_subdomy);
-  const int ixc = (wx > 0) ? (int)floor((x - p.x_min) / wx) : 0;
-  const int iyc = (wy > 0) ? (int)floor((y - p.y_min) / wy) : 0;
+  int X = 0, Y = 0;
+  const bool lat = on_half_lattice(x, X) && on_half_lattice(y, Y);
+  const int2 rx_ = axis_range(bx, x, lat, X);
+  const int2 ry_ = axis_range(by, y, lat, Y);
   double sx = 0.0, sy = 0.0, nrm = 0.0;
-  for (int iy = clampi(iyc - 2, 0, p.nb_subdomy - 1); iy <= clampi(iyc + 2, 0, p.nb_subdomy - 1); ++iy)
-    for (int ix = clampi(ixc - 2, 0, p.nb_subdomx - 1); ix <= clampi(ixc + 2, 0, p.nb_subdomx - 1); ++ix) {
-      const Limits L = subdom_limits(p, ix, iy);
-      if (!inside(L, x, y)) continue;
+  for (int iy = ry_.x; iy < ry_.y; ++iy)
+    for (int ix = rx_.x; ix < rx_.y; ++ix) {
       const int sd = iy * p.nb_subdomx + ix;
       const int64_t off = noffsets[sd];
       int lo = 0, hi = ncounts[sd] - 1;
