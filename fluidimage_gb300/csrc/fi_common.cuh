@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/fluidimage_gb300.h"
 
 namespace fi {
@@ -32,6 +34,25 @@ void add_launches(int k);
       return FI_ERR_INVALID;                                                  \
     }                                                                         \
   } while (0)
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` (above the 48 KB
+// default), calling the runtime only when the limit has to grow: `current` is the
+// call site's record of the limit set so far, read and written under one mutex so
+// that host threads launching concurrently never lower it.
+inline std::mutex& smem_limit_mutex() {
+  static std::mutex m;
+  return m;
+}
+template <typename Kernel>
+inline cudaError_t raise_smem_limit(Kernel* kernel, size_t bytes, size_t& current) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(smem_limit_mutex());
+  if (bytes <= current) return cudaSuccess;
+  const cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) current = bytes;
+  return e;
+}
 
 inline int check_launch(const char* what, int kernels = 1) {
   add_launches(kernels);

@@ -1358,14 +1358,11 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
   const size_t smem = lay.bytes;
   FI_REQUIRE(smem <= 220 * 1024, "fi_tps_solve_mp: subdomain of %d vectors too large",
              max_members);
-  if (smem > 48 * 1024) {
-    if (wide)
-      FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_solve_mp<512>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    else
-      FI_CUDA_TRY(cudaFuncSetAttribute(k_tps_solve_mp<256>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  }
+  static size_t limit_wide = 0, limit_narrow = 0;
+  if (wide)
+    FI_CUDA_TRY(raise_smem_limit(k_tps_solve_mp<512>, smem, limit_wide));
+  else
+    FI_CUDA_TRY(raise_smem_limit(k_tps_solve_mp<256>, smem, limit_narrow));
   if (wide) {
     // clusters of S CTAs per subdomain while the subdomains leave SMs idle
     const int S = (4 * nb_subdom <= nsm) ? 4 : (2 * nb_subdom <= nsm) ? 2 : 1;
