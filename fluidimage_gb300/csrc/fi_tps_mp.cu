@@ -313,6 +313,95 @@ __device__ __forceinline__ void potrf_tile(float (&a)[32], float* B, int m, int 
   Lkk[lane * TS + 32] = 1.f / dg;
 }
 
+// Swizzle of the shared tile column: element (t, r) of a 32 x 32 tile (t the column
+// of L_ik, r its row) sits at t * 32 + (r ^ pswz(t)).  The tensor-core fragments read
+// rows r = 8a + g (g = lane / 4) of columns t = 8b + q (q = lane % 4): the XOR sends
+// the four q to four different groups of eight banks.  An aligned group of four r
+// stays contiguous and in order (float4 reads of a row).
+__device__ __forceinline__ int pswz(int t) { return (t & 3) << 3; }
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+// x = hi + lo with hi and lo TF32 (the split of the 3xTF32 products: Ootomo and
+// Yokota, "Recovering single precision accuracy from Tensor Cores while surpassing
+// the FP32 theoretical peak performance", IJHPCA 2022)
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Tile (i, j) of B -= L_ik L_jk^T on the tensor cores (warp-level m16n8k8 TF32 MMA),
+// FP32-accurate by the 3xTF32 split (hi*hi + hi*lo + lo*hi, FP32 accumulation): the
+// factor only preconditions the double-float refinement, which absorbs the ~2^-21
+// relative rounding like the FP32 one.  The 32 x 32 tile is 2 x 4 fragments of
+// 16 x 8; Pi, Pj: the swizzled shared tiles of L_ik and L_jk.  Entries past m are
+// neither read nor written; a diagonal tile keeps its upper triangle.
+__device__ __forceinline__ void tile_update_mma(float* B, int m, int ld, int ti, int tj,
+                                                const float* Pi, const float* Pj, int lane) {
+  const int g = lane >> 2, q = lane & 3;
+  float c[2][4][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int r = 32 * ti + 16 * mt + g + 8 * (e >> 1);
+        const int col = 32 * tj + 8 * nt + 2 * q + (e & 1);
+        c[mt][nt][e] = (r < m && col < m) ? B[(int64_t)col * ld + r] : 0.f;
+      }
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const int t0 = 8 * ks + q, t1 = t0 + 4;  // both have (t & 3) == q
+    const int sw = q << 3;
+    uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const int r0 = (16 * mt + g) ^ sw, r1 = (16 * mt + g + 8) ^ sw;
+      split_tf32(-Pi[t0 * 32 + r0], ah[mt][0], al[mt][0]);
+      split_tf32(-Pi[t0 * 32 + r1], ah[mt][1], al[mt][1]);
+      split_tf32(-Pi[t1 * 32 + r0], ah[mt][2], al[mt][2]);
+      split_tf32(-Pi[t1 * 32 + r1], ah[mt][3], al[mt][3]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int rn = (8 * nt + g) ^ sw;
+      split_tf32(Pj[t0 * 32 + rn], bh[nt][0], bl[nt][0]);
+      split_tf32(Pj[t1 * 32 + rn], bh[nt][1], bl[nt][1]);
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        mma_tf32(c[mt][nt], al[mt], bh[nt]);
+        mma_tf32(c[mt][nt], ah[mt], bl[nt]);
+        mma_tf32(c[mt][nt], ah[mt], bh[nt]);
+      }
+  }
+  const bool diag = ti == tj;
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int rl = 16 * mt + g + 8 * (e >> 1), cl = 8 * nt + 2 * q + (e & 1);
+        const int r = 32 * ti + rl, col = 32 * tj + cl;
+        if (r < m && col < m && (!diag || cl <= rl)) B[(int64_t)col * ld + r] = c[mt][nt][e];
+      }
+}
+
 // Shared memory of chol_factor for an m x m matrix: two L_kk tiles (rows of TS
 // floats) and the current tile column, transposed (T - 1 tiles of 32 x 32).
 __host__ __device__ inline size_t chol_scratch_bytes(int m) {
@@ -323,9 +412,9 @@ __host__ __device__ inline size_t chol_scratch_bytes(int m) {
 // Right-looking tiled Cholesky (lower) of the m x m matrix B (column-major, ld), in
 // place (lower triangle).  Per tile column k: warps solve the tiles below the
 // diagonal (one row per lane, rows of L_kk read as float4 broadcasts) and keep them,
-// transposed, in shared memory; then they update the trailing tile pairs (register
-// accumulators, packed FP32x2 FMAs, both factors read from the shared tile column:
-// the update loads only its own tile).  Lookahead: warp 0 first updates the next
+// transposed and swizzled, in shared memory; then they update the trailing tile
+// pairs on the tensor cores (3xTF32 warp MMA, both factors read from the shared tile
+// column: the update loads only its own tile).  Lookahead: warp 0 first updates the next
 // diagonal tile and factorises it in registers (shuffles) while the other warps
 // update the rest; the tiles go to the warps in the order they finish.
 // scratch: chol_scratch_bytes(m), 16-byte aligned.  False on a non-positive pivot.
@@ -339,7 +428,8 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
   // two L_kk buffers (step k reads buffer k & 1 while step k + 1's is written); row
   // j: L_kk[j][c] for c < j (0 elsewhere), [32] = 1 / L_jj
   float* Lkk0 = scratch;
-  // tile column k: tile i > k at P + (i - k - 1) * 1024, element [t * 32 + r] = L_ik[r][t]
+  // tile column k: tile i > k at P + (i - k - 1) * 1024, element
+  // [t * 32 + (r ^ pswz(t))] = L_ik[r][t]
   float* P = scratch + 2 * 32 * TS;
   if (threadIdx.x == 0) *s_flag = 0;
   __syncthreads();
@@ -373,7 +463,7 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       float* Pi = P + (i - k - 1) * 1024;
       const bool rin = 32 * i + lane < m;  // rows past m: zero (their updates are unused)
 #pragma unroll
-      for (int t = 0; t < 32; ++t) Pi[t * 32 + lane] = rin ? b[t] : 0.f;
+      for (int t = 0; t < 32; ++t) Pi[t * 32 + (lane ^ pswz(t))] = rin ? b[t] : 0.f;
     }
     if (threadIdx.x == 0) *s_next = NW;
     __syncthreads();
@@ -390,30 +480,34 @@ __device__ bool chol_factor(float* B, int m, int ld, float* scratch, int* s_flag
       const int i = k + 1 + ii, j = k + 1 + jj;
       const float* Pi = P + ii * 1024;
       const float* Pj = P + jj * 1024;
-      float acc[32];
-      tile_load(B, m, ld, i, j, acc, lane);
-      // acc -= L_ik L_jk^T: L_ik[lane][t] and the row t of L_jk^T from shared memory
+      if (pidx == 0) {
+        // the next diagonal tile in row layout (one row per lane) for its
+        // factorisation: acc -= L_ik L_jk^T with L_ik[lane][t] and the row t of L_jk^T
+        // from shared memory, packed FP32x2 FMAs
+        float acc[32];
+        tile_load(B, m, ld, i, j, acc, lane);
 #pragma unroll 4
-      for (int t = 0; t < 32; ++t) {
-        const float l = -Pi[t * 32 + lane];
-        const float2 lr = make_float2(l, l);
+        for (int t = 0; t < 32; ++t) {
+          const int sw = pswz(t);
+          const float l = -Pi[t * 32 + (lane ^ sw)];
+          const float2 lr = make_float2(l, l);
 #pragma unroll
-        for (int c4 = 0; c4 < 8; ++c4) {
-          const float4 q = *reinterpret_cast<const float4*>(Pj + t * 32 + 4 * c4);
-          float2 a01 = make_float2(acc[4 * c4], acc[4 * c4 + 1]);
-          float2 a23 = make_float2(acc[4 * c4 + 2], acc[4 * c4 + 3]);
-          a01 = __ffma2_rn(lr, make_float2(q.x, q.y), a01);
-          a23 = __ffma2_rn(lr, make_float2(q.z, q.w), a23);
-          acc[4 * c4] = a01.x;
-          acc[4 * c4 + 1] = a01.y;
-          acc[4 * c4 + 2] = a23.x;
-          acc[4 * c4 + 3] = a23.y;
+          for (int c4 = 0; c4 < 8; ++c4) {
+            const float4 q = *reinterpret_cast<const float4*>(Pj + t * 32 + ((4 * c4) ^ sw));
+            float2 a01 = make_float2(acc[4 * c4], acc[4 * c4 + 1]);
+            float2 a23 = make_float2(acc[4 * c4 + 2], acc[4 * c4 + 3]);
+            a01 = __ffma2_rn(lr, make_float2(q.x, q.y), a01);
+            a23 = __ffma2_rn(lr, make_float2(q.z, q.w), a23);
+            acc[4 * c4] = a01.x;
+            acc[4 * c4 + 1] = a01.y;
+            acc[4 * c4 + 2] = a23.x;
+            acc[4 * c4 + 3] = a23.y;
+          }
         }
-      }
-      if (pidx == 0)
         potrf_tile(acc, B, m, ld, k + 1, Lkk0 + ((k + 1) & 1) * 32 * TS, lane, s_flag);
-      else
-        tile_store(B, m, ld, i, j, acc, lane, i == j);
+      } else {
+        tile_update_mma(B, m, ld, i, j, Pi, Pj, lane);
+      }
       int nxt = 0;
       if (lane == 0) nxt = atomicAdd(s_next, 1);
       pidx = __shfl_sync(full, nxt, 0);
