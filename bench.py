@@ -49,8 +49,8 @@ SAMPLE_SHAPE = (512, 512)
 # one CTA of 16 warps per subdomain (launches of at most one subdomain per SM; 72
 # subdomains of the config-2 recipe at 1024^2) and two 8-warp CTAs per SM (the
 # 342-subdomain launch of the 2048^2 workload)
-TPS_DRAM_BYTES_PER_SUBDOMAIN_WIDE = (121.511168e6 + 80.277248e6) / 72
-TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW = (845.531136e6 + 590.625792e6) / 342
+TPS_DRAM_BYTES_PER_SUBDOMAIN_WIDE = (126.285056e6 + 80.334336e6) / 72
+TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW = (837.309952e6 + 579.323136e6) / 342
 
 
 def parse_args():
