@@ -251,7 +251,7 @@ struct SearchBox {
 // nan_indices_max + _compute_indices_max on the group's plane (correl.py:88-164).
 template <int N>
 __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchBox& box,
-                             const NanBoxes& nb, double norm, int t, int g, double* red) {
+                             const NanBoxes& nb, float normf, int t, int g, double* red) {
   using C = Cfg<N>;
   Peak p{-INFINITY, -1, -INFINITY};
   if (t < N && t >= box.i1s && t < box.i1e) {
@@ -280,7 +280,7 @@ __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchB
   o.i1 = p.f % N;
   o.tie = (p.v - p.v2) <= 1e-6f * fabsf(p.v);
   const float val = PL[o.i0 * C::LDP + o.i1];
-  o.cmax = (norm == 0.0) ? 0.0f : __fdiv_rn(val, (float)norm);
+  o.cmax = (normf == 0.0f) ? 0.0f : __fdiv_rn(val, normf);
   if (o.i0 == 0 || o.i0 == N - 1 || o.i1 == 0 || o.i1 == N - 1) {
     o.err = FI_VEC_PEAK_BOUNDARY;
   } else {
@@ -530,12 +530,12 @@ struct VecResult {
 };
 
 template <int N>
-__device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double norm, int t,
+__device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, float normf, int t,
                                      int g, double* red, const SecondaryOut* so) {
   const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
   NanBoxes boxes;
   boxes.n = 0;
-  PeakOut p1 = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
+  PeakOut p1 = find_peak<N>(PL, pa.mask, pa.box, boxes, normf, t, g, red);
   VecResult r;
   r.tie = p1.tie;
   r.subpix_tie = false;
@@ -545,7 +545,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
   if (p1.err == FI_VEC_PEAK_BOUNDARY || p1.err == FI_VEC_PEAK_NAN) {
     boxes.add(p1.i0, p1.i1, pa.radius, N);
     if (boxes.n) r.nb = boxes.b[0];
-    PeakOut p2 = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
+    PeakOut p2 = find_peak<N>(PL, pa.mask, pa.box, boxes, normf, t, g, red);
     r.tie = r.tie || p2.tie;
     if (p2.err == FI_VEC_OK) {
       fin = p2;
@@ -584,7 +584,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, double
       const int K = pa.nb_peaks - 1;
       for (int k = 0; k < K; ++k) {
         boxes.add(a0, a1, pa.radius, N);
-        const PeakOut q = find_peak<N>(PL, pa.mask, pa.box, boxes, norm, t, g, red);
+        const PeakOut q = find_peak<N>(PL, pa.mask, pa.box, boxes, normf, t, g, red);
         r.sec_tie = r.sec_tie || q.tie;
         if (q.err != FI_VEC_OK) break;
         a0 = q.i0;
@@ -728,10 +728,9 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     }
   }
   double sums[4];
+  unsigned long long u[4] = {si0, qi0, si1, qi1};
   if (intpath) {
-    unsigned long long u[4] = {si0, qi0, si1, qi1};
     gsum4u<C::G>(u, g, red);
-    for (int i = 0; i < 4; ++i) sums[i] = (double)u[i];
   } else {
     sums[0] = (double)sf0;
     sums[1] = (double)qf0 - (double)cf0;
@@ -740,40 +739,64 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     gsum4<C::G>(sums, g, red);
   }
   gminmax4<C::G>(mm, g, red);
-  // per-window scalars: one thread computes them (FP64 is narrow on this GPU) and
-  // the group reads them back from its scratch
+  // per-window scalars: one thread computes them and the group reads them back from
+  // its scratch.  FP64 is narrow on this GPU (an FP64 instruction costs the whole
+  // warp's FP64 issue even with one lane active), so the integer-image,
+  // power-of-two-window case uses exact integer sums and float32 only.
   if (t == 0) {
-    const double NN = (double)N * (double)N;
     // a constant window has an exactly zero spectrum (and plane) upstream
     const bool flat0 = mm[0] == mm[2], flat1 = mm[1] == mm[3];
     float* rf = reinterpret_cast<float*>(red + 17);
     int e0 = 0, e1 = 0;
-    double S0, S1;
+    float normf;
     if constexpr ((N & (N - 1)) == 0) {
-      // N^2 a power of two: the divisions by N^2 are exact products by 2^-2L, and the
-      // exponent of sqrt(S / N^2) follows from the one of S (frexp(sqrt(m 2^x)) has
-      // exponent (x + 1) >> 1): the same values with a few FP64 instructions (this
-      // thread issues them for the whole window; FP64 is narrow on this GPU)
       constexpr int L = (N == 16) ? 4 : (N == 32) ? 5 : (N == 64) ? 6 : 3;
-      constexpr double INN = 1.0 / ((double)N * (double)N);
-      S0 = flat0 ? 0.0 : fmax(sums[1] - (sums[0] * sums[0]) * INN, 0.0);
-      S1 = flat1 ? 0.0 : fmax(sums[3] - (sums[2] * sums[2]) * INN, 0.0);
-      int x0 = 0, x1 = 0;
-      if (S0 > 0.0) {
-        frexp(S0, &x0);
-        e0 = (x0 - 2 * L + 1) >> 1;
+      if (intpath) {
+        // N^2 S = N^2 sum v^2 - (sum v)^2, exact in 64 bits (v < 2^16: both terms
+        // below 2^(4L + 32)); S = (N^2 S) 2^-2L, so frexp(S) has exponent
+        // bitlength(N^2 S) - 2L
+        const unsigned long long SN0 = flat0 ? 0ull : (u[1] << (2 * L)) - u[0] * u[0];
+        const unsigned long long SN1 = flat1 ? 0ull : (u[3] << (2 * L)) - u[2] * u[2];
+        if (SN0 != 0ull) e0 = ((64 - __clzll((long long)SN0) - 2 * L) - 2 * L + 1) >> 1;
+        if (SN1 != 0ull) e1 = ((64 - __clzll((long long)SN1) - 2 * L) - 2 * L + 1) >> 1;
+        // the window sums are below 2^32: the float mean rounds once, like the
+        // float64 product rounded to float32
+        rf[0] = ldexpf(__uint2float_rn((unsigned)u[0]), -2 * L);
+        rf[1] = ldexpf(__uint2float_rn((unsigned)u[2]), -2 * L);
+        const float S0f = ldexpf(__ull2float_rn(SN0), -2 * L);
+        const float S1f = ldexpf(__ull2float_rn(SN1), -2 * L);
+        normf = __fsqrt_rn(__fmul_rn(S0f, S1f));
+        // float64 norm only for the caller's norms array
+        red[16] = a.norms ? ldexp(sqrt((double)SN0 * (double)SN1), -2 * L) : 0.0;
+      } else {
+        // N^2 a power of two: the divisions by N^2 are exact products by 2^-2L, and
+        // the exponent of sqrt(S / N^2) follows from the one of S (frexp(sqrt(m 2^x))
+        // has exponent (x + 1) >> 1)
+        constexpr double INN = 1.0 / ((double)N * (double)N);
+        const double S0 = flat0 ? 0.0 : fmax(sums[1] - (sums[0] * sums[0]) * INN, 0.0);
+        const double S1 = flat1 ? 0.0 : fmax(sums[3] - (sums[2] * sums[2]) * INN, 0.0);
+        int x0 = 0, x1 = 0;
+        if (S0 > 0.0) {
+          frexp(S0, &x0);
+          e0 = (x0 - 2 * L + 1) >> 1;
+        }
+        if (S1 > 0.0) {
+          frexp(S1, &x1);
+          e1 = (x1 - 2 * L + 1) >> 1;
+        }
+        rf[0] = (float)(sums[0] * INN);
+        rf[1] = (float)(sums[2] * INN);
+        red[16] = sqrt(S0 * S1);
+        normf = (float)red[16];
       }
-      if (S1 > 0.0) {
-        frexp(S1, &x1);
-        e1 = (x1 - 2 * L + 1) >> 1;
-      }
-      rf[0] = (float)(sums[0] * INN);
-      rf[1] = (float)(sums[2] * INN);
       // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1) = 2^(e0 + e1 - 2 - 2L)
       reinterpret_cast<float*>(red + 20)[0] = ldexpf(1.0f, e0 + e1 - 2 - 2 * L);
     } else {
-      S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
-      S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
+      if (intpath)
+        for (int i = 0; i < 4; ++i) sums[i] = (double)u[i];
+      const double NN = (double)N * (double)N;
+      const double S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
+      const double S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
       if (S0 > 0.0) frexp(sqrt(S0 / NN), &e0);
       if (S1 > 0.0) frexp(sqrt(S1 / NN), &e1);
       rf[0] = (float)(sums[0] / NN);
@@ -781,14 +804,17 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
       // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1), sc0 sc1 a power of two
       reinterpret_cast<float*>(red + 20)[0] =
           (float)(0.25 / (NN * (double)ldexpf(1.0f, -e0) * (double)ldexpf(1.0f, -e1)));
+      red[16] = sqrt(S0 * S1);
+      normf = (float)red[16];
     }
-    red[16] = sqrt(S0 * S1);
     rf[2] = ldexpf(1.0f, -e0);
     rf[3] = ldexpf(1.0f, -e1);
     reinterpret_cast<int*>(red + 19)[0] = (flat0 || flat1) ? 1 : 0;
+    reinterpret_cast<float*>(red + 20)[1] = normf;
   }
   gsync<C::G>(g);
-  const double norm = red[16];
+  const float normf = reinterpret_cast<const float*>(red + 20)[1];
+  const double norm_out = red[16];  // the caller's norms array only
   const float mean0 = reinterpret_cast<const float*>(red + 17)[0];
   const float mean1 = reinterpret_cast<const float*>(red + 17)[1];
   const float sc0 = reinterpret_cast<const float*>(red + 17)[2];
@@ -868,7 +894,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     pa.minv = a.subpix_minv;
     pa.nb_peaks = a.nb_peaks;
     SecondaryOut so{a.peaks_count, a.peaks, a.peaks_err, w, a.dxin != nullptr, dinx, diny};
-    res = peak_and_subpix<N>(PL, pa, norm, t, g, red, a.nb_peaks > 1 ? &so : nullptr);
+    res = peak_and_subpix<N>(PL, pa, normf, t, g, red, a.nb_peaks > 1 ? &so : nullptr);
     if (!valid && a.nb_peaks > 1 && t == 0) a.peaks_count[w] = -1;
   }
 
@@ -883,7 +909,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS, Cfg<N>::MIN_BLOCKS)
     }
   }
   if (t == 0) {
-    if (a.norms) a.norms[w] = norm;
+    if (a.norms) a.norms[w] = norm_out;
     if (do_peaks) {
       float dxo = res.dx, dyo = res.dy, cm = res.cmax;
       int err = res.err;
@@ -935,7 +961,8 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS)
     for (int i0 = 0; i0 < N; ++i0) PL[i0 * C::LDP + t] = in[i0 * N + t];
   gsync<C::G>(g);
   SecondaryOut so{pcount, peaks, perr, w, false, 0, 0};
-  VecResult r = peak_and_subpix<N>(PL, pa, norms[w], t, g, red, pa.nb_peaks > 1 ? &so : nullptr);
+  VecResult r =
+      peak_and_subpix<N>(PL, pa, (float)norms[w], t, g, red, pa.nb_peaks > 1 ? &so : nullptr);
   if (pa.mask == nullptr && t < N && (r.nb.r1 > r.nb.r0))
     for (int i0 = 0; i0 < N; ++i0)
       if (r.nb.has(i0, t)) in[i0 * N + t] = NAN;
