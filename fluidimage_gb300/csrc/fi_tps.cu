@@ -275,52 +275,107 @@ __global__ void k_set_int(int32_t* p, int32_t v) { *p = v; }
 // [lo, hi) can only hold points of tiles [first j with tile_pmax[j] >= lo, first j
 // with tile_smin[j] >= hi).
 constexpr int YB_TILE = 256;
+// Order-preserving 64-bit keys of doubles (NaN excluded): max / min of doubles as
+// integer max / min on the ALU pipe (FP64 is narrow on this GPU).
+__device__ __forceinline__ unsigned long long dkey(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) {
+  return a < b ? a : b;
+}
+
 __global__ void __launch_bounds__(YB_TILE) k_y_tiles(const double* py, int n, double* tmax,
                                                       double* tmin) {
-  __shared__ double red[33];
+  __shared__ unsigned long long smx[YB_TILE / 32], smn[YB_TILE / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i = blockIdx.x * YB_TILE + threadIdx.x;
   const double y = (i < n) ? py[i] : NAN;
-  const double mx = block_reduce_d(isnan(y) ? -INFINITY : y, red, true);
-  const double mn = block_reduce_d(isnan(y) ? INFINITY : y, red, false);
+  unsigned long long kx = isnan(y) ? dkey(-INFINITY) : dkey(y);
+  unsigned long long kn = isnan(y) ? dkey(INFINITY) : dkey(y);
+  for (int o = 16; o > 0; o >>= 1) {
+    kx = umax64(kx, __shfl_xor_sync(0xffffffffu, kx, o));
+    kn = umin64(kn, __shfl_xor_sync(0xffffffffu, kn, o));
+  }
+  if (lane == 0) {
+    smx[wid] = kx;
+    smn[wid] = kn;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    tmax[blockIdx.x] = mx;
-    tmin[blockIdx.x] = mn;
+    for (int w = 1; w < YB_TILE / 32; ++w) {
+      kx = umax64(kx, smx[w]);
+      kn = umin64(kn, smn[w]);
+    }
+    tmax[blockIdx.x] = dkey_inv(kx);
+    tmin[blockIdx.x] = dkey_inv(kn);
   }
 }
 
 // In place: running max forward, running min backward over the tiles (one block;
-// chunks of 1024 tiles, a Hillis-Steele scan per chunk in shared memory).
+// chunks of 1024 tiles, warp shuffle scans on order-preserving integer keys).
 __global__ void __launch_bounds__(1024) k_y_tiles_scan(int ntiles, double* tmax, double* tmin) {
-  __shared__ double a[1024], b[1024];
-  __shared__ double carry[2];
-  const int t = threadIdx.x;
+  __shared__ unsigned long long wa[32], wb[32];
+  __shared__ unsigned long long carry[2];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const unsigned long long kneg = dkey(-INFINITY), kpos = dkey(INFINITY);
   if (t == 0) {
-    carry[0] = -INFINITY;
-    carry[1] = INFINITY;
+    carry[0] = kneg;
+    carry[1] = kpos;
   }
   __syncthreads();
   for (int base = 0; base < ntiles; base += 1024) {
     const int i = base + t;
     const int ir = ntiles - 1 - i;  // backward scan reads from the end
-    a[t] = (i < ntiles) ? tmax[i] : -INFINITY;
-    b[t] = (i < ntiles) ? tmin[ir] : INFINITY;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-      const double va = (t >= o) ? a[t - o] : -INFINITY;
-      const double vb = (t >= o) ? b[t - o] : INFINITY;
-      __syncthreads();
-      a[t] = fmax(a[t], va);
-      b[t] = fmin(b[t], vb);
-      __syncthreads();
+    unsigned long long ka = (i < ntiles) ? dkey(tmax[i]) : kneg;
+    unsigned long long kb = (i < ntiles) ? dkey(tmin[ir]) : kpos;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long ua = __shfl_up_sync(0xffffffffu, ka, o);
+      const unsigned long long ub = __shfl_up_sync(0xffffffffu, kb, o);
+      if (lane >= o) {
+        ka = umax64(ka, ua);
+        kb = umin64(kb, ub);
+      }
     }
+    if (lane == 31) {
+      wa[wid] = ka;
+      wb[wid] = kb;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      unsigned long long x = wa[lane], y = wb[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long ux = __shfl_up_sync(0xffffffffu, x, o);
+        const unsigned long long uy = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) {
+          x = umax64(x, ux);
+          y = umin64(y, uy);
+        }
+      }
+      wa[lane] = x;
+      wb[lane] = y;
+    }
+    __syncthreads();
+    if (wid > 0) {
+      ka = umax64(ka, wa[wid - 1]);
+      kb = umin64(kb, wb[wid - 1]);
+    }
+    ka = umax64(ka, carry[0]);
+    kb = umin64(kb, carry[1]);
     if (i < ntiles) {
-      tmax[i] = fmax(a[t], carry[0]);
-      tmin[ir] = fmin(b[t], carry[1]);
+      tmax[i] = dkey_inv(ka);
+      tmin[ir] = dkey_inv(kb);
     }
     __syncthreads();
     if (t == 0) {
-      carry[0] = fmax(carry[0], a[1023]);
-      carry[1] = fmin(carry[1], b[1023]);
+      carry[0] = umax64(carry[0], wa[31]);
+      carry[1] = umin64(carry[1], wb[31]);
     }
     __syncthreads();
   }
