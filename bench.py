@@ -337,7 +337,7 @@ def run_gpu(args):
 
     for _ in work.calcul_series(couples(len(series))):
         pass
-    n_series = max(args.e2e_steps, 8)
+    n_series = max(args.e2e_steps, 16)
     torch.cuda.synchronize()
     t_start = time.perf_counter()
     for _ in work.calcul_series(couples(n_series)):
