@@ -15,6 +15,7 @@
 //
 // Layout arithmetic (linspace, buffers, norm coefs) uses round-to-nearest
 // intrinsics so that it reproduces numpy's float64 results bit for bit.
+#include <climits>
 #include <cmath>
 
 #include "fi_common.cuh"
@@ -1001,6 +1002,7 @@ __global__ void __launch_bounds__(256)
   const bool qlat = s_lat && table != nullptr && X2 == rint(X2) && Y2 == rint(Y2) &&
                     fabs(X2) < 1073741824.0 && fabs(Y2) < 1073741824.0;
   if (qlat && table2 != nullptr) {  // 4 r^2 in integers, double-float sums
+    const int tsz32 = (int)(tsize < (int64_t)INT_MAX ? tsize : (int64_t)INT_MAX);
     const int QX = (int)X2, QY = (int)Y2;
     float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
     constexpr int U = 8;  // table loads issued ahead of their use
@@ -1013,10 +1015,13 @@ __global__ void __launch_bounds__(256)
         far[u] = false;
         f[u] = make_float2(0.f, 0.f);
         if (j < N) {
+          // 32-bit 4 r^2 (lattice coordinates below 2^30; |dx|, |dy| <= 32767 keeps
+          // the sum below 2^31, farther pairs are beyond the table)
           const int2 c = sxy2[j];
-          const int64_t dx = (int64_t)(QX - c.x), dy = (int64_t)(QY - c.y);
-          const int64_t kq = dy * dy + dx * dx;
-          far[u] = kq >= tsize;
+          const int dx = QX - c.x, dy = QY - c.y;
+          const bool near = (unsigned)dx + 32767u <= 65534u && (unsigned)dy + 32767u <= 65534u;
+          const int kq = near ? dy * dy + dx * dx : INT_MAX;
+          far[u] = kq >= tsz32;
           if (!far[u]) f[u] = __ldg(table2 + kq);
         }
       }

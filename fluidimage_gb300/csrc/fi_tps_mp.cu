@@ -26,6 +26,7 @@
 // put every PIV vector there); other distances use log() directly.
 #include <cooperative_groups.h>
 
+#include <climits>
 #include <cmath>
 
 #include "fi_common.cuh"
@@ -850,15 +851,20 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   // entries (i, j0 .. j0 + cnt - 1) of A as pairs (0 < cnt <= 8, the rest zero): on the
   // lattice the eight table loads are issued before any is used (the loads, mostly
   // L2 hits, bound these phases), the diagonal and far entries patched afterwards
+  const int tsz32 = (int)(table_size < (int64_t)INT_MAX ? table_size : (int64_t)INT_MAX);
   auto a_batch_df = [&](int i, int2 ci, int j0, int cnt, float2(&out)[8]) {
     if (lat && phi_table2 != nullptr) {
-      int64_t kq[8];
+      // 4 r^2 in 32-bit integers: the lattice coordinates are below 2^30 in magnitude,
+      // so their differences fit, and |dx|, |dy| <= 32767 keeps dx^2 + dy^2 below
+      // 2^31; farther pairs (beyond the table anyway) take the direct kernel value
+      int kq[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int2 cj = cxy[j0 + min(u, cnt - 1)];
-        const int64_t dx = (int64_t)(ci.x - cj.x), dy = (int64_t)(ci.y - cj.y);
-        kq[u] = dy * dy + dx * dx;
-        out[u] = phi_table2[kq[u] < table_size ? kq[u] : 0];
+        const int dx = ci.x - cj.x, dy = ci.y - cj.y;
+        const bool near = (unsigned)dx + 32767u <= 65534u && (unsigned)dy + 32767u <= 65534u;
+        kq[u] = near ? dy * dy + dx * dx : INT_MAX;
+        out[u] = phi_table2[kq[u] < tsz32 ? kq[u] : 0];
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -867,7 +873,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
           out[u] = make_float2(0.f, 0.f);
         else if (j == i)
           out[u] = lam2;
-        else if (kq[u] >= table_size)
+        else if (kq[u] >= tsz32)
           out[u] = df_split(phi_pair(xc[i], yc[i], xc[j], yc[j], nullptr, 0));
       }
     } else {
