@@ -32,6 +32,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -520,8 +521,7 @@ def run_preproc(args):
                 "t0 = time.perf_counter(); getattr(O, %r)(a, **json.loads(sys.argv[2])); "
                 "print(a.size / (time.perf_counter() - t0) / 1e6)" % (str(ROOT), name))
         crop = host[..., :512, :512]
-        tmp = ROOT / "gpurun_out" if (ROOT / "gpurun_out").exists() else Path("/tmp")
-        path = tmp / f"_preproc_{name}.npy"
+        path = Path(tempfile.gettempdir()) / f"_preproc_{name}_{os.getpid()}.npy"
         np.save(path, np.ascontiguousarray(crop))
         env = dict(os.environ, OMP_NUM_THREADS="1")
         cpu = float(subprocess.run([sys.executable, "-c", code, str(path), json.dumps(kw)],
