@@ -95,6 +95,78 @@ __device__ __forceinline__ int64_t extend(int64_t i, int64_t n, int mode) {
   }
 }
 
+// ------------------------------------------------------------------ gaussian
+// One axis of scipy.ndimage.gaussian_filter1d (ndimage/_filters.py; the C line
+// correlation with a symmetric kernel) over a (nt, ny, nx) stack: the line values as
+// float64, out = w_0 x_0, then, from the outermost pair of taps inwards,
+// out += (x_-j + x_j) w_j, each product and sum rounded (no contraction); 'reflect'
+// extension; the result cast to the image dtype as a C cast (truncation for the
+// integer types, round to nearest for float32).
+__device__ __forceinline__ void store_cast(void* p, int dtype, int64_t i, double v) {
+  switch (dtype) {
+    case FI_PRE_U8: static_cast<uint8_t*>(p)[i] = (uint8_t)v; break;
+    case FI_PRE_U16: static_cast<uint16_t*>(p)[i] = (uint16_t)v; break;
+    case FI_PRE_F32: static_cast<float*>(p)[i] = __double2float_rn(v); break;
+    default: static_cast<double*>(p)[i] = v;
+  }
+}
+
+__global__ void k_gauss_axis(const void* in, void* out, int dtype, int nt, int ny, int nx,
+                             int axis, const double* __restrict__ w, int radius) {
+  const int64_t count = (int64_t)nt * ny * nx;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < count;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(idx % nx);
+    const int y = (int)((idx / nx) % ny);
+    const int64_t base = idx - (axis == 1 ? x : (int64_t)y * nx);
+    const int64_t n = axis == 1 ? nx : ny;
+    const int64_t step = axis == 1 ? 1 : nx;
+    const int pos = axis == 1 ? x : y;
+    double acc = __dmul_rn(load_d(in, dtype, base + (int64_t)pos * step), w[radius]);
+    for (int j = radius; j >= 1; --j) {
+      const double a = load_d(in, dtype, base + extend(pos - j, n, FI_MODE_REFLECT) * step);
+      const double b = load_d(in, dtype, base + extend(pos + j, n, FI_MODE_REFLECT) * step);
+      acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(a, b), w[radius - j]));
+    }
+    store_cast(out, dtype, idx, acc);
+  }
+}
+
+// out = blurred + alpha * (blurred - filtered) with numpy's promotions (sharpen,
+// _toolbox_py.py:472-490): integer images subtract in their own type (wrapping) and
+// give float64; float32 stays float32 (alpha rounded to float32); float64 is float64.
+__global__ void k_sharpen_combine(const void* blurred, const void* filtered, int dtype,
+                                  int64_t count, double alpha, void* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    switch (dtype) {
+      case FI_PRE_U8: {
+        const uint8_t b = static_cast<const uint8_t*>(blurred)[i];
+        const uint8_t d = (uint8_t)(b - static_cast<const uint8_t*>(filtered)[i]);
+        static_cast<double*>(out)[i] = __dadd_rn((double)b, __dmul_rn(alpha, (double)d));
+        break;
+      }
+      case FI_PRE_U16: {
+        const uint16_t b = static_cast<const uint16_t*>(blurred)[i];
+        const uint16_t d = (uint16_t)(b - static_cast<const uint16_t*>(filtered)[i]);
+        static_cast<double*>(out)[i] = __dadd_rn((double)b, __dmul_rn(alpha, (double)d));
+        break;
+      }
+      case FI_PRE_F32: {
+        const float b = static_cast<const float*>(blurred)[i];
+        const float d = __fsub_rn(b, static_cast<const float*>(filtered)[i]);
+        static_cast<float*>(out)[i] = __fadd_rn(b, __fmul_rn(__double2float_rn(alpha), d));
+        break;
+      }
+      default: {
+        const double b = static_cast<const double*>(blurred)[i];
+        const double d = __dsub_rn(b, static_cast<const double*>(filtered)[i]);
+        static_cast<double*>(out)[i] = __dadd_rn(b, __dmul_rn(alpha, d));
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------------ min / max
 // One axis of a separable minimum or maximum filter over a (nt, ny, nx) stack.
 // Keys compare like the values; cval enters as its key.
@@ -416,4 +488,31 @@ extern "C" int fi_tanh_rescale(const void* in, int dtype, int64_t count, double 
   k_tanh_rescale<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, threshold,
                                                                    scale, out);
   return check_launch("fi_tanh_rescale");
+}
+
+extern "C" int fi_gaussian_filter(const void* in, void* out, void* tmp, int dtype, int nt, int ny,
+                                  int nx, const double* weights, int radius, void* stream) {
+  FI_REQUIRE(in && out && tmp && weights, "fi_gaussian_filter: null pointer");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_gaussian_filter: bad dtype %d",
+             dtype);
+  FI_REQUIRE(nt > 0 && ny > 0 && nx > 0 && radius >= 0, "fi_gaussian_filter: bad sizes");
+  const int64_t count = (int64_t)nt * ny * nx;
+  int blocks = (int)((count + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_gauss_axis<<<blocks, 256, 0, s>>>(in, tmp, dtype, nt, ny, nx, 0, weights, radius);
+  k_gauss_axis<<<blocks, 256, 0, s>>>(tmp, out, dtype, nt, ny, nx, 1, weights, radius);
+  return check_launch("fi_gaussian_filter", 2);
+}
+
+extern "C" int fi_sharpen_combine(const void* blurred, const void* filtered, int dtype,
+                                  int64_t count, double alpha, void* out, void* stream) {
+  FI_REQUIRE(blurred && filtered && out && count > 0, "fi_sharpen_combine: bad arguments");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_sharpen_combine: bad dtype %d",
+             dtype);
+  int blocks = (int)((count + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_sharpen_combine<<<blocks, 256, 0, (cudaStream_t)stream>>>(blurred, filtered, dtype, count,
+                                                             alpha, out);
+  return check_launch("fi_sharpen_combine");
 }

@@ -14,11 +14,13 @@ works/preproc/_toolbox_py.py:
   ``img - weight * filtered`` in numpy's result dtype, negatives set to 0;
 * ``temporal_minima / temporal_median / temporal_percentile`` (:189-256): the rank
   filter over the stack with ``window_shape`` (nt, ny, nx), no clamping;
-* ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355).
+* ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355);
+* ``sharpen`` (:472-490): scipy.ndimage's gaussian filters (float64 line sums in
+  scipy's order, each axis cast to the image dtype) and the final combination.
 
 The tools built on scikit-image (``adaptive_threshold``, ``rescale_intensity``,
-``equalize_hist_*``, ``gamma_correction``) and ``sharpen`` keep their parameters
-but raise ``NotImplementedError`` when enabled.
+``equalize_hist_*``, ``gamma_correction``) keep their parameters but raise
+``NotImplementedError`` when enabled.
 """
 
 from __future__ import annotations
@@ -305,11 +307,55 @@ def _tanh_one(img, threshold):
     return out
 
 
+def _gauss_weights(sigma, truncate=4.0):
+    """scipy.ndimage's ``_gaussian_kernel1d`` (order 0, ndimage/_filters.py), reversed
+    for the correlation as ``gaussian_filter1d`` does, and its radius."""
+    radius = int(truncate * float(sigma) + 0.5)
+    sigma2 = float(sigma) * float(sigma)
+    x = np.arange(-radius, radius + 1)
+    phi = np.exp(-0.5 / sigma2 * x ** 2)
+    phi = phi / phi.sum()
+    return np.ascontiguousarray(phi[::-1]), radius
+
+
+def gaussian_filter(img, sigma):
+    """scipy.ndimage.gaussian_filter(img, sigma) of each image of a stack (or of one
+    image): axis y then x, 'reflect', truncate 4, the image dtype after each axis."""
+    torch = _torch()
+    x, single = _stack(img)
+    x = x.contiguous()
+    nt, ny, nx = x.shape
+    w, radius = _gauss_weights(sigma)
+    wd = torch.from_numpy(w).to(x.device)
+    out = torch.empty_like(x)
+    tmp = torch.empty_like(x)
+    L.check(L.load().fi_gaussian_filter(L.ptr(x), L.ptr(out), L.ptr(tmp), _DT[_dtype_of(x)],
+                                        nt, ny, nx, L.ptr(wd), radius, L.stream_handle()),
+            "fi_gaussian_filter")
+    return out[0] if single else out
+
+
+@_per_image
+def sharpen(img, sigma1=3.0, sigma2=1.0, alpha=30.0):
+    """_toolbox_py.py:472-490: two chained gaussian filters in the image dtype, then
+    ``blurred + alpha * (blurred - filter_blurred)`` with numpy's promotions (integer
+    images: the difference wraps in their type, the result is float64)."""
+    blurred = gaussian_filter(img, sigma1)
+    filtered = gaussian_filter(blurred, sigma2)
+    dtype = _dtype_of(blurred)
+    out_dt = np.dtype(np.float32) if dtype == np.float32 else np.dtype(np.float64)
+    out = _empty(tuple(blurred.shape), out_dt, blurred.device)
+    L.check(L.load().fi_sharpen_combine(L.ptr(blurred), L.ptr(filtered), _DT[dtype],
+                                        blurred.numel(), float(alpha), L.ptr(out),
+                                        L.stream_handle()), "fi_sharpen_combine")
+    return out
+
+
 def _not_provided(name):
     def tool(img, **kwargs):
         raise NotImplementedError(
             f"preprocessing tool {name!r} is not provided by this backend (upstream builds it "
-            "on scikit-image or chained gaussian filters)")
+            "on scikit-image)")
 
     tool.__name__ = name
     return tool
@@ -324,6 +370,7 @@ TOOLS = {
     "temporal_percentile": temporal_percentile,
     "global_threshold": global_threshold,
     "rescale_intensity_tanh": rescale_intensity_tanh,
+    "sharpen": sharpen,
 }
 for _name in AVAILABLE_TOOLS:
     TOOLS.setdefault(_name, _not_provided(_name))

@@ -520,6 +520,25 @@ int fi_sq_sum_max(const void* in, int dtype, int64_t count, double* part_sum, do
 int fi_tanh_rescale(const void* in, int dtype, int64_t count, double threshold, double scale,
                     double* out, void* stream);
 
+/*
+ * scipy.ndimage.gaussian_filter of each image of a (nt, ny, nx) stack (axis y then x;
+ * the call of sharpen, _toolbox_py.py:486-487): one symmetric 1-D correlation per
+ * axis in float64 ('reflect' boundaries; out = w_0 x_0, then the tap pairs from the
+ * outermost inwards, no contraction), each pass cast to the image dtype (truncation
+ * for the integer types).  weights: device array of 2 radius + 1 float64 (scipy's
+ * normalised kernel, _gaussian_kernel1d); tmp: a buffer like out.
+ */
+int fi_gaussian_filter(const void* in, void* out, void* tmp, int dtype, int nt, int ny, int nx,
+                       const double* weights, int radius, void* stream);
+
+/*
+ * sharpen's last line (_toolbox_py.py:489): out = blurred + alpha * (blurred -
+ * filtered) with numpy's promotions: integer images subtract in their own type
+ * (wrapping) and give float64, float32 stays float32, float64 is float64.
+ */
+int fi_sharpen_combine(const void* blurred, const void* filtered, int dtype, int64_t count,
+                       double alpha, void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

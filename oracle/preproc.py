@@ -102,3 +102,15 @@ def rescale_intensity_tanh(img, threshold=None):
         out = np.tanh(im / thr)
         return np.floor(np.max(im) / np.max(out) * out)
     return _per_image(one, img)
+
+
+def sharpen(img, sigma1=3.0, sigma2=1.0, alpha=30.0):
+    """_toolbox_py.py:472-490 (scipy.ndimage gaussian filters in the image dtype, numpy
+    promotions in the combination)."""
+
+    def one(im):
+        blurred = ndi.gaussian_filter(im, sigma1)
+        filter_blurred = ndi.gaussian_filter(blurred, sigma2)
+        return blurred + alpha * (blurred - filter_blurred)
+
+    return _per_image(one, img)

@@ -295,6 +295,9 @@ PREPROC_CASES = [
     ("threshold_u16_default", "global_threshold", "u16", dict(minima=50)),
     ("tanh_u8", "rescale_intensity_tanh", "u8", dict()),
     ("tanh_u16_thr", "rescale_intensity_tanh", "u16", dict(threshold=900.0)),
+    ("sharpen_u8", "sharpen", "u8", dict()),
+    ("sharpen_u16_s2", "sharpen", "u16", dict(sigma1=2.0, sigma2=0.8, alpha=10.0)),
+    ("sharpen_f32", "sharpen", "f32", dict(sigma1=1.5, sigma2=1.0, alpha=5.0)),
 ]
 
 

@@ -1,7 +1,7 @@
 """GPU preprocessing tools against the fixture recorded from the upstream tools.
 
-Rank filters, the weighted subtraction and the clamp are exact (integer keys and
-the same float arithmetic); rescale_intensity_tanh floors float64 values computed
+Rank filters, the weighted subtraction, the clamp and sharpen's gaussian filters
+are exact (integer keys and the same float arithmetic in the same order); rescale_intensity_tanh floors float64 values computed
 with CUDA's tanh, which may differ from numpy's by one ulp, so at most 0.1 % of the
 pixels may differ by one count.
 """
