@@ -496,6 +496,7 @@ def run_preproc(args):
         ("sliding_minima", dict(window_size=30), t_img, im0),
         ("sliding_median", dict(window_size=30), t_img, im0),
         ("temporal_minima", dict(), t_stack, frames),
+        ("sharpen", dict(), t_img, im0),
     ]
     out = {"metric": "preprocessing Mpixel/s", "unit": "Mpixel/s", "workload":
            f"{args.size}x{args.size} uint16 frames of the config-2 pair", "tools": {}}
