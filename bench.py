@@ -366,7 +366,7 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FFT correlation), f64 (TPS solve)",
+        "vs_baseline": None, "dtype": "f32 (FFT correlation); TPS to f64 accuracy (double-float projection, f32 + 3xTF32 Cholesky, double-float refinement)",
         "data": "synthetic",
         "config": {"workload": WORKLOAD if args.size == 2048 else
                    WORKLOAD.replace("2048x2048", f"{args.size}x{args.size}"),
