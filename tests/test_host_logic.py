@@ -116,3 +116,17 @@ def test_synthetic_pairs_are_deterministic():
     r = np.linspace(1, 1500, 20000)
     dx, dy = f(1023.5 + r, np.full_like(r, 1023.5))
     assert abs(np.hypot(dx, dy).max() - 8.0) < 1e-3
+
+
+@pytest.mark.parametrize("sigma", [0.8, 1.0, 1.5, 2.0, 3.0])
+def test_gaussian_weights_match_scipy(sigma):
+    """The host-side kernel of ``preproc.gaussian_filter`` is scipy.ndimage's
+    (``_gaussian_kernel1d`` reversed, radius ``int(4 sigma + 0.5)``), bit for bit."""
+    from scipy.ndimage import _filters
+
+    from fluidimage_gb300 import preproc as P
+
+    w, radius = P._gauss_weights(sigma)
+    assert radius == int(4.0 * sigma + 0.5)
+    want = _filters._gaussian_kernel1d(sigma, 0, radius)[::-1]
+    np.testing.assert_array_equal(w, want)
