@@ -66,6 +66,13 @@ def test_invalid_arguments_are_rejected_on_the_host(lib):
     with pytest.raises(_lib.CudaLibError, match="bad arguments"):
         _lib.check(lib.fi_tps_members(None, 0, None, None, 0, 0, None, None, None, None, None,
                                       None, None, None, None))
+    assert lib.fi_gaussian_filter(None, None, None, 0, 1, 1, 1, None, 1, None) == -1
+    assert b"null pointer" in lib.fi_last_error()
+    buf = C.create_string_buffer(64)
+    assert lib.fi_gaussian_filter(buf, buf, buf, 7, 1, 1, 1, buf, 1, None) == -1
+    assert b"bad dtype" in lib.fi_last_error()
+    assert lib.fi_sharpen_combine(buf, buf, 0, 0, 1.0, buf, None) == -1
+    assert b"bad arguments" in lib.fi_last_error()
 
 
 def test_version(lib):
