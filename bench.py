@@ -13,13 +13,20 @@ field's (65025 per pair).
   (host<->device copies inside the timed region): ``WorkPIV.calcul_series`` over a
   series of pairs (two pairs in flight, each on its own host thread and CUDA
   stream), and ``single_call``: ``WorkPIV.calcul``, one pair per call.
-* ``roofline``: the dominant kernel, timed with CUDA events inside the timed
-  steps, against MEASURED_PEAKS.json.
+* ``roofline``: the dominant kernel (the TPS subdomain solve), timed with CUDA
+  events inside the timed steps: its algorithmic bytes (one write and one read of
+  each subdomain's FP64-sized system) per launch over the launch time, against the
+  measured HBM copy bandwidth of MEASURED_PEAKS.json; ``traffic`` is the DRAM
+  bytes ncu measured for that kernel.  ``passes`` gives the same for each
+  correlation pass: FP32 FFT flops and unique image bytes over the pass time.
+* ``accuracy_vs_fp64``: the timed result against the FP64 oracle (complex128
+  FFTs, float64 fit): displacement and final-field errors in px.
 * ``cpu_baseline``: the CPU oracle (numpy restatement of the reference path), one
-  thread, on a 512x512 crop of the same workload.
+  thread, on pairs of the same 2048x2048 workload.
 
 ``--impl reference`` times that CPU oracle on all host cores (one process per
-core, one 512x512 sample pair per process and step) with the same metric.
+core, one 2048x2048 pair of the workload per process and step) with the same
+metric.
 
 Multi-GPU: replicas only (pairs are independent; no collective on the data path).
 """
@@ -45,7 +52,14 @@ sys.path.insert(0, str(ROOT))
 METRIC = "PIV vectors/s at <=0.005 px vs FP64; plain FP32 vs batched tensor-core form"
 UNIT = "vectors/s"
 WORKLOAD = "config2: 2048x2048 uint16 pair, Oseen vortex, 3 passes 64/32/16 px, overlap 0.5, fix thr 2, TPS subdom 200 smoothing 0.5"
-SAMPLE_SHAPE = (512, 512)
+SAMPLE_SHAPE = (2048, 2048)
+#: FP32 FFT work per window of n x n (2 R2C + 1 C2R at 2.5 N log2 N, plus the
+#: conjugate product and energies)
+def fft_flops(n):
+    import math
+
+    return 3 * 2.5 * n * n * math.log2(n * n) + 5 * n * n
+
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tps_solve_mp per subdomain:
 # one CTA of 16 warps per subdomain (launches of at most one subdomain per SM; 72
 # subdomains of the config-2 recipe at 1024^2) and two 8-warp CTAs per SM (the
@@ -73,7 +87,7 @@ def parse_args():
 # CPU oracle (reference arm and cpu_baseline): runs in separate processes
 # ------------------------------------------------------------------------------------
 def _oracle_sample(pair):
-    """Run the oracle multipass on one 512x512 sample pair; returns (vectors, seconds)."""
+    """Run the oracle multipass on one pair of the workload; returns (vectors, seconds)."""
     from fluidimage_gb300 import WorkPIV, workloads
     from oracle import piv as O
 
@@ -85,12 +99,8 @@ def _oracle_sample(pair):
     return int(res[-1].deltaxs.size), dt
 
 
-def _oracle_worker(pair, q):
-    q.put(_oracle_sample(pair))
-
-
 def _oracle_samples(min_seconds):
-    """Oracle multipass on successive 512x512 sample pairs until ``min_seconds`` of
+    """Oracle multipass on successive pairs of the workload until ``min_seconds`` of
     work; returns (vectors, seconds, pairs)."""
     nvec, dt, n = 0, 0.0, 0
     while dt < min_seconds and n < 200:
@@ -114,8 +124,30 @@ def cpu_baseline_single(min_seconds=10.0):
                       "numpy oracle, 1 thread"}
 
 
+_PAIR_CACHE = {}
+
+
+def _oracle_step(pair):
+    """One reference-arm task: the oracle multipass on pair ``pair`` of the workload
+    (images generated on the first call of the worker process and kept); returns
+    (vectors, seconds)."""
+    from fluidimage_gb300 import WorkPIV, workloads
+    from oracle import piv as O
+
+    if pair not in _PAIR_CACHE:
+        (im0, im1), _ = workloads.config2_images(pair=pair, shape=SAMPLE_SHAPE)
+        _PAIR_CACHE[pair] = (im0, im1)
+    im0, im1 = _PAIR_CACHE[pair]
+    params = workloads.config2_params(WorkPIV.create_default_params())
+    t0 = time.perf_counter()
+    res = O.multipass(im0, im1, params)
+    return int(res[-1].deltaxs.size), time.perf_counter() - t0
+
+
 def run_reference(args):
-    """Reference arm: the CPU oracle on all host cores, one process per core."""
+    """Reference arm: the CPU oracle on all host cores, one worker process per core,
+    each processing one pair of the workload per step (the reference's own
+    parallelism: one process per image pair)."""
     import multiprocessing as mp
 
     rank = int(os.environ.get("RANK", "0"))
@@ -125,31 +157,26 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     step_times, nvec_total = [], 0
-    for step in range(args.warmup + args.steps):
-        q = ctx.Queue()
-        procs = [ctx.Process(target=_oracle_worker, args=(1000 * step + c, q))
-                 for c in range(cores)]
-        t0 = time.perf_counter()
-        for p in procs:
-            p.start()
-        res = [q.get() for _ in procs]
-        for p in procs:
-            p.join()
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            step_times.append(dt)
-            nvec_total = sum(r[0] for r in res)
+    with ctx.Pool(cores) as pool:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_step, range(cores), chunksize=1)
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                step_times.append(dt)
+                nvec_total = sum(r[0] for r in res)
     ms = 1e3 * statistics.mean(step_times)
     value = nvec_total / (ms / 1e3)
+    sample = (f"{cores} worker processes x one {SAMPLE_SHAPE[0]}x{SAMPLE_SHAPE[1]} pair of "
+              "the workload each per step (numpy oracle, 1 thread per process)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": WORKLOAD,
-                                        "sample": f"{cores} pairs of {SAMPLE_SHAPE} per step"},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "same_config": True,
+                                        "sample": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x one {SAMPLE_SHAPE[0]}x"
-                                   f"{SAMPLE_SHAPE[1]} pair each per step (numpy oracle)"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -359,9 +386,8 @@ def run_gpu(args):
         return
 
     kern = timer.summary()
-    dominant = max(kern.items(), key=lambda kv: kv[1]["total_ms"])
     peaks, peak_kind = _peaks()
-    roof = roofline(dominant, outs, work, peaks, peak_kind, args.steps)
+    roof = roofline(kern, outs, work, peaks, peak_kind)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -389,9 +415,11 @@ def run_gpu(args):
         "tps_outer_iterations": _iter_stats(outs),
         "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kern.items()},
         "roofline": roof,
+        "correlation": pass_lines(kern, outs, work),
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
+        line["accuracy_vs_fp64"] = accuracy_vs_fp64(res, im0, im1, params)
         line["cpu_baseline"] = cpu_baseline_single()
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -425,57 +453,102 @@ def _result_bytes(res):
     return total
 
 
-def roofline(dominant, outs, work, peaks, peak_kind, steps):
-    """Roofline of the dominant library entry point (algorithmic work per launch)."""
-    name, stats = dominant
+def _tps_calls(outs):
+    return [t for pd in outs for t in (pd.tps_next, pd.tps_final)
+            if t is not None and hasattr(t, "nb_subdom")]
+
+
+def roofline(kern, outs, work, peaks, peak_kind):
+    """Roofline of the dominant library entry point (largest total time in the timed
+    steps), from its algorithmic bytes per launch and its CUDA-event time per
+    launch, against the measured HBM copy bandwidth."""
+    name, stats = max(kern.items(), key=lambda kv: kv[1]["total_ms"])
     avg_s = stats["avg_ms"] / 1e3
+    peak = float(peaks["hbm_gbs"])
     if name in ("fi_tps_solve", "fi_tps_solve_mp"):
-        # The reference solves each subdomain system with FP64 LU (gesv), once per
-        # component and outlier iteration: 2/3 (N+3)^3 flops each.  Bound: the FP64
-        # pipe (MEASURED_PEAKS.json has no FP64 figure: nominal 1.25 TFLOP/s).
-        flops = 0.0
-        nlaunch = 0
-        for pd in outs:
-            for tps in (pd.tps_next, pd.tps_final):
-                if tps is not None:
-                    n = tps.counts.astype(np.float64) + 3
-                    it = tps.iters.cpu().numpy().reshape(-1, 2).sum(axis=1)
-                    flops += float((2.0 / 3.0 * n**3 * it).sum())
-                    nlaunch += 1
-        per_launch = flops / max(nlaunch, 1)
-        achieved = per_launch / avg_s / 1e12
-        peak = 1.25
-        # DRAM bytes per subdomain from ncu captures of this kernel (one per launch
-        # shape), times the subdomains of each launch, averaged over the launches
         import torch
 
+        calls = _tps_calls(outs)
+        # algorithmic bytes: one write and one read of each subdomain's
+        # (N+3) x (N+3) system at 8 bytes per entry (the reference's FP64 matrix)
+        nbytes = sum(float((16.0 * (t.counts.astype(np.float64) + 3) ** 2).sum())
+                     for t in calls)
+        per_launch = nbytes / max(len(calls), 1)
+        achieved = per_launch / avg_s / 1e9
+        # DRAM bytes per subdomain from ncu captures of this kernel (one per launch
+        # shape), times the subdomains of each launch, averaged over the launches
         nsm = torch.cuda.get_device_properties(0).multi_processor_count
         traffic = sum(
             t.nb_subdom * (TPS_DRAM_BYTES_PER_SUBDOMAIN_WIDE if t.nb_subdom <= nsm
                            else TPS_DRAM_BYTES_PER_SUBDOMAIN_NARROW)
-            for pd in outs for t in (pd.tps_next, pd.tps_final) if t is not None
-        ) / max(nlaunch, 1)
-        return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+            for t in calls) / max(len(calls), 1)
+        # the reference's work for the same solves (FP64 LU, 2/3 (N+3)^3 flops per
+        # solve and outlier iteration): a speed note, not a roofline
+        lu = 0.0
+        for t in calls:
+            it = t.iters.cpu().numpy().reshape(-1, 2).sum(axis=1)
+            lu += float((2.0 / 3.0 * (t.counts.astype(np.float64) + 3) ** 3 * it).sum())
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch,
+                "work": "one write + one read of each subdomain's (N+3)^2 system at 8 B "
+                        "per entry, per launch",
                 "traffic_source": "ncu dram__bytes_read+write per subdomain (captures of "
                                   "both launch shapes) x subdomains, per launch",
-                "work": "reference-equivalent FP64 LU flops, sum 2/3 (N+3)^3 per solve",
-                "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)",
+                "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
+                "note": "latency-bound kernel (block-synchronous 32-wide tile steps); "
+                        "reference-equivalent FP64 LU rate "
+                        f"{lu / max(len(calls), 1) / avg_s / 1e12:.2f} TFLOP/s",
                 "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
-    # correlation / other: HBM bound by the unique image bytes + outputs
-    nbytes = 0.0
-    nlaunch = 0
-    for pd in outs:
-        H, W = work._pipelines[next(iter(work._pipelines))].imshape, None
-        lay = pd.layout
-        nbytes += 2 * H[0] * H[1] * 2 + 16 * lay.nvec
-        nlaunch += 1
-    per_launch = nbytes / max(nlaunch, 1)
+    H, W = work._pipelines[next(iter(work._pipelines))].imshape
+    per_launch = 2.0 * H * W * 2
     achieved = per_launch / avg_s / 1e9
-    peak = float(peaks["hbm_gbs"])
     return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({peak_kind})",
             "avg_ms": stats["avg_ms"], "launches": stats["launches"]}
+
+
+def pass_lines(kern, outs, work):
+    """Per correlation pass (one window size): windows, time, FP32 FFT work rate
+    and unique image bytes rate (CUDA events around each launch)."""
+    import torch
+
+    H, W = work._pipelines[next(iter(work._pipelines))].imshape
+    props = torch.cuda.get_device_properties(0)
+    lines = []
+    for pd in outs:
+        n = pd.layout.n
+        st = kern.get(f"fi_piv_pass[n={n}]")
+        if st is None:
+            continue
+        s = st["avg_ms"] / 1e3
+        nwin = pd.layout.nvec
+        lines.append({
+            "n": n, "windows": nwin, "ms": st["avg_ms"],
+            "fp32_tflops": nwin * fft_flops(n) / s / 1e12,
+            "image_gbs": 2.0 * H * W * 2 / s / 1e9,
+            "vectors_per_s": nwin / s,
+        })
+    # nominal FP32 FMA rate of the SMs (128 lanes x 2 flops x max clock)
+    clock = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz", 2070.0) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else 2070.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * clock * 1e6 / 1e12
+    for ln in lines:
+        ln["fp32_frac_of_nominal"] = ln["fp32_tflops"] / fp32_peak
+    return {"fp32_nominal_tflops": fp32_peak, "passes": lines}
+
+
+def accuracy_vs_fp64(res, im0, im1, params):
+    """The timed result against the FP64 oracle (the checker)."""
+    from oracle import accuracy as A
+
+    t0 = time.perf_counter()
+    ref = A.fp64_multipass(im0, im1, params)
+    acc = A.summary(res.passes, ref)
+    acc.pop("passes", None)
+    acc["oracle_seconds"] = round(time.perf_counter() - t0, 1)
+    return acc
 
 
 def run_preproc(args):

@@ -36,21 +36,30 @@ void add_launches(int k);
   } while (0)
 
 // Raises a kernel's dynamic shared-memory limit to at least `bytes` (above the 48 KB
-// default), calling the runtime only when the limit has to grow: `current` is the
-// call site's record of the limit set so far, read and written under one mutex so
-// that host threads launching concurrently never lower it.
+// default) on the current device, calling the runtime only when the limit has to
+// grow there.  The attribute is per device, so the call site's record keeps the
+// limit set so far for each device, read and written under one mutex so that host
+// threads launching concurrently never lower it.
 inline std::mutex& smem_limit_mutex() {
   static std::mutex m;
   return m;
 }
+constexpr int FI_SMEM_DEVICES = 64;
+struct SmemLimit {
+  size_t bytes[FI_SMEM_DEVICES] = {};
+};
 template <typename Kernel>
-inline cudaError_t raise_smem_limit(Kernel* kernel, size_t bytes, size_t& current) {
+inline cudaError_t raise_smem_limit(Kernel* kernel, size_t bytes, SmemLimit& rec) {
   if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  const cudaError_t ed = cudaGetDevice(&dev);
+  if (ed != cudaSuccess) return ed;
   std::lock_guard<std::mutex> lock(smem_limit_mutex());
-  if (bytes <= current) return cudaSuccess;
+  const bool cached = dev >= 0 && dev < FI_SMEM_DEVICES;
+  if (cached && bytes <= rec.bytes[dev]) return cudaSuccess;
   const cudaError_t e =
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) current = bytes;
+  if (e == cudaSuccess && cached) rec.bytes[dev] = bytes;
   return e;
 }
 

@@ -1054,12 +1054,8 @@ template <int N, bool FW>
 static int launch_pass(const fi_piv_pass_args& a, const float* w0, const float* w1, int nvec,
                        int npad, int do_peaks, cudaStream_t s) {
   using C = Cfg<N>;
-  static bool attr_done = false;
-  if (!attr_done) {
-    FI_CUDA_TRY(cudaFuncSetAttribute(k_piv_pass<N, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     C::SMEM));
-    attr_done = true;
-  }
+  static SmemLimit limit;
+  FI_CUDA_TRY(raise_smem_limit(k_piv_pass<N, FW>, C::SMEM, limit));
   const int blocks = (nvec + C::WPB - 1) / C::WPB;
   k_piv_pass<N, FW><<<blocks, C::THREADS, C::SMEM, s>>>(a, w0, w1, nvec, npad, do_peaks);
   return check_launch("k_piv_pass");
@@ -1071,12 +1067,8 @@ static int launch_peaks(float* planes, const double* norms, int count, const Pea
                         int32_t* pi1, int32_t* pcount, float* peaks, uint8_t* perr,
                         cudaStream_t s) {
   using C = Cfg<N>;
-  static bool attr_done = false;
-  if (!attr_done) {
-    FI_CUDA_TRY(
-        cudaFuncSetAttribute(k_peaks<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    attr_done = true;
-  }
+  static SmemLimit limit;
+  FI_CUDA_TRY(raise_smem_limit(k_peaks<N>, C::SMEM, limit));
   const int blocks = (count + C::WPB - 1) / C::WPB;
   k_peaks<N><<<blocks, C::THREADS, C::SMEM, s>>>(planes, norms, count, pa, dxs, dys, cm, errs,
                                                   pi0, pi1, pcount, peaks, perr);

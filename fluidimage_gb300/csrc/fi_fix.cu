@@ -235,21 +235,22 @@ extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
   const float dmax2 = (float)((double)a.displacement_max * (double)a.displacement_max);
   const float thr2 = (float)((double)a.threshold * (double)a.threshold);
   const int threads = 256, blocks = (nvec + threads - 1) / threads;
+  int kernels = 1;  // launches counted by check_launch
   if (a.use_threshold) {
     float* wx = a.work;
     float* wy = a.work + nvec;
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
     k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
-    add_launches(1);
+    kernels = 2;
     if (a.nb_peaks > 1) {
       k_fix_c<<<blocks, threads, 0, s>>>(a, wx, wy);
-      add_launches(1);
+      kernels = 3;
     }
   } else {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
                                        a.deltays_out);
   }
-  return check_launch("fi_fix");
+  return check_launch("fi_fix", kernels);
 }
 
 // Allocation-free variant of fi_fix: same kernels, scratch in g_fix_scratch.
@@ -273,6 +274,7 @@ extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
   const float dmax2 = (float)((double)a.displacement_max * (double)a.displacement_max);
   const float thr2 = (float)((double)a.threshold * (double)a.threshold);
   const int threads = 256, blocks = (nvec + threads - 1) / threads;
+  int kernels = 1;  // launches counted by check_launch
   if (a.use_threshold) {
     // stage A writes every scratch entry it uses before stage B reads it, so
     // nothing left by an earlier call is ever read
@@ -280,14 +282,14 @@ extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
     float* wy = scratch + nvec;
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, wx, wy);
     k_fix_b<<<blocks, threads, 0, s>>>(a, wx, wy, thr2);
-    add_launches(1);
+    kernels = 2;
     if (a.nb_peaks > 1) {
       k_fix_c<<<blocks, threads, 0, s>>>(a, wx, wy);
-      add_launches(1);
+      kernels = 3;
     }
   } else {
     k_fix_a<<<blocks, threads, 0, s>>>(a, nvec, a.correl_min, dmax2, a.deltaxs_out,
                                        a.deltays_out);
   }
-  return check_launch("fi_fix_static");
+  return check_launch("fi_fix_static", kernels);
 }

@@ -443,7 +443,7 @@ extern "C" int fi_rank_filter(const void* in, void* out, int dtype, int nt, int 
   }
   const size_t tile_smem = (size_t)(RS_TX + sx - 1) * (RS_TY + sy - 1) * sizeof(uint32_t);
   if (st == 1 && dtype != FI_PRE_F64 && tile_smem <= RS_MAX_SMEM) {
-    static size_t limit = 0;
+    static SmemLimit limit;
     FI_CUDA_TRY(raise_smem_limit(k_rank_select_tile, tile_smem, limit));
     const dim3 grid((unsigned)((nx + RS_TX - 1) / RS_TX), (unsigned)((ny + RS_TY - 1) / RS_TY),
                     (unsigned)nt);

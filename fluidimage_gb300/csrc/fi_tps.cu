@@ -1232,7 +1232,7 @@ extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_memb
   FI_REQUIRE(nb_subdom > 0, "fi_tps_solve: no subdomain");
   const size_t smem = (size_t)(max_members + 3) * sizeof(double) + (size_t)max_members * 4 + 16;
   FI_REQUIRE(smem <= 200 * 1024, "fi_tps_solve: subdomain of %d vectors too large", max_members);
-  static size_t limit = 0;
+  static SmemLimit limit;
   FI_CUDA_TRY(raise_smem_limit(k_tps_solve, smem, limit));
   k_tps_solve<<<nb_subdom, 512, smem, (cudaStream_t)stream>>>(
       plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, pivots, threshold,
@@ -1279,7 +1279,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                       (size_t)2 * max_members * sizeof(float2);
   FI_REQUIRE(smem <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
              max_members);
-  static size_t limit = 0;
+  static SmemLimit limit;
   FI_CUDA_TRY(raise_smem_limit(k_tps_eval, smem, limit));
   if (max_new_members > 0) {
     const int threads = 256;

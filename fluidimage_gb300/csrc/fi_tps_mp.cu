@@ -958,6 +958,9 @@ __global__ void __launch_bounds__(NT, 512 / NT)
     Vd[2 * np + i] = in ? df_split(V2[i]) : make_float2(0.f, 0.f);
   }
   __syncthreads();
+  // every CTA of the cluster has started (and holds its V) before any CTA writes
+  // into a peer's shared memory below
+  cluster.sync();
   // ---- Y = A V in double-float on the FP32 pipe.  A is symmetric: lane = column c,
   // the rows r in chunks (jobs = column block x chunk, a multiple of the warp count
   // when the scratch allows); the chunks' partial sums are added in a fixed order.
@@ -1458,7 +1461,7 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
   const size_t smem = lay.bytes;
   FI_REQUIRE(smem <= 220 * 1024, "fi_tps_solve_mp: subdomain of %d vectors too large",
              max_members);
-  static size_t limit_wide = 0, limit_narrow = 0;
+  static SmemLimit limit_wide, limit_narrow;
   if (wide)
     FI_CUDA_TRY(raise_smem_limit(k_tps_solve_mp<512>, smem, limit_wide));
   else

@@ -225,24 +225,36 @@ PHI_TABLE_SIZE = 1 << 22
 #: largest subdomain handled by the mixed-precision solver (shared-memory bound)
 MP_MAX_MEMBERS = 800
 _PHI_TABLES = {}
+_PHI_LOCK = threading.Lock()
 
 
 def phi_table(device, pairs=False):
-    """The per-device table of the TPS kernel values, float64 or (hi, lo) float pairs
-    (built on first use)."""
+    """The per-device table of the TPS kernel values, float64 or (hi, lo) float pairs.
+
+    Built on first use under a lock, on the calling thread's current stream, which
+    is synchronised before the table is published: a table taken from the cache is
+    complete whatever stream then reads it (``calcul_series`` runs couples on
+    several host threads and streams).  ``PIVPipeline`` builds the tables it needs
+    when it is constructed."""
     torch = _torch()
     key = (device.type, device.index if device.index is not None else torch.cuda.current_device(),
            pairs)
-    if key not in _PHI_TABLES:
-        if pairs:
-            table = torch.empty(2 * PHI_TABLE_SIZE, dtype=torch.float32, device=device)
-            fn, name = L.load().fi_tps_phi_table2, "fi_tps_phi_table2"
-        else:
-            table = torch.empty(PHI_TABLE_SIZE, dtype=torch.float64, device=device)
-            fn, name = L.load().fi_tps_phi_table, "fi_tps_phi_table"
-        L.check(fn(L.ptr(table), PHI_TABLE_SIZE, L.stream_handle()), name)
-        _PHI_TABLES[key] = table
-    return _PHI_TABLES[key]
+    table = _PHI_TABLES.get(key)
+    if table is not None:
+        return table
+    with _PHI_LOCK:
+        if key not in _PHI_TABLES:
+            if pairs:
+                table = torch.empty(2 * PHI_TABLE_SIZE, dtype=torch.float32, device=device)
+                fn, name = L.load().fi_tps_phi_table2, "fi_tps_phi_table2"
+            else:
+                table = torch.empty(PHI_TABLE_SIZE, dtype=torch.float64, device=device)
+                fn, name = L.load().fi_tps_phi_table, "fi_tps_phi_table"
+            stream = torch.cuda.current_stream(device)
+            L.check(fn(L.ptr(table), PHI_TABLE_SIZE, stream.cuda_stream), name)
+            stream.synchronize()
+            _PHI_TABLES[key] = table
+        return _PHI_TABLES[key]
 
 
 def lattice_coords(px, py, npts, stream=None):
@@ -585,6 +597,12 @@ class PIVPipeline:
             lay.dev["lattice"] = (torch.as_tensor(xy2, device=self.device),
                                   torch.ones(1, dtype=torch.int32, device=self.device))
             self.layouts.append(lay)
+        if mp.use_tps is True or (mp.use_tps == "last" and interp_last):
+            # the TPS tables, built here (the constructing thread) before any run
+            dev = self.device if self.device.index is not None else torch.device(
+                "cuda", torch.cuda.current_device())
+            phi_table(dev)
+            phi_table(dev, pairs=True)
 
     # ----------------------------------------------------------------------
     def run(self, im0, im1, stream=None) -> List[PassDevice]:
@@ -691,7 +709,7 @@ class PIVPipeline:
         a.nb_peaks = self.nb_peaks
         a.peaks_count, a.peaks, a.peaks_err = (L.ptr(out.peaks_count), L.ptr(out.peaks),
                                                L.ptr(out.peaks_err))
-        with _timed("fi_piv_pass"):
+        with _timed(f"fi_piv_pass[n={lay.n}]"):
             L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
         return out
 

@@ -109,8 +109,8 @@ class WorkPIV:
     keep_correls : store the correlation planes in ``HeavyPIVResults.correls``
         (upstream always stores them; here they cost a device-to-host copy).
     device : torch device (default ``cuda``).
-    interp_last : compute the final interpolation (``deltaxs_final``...); it is
-        TPS here, so ``use_tps=False`` (upstream: griddata) needs ``False``.
+    interp_last : compute the final interpolation (``deltaxs_final``...): TPS for
+        ``use_tps`` True or ``'last'``, griddata for ``use_tps=False``, as upstream.
     """
 
     @classmethod

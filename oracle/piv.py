@@ -387,35 +387,39 @@ def secondary_peaks(work, norms, err, i0, i1, shape_crop, box0, box1, nb_peaks,
 # a11: subpixel fit — calcul/subpix.py:16-61 ('2d_gaussian2'), :107-218 (SubPix)
 # ----------------------------------------------------------------------------------
 def _gaussian2(crops):
-    """'2d_gaussian2' on a stack of 3x3 float32 crops (subpix.py:16-61)."""
-    c = crops.astype(np.float32, copy=True)
+    """'2d_gaussian2' on a stack of 3x3 crops (subpix.py:16-61): float32 like the
+    upstream code for float32 planes, float64 throughout for float64 planes (the
+    FP64 oracle)."""
+    real = np.float64 if crops.dtype == np.float64 else np.float32
+    pow2 = _f32_pow2 if real is np.float32 else (lambda a: a * a)
+    c = crops.astype(real, copy=True)
     cmin = c.reshape(-1, 9).min(axis=1)
     c -= cmin[:, None, None]
     cmax = c.reshape(-1, 9).max(axis=1)
     with np.errstate(invalid="ignore", divide="ignore"):
         c /= cmax[:, None, None]
-    c[c == 0] = _F32_1EM8
+    c[c == 0] = real(1e-8)
     with np.errstate(invalid="ignore", divide="ignore"):
         L = np.log(c)
-    z = np.zeros(c.shape[0], dtype=np.float32)
+    z = np.zeros(c.shape[0], dtype=real)
     c10, c01, c11, c20, c02 = z.copy(), z.copy(), z.copy(), z.copy(), z.copy()
     with np.errstate(invalid="ignore", over="ignore"):
         for a in range(3):
             for b in range(3):
                 l = L[:, a, b]
-                c10 = c10 + np.float32(b - 1) * l
-                c01 = c01 + np.float32(a - 1) * l
-                c11 = c11 + np.float32((b - 1) * (a - 1)) * l
-                c20 = c20 + np.float32(3 * (b - 1) ** 2 - 2) * l
-                c02 = c02 + np.float32(3 * (a - 1) ** 2 - 2) * l
-        c10 = c10 / np.float32(6)
-        c01 = c01 / np.float32(6)
-        c11 = c11 / np.float32(4)
-        c20 = c20 / np.float32(6)
-        c02 = c02 / np.float32(6)
-        den = np.float32(4) * c20 * c02 - _f32_pow2(c11)
-        deplx = (c11 * c01 - np.float32(2) * c10 * c02) / den
-        deply = (c11 * c10 - np.float32(2) * c01 * c20) / den
+                c10 = c10 + real(b - 1) * l
+                c01 = c01 + real(a - 1) * l
+                c11 = c11 + real((b - 1) * (a - 1)) * l
+                c20 = c20 + real(3 * (b - 1) ** 2 - 2) * l
+                c02 = c02 + real(3 * (a - 1) ** 2 - 2) * l
+        c10 = c10 / real(6)
+        c01 = c01 / real(6)
+        c11 = c11 / real(4)
+        c20 = c20 / real(6)
+        c02 = c02 / real(6)
+        den = real(4) * c20 * c02 - pow2(c11)
+        deplx = (c11 * c01 - real(2) * c10 * c02) / den
+        deply = (c11 * c10 - real(2) * c01 * c20) / den
     return deplx, deply
 
 
@@ -424,7 +428,8 @@ _YC = _XC.T.copy()
 
 
 def subpix_2d_gaussian2(planes, i0, i1, shape_crop):
-    """``apply_subpix`` with method '2d_gaussian2' and its centroid fallback.
+    """``apply_subpix`` with method '2d_gaussian2' and its centroid fallback (float32
+    arithmetic for float32 planes, float64 for the FP64 oracle's float64 planes).
 
     Returns ``(deltax, deltay, wrong)``; where ``wrong`` is True the upstream code
     raises ``PIVError('wrong subpix')`` and keeps the integer displacement.
@@ -436,14 +441,16 @@ def subpix_2d_gaussian2(planes, i0, i1, shape_crop):
     c = i1[:, None, None] + np.arange(-1, 2)[None, None, :]
     crops = planes[idx[:, None, None], r, c]
     deplx, deply = _gaussian2(crops)
+    real = deplx.dtype.type
+    pow2 = _f32_pow2 if real is np.float32 else (lambda a: a * a)
     with np.errstate(invalid="ignore", over="ignore"):
-        big = (_f32_pow2(deplx) + _f32_pow2(deply)) > np.float32(4.5)
-    dx = np.empty(nvec, dtype=np.float32)
-    dy = np.empty(nvec, dtype=np.float32)
+        big = (pow2(deplx) + pow2(deply)) > real(4.5)
+    dx = np.empty(nvec, dtype=real)
+    dy = np.empty(nvec, dtype=real)
     wrong = np.zeros(nvec, dtype=bool)
     with np.errstate(invalid="ignore", over="ignore"):
-        gx = np.float32(ix0) - (deplx + i1.astype(np.float32))
-        gy = np.float32(iy0) - (deply + i0.astype(np.float32))
+        gx = real(ix0) - (deplx + i1.astype(real))
+        gy = real(iy0) - (deply + i0.astype(real))
     dx[:] = gx
     dy[:] = gy
     for k in np.nonzero(big)[0]:
@@ -548,8 +555,10 @@ def piv_pass(im0, im1, shape_crop, overlap, *, grid=None, dxin=None, dyin=None,
     nvec = gx.size
     dmax = parse_displacement_max(displacement_max, shape_crop)
 
-    deltaxs = np.full(nvec, np.nan, dtype=np.float32)
-    deltays = np.full(nvec, np.nan, dtype=np.float32)
+    # float32 results like upstream; float64 ones for the FP64 oracle
+    real = np.float32 if dtype_complex == np.complex64 else np.float64
+    deltaxs = np.full(nvec, np.nan, dtype=real)
+    deltays = np.full(nvec, np.nan, dtype=real)
     correls_max = np.full(nvec, np.nan, dtype=np.float32)
     err = np.full(nvec, ERR_BAD_CROP, dtype=np.uint8)
     planes_all = None
@@ -565,8 +574,8 @@ def piv_pass(im0, im1, shape_crop, overlap, *, grid=None, dxin=None, dyin=None,
         if nb_peaks_to_search > 1:
             for j, k in enumerate(iv):
                 secondary[k] = out[6][j]
-        fdx = dx.astype(np.float32)
-        fdy = dy.astype(np.float32)
+        fdx = dx.astype(real)
+        fdy = dy.astype(real)
         ok = e == 0
         if apply_subpix and ok.any():
             k = np.nonzero(ok)[0]

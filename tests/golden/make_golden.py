@@ -2,7 +2,8 @@
 
 Run from the repository root (needs the upstream sources, not needed afterwards):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [case ...]
+    FLUIDIMAGE_REFERENCE_SRC=<upstream checkout>/src PYTHONDONTWRITEBYTECODE=1 \
+        python tests/golden/make_golden.py [case ...]
 
 Each case writes ``tests/golden/<case>.npz`` holding the input images, the
 parameters (JSON) and the upstream outputs of ``WorkPIV.calcul`` (every pass:
@@ -116,6 +117,9 @@ def case_correl_window():
         ("sq32_dmax", (32, 32), (3.3, 5.8), "50%"),
         ("sq16", (16, 16), (-2.4, 1.6), None),
         ("sq64", (64, 64), (7.7, -4.2), None),
+        ("sq24", (24, 24), (2.6, -3.1), None),
+        ("sq48", (48, 48), (-5.3, 4.4), None),
+        ("sq48_dmax", (48, 48), (-5.3, 4.4), 9.0),
     ]
     for icase, (tag, shape, shift, dmax) in enumerate(rng_cases):
         model = synthetic.ParticleModel(density=0.06, noise=2.0, dtype="uint8")
@@ -273,6 +277,44 @@ def case_subpix_methods():
         }, keep_planes=True)
 
 
+def case_window_48_24():
+    """Upstream's default first window (shape_crop_im0 = 48) in two passes, 48 -> 24
+    px (the radix-3 FFT sizes), overlap 0.5, TPS between passes and at the end, on a
+    320x320 uint16 12-bit Oseen pair."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = synthetic.oseen_vortex((320, 320), d_max=6.0, rc=50.0)
+    im0, im1 = synthetic.make_pair((320, 320), field, model, seed=9000)
+    run_workpiv("multipass_48_24", im0, im1, {
+        "piv0.shape_crop_im0": 48, "piv0.grid.overlap": 0.5,
+        "multipass.number": 2, "multipass.coeff_zoom": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 200, "multipass.smoothing_coef": 0.5,
+        "fix.threshold_diff_neighbour": 2,
+    })
+
+
+def case_overlap_075():
+    """Overlap 0.75: 24 px windows in one pass (step 6 px) with the final TPS, and 64
+    -> 32 px windows in two passes (the overlap of the batched workloads), uint8."""
+    model = synthetic.ParticleModel(density=0.05, noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((160, 192), synthetic.sinusoid(3.0, 160.0), model,
+                                   seed=9100)
+    run_workpiv("single_pass_24_ov75", im0, im1, {
+        "piv0.shape_crop_im0": 24, "piv0.grid.overlap": 0.75,
+        "multipass.number": 1, "multipass.use_tps": "last",
+        "multipass.subdom_size": 150, "multipass.smoothing_coef": 1.0,
+        "fix.threshold_diff_neighbour": 3,
+    })
+    field = synthetic.oseen_vortex((256, 256), d_max=5.0, rc=50.0)
+    im0, im1 = synthetic.make_pair((256, 256), field, model, seed=9200)
+    run_workpiv("multipass_64_32_ov75", im0, im1, {
+        "piv0.shape_crop_im0": 64, "piv0.grid.overlap": 0.75,
+        "multipass.number": 2, "multipass.coeff_zoom": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 200, "multipass.smoothing_coef": 0.5,
+        "fix.threshold_diff_neighbour": 2,
+    })
+
+
 PREPROC_CASES = [
     # (name, function, image key, kwargs)
     ("minima_u8_w7", "sliding_minima", "u8", dict(window_size=7)),
@@ -352,6 +394,8 @@ CASES = {
     "griddata_oseen_three_pass": case_griddata_oseen,
     "secondary_peaks_two_pass": case_secondary_peaks,
     "subpix_methods": case_subpix_methods,
+    "multipass_48_24": case_window_48_24,
+    "overlap_075": case_overlap_075,
     "preproc": case_preproc,
 }
 

@@ -20,7 +20,9 @@ import sys
 import types
 from pathlib import Path
 
-DEFAULT_SRC = Path(os.environ.get("FLUIDIMAGE_REFERENCE_SRC", "/root/reference/src"))
+#: environment variable naming the upstream ``src`` directory (the one holding the
+#: ``fluidimage`` package); ``install`` also takes the path as its argument
+SRC_ENV = "FLUIDIMAGE_REFERENCE_SRC"
 
 
 class _Stub(types.ModuleType):
@@ -91,9 +93,17 @@ class _ArrayFactory:
         return object
 
 
-def install(src: Path | str = DEFAULT_SRC):
-    """Install the stand-ins and the ``fluidimage`` namespace package."""
+def install(src: Path | str | None = None):
+    """Install the stand-ins and the ``fluidimage`` namespace package from the
+    upstream ``src`` directory ``src`` (default: the ``FLUIDIMAGE_REFERENCE_SRC``
+    environment variable)."""
+    if src is None:
+        src = os.environ.get(SRC_ENV)
+    if not src:
+        raise RuntimeError(f"give the upstream src directory (argument or ${SRC_ENV})")
     src = Path(src)
+    if not (src / "fluidimage" / "works" / "piv").is_dir():
+        raise RuntimeError(f"{src} does not hold the upstream fluidimage package")
     if "fluidimage" in sys.modules and getattr(sys.modules["fluidimage"], "_graft_harness", False):
         return sys.modules["fluidimage"]
     sys.dont_write_bytecode = True

@@ -210,10 +210,29 @@ def _compare_secondary(z, ip, r, tie, report):
                                   "edges_single_pass", "secondary_peaks_two_pass",
                                   "griddata_two_pass", "griddata_oseen_three_pass",
                                   "subpix_gaussian_single", "subpix_centroid2_single",
-                                  "subpix_none_single"])
+                                  "subpix_none_single", "multipass_48_24",
+                                  "single_pass_24_ov75", "multipass_64_32_ov75"])
 def test_workpiv_matches_reference(name):
     z, res = _run(name)
     assert len(res.passes) == int(z["nb_passes"])
+    report = []
+    prev = None
+    for ip, r in enumerate(res.passes):
+        _compare_pass(z, ip, r, report, prev)
+        prev = r
+    print(name, report)
+
+
+@pytest.mark.parametrize("name", ["multipass_small", "multipass_48_24"])
+def test_tps_lu_fallback_matches_reference(name, monkeypatch):
+    """Every TPS subdomain through the FP64 LU kernel (the path of the subdomains the
+    mixed-precision solver hands over: rank-deficient P, a non-positive pivot, no
+    convergence, or more members than its shared-memory tiles hold), forced by a
+    member limit of 0: same results as upstream, and every subdomain flagged."""
+    from fluidimage_gb300 import engine
+
+    monkeypatch.setattr(engine, "MP_MAX_MEMBERS", 0)
+    z, res = _run(name, device="cuda")
     report = []
     prev = None
     for ip, r in enumerate(res.passes):
