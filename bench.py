@@ -78,6 +78,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=2048,
                     help="image side (2048 = the config; smaller sizes for profiling)")
+    ap.add_argument("--no-precision-sweep", action="store_true",
+                    help="skip the tensor-core precision sweep (the 4096^2 single-pass workload)")
     ap.add_argument("--preproc", action="store_true",
                     help="time the preprocessing tools instead (second JSON line format)")
     return ap.parse_args()
@@ -418,6 +420,8 @@ def run_gpu(args):
         "correlation": pass_lines(kern, outs, work),
         "clocks": clk,
     }
+    if not args.no_precision_sweep:
+        line["precision_sweep"] = precision_sweep(args, dev, flush, peaks, peak_kind)
     if not args.no_cpu_baseline:
         line["accuracy_vs_fp64"] = accuracy_vs_fp64(res, im0, im1, params)
         line["cpu_baseline"] = cpu_baseline_single()
@@ -537,6 +541,91 @@ def pass_lines(kern, outs, work):
     for ln in lines:
         ln["fp32_frac_of_nominal"] = ln["fp32_tflops"] / fp32_peak
     return {"fp32_nominal_tflops": fp32_peak, "passes": lines}
+
+
+TC_FORMS = ("fp32_fft", "bf16x1", "bf16x3", "fp16x3")
+
+
+def precision_sweep(args, dev, flush, peaks, peak_kind):
+    """The plain FP32 FFT pass against the tensor-core DFT pass in its three forms on
+    the precision-sweep workload: one 4096^2 uint16 pair, 32 px windows at overlap
+    0.75 (259 081 vectors), sinusoidal displacement, WorkFIX and the final TPS.
+    Per form: the correlation pass alone and the whole step (device-resident
+    images, CUDA events, L2 flushed between steps), the tensor pipe's executed
+    flops, and the error against the FP64 oracle on a 4096 x 768 band."""
+    import torch
+
+    from fluidimage_gb300 import WorkPIV, engine, workloads
+    from oracle import accuracy as A
+
+    shape = (4096, 4096)
+    (im0, im1), _ = workloads.config4_images(shape=shape)
+    t0 = torch.from_numpy(im0.view(np.int16)).to(dev)
+    t1 = torch.from_numpy(im1.view(np.int16)).to(dev)
+    band = (slice(0, 768), slice(None))
+    b0, b1 = np.ascontiguousarray(im0[band]), np.ascontiguousarray(im1[band])
+    params_ref = workloads.config4_params(WorkPIV.create_default_params())
+    ref = A.fp64_multipass(b0, b1, params_ref)
+    out = {"workload": "4096x4096 uint16 12-bit, density 0.06, diameter 2.5 px, noise 1 %, "
+                       "d = 5 (sin 2 pi y/512, cos 2 pi x/512) px, 32 px windows overlap 0.75, "
+                       "WorkFIX thr 2, final TPS subdom 256",
+           "accuracy_band": "rows 0-767 (all columns)", "forms": {}}
+    steps = max(3, min(args.steps, 10))
+    for form in TC_FORMS:
+        params = workloads.config4_params(WorkPIV.create_default_params())
+        params.piv0.method_correl = "gb300" if form == "fp32_fft" else f"gb300_tc_{form}"
+        work = WorkPIV(params, device=dev)
+        for _ in range(2):
+            outs = work.calcul_device(t0, t1)
+        torch.cuda.synchronize()
+        timer = engine.KernelTimer()
+        step_ms = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            engine.TIMER = timer
+            e0.record()
+            outs = work.calcul_device(t0, t1)
+            e1.record()
+            engine.TIMER = None
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+        kern = timer.summary()
+        name = "fi_piv_pass[n=32]" if form == "fp32_fft" else "fi_piv_pass_tc[n=32]"
+        pass_ms = kern[name]["avg_ms"]
+        nvec = outs[0].layout.nvec
+        entry = {"pass_ms": pass_ms, "pass_vectors_per_s": nvec / (pass_ms / 1e3),
+                 "step_ms": statistics.mean(step_ms),
+                 "step_vectors_per_s": nvec / (statistics.mean(step_ms) / 1e3),
+                 "vectors": nvec}
+        if form == "fp32_fft":
+            entry["fp32_tflops"] = nvec * fft_flops(32) / (pass_ms / 1e3) / 1e12
+        else:
+            terms = 1 if form == "bf16x1" else 3
+            # executed dense MMA flops per window: 4 stages of M 128 tiles over 8
+            # windows: 2 x (2 x 2 x 128 x 32 x 32) + 2 x 128 x 64 x 64 x 2 +
+            # 2 x 128 x 64 x 64 + 2 x 2 x 128 x 32 x 32, per term
+            flops = terms * (2 * 2 * 2 * 128 * 32 * 32 + 2 * 2 * 128 * 64 * 64
+                             + 2 * 128 * 64 * 64 + 2 * 2 * 128 * 32 * 32) / 8
+            achieved = nvec * flops / (pass_ms / 1e3) / 1e12
+            entry.update({"tensor_tflops_executed": achieved,
+                          "tensor_frac_of_bf16_peak": achieved / float(peaks["bf16_tflops"]),
+                          "peak_source": f"bf16_tflops of MEASURED_PEAKS.json ({peak_kind})",
+                          "mma_flops_per_window": flops})
+        wb = WorkPIV(params, device=dev)
+        resb = wb.calcul({"arrays": (b0, b1), "names": ("im0", "im1")})
+        acc = A.summary(resb.passes, ref)
+        acc.pop("passes", None)
+        entry["accuracy_vs_fp64"] = acc
+        out["forms"][form] = entry
+    base = out["forms"]["fp32_fft"]
+    for form in TC_FORMS[1:]:
+        f = out["forms"][form]
+        f["pass_speedup_vs_fp32_fft"] = base["pass_ms"] / f["pass_ms"]
+        f["step_speedup_vs_fp32_fft"] = base["step_ms"] / f["step_ms"]
+    return out
 
 
 def accuracy_vs_fp64(res, im0, im1, params):

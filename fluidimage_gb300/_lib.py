@@ -33,6 +33,10 @@ FIX_REPLACED = 8
 FIX_STATIC_MAX_VECTORS = 262144
 
 SUBPIX_METHODS = {"2d_gaussian2": 0, "2d_gaussian": 1, "centroid": 2, "no_subpix": 3}
+#: precision forms of the tensor-core pass (FI_TC_*)
+TC_FORMS = {"bf16x1": 0, "bf16x3": 1, "fp16x3": 2}
+#: window size of the tensor-core pass
+TC_WINDOW = 32
 MAX_NSUBPIX = 4
 MAX_PEAKS = 4
 PEAK_FIELDS = 5
@@ -90,6 +94,7 @@ _SIGNATURES = {
     "fi_launch_count": (C.c_longlong, []),
     "fi_images_min": (C.c_int, [P, P, C.c_int, C.c_int64, P, P]),
     "fi_piv_pass": (C.c_int, [P, P]),
+    "fi_piv_pass_tc": (C.c_int, [P, C.c_int, P, P]),
     "fi_correl_windows": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P]),
     "fi_peaks_from_planes": (
         C.c_int,

@@ -526,6 +526,7 @@ class PassDevice:
     peaks: object = None
     peaks_err: object = None
     replaced: object = None  # [nvec, 3] old dx, dy, correl_max of replaced vectors
+    tc_status: object = None  # device status word of the tensor-core pass (if it ran)
     tps_next: Optional[object] = None  # TpsOutput or GridOutput: this pass on the next grid
     tps_final: Optional[object] = None  # TpsOutput or GridOutput: on its own grid
 
@@ -542,6 +543,14 @@ class PIVPipeline:
         if self.dtype not in _DTYPES:
             raise TypeError(f"image dtype {self.dtype} not supported (uint8, uint16, float32)")
         self.device = torch.device(device if device is not None else "cuda")
+        from .piv import TC_TAGS
+
+        form = TC_TAGS.get(params.piv0.method_correl)
+        #: FI_TC_* form of the tensor-core pass (32 px passes), None: FP32 FFT pass
+        self.tc_form = None if form is None else L.TC_FORMS[form]
+        #: device status word of the tensor-core passes (non-zero: a wait timed out)
+        self.tc_status = (torch.zeros(1, dtype=torch.int32, device=self.device)
+                          if self.tc_form is not None else None)
         self.keep_correls = keep_correls
         self.interp_last = interp_last
         p0, mp = params.piv0, params.multipass
@@ -709,8 +718,14 @@ class PIVPipeline:
         a.nb_peaks = self.nb_peaks
         a.peaks_count, a.peaks, a.peaks_err = (L.ptr(out.peaks_count), L.ptr(out.peaks),
                                                L.ptr(out.peaks_err))
-        with _timed(f"fi_piv_pass[n={lay.n}]"):
-            L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
+        if self.tc_form is not None and lay.n == L.TC_WINDOW:
+            out.tc_status = self.tc_status
+            with _timed(f"fi_piv_pass_tc[n={lay.n}]"):
+                L.check(lib.fi_piv_pass_tc(C.byref(a), self.tc_form, L.ptr(self.tc_status), s),
+                        "fi_piv_pass_tc")
+        else:
+            with _timed(f"fi_piv_pass[n={lay.n}]"):
+                L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
         return out
 
     def _run_fix(self, cur: PassDevice, fx, s):

@@ -22,8 +22,12 @@ from .errors import InterpError
 from .params import ParamContainer
 
 #: correlation tags computed by this backend (FFT cross-correlation semantics of
-#: CorrelFFTNumpy / CorrelFFTW, calcul/correl.py:639-692)
-FFT_TAGS = ("gb300", "np.fft", "fftw")
+#: CorrelFFTNumpy / CorrelFFTW, calcul/correl.py:639-692): the FP32 FFT pass, and the
+#: tensor-core DFT pass in one of its precision forms (32 px passes; passes of other
+#: window sizes run the FP32 FFT pass)
+TC_TAGS = {"gb300_tc_bf16x1": "bf16x1", "gb300_tc_bf16x3": "bf16x3",
+           "gb300_tc_fp16x3": "fp16x3"}
+FFT_TAGS = ("gb300", "np.fft", "fftw") + tuple(TC_TAGS)
 
 
 def _complete_params_piv0(params):
@@ -255,6 +259,8 @@ class WorkPIV:
                 want[(k, key)] = getattr(pd, key)
             if pd.planes is not None:
                 want[(k, "planes")] = pd.planes
+            if pd.tc_status is not None:
+                want[(k, "tc_status")] = pd.tc_status
             if pd.dxin is not None:
                 want[(k, "dxin")], want[(k, "dyin")] = pd.dxin, pd.dyin
             if pd.peaks_count is not None:
@@ -297,6 +303,8 @@ class WorkPIV:
         hosts = []
         for k, pd in enumerate(outs):
             lay = pd.layout
+            if pd.tc_status is not None and int(got[(k, "tc_status")][0]) != 0:
+                raise RuntimeError("tensor-core PIV pass: a wait on the tensor cores timed out")
             h = {key: got[(k, key)] for key in keys}
             errors = error_dict(h["errors"], h["fix_flags"], h["diff2"],
                                 fx.threshold_diff_neighbour)

@@ -47,3 +47,26 @@ def config2_params(params):
     params.multipass.smoothing_coef = 0.5
     params.fix.threshold_diff_neighbour = 2
     return params
+
+
+def config4_images(pair=0, shape=(4096, 4096)):
+    """Precision-sweep pair: uint16 12-bit, density 0.06 particles/px, diameter 2.5 px,
+    noise 1 % of the maximum, d = 5 (sin(2 pi y / 512), cos(2 pi x / 512)) px."""
+    model = synthetic.ParticleModel(density=0.06, diameter=(2.5, 2.5), intensity=(1000, 4000),
+                                    noise=0.01 * 4095, dtype="uint16", max_value=4095)
+    field = synthetic.sinusoid(5.0, 512.0)
+    return synthetic.make_pair(shape, field, model, seed=4000 + pair), field
+
+
+def config4_params(params):
+    """One pass of 32 px windows at overlap 0.75 (509 x 509 = 259 081 vectors at
+    4096^2), WorkFIX with neighbour threshold 2, final TPS on subdomains of 256
+    vectors."""
+    params.piv0.shape_crop_im0 = 32
+    params.piv0.grid.overlap = 0.75
+    params.multipass.number = 1
+    params.multipass.use_tps = "last"
+    params.multipass.subdom_size = 256
+    params.multipass.smoothing_coef = 0.5
+    params.fix.threshold_diff_neighbour = 2
+    return params

@@ -142,6 +142,24 @@ typedef struct fi_piv_pass_args {
  */
 int fi_piv_pass(const fi_piv_pass_args* args, void* stream);
 
+/* Precision forms of the tensor-core pass (fi_piv_pass_tc). */
+#define FI_TC_BF16X1 0 /* one bf16 term per operand                              */
+#define FI_TC_BF16X3 1 /* bf16 hi + lo, products hi*hi + hi*lo + lo*hi           */
+#define FI_TC_FP16X3 2 /* fp16 hi + lo, 3-term products, power-of-two scaling     */
+
+/*
+ * The PIV pass of fi_piv_pass (same arguments, same outputs, same peak search,
+ * second chance and subpixel fit) with the correlation planes computed on the
+ * tensor cores: the 2-D DFTs of CorrelFFTNumpy.__call__ (calcul/correl.py:671-685
+ * with calcul/fft.py:254-269, F[0,0] = 0, _like_fftshift layout) as dense
+ * contractions F W F^T in `form` precision (FI_TC_*), accumulated in FP32.
+ * 32 x 32 windows.  status: nullable device int, OR-ed with 1 when a wait of the
+ * kernel on its tensor-core work timed out (the affected windows are not written).
+ * Near-tie flags (FI_FLAG_NEAR_TIE) use the form's plane error as tolerance:
+ * 3e-2 (BF16X1), 1e-4 (BF16X3), 1e-5 (FP16X3) relative to the peak.
+ */
+int fi_piv_pass_tc(const fi_piv_pass_args* args, int form, int* status, void* stream);
+
 /*
  * Per-window plugin contract: correlation planes and norms of `count` window
  * pairs (float32, n x n each, C order), like CorrelFFTNumpy.__call__

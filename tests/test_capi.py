@@ -77,3 +77,18 @@ def test_invalid_arguments_are_rejected_on_the_host(lib):
 
 def test_version(lib):
     assert lib.fi_version().startswith(b"fluidimage_gb300")
+
+
+def test_tc_pass_argument_checks(lib):
+    """fi_piv_pass_tc refuses window sizes other than 32 and unknown forms before any
+    CUDA call."""
+    from fluidimage_gb300 import _lib as L
+
+    a = L.PivPassArgs()
+    a.n = 16
+    assert lib.fi_piv_pass_tc(C.byref(a), 1, None, None) == -1
+    assert b"window size" in lib.fi_last_error()
+    a.n = 32
+    assert lib.fi_piv_pass_tc(C.byref(a), 7, None, None) == -1
+    assert b"bad form" in lib.fi_last_error()
+    assert lib.fi_piv_pass_tc(None, 1, None, None) == -1
