@@ -91,7 +91,9 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 }
 
 // Shared-memory matrix descriptor, no swizzle: start address, leading and stride
-// byte offsets (K-major: leading = K direction; MN-major: leading = M/N direction).
+// byte offsets between core matrices (8 rows x 16 bytes, stored contiguously).
+// K-major: leading = K direction, stride = M/N direction.  MN-major: leading = K
+// direction, stride = M/N direction as well (the canonical no-swizzle layouts).
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
   d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
@@ -553,8 +555,8 @@ __global__ void __launch_bounds__(THREADS, 2)
       const uint32_t id = idesc(F16, true, 64);
       for (int img = 0; img < 2; ++img)
         for (int ks = 0; ks < 4; ++ks)
-          mma_terms(tmem + 128 + 64 * img, sA_u + (img * 2) * A2_PART + ks * 4096, A2_PART, 128,
-                    2048, sB2 + ks * 256, B2_BYTES, 128, 1024, id, ks == 0);
+          mma_terms(tmem + 128 + 64 * img, sA_u + (img * 2) * A2_PART + ks * 4096, A2_PART, 2048,
+                    128, sB2 + ks * 256, B2_BYTES, 128, 1024, id, ks == 0);
     });
     if (!ok) break;
     // ---------------- epilogue 2: cross spectrum P = conj(F0) F1 ----------------
@@ -664,7 +666,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       const uint32_t id = idesc(F16, true, 32);
       for (int t = 0; t < 2; ++t)
         for (int ks = 0; ks < 2; ++ks)
-          mma_terms(tmem + 128 + 32 * t, sA_u + (t * 2) * A4_PART + ks * 4096, A4_PART, 128, 2048,
+          mma_terms(tmem + 128 + 32 * t, sA_u + (t * 2) * A4_PART + ks * 4096, A4_PART, 2048, 128,
                     sB4 + ks * 256, B4_BYTES, 128, 512, id, ks == 0);
     });
     if (!ok) break;
