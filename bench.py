@@ -80,6 +80,12 @@ def parse_args():
                     help="image side (2048 = the config; smaller sizes for profiling)")
     ap.add_argument("--no-precision-sweep", action="store_true",
                     help="skip the tensor-core precision sweep (the 4096^2 single-pass workload)")
+    ap.add_argument("--sweep-only", action="store_true",
+                    help="run only the precision sweep (one JSON line; for profiling)")
+    ap.add_argument("--forms", default=",".join(TC_FORMS),
+                    help="forms of the precision sweep (fp32_fft, bf16x1, bf16x3, fp16x3)")
+    ap.add_argument("--sweep-size", type=int, default=4096,
+                    help="image side of the precision sweep (4096 = the workload)")
     ap.add_argument("--preproc", action="store_true",
                     help="time the preprocessing tools instead (second JSON line format)")
     return ap.parse_args()
@@ -546,7 +552,7 @@ def pass_lines(kern, outs, work):
 TC_FORMS = ("fp32_fft", "bf16x1", "bf16x3", "fp16x3")
 
 
-def precision_sweep(args, dev, flush, peaks, peak_kind):
+def precision_sweep(args, dev, flush, peaks, peak_kind, accuracy=True):
     """The plain FP32 FFT pass against the tensor-core DFT pass in its three forms on
     the precision-sweep workload: one 4096^2 uint16 pair, 32 px windows at overlap
     0.75 (259 081 vectors), sinusoidal displacement, WorkFIX and the final TPS.
@@ -558,24 +564,25 @@ def precision_sweep(args, dev, flush, peaks, peak_kind):
     from fluidimage_gb300 import WorkPIV, engine, workloads
     from oracle import accuracy as A
 
-    shape = (4096, 4096)
+    shape = (args.sweep_size, args.sweep_size)
     (im0, im1), _ = workloads.config4_images(shape=shape)
     t0 = torch.from_numpy(im0.view(np.int16)).to(dev)
     t1 = torch.from_numpy(im1.view(np.int16)).to(dev)
     band = (slice(0, 768), slice(None))
     b0, b1 = np.ascontiguousarray(im0[band]), np.ascontiguousarray(im1[band])
     params_ref = workloads.config4_params(WorkPIV.create_default_params())
-    ref = A.fp64_multipass(b0, b1, params_ref)
-    out = {"workload": "4096x4096 uint16 12-bit, density 0.06, diameter 2.5 px, noise 1 %, "
+    ref = A.fp64_multipass(b0, b1, params_ref) if accuracy else None
+    out = {"workload": f"{shape[0]}x{shape[1]} uint16 12-bit, density 0.06, diameter 2.5 px, noise 1 %, "
                        "d = 5 (sin 2 pi y/512, cos 2 pi x/512) px, 32 px windows overlap 0.75, "
                        "WorkFIX thr 2, final TPS subdom 256",
            "accuracy_band": "rows 0-767 (all columns)", "forms": {}}
-    steps = max(3, min(args.steps, 10))
-    for form in TC_FORMS:
+    steps = max(1, min(args.steps, 10))
+    forms = [f for f in args.forms.split(",") if f]
+    for form in forms:
         params = workloads.config4_params(WorkPIV.create_default_params())
         params.piv0.method_correl = "gb300" if form == "fp32_fft" else f"gb300_tc_{form}"
         work = WorkPIV(params, device=dev)
-        for _ in range(2):
+        for _ in range(max(1, args.warmup)):
             outs = work.calcul_device(t0, t1)
         torch.cuda.synchronize()
         timer = engine.KernelTimer()
@@ -614,14 +621,17 @@ def precision_sweep(args, dev, flush, peaks, peak_kind):
                           "tensor_frac_of_bf16_peak": achieved / float(peaks["bf16_tflops"]),
                           "peak_source": f"bf16_tflops of MEASURED_PEAKS.json ({peak_kind})",
                           "mma_flops_per_window": flops})
-        wb = WorkPIV(params, device=dev)
-        resb = wb.calcul({"arrays": (b0, b1), "names": ("im0", "im1")})
-        acc = A.summary(resb.passes, ref)
-        acc.pop("passes", None)
-        entry["accuracy_vs_fp64"] = acc
+        if accuracy:
+            wb = WorkPIV(params, device=dev)
+            resb = wb.calcul({"arrays": (b0, b1), "names": ("im0", "im1")})
+            acc = A.summary(resb.passes, ref)
+            acc.pop("passes", None)
+            entry["accuracy_vs_fp64"] = acc
         out["forms"][form] = entry
-    base = out["forms"]["fp32_fft"]
-    for form in TC_FORMS[1:]:
+    base = out["forms"].get("fp32_fft")
+    for form in forms:
+        if form == "fp32_fft" or base is None:
+            continue
         f = out["forms"][form]
         f["pass_speedup_vs_fp32_fft"] = base["pass_ms"] / f["pass_ms"]
         f["step_speedup_vs_fp32_fft"] = base["step_ms"] / f["step_ms"]
@@ -697,10 +707,23 @@ def run_preproc(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sweep_only(args):
+    """The precision sweep alone (no accuracy check), one JSON line."""
+    import torch
+
+    dev = torch.device("cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    peaks, peak_kind = _peaks()
+    out = precision_sweep(args, dev, flush, peaks, peak_kind, accuracy=False)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.preproc:
         run_preproc(args)
+    elif args.sweep_only:
+        run_sweep_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -209,6 +209,25 @@ __device__ __forceinline__ void store8(unsigned char* hi_ptr, int lo_off, const 
   if constexpr (LO) *reinterpret_cast<uint4*>(hi_ptr + lo_off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// 2^k as a float (|k| < 127): exact scaling by a product
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+
+// One value -> its hi term at `hi_ptr` and, for the 3-term forms, its lo term at
+// `hi_ptr + lo_off` (16-bit stores).
+template <bool F16, bool LO>
+__device__ __forceinline__ void put2(unsigned char* hi_ptr, int lo_off, float v) {
+  if constexpr (F16) {
+    const __half h = __float2half_rn(v);
+    *reinterpret_cast<__half*>(hi_ptr) = h;
+    if constexpr (LO) *reinterpret_cast<__half*>(hi_ptr + lo_off) = __float2half_rn(v - __half2float(h));
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    *reinterpret_cast<__nv_bfloat16*>(hi_ptr) = h;
+    if constexpr (LO)
+      *reinterpret_cast<__nv_bfloat16*>(hi_ptr + lo_off) = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
 // cos / sin of 2 pi j / 32
 __device__ __forceinline__ float cos32(int j) {
   float s, c;
@@ -481,6 +500,9 @@ __global__ void __launch_bounds__(THREADS, 2)
         frexpf(fmaxf(fabsf(mm[3]), fabsf(mm[1])), &x1);
         e0 = max(e0, x0 - 15);
         e1 = max(e1, x1 - 15);
+        // (float images only can reach these bounds; pow2f needs |e| < 127)
+        e0 = min(max(e0, -100), 100);
+        e1 = min(max(e1, -100), 100);
         const double s0d = intpath ? (double)u[0] : sums[0];
         const double s1d = intpath ? (double)u[2] : sums[2];
         tw.dc0 = (float)ldexp(s0d, -e0 - 5);
@@ -496,11 +518,11 @@ __global__ void __launch_bounds__(THREADS, 2)
         wins[warp] = tw;
       }
       __syncwarp();
-      const int e0 = wins[warp].e0, e1 = wins[warp].e1;
+      const float s0 = pow2f(-wins[warp].e0), s1 = pow2f(-wins[warp].e1);
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
-        f0[i] = ldexpf(f0[i], -e0);
-        f1[i] = ldexpf(f1[i], -e1);
+        f0[i] *= s0;
+        f1[i] *= s1;
       }
       // A1[img][tile][part], K-major (K = x): row m = 32 (warp % 4) + lane
       const int t = warp >> 2, m = 32 * (warp & 3) + lane;
@@ -582,58 +604,49 @@ __global__ void __launch_bounds__(THREADS, 2)
         }
       }
       __syncthreads();
+      // rows kx' >= 1: P = conj(F0) F1 (the row kx' = 0 lanes compute a value that is
+      // not stored)
       float pr[16], pi[16];
-      if (kxp != 0) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          pr[j] = fmaf(y0r[j], y1r[j], y0i[j] * y1i[j]);
-          pi[j] = fmaf(y0r[j], y1i[j], -(y0i[j] * y1r[j]));
-        }
-      } else {
-        // row kx' = 0 holds Z = F(kx=0) + i F(kx=16): separate with the mirror -ky
-        const float* xo = xbuf + (wl * 2 + (1 - h)) * 64;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int ky = 16 * h + j;
-          float m0r, m0i, m1r, m1i;  // Z0[-ky], Z1[-ky]
-          if (j == 0) {
-            m0r = y0r[0];
-            m0i = y0i[0];
-            m1r = y1r[0];
-            m1i = y1i[0];
-          } else {
-            m0r = xo[16 - j];
-            m0i = xo[16 + 16 - j];
-            m1r = xo[32 + 16 - j];
-            m1i = xo[48 + 16 - j];
-          }
-          // F(0) = (Z + conj(Zm)) / 2, F(16) = (Z - conj(Zm)) / (2i)
-          const float a0r = 0.5f * (y0r[j] + m0r), a0i = 0.5f * (y0i[j] - m0i);
-          const float b0r = 0.5f * (y0i[j] + m0i), b0i = 0.5f * (m0r - y0r[j]);
-          const float a1r = 0.5f * (y1r[j] + m1r), a1i = 0.5f * (y1i[j] - m1i);
-          const float b1r = 0.5f * (y1i[j] + m1i), b1i = 0.5f * (m1r - y1r[j]);
-          // P(kx=0) = conj(a0) a1 (zero at ky = 0: F[0,0] = 0), P(kx=16) = conj(b0) b1
-          float p0r = fmaf(a0r, a1r, a0i * a1i), p0i = fmaf(a0r, a1i, -(a0i * a1r));
-          if (ky == 0) p0r = p0i = 0.f;
-          const float p16r = fmaf(b0r, b1r, b0i * b1i), p16i = fmaf(b0r, b1i, -(b0i * b1r));
-          // packed row: P(0) + i P(16)
-          pr[j] = p0r - p16i;
-          pi[j] = p0i + p16r;
-        }
-      }
-      const float sp = ldexpf(1.0f, -SCALE_P);
+      const float sp = pow2f(-SCALE_P);
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        pr[j] *= sp;
-        pi[j] *= sp;
+        pr[j] = fmaf(y0r[j], y1r[j], y0i[j] * y1i[j]) * sp;
+        pi[j] = fmaf(y0r[j], y1i[j], -(y0i[j] * y1r[j])) * sp;
       }
       // A3[part], K-major (row = 16 window + kx' = 32 (warp % 4) + lane,
       // K = [Im P(ky) | Re P(ky)])
       const int m = 32 * (warp & 3) + lane;
-      store8<F16, LO>(sA + kmaj(m, 16 * h, 8), A3_PART, pi);
-      store8<F16, LO>(sA + kmaj(m, 16 * h + 8, 8), A3_PART, pi + 8);
-      store8<F16, LO>(sA + kmaj(m, 32 + 16 * h, 8), A3_PART, pr);
-      store8<F16, LO>(sA + kmaj(m, 32 + 16 * h + 8, 8), A3_PART, pr + 8);
+      if (kxp != 0) {
+        store8<F16, LO>(sA + kmaj(m, 16 * h, 8), A3_PART, pi);
+        store8<F16, LO>(sA + kmaj(m, 16 * h + 8, 8), A3_PART, pi + 8);
+        store8<F16, LO>(sA + kmaj(m, 32 + 16 * h, 8), A3_PART, pr);
+        store8<F16, LO>(sA + kmaj(m, 32 + 16 * h + 8, 8), A3_PART, pr + 8);
+      }
+      // row kx' = 0 holds Z = F(kx=0) + i F(kx=16): lane j of each half warp separates
+      // the two with the mirror -ky for ky = 16 h + j, from the exchanged rows
+      {
+        const int j = kxp;
+        const int ky = 16 * h + j;
+        const float* xs = xbuf + (wl * 2 + h) * 64;
+        const float* xo = (j == 0) ? xs : xbuf + (wl * 2 + (1 - h)) * 64;
+        const int jm = (j == 0) ? 0 : 16 - j;  // index of -ky in its half
+        const float z0r = xs[j], z0i = xs[16 + j], z1r = xs[32 + j], z1i = xs[48 + j];
+        const float m0r = xo[jm], m0i = xo[16 + jm], m1r = xo[32 + jm], m1i = xo[48 + jm];
+        // F(0) = (Z + conj(Zm)) / 2, F(16) = (Z - conj(Zm)) / (2i)
+        const float a0r = 0.5f * (z0r + m0r), a0i = 0.5f * (z0i - m0i);
+        const float b0r = 0.5f * (z0i + m0i), b0i = 0.5f * (m0r - z0r);
+        const float a1r = 0.5f * (z1r + m1r), a1i = 0.5f * (z1i - m1i);
+        const float b1r = 0.5f * (z1i + m1i), b1i = 0.5f * (m1r - z1r);
+        // P(kx=0) = conj(a0) a1 (zero at ky = 0: F[0,0] = 0), P(kx=16) = conj(b0) b1
+        float p0r = fmaf(a0r, a1r, a0i * a1i), p0i = fmaf(a0r, a1i, -(a0i * a1r));
+        if (ky == 0) p0r = p0i = 0.f;
+        const float p16r = fmaf(b0r, b1r, b0i * b1i), p16i = fmaf(b0r, b1i, -(b0i * b1r));
+        // packed row: P(0) + i P(16), written element by element into row 16 wl
+        const float vr = (p0r - p16i) * sp, vi = (p0i + p16r) * sp;
+        const int m0 = 16 * wl;
+        put2<F16, LO>(sA + kmaj(m0, ky, 8), A3_PART, vi);
+        put2<F16, LO>(sA + kmaj(m0, 32 + ky, 8), A3_PART, vr);
+      }
     }
     // ---------------- stage 3: Q = inverse DFT over ky ----------------
     ok = run_stage([&] {
@@ -651,7 +664,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       float q[32];
       tmem_ld32(tmem + lane_base + 32 * h, q);
       tmem_wait_ld();
-      const float sq = ldexpf(1.0f, -SCALE_Q);
+      const float sq = pow2f(-SCALE_Q);
 #pragma unroll
       for (int i = 0; i < 32; ++i) q[i] *= sq;
       const int k4 = h ? kxp : 16 + kxp;
