@@ -7,6 +7,10 @@
   (``params.piv0.method_correl = "gb300"``).
 * ``WorkBOS``: background-oriented schlieren (PIV against a reference image kept
   on the GPU).
+* ``PIVBatch``: single-pass PIV of many pairs of mixed image and window sizes in a
+  few persistent launches (one per window size), replayable as a CUDA graph.
+* ``params.piv0.method_correl = "gb300_tc_fp16x3"`` (or ``_bf16x3``, ``_bf16x1``):
+  32 px passes on the tensor cores (DFT as dense contractions).
 
 Importing the package is cheap: the CUDA library is loaded on first use by
 ``fluidimage_gb300._lib`` and fails loudly when it is missing (no CPU fallback).
@@ -20,8 +24,9 @@ from .errors import InterpError, PIVError  # noqa: E402
 from .params import ParamContainer  # noqa: E402
 from .piv import WorkPIV  # noqa: E402
 from .bos import WorkBOS  # noqa: E402
+from .batch import PIVBatch  # noqa: E402
 
 __all__ = [
-    "WorkPIV", "WorkBOS", "CorrelGB300", "correlation_classes", "register_upstream", "ArrayCouple",
+    "WorkPIV", "WorkBOS", "PIVBatch", "CorrelGB300", "correlation_classes", "register_upstream", "ArrayCouple",
     "HeavyPIVResults", "MultipassPIVResults", "PIVError", "InterpError", "ParamContainer",
 ]

@@ -37,6 +37,8 @@ SUBPIX_METHODS = {"2d_gaussian2": 0, "2d_gaussian": 1, "centroid": 2, "no_subpix
 TC_FORMS = {"bf16x1": 0, "bf16x3": 1, "fp16x3": 2}
 #: window size of the tensor-core pass
 TC_WINDOW = 32
+#: windows per work item of the batch kernel, per window size (autotuner choices)
+BATCH_WPB = {16: (16, 8), 24: (8, 4), 32: (8, 4), 48: (2, 1), 64: (2, 1)}
 MAX_NSUBPIX = 4
 MAX_PEAKS = 4
 PEAK_FIELDS = 5
@@ -95,6 +97,11 @@ _SIGNATURES = {
     "fi_images_min": (C.c_int, [P, P, C.c_int, C.c_int64, P, P]),
     "fi_piv_pass": (C.c_int, [P, P]),
     "fi_piv_pass_tc": (C.c_int, [P, C.c_int, P, P]),
+    "fi_piv_pass_batch": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P]),
+    "fi_piv_batch_items": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "fi_piv_batch_max_blocks": (C.c_int, [C.c_int, C.c_int]),
+    "fi_images_min_batch": (C.c_int, [P, C.c_int, P, P]),
+    "fi_fix_batch": (C.c_int, [P, P, C.c_int, C.c_int, P]),
     "fi_correl_windows": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P]),
     "fi_peaks_from_planes": (
         C.c_int,

@@ -503,10 +503,11 @@ __global__ void __launch_bounds__(THREADS, 2)
         // (float images only can reach these bounds; pow2f needs |e| < 127)
         e0 = min(max(e0, -100), 100);
         e1 = min(max(e1, -100), 100);
-        const double s0d = intpath ? (double)u[0] : sums[0];
-        const double s1d = intpath ? (double)u[2] : sums[2];
-        tw.dc0 = (float)ldexp(s0d, -e0 - 5);
-        tw.dc1 = (float)ldexp(s1d, -e1 - 5);
+        // (sum v) 2^-e / N: the sum rounded once to float32, then an exact scaling
+        const float s0f = intpath ? __ull2float_rn(u[0]) : (float)sums[0];
+        const float s1f = intpath ? __ull2float_rn(u[2]) : (float)sums[2];
+        tw.dc0 = s0f * pow2f(-e0 - 5);
+        tw.dc1 = s1f * pow2f(-e1 - 5);
         tw.normf = ws.normf;
         tw.norm64 = ws.norm64;
         tw.flat = (flat0 || flat1) ? 1 : 0;
@@ -733,10 +734,8 @@ __global__ void __launch_bounds__(THREADS, 2)
             err = FI_VEC_BAD_CROP;
           }
           if (a.dxin) {
-            dxo = (abs(wp.dinx) < (1 << 24)) ? __fadd_rn(dxo, (float)wp.dinx)
-                                             : (float)((double)dxo + (double)wp.dinx);
-            dyo = (abs(wp.diny) < (1 << 24)) ? __fadd_rn(dyo, (float)wp.diny)
-                                             : (float)((double)dyo + (double)wp.diny);
+            dxo = add_shift(dxo, wp.dinx);
+            dyo = add_shift(dyo, wp.diny);
           }
           a.deltaxs[vec] = dxo;
           a.deltays[vec] = dyo;
@@ -748,8 +747,8 @@ __global__ void __launch_bounds__(THREADS, 2)
                                              (res.sec_tie ? FI_FLAG_SECONDARY_TIE : 0))
                                  : (uint8_t)0;
           const int sx = wp.ixs0 + wp.ixs1, sy = wp.iys0 + wp.iys1;
-          a.xs[vec] = (abs(sx) < (1 << 24)) ? __fmul_rn((float)sx, 0.5f) : (float)((double)sx * 0.5);
-          a.ys[vec] = (abs(sy) < (1 << 24)) ? __fmul_rn((float)sy, 0.5f) : (float)((double)sy * 0.5);
+          a.xs[vec] = midpoint(sx);
+          a.ys[vec] = midpoint(sy);
         }
       }
       // the planes alias the operand region of the next tile

@@ -40,9 +40,9 @@ static int fix_scratch_address(float** out) {
   return FI_OK;
 }
 
-__global__ void k_fix_a(fi_fix_args a, int nvec, float cmin, float dmax2, float* ox, float* oy) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nvec) return;
+// Stage A of vector i.
+__device__ __forceinline__ void fix_a_one(const fi_fix_args& a, int i, float cmin, float dmax2,
+                                          float* ox, float* oy) {
   float dx = a.deltaxs[i], dy = a.deltays[i];
   bool wrong = a.errors[i] != 0;
   uint8_t flags = 0;
@@ -64,6 +64,12 @@ __global__ void k_fix_a(fi_fix_args a, int nvec, float cmin, float dmax2, float*
   oy[i] = dy;
   a.fix_flags[i] = flags;
   if (a.diff2) a.diff2[i] = NAN;
+}
+
+__global__ void k_fix_a(fi_fix_args a, int nvec, float cmin, float dmax2, float* ox, float* oy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  fix_a_one(a, i, cmin, dmax2, ox, oy);
 }
 
 // a[i0][i1] (0 where NaN) and validity b, read from the stage-A output.
@@ -121,10 +127,9 @@ __device__ __forceinline__ float nsum(const Grid& g, int i0, int i1) {
   return s;
 }
 
-__global__ void k_fix_b(fi_fix_args a, const float* ix, const float* iy, float thr2) {
-  const int nvec = a.nx * a.ny;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nvec) return;
+// Stage B of vector i.
+__device__ __forceinline__ void fix_b_one(const fi_fix_args& a, int i, const float* ix,
+                                          const float* iy, float thr2) {
   Grid g{ix, iy, a.ny, a.nx};
   const int i0 = i / a.nx, i1 = i % a.nx;
   const float dx = ix[i], dy = iy[i];
@@ -145,6 +150,53 @@ __global__ void k_fix_b(fi_fix_args a, const float* ix, const float* iy, float t
   }
   a.deltaxs_out[i] = ox;
   a.deltays_out[i] = oy;
+}
+
+__global__ void k_fix_b(fi_fix_args a, const float* ix, const float* iy, float thr2) {
+  const int nvec = a.nx * a.ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec) return;
+  fix_b_one(a, i, ix, iy, thr2);
+}
+
+// Batched stages A and B over the vectors of many passes (vec_start: the first
+// vector of each pass, npass + 1 entries).  The squared thresholds are float32
+// products of the float32 thresholds, equal to the float64 square rounded to
+// float32 (the float64 product of two float32 values is exact).
+__device__ __forceinline__ int batch_pass_of(const int32_t* vec_start, int npass, int i) {
+  int lo = 0, hi = npass - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(vec_start + mid) <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_fix_batch_a(const fi_fix_args* __restrict__ args,
+                              const int32_t* __restrict__ vec_start, int npass) {
+  const int total = __ldg(vec_start + npass);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int p = batch_pass_of(vec_start, npass, i);
+    const fi_fix_args& a = args[p];
+    const int nvec = a.nx * a.ny;
+    const float dmax2 = __fmul_rn(a.displacement_max, a.displacement_max);
+    float* ox = a.use_threshold ? a.work : a.deltaxs_out;
+    float* oy = a.use_threshold ? a.work + nvec : a.deltays_out;
+    fix_a_one(a, i - __ldg(vec_start + p), a.correl_min, dmax2, ox, oy);
+  }
+}
+
+__global__ void k_fix_batch_b(const fi_fix_args* __restrict__ args,
+                              const int32_t* __restrict__ vec_start, int npass) {
+  const int total = __ldg(vec_start + npass);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int p = batch_pass_of(vec_start, npass, i);
+    const fi_fix_args& a = args[p];
+    if (!a.use_threshold) continue;
+    const int nvec = a.nx * a.ny;
+    fix_b_one(a, i - __ldg(vec_start + p), a.work, a.work + nvec,
+              __fmul_rn(a.threshold, a.threshold));
+  }
 }
 
 // Stage C (fix.py:135-236): a vector whose secondary peaks (correl ratio > 0.6,
@@ -292,4 +344,15 @@ extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
                                        a.deltays_out);
   }
   return check_launch("fi_fix_static", kernels);
+}
+
+extern "C" int fi_fix_batch(const fi_fix_args* fix_args, const int32_t* vec_start, int npass,
+                            int total, void* stream) {
+  FI_REQUIRE(fix_args && vec_start && npass > 0 && total > 0, "fi_fix_batch: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int threads = 256;
+  const int blocks = (total + threads - 1) / threads;
+  k_fix_batch_a<<<blocks, threads, 0, s>>>(fix_args, vec_start, npass);
+  k_fix_batch_b<<<blocks, threads, 0, s>>>(fix_args, vec_start, npass);
+  return check_launch("fi_fix_batch", 2);
 }

@@ -234,15 +234,30 @@ __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchB
   using C = Cfg<N>;
   Peak p{-INFINITY, -1, -INFINITY};
   if (t < N && t >= box.i1s && t < box.i1e) {
-    for (int i0 = box.i0s; i0 < box.i0e; ++i0) {
-      if (excluded<N>(PL, mask, nb, i0, t)) continue;
-      const float v = PL[i0 * C::LDP + t];
-      if (v >= p.v) {
-        p.v2 = p.v;
-        p.v = v;
-        p.f = i0 * N + t;
-      } else if (v > p.v2) {
-        p.v2 = v;
+    if (mask == nullptr && nb.n == 0) {
+      // nothing excluded but NaNs, which never compare greater or equal
+#pragma unroll 8
+      for (int i0 = box.i0s; i0 < box.i0e; ++i0) {
+        const float v = PL[i0 * C::LDP + t];
+        if (v >= p.v) {
+          p.v2 = p.v;
+          p.v = v;
+          p.f = i0 * N + t;
+        } else if (v > p.v2) {
+          p.v2 = v;
+        }
+      }
+    } else {
+      for (int i0 = box.i0s; i0 < box.i0e; ++i0) {
+        if (excluded<N>(PL, mask, nb, i0, t)) continue;
+        const float v = PL[i0 * C::LDP + t];
+        if (v >= p.v) {
+          p.v2 = p.v;
+          p.v = v;
+          p.f = i0 * N + t;
+        } else if (v > p.v2) {
+          p.v2 = v;
+        }
       }
     }
   }
@@ -372,16 +387,21 @@ struct SubpixOut {
   bool tie;
 };
 
+// want64: also the float64 displacement (dx64, dy64) of the '2d_gaussian2' fit and
+// of integer results (the other methods compute in float64 anyway).
 static __device__ int subpix_any(const float* PL, int ld, int N, int i0, int i1, int method, int nsub,
-                          const double* minv, const NanBox& cbox, SubpixOut* o) {
+                          const double* minv, const NanBox& cbox, SubpixOut* o,
+                          bool want64 = false) {
   const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
   const int n = (method == FI_SUBPIX_GAUSSIAN2) ? 1 : nsub;
   o->tie = false;
   auto integer = [&](int err) {
     o->dx32 = (float)(ix0 - i1);
     o->dy32 = (float)(iy0 - i0);
-    o->dx64 = (double)(ix0 - i1);
-    o->dy64 = (double)(iy0 - i0);
+    if (want64) {
+      o->dx64 = (double)(ix0 - i1);
+      o->dy64 = (double)(iy0 - i0);
+    }
     return err;
   };
   if (i0 - n < 0 || i0 + n + 1 > N || i1 - n < 0 || i1 + n + 1 > N)
@@ -405,8 +425,10 @@ static __device__ int subpix_any(const float* PL, int ld, int N, int i0, int i1,
     if (gauss2_depl(c, &deplx, &deply, &o->tie)) {
       o->dx32 = __fsub_rn((float)ix0, __fadd_rn(deplx, (float)i1));
       o->dy32 = __fsub_rn((float)iy0, __fadd_rn(deply, (float)i0));
-      o->dx64 = __dsub_rn((double)ix0, __dadd_rn((double)deplx, (double)i1));
-      o->dy64 = __dsub_rn((double)iy0, __dadd_rn((double)deply, (double)i0));
+      if (want64) {
+        o->dx64 = __dsub_rn((double)ix0, __dadd_rn((double)deplx, (double)i1));
+        o->dy64 = __dsub_rn((double)iy0, __dadd_rn((double)deply, (double)i0));
+      }
       return FI_VEC_OK;
     }
     m = FI_SUBPIX_CENTROID;
@@ -556,7 +578,7 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, float 
         if (t == 0) {
           SubpixOut sp;
           const int e = subpix_any(PL, Cfg<N>::LDP, N, a0, a1, pa.subpix_method, pa.nsubpix,
-                                   pa.minv, cbox, &sp);
+                                   pa.minv, cbox, &sp, so->has_in);
           float* o = so->peaks + ((int64_t)so->w * K + k) * FI_PEAK_FIELDS;
           o[0] = (float)(ix0 - a1);
           o[1] = (float)(iy0 - a0);
@@ -575,6 +597,20 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, float 
   return r;
 }
 
+
+// float32 of a float32 displacement plus an int32 input shift, as upstream's
+// float64 sum rounded to float32: exact operands and one rounding for shifts below
+// 2^24; larger shifts through float64 (kept out of line: never taken in practice).
+static __device__ __noinline__ float add_shift_f64(float d, int s) {
+  return (float)((double)d + (double)s);
+}
+__device__ __forceinline__ float add_shift(float d, int s) {
+  return (abs(s) < (1 << 24)) ? __fadd_rn(d, (float)s) : add_shift_f64(d, s);
+}
+
+// Vector position (i0 + i1) / 2 (singlepass.py:862-863) as float32: float64 / 2 then
+// float32 equals rounding the integer sum to float32 then halving (exact).
+__device__ __forceinline__ float midpoint(int sum) { return __fmul_rn(__int2float_rn(sum), 0.5f); }
 
 // Window origins of one vector in the unpadded image (pass 0: the grid; pass >= 1:
 // windows shifted by the integer input displacement, with upstream's fix-ups of

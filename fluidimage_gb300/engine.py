@@ -527,6 +527,7 @@ class PassDevice:
     peaks_err: object = None
     replaced: object = None  # [nvec, 3] old dx, dy, correl_max of replaced vectors
     tc_status: object = None  # device status word of the tensor-core pass (if it ran)
+    fix_work: object = None  # WorkFIX scratch of the pass
     tps_next: Optional[object] = None  # TpsOutput or GridOutput: this pass on the next grid
     tps_final: Optional[object] = None  # TpsOutput or GridOutput: on its own grid
 
@@ -674,8 +675,21 @@ class PIVPipeline:
         return lay.dev["ixvecs"], lay.dev["iyvecs"], lay.ixvecs.size, lay.iyvecs.size
 
     def _run_pass(self, lay, im0, im1, im_min, dxin, dyin, dt, s) -> PassDevice:
-        torch = _torch()
         lib = L.load()
+        out, a = self.make_pass(lay, im0, im1, im_min, dxin, dyin, dt)
+        if self.tc_form is not None and lay.n == L.TC_WINDOW:
+            out.tc_status = self.tc_status
+            with _timed(f"fi_piv_pass_tc[n={lay.n}]"):
+                L.check(lib.fi_piv_pass_tc(C.byref(a), self.tc_form, L.ptr(self.tc_status), s),
+                        "fi_piv_pass_tc")
+        else:
+            with _timed(f"fi_piv_pass[n={lay.n}]"):
+                L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
+        return out
+
+    def make_pass(self, lay, im0, im1, im_min, dxin, dyin, dt):
+        """The outputs of a pass (device tensors) and its fi_piv_pass_args."""
+        torch = _torch()
         nvec, dev = lay.nvec, self.device
         f32 = dict(dtype=torch.float32, device=dev)
         u8 = dict(dtype=torch.uint8, device=dev)
@@ -718,19 +732,17 @@ class PIVPipeline:
         a.nb_peaks = self.nb_peaks
         a.peaks_count, a.peaks, a.peaks_err = (L.ptr(out.peaks_count), L.ptr(out.peaks),
                                                L.ptr(out.peaks_err))
-        if self.tc_form is not None and lay.n == L.TC_WINDOW:
-            out.tc_status = self.tc_status
-            with _timed(f"fi_piv_pass_tc[n={lay.n}]"):
-                L.check(lib.fi_piv_pass_tc(C.byref(a), self.tc_form, L.ptr(self.tc_status), s),
-                        "fi_piv_pass_tc")
-        else:
-            with _timed(f"fi_piv_pass[n={lay.n}]"):
-                L.check(lib.fi_piv_pass(C.byref(a), s), "fi_piv_pass")
-        return out
+        return out, a
 
     def _run_fix(self, cur: PassDevice, fx, s):
-        torch = _torch()
         lib = L.load()
+        a = self.make_fix(cur, fx)
+        with _timed("fi_fix"):
+            L.check(lib.fi_fix(C.byref(a), s), "fi_fix")
+
+    def make_fix(self, cur: PassDevice, fx):
+        """The fi_fix_args of a pass's WorkFIX (its work buffer kept on ``cur``)."""
+        torch = _torch()
         lay = cur.layout
         a = L.FixArgs()
         a.nx, a.ny = lay.ixvecs.size, lay.iyvecs.size
@@ -743,8 +755,8 @@ class PIVPipeline:
         a.threshold = float(fx.threshold_diff_neighbour or 0.0)
         a.deltaxs_out, a.deltays_out = L.ptr(cur.deltaxs), L.ptr(cur.deltays)
         a.fix_flags, a.diff2 = L.ptr(cur.fix_flags), L.ptr(cur.diff2)
-        work = torch.empty(2 * lay.nvec, dtype=torch.float32, device=self.device)
-        a.work = L.ptr(work)
+        cur.fix_work = torch.empty(2 * lay.nvec, dtype=torch.float32, device=self.device)
+        a.work = L.ptr(cur.fix_work)
         a.nb_peaks = self.nb_peaks
         if self.nb_peaks > 1:  # WorkFIX secondary peaks (fix.py:135-236)
             a.peaks_count, a.peaks, a.peaks_err = (L.ptr(cur.peaks_count), L.ptr(cur.peaks),
@@ -754,8 +766,7 @@ class PIVPipeline:
             a.displacement_max64 = float(fx.displacement_max or 0.0)
             a.correls_max_out = L.ptr(cur.correls_max)
             a.replaced = L.ptr(cur.replaced)
-        with _timed("fi_fix"):
-            L.check(lib.fi_fix(C.byref(a), s), "fi_fix")
+        return a
 
 
 # --------------------------------------------------------------------------------

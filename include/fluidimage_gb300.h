@@ -142,6 +142,33 @@ typedef struct fi_piv_pass_args {
  */
 int fi_piv_pass(const fi_piv_pass_args* args, void* stream);
 
+/*
+ * Batched passes: all passes of window size n of a batch of independent image
+ * pairs (each with its own images, shape, dtype, grid, overlap and outputs: one
+ * fi_piv_pass_args per pass, in DEVICE memory at pass_args) run in one persistent
+ * launch of `blocks` blocks that take work items (wpb consecutive windows of one
+ * pass) from the device counter `counter` (reset by the call).  item_start: device
+ * int32 [npass + 1], the first item of each pass (fi_piv_batch_items per pass,
+ * accumulated).  Same per-window computation and outputs as fi_piv_pass
+ * (works/piv/singlepass.py:262-361 for each pass); nb_peaks must be 1.  The role of
+ * a topology's parallel executors over a series of couples (topologies/piv.py:143-151,
+ * executors/multi_exec_async.py:114-158), on one GPU.  wpb: 16 or 8 (n = 16), 8 or 4
+ * (n = 24, 32), 2 or 1 (n = 48, 64).
+ */
+int fi_piv_pass_batch(const fi_piv_pass_args* pass_args, const int32_t* item_start, int npass,
+                      int n, int wpb, int blocks, int32_t* counter, void* stream);
+/* Work items of a pass of nvec windows of size n at wpb windows per item (-1: bad). */
+int fi_piv_batch_items(int n, int nvec, int wpb);
+/* Resident blocks of the batch kernel for (n, wpb) on the current device (-1: bad). */
+int fi_piv_batch_max_blocks(int n, int wpb);
+/*
+ * Image minima of every pass of a batch (the "im - im.min()" of _pad_images,
+ * works/piv/singlepass.py:196-208), written through each pass's im_min pointer;
+ * keys: device uint32 scratch [2 * npass].
+ */
+int fi_images_min_batch(const fi_piv_pass_args* pass_args, int npass, uint32_t* keys,
+                        void* stream);
+
 /* Precision forms of the tensor-core pass (fi_piv_pass_tc). */
 #define FI_TC_BF16X1 0 /* one bf16 term per operand                              */
 #define FI_TC_BF16X3 1 /* bf16 hi + lo, products hi*hi + hi*lo + lo*hi           */
@@ -239,6 +266,16 @@ typedef struct fi_fix_args {
  * secondary peak closest to the neighbour mean (FI_FIX_REPLACED).
  */
 int fi_fix(const fi_fix_args* args, void* stream);
+
+/*
+ * WorkFIX stages A and B (works/piv/fix.py:66-133) over the vectors of many passes
+ * in two launches: fix_args, device array [npass] (each with its own work buffer
+ * when use_threshold); vec_start: device int32 [npass + 1], first vector of each
+ * pass; total = vec_start[npass].  Secondary peaks (nb_peaks > 1) are not handled
+ * here (fi_fix per pass).
+ */
+int fi_fix_batch(const fi_fix_args* fix_args, const int32_t* vec_start, int npass, int total,
+                 void* stream);
 
 /*
  * fi_fix without a caller-provided work buffer, for callers that cannot allocate
