@@ -80,6 +80,10 @@ def parse_args():
                     help="image side (2048 = the config; smaller sizes for profiling)")
     ap.add_argument("--no-precision-sweep", action="store_true",
                     help="skip the tensor-core precision sweep (the 4096^2 single-pass workload)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched heterogeneous workload (256 single-pass pairs)")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the batched heterogeneous workload (one JSON line)")
     ap.add_argument("--sweep-only", action="store_true",
                     help="run only the precision sweep (one JSON line; for profiling)")
     ap.add_argument("--forms", default=",".join(TC_FORMS),
@@ -428,6 +432,8 @@ def run_gpu(args):
     }
     if not args.no_precision_sweep:
         line["precision_sweep"] = precision_sweep(args, dev, flush, peaks, peak_kind)
+    if not args.no_batched:
+        line["batched"] = batched_workload(args, dev, flush)
     if not args.no_cpu_baseline:
         line["accuracy_vs_fp64"] = accuracy_vs_fp64(res, im0, im1, params)
         line["cpu_baseline"] = cpu_baseline_single()
@@ -638,6 +644,91 @@ def precision_sweep(args, dev, flush, peaks, peak_kind, accuracy=True):
     return out
 
 
+def batched_workload(args, dev, flush):
+    """The batched heterogeneous workload: 256 single-pass jobs, image sizes drawn from
+    512^2, 1024x768, 2048^2, 4096x2160 (4 distinct uint16 pairs each), windows from
+    16-64 px, overlap 0.5 or 0.75, WorkFIX.  One pair at a time
+    (WorkPIV.calcul_device per pair, the schedule of the multipass workload) against
+    PIVBatch (one persistent launch per window size, batched minima and WorkFIX)
+    launched directly, after its autotuner, and replayed as a CUDA graph.
+    Device-resident images, CUDA events, L2 flushed between steps."""
+    import torch
+
+    from fluidimage_gb300 import PIVBatch, WorkPIV, _lib, workloads
+
+    t_gen = time.perf_counter()
+    jobs, draws = workloads.config3_jobs(WorkPIV.create_default_params)
+    gen_s = time.perf_counter() - t_gen
+    dev_pairs, djobs = {}, []
+    for im0, im1, params in jobs:
+        if id(im0) not in dev_pairs:
+            dev_pairs[id(im0)] = (torch.from_numpy(im0.view(np.int16)).to(dev),
+                                  torch.from_numpy(im1.view(np.int16)).to(dev))
+        djobs.append((*dev_pairs[id(im0)], params))
+    works = [WorkPIV(p, device=dev, interp_last=False) for _, _, p in djobs]
+    steps = max(3, min(args.steps, 10))
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.mean(ms)
+
+    def one_at_a_time():
+        for w, (t0, t1, _) in zip(works, djobs):
+            w.calcul_device(t0, t1)
+
+    ms_single = timed(one_at_a_time)
+    batch = PIVBatch(djobs, device=dev)
+    ms_launch = timed(batch.run)
+    tuning = batch.autotune()
+    ms_tuned = timed(batch.run)
+    batch.capture()
+    ms_graph = timed(batch.run)
+    nvec = batch.total_vectors
+    lib = _lib.load()
+    launches0 = lib.fi_launch_count()
+    batch.launches()
+    torch.cuda.synchronize()
+    per_run = lib.fi_launch_count() - launches0
+    return {
+        "workload": "256 single-pass jobs over 16 distinct uint16 12-bit pairs (4 per size "
+                    "512^2, 1024x768, 2048^2, 4096x2160), windows 16/24/32/48/64, overlap "
+                    "0.5/0.75, WorkFIX; uniform shifts or 4-Oseen superpositions (<= 6 px)",
+        "jobs_per_window_size": {str(n): sum(1 for d in draws if d[1] == n)
+                                 for n in sorted({d[1] for d in draws})},
+        "vectors": nvec, "image_generation_s": round(gen_s, 1),
+        "one_at_a_time": {"ms": ms_single, "vectors_per_s": nvec / (ms_single / 1e3),
+                          "api": "WorkPIV.calcul_device per pair"},
+        "batched": {"ms": ms_launch, "vectors_per_s": nvec / (ms_launch / 1e3)},
+        "batched_autotuned": {"ms": ms_tuned, "vectors_per_s": nvec / (ms_tuned / 1e3),
+                              "choices": {str(k): v for k, v in tuning.items()}},
+        "batched_graph": {"ms": ms_graph, "vectors_per_s": nvec / (ms_graph / 1e3),
+                          "kernel_launches_per_run": int(per_run)},
+        "speedup_graph_vs_one_at_a_time": ms_single / ms_graph,
+    }
+
+
+def run_batched_only(args):
+    """The batched heterogeneous workload alone, one JSON line."""
+    import torch
+
+    dev = torch.device("cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    print(json.dumps(batched_workload(args, dev, flush)), flush=True)
+
+
 def accuracy_vs_fp64(res, im0, im1, params):
     """The timed result against the FP64 oracle (the checker)."""
     from oracle import accuracy as A
@@ -724,6 +815,8 @@ def main():
         run_preproc(args)
     elif args.sweep_only:
         run_sweep_only(args)
+    elif args.batched_only:
+        run_batched_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -70,3 +70,77 @@ def config4_params(params):
     params.multipass.smoothing_coef = 0.5
     params.fix.threshold_diff_neighbour = 2
     return params
+
+
+CONFIG3_SIZES = ((512, 512), (768, 1024), (2048, 2048), (2160, 4096))
+CONFIG3_WINDOWS = (16, 24, 32, 48, 64)
+CONFIG3_OVERLAPS = (0.5, 0.75)
+
+
+def _oseen_superposition(shape, rng, count=4, peak=6.0):
+    """Sum of ``count`` Oseen vortices at random centres, core radii and signs, each
+    of peak ``peak / count`` px (the sum stays below ``peak`` px)."""
+    ny, nx = shape
+    fields = []
+    for _ in range(count):
+        centre = (rng.uniform(0, nx), rng.uniform(0, ny))
+        rc = rng.uniform(0.05, 0.2) * min(nx, ny)
+        sign = rng.choice((-1.0, 1.0))
+        fields.append((sign, synthetic.oseen_vortex(shape, d_max=peak / count, rc=rc,
+                                                    center=centre)))
+
+    def field_(x, y):
+        dx = 0.0
+        dy = 0.0
+        for sign, f in fields:
+            a, b = f(x, y)
+            dx = dx + sign * a
+            dy = dy + sign * b
+        return dx, dy
+
+    field_.max_displacement = peak
+    return field_
+
+
+def config3_pair(size_index, k, seed):
+    """One image pair of the batched heterogeneous workload: uint16 12-bit, density
+    U[0.02, 0.08], diameter U[2, 4] px; a uniform shift U[-6, 6]^2 px (even k) or a
+    superposition of 4 Oseen vortices of peak <= 6 px (odd k)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    shape = CONFIG3_SIZES[size_index]
+    model = synthetic.ParticleModel(density=rng.uniform(0.02, 0.08), diameter=(2.0, 4.0),
+                                    intensity=(1000, 4000), noise=20.0, dtype="uint16",
+                                    max_value=4095)
+    if k % 2 == 0:
+        field = synthetic.uniform_shift(*rng.uniform(-6.0, 6.0, 2))
+    else:
+        field = _oseen_superposition(shape, rng)
+    return synthetic.make_pair(shape, field, model, seed=seed + 1)
+
+
+def config3_jobs(params_factory, npairs=256, per_size=4, seed=3000):
+    """The batched heterogeneous workload: ``npairs`` single-pass jobs (image size,
+    window size and overlap drawn uniformly) over ``per_size`` distinct image pairs of
+    each size; returns [(im0, im1, params)] (host arrays; the jobs of one image pair
+    share its arrays) and the draws (shape, window, overlap)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    pool = {(s, k): config3_pair(s, k, seed + 100 * s + k)
+            for s in range(len(CONFIG3_SIZES)) for k in range(per_size)}
+    jobs, draws = [], []
+    for _ in range(npairs):
+        s = int(rng.integers(len(CONFIG3_SIZES)))
+        k = int(rng.integers(per_size))
+        n = int(rng.choice(CONFIG3_WINDOWS))
+        ov = float(rng.choice(CONFIG3_OVERLAPS))
+        params = params_factory()
+        params.piv0.shape_crop_im0 = n
+        params.piv0.grid.overlap = ov
+        params.multipass.number = 1
+        im0, im1 = pool[(s, k)]
+        jobs.append((im0, im1, params))
+        draws.append((CONFIG3_SIZES[s], n, ov))
+    return jobs, draws
