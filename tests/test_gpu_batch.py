@@ -1,8 +1,10 @@
 """Batched single-pass PIV (PIVBatch): pairs of mixed image sizes, dtypes, window
-sizes (16-64 px) and overlaps in one batch give exactly the results of WorkPIV on
-each pair alone (the same per-window kernel code and WorkFIX arithmetic, so the
-comparison is exact), with direct launches, after autotuning and through a CUDA
-graph replay."""
+sizes (16-64 px) and overlaps in one batch give the results of WorkPIV on each
+pair alone, with direct launches, after autotuning and through a CUDA graph replay.
+The per-window code is the same, compiled into another kernel, so float32 rounding
+may differ by an ulp: validity, error strings and vector positions must be equal,
+displacements within 1e-5 px and correls_max within 1e-5 relative outside the
+windows flagged as near-ties."""
 
 import numpy as np
 import pytest
@@ -42,11 +44,17 @@ def _jobs():
 def _check(got, want):
     assert len(got) == len(want)
     for r, w in zip(got, want):
-        np.testing.assert_array_equal(r.deltaxs, w.deltaxs)
-        np.testing.assert_array_equal(r.deltays, w.deltays)
-        np.testing.assert_array_equal(r.correls_max, w.correls_max)
+        nt = (w.near_tie_flags == 0) & (r.near_tie_flags == 0)
+        np.testing.assert_array_equal(np.isnan(r.deltaxs)[nt], np.isnan(w.deltaxs)[nt])
+        ok = nt & ~np.isnan(w.deltaxs)
+        np.testing.assert_allclose(r.deltaxs[ok], w.deltaxs[ok], rtol=0, atol=1e-5)
+        np.testing.assert_allclose(r.deltays[ok], w.deltays[ok], rtol=0, atol=1e-5)
+        okc = nt & ~np.isnan(w.correls_max)
+        np.testing.assert_allclose(r.correls_max[okc], w.correls_max[okc], rtol=1e-5, atol=1e-6)
         np.testing.assert_array_equal(np.asarray(r.xs), np.asarray(w.xs))
-        assert r.errors == w.errors
+        skip = set(np.nonzero(~nt)[0].tolist())
+        assert {k: v for k, v in r.errors.items() if k not in skip} == \
+            {k: v for k, v in w.errors.items() if k not in skip}
 
 
 def test_batch_matches_workpiv():
