@@ -115,6 +115,10 @@ class WorkPIV:
     device : torch device (default ``cuda``).
     interp_last : compute the final interpolation (``deltaxs_final``...): TPS for
         ``use_tps`` True or ``'last'``, griddata for ``use_tps=False``, as upstream.
+    deform : passes after the first deform im1 by the interpolated field of the
+        previous pass (bilinear, ``fluidimage_gb300.deform.warp``) and measure the
+        residual at unshifted windows, instead of shifting the windows by the
+        rounded field (the reference's method; its to-do at singlepass.py:736-738).
     """
 
     @classmethod
@@ -127,7 +131,7 @@ class WorkPIV:
         return params
 
     def __init__(self, params=None, keep_correls=False, device=None, verbose=False,
-                 interp_last=True):
+                 interp_last=True, deform=False):
         if params is None:
             params = self.create_default_params()
         self.params = params
@@ -141,6 +145,7 @@ class WorkPIV:
             raise ValueError("params.piv0.grid.overlap has to be smaller than 1")
         self.keep_correls = keep_correls
         self.interp_last = interp_last
+        self.deform = deform
         self.device = device
         self.verbose = verbose
         self._pipelines = {}
@@ -151,7 +156,8 @@ class WorkPIV:
         if key not in self._pipelines:
             self._pipelines[key] = PIVPipeline(self.params, imshape, dtype, device=self.device,
                                                keep_correls=self.keep_correls,
-                                               interp_last=self.interp_last)
+                                               interp_last=self.interp_last,
+                                               deform=self.deform)
         return self._pipelines[key]
 
     def _xy_offsets(self):

@@ -169,6 +169,46 @@ int fi_piv_batch_max_blocks(int n, int wpb);
 int fi_images_min_batch(const fi_piv_pass_args* pass_args, int npass, uint32_t* keys,
                         void* stream);
 
+/*
+ * Image deformation and the differentiable deform-and-correlate chain.  The
+ * reference leaves the deformation of im1 between passes as a to-do
+ * (works/piv/singlepass.py:736-738); these entry points have no other counterpart.
+ *
+ * Field: `batch` fields of nodes at sorted coordinates xn[nx], yn[ny] (device
+ * float32, nx, ny >= 2), values u, v as [batch][2][ny][nx] device float32; the
+ * displacement at a pixel is the bilinear interpolation of its cell's four nodes,
+ * constant beyond the outer nodes.
+ */
+/* out[b][y][x] = im1[b] sampled bilinearly at (x + u, y + v), replicated borders. */
+int fi_dc_warp(const float* nodes, const float* xn, int nx, const float* yn, int ny,
+               const void* im1, int dtype, int batch, int height, int width, float* out,
+               void* stream);
+/*
+ * Per non-overlapping 32 x 32 window (batch x height/32 x width/32, row-major): the
+ * normalised circular correlation c(m) of (im0, im1w) windows (the plane of
+ * CorrelFFTNumpy.__call__, calcul/correl.py:671-685, over its norm) read out by a
+ * soft-argmax over the lags m in [-15, 15]^2 at `temperature`:
+ * r = sum_m softmax(c / T)(m) m, written as r[w][2] (x, y).  c_zero[w] = c(0),
+ * c_peak[w] = max c (both nullable).  float32 images [batch][height][width].
+ */
+int fi_dc_windows(const float* im0, const float* im1w, int batch, int height, int width,
+                  float temperature, float* r, float* c_zero, float* c_peak, void* stream);
+/*
+ * Adjoint of fi_dc_windows with respect to im1w: grad_im1w (covered pixels written)
+ * from grad_r[w][2].  The correlation planes are recomputed, not stored.
+ */
+int fi_dc_windows_backward(const float* im0, const float* im1w, int batch, int height,
+                           int width, float temperature, const float* grad_r, float* grad_im1w,
+                           void* stream);
+/*
+ * Adjoint of fi_dc_warp: grad_nodes (device, zeroed by the caller, accumulated) and,
+ * when not NULL, grad_im1 (float32, zeroed by the caller, accumulated) from
+ * grad_out[batch][height][width].
+ */
+int fi_dc_warp_backward(const float* nodes, const float* xn, int nx, const float* yn, int ny,
+                        const void* im1, int dtype, int batch, int height, int width,
+                        const float* grad_out, float* grad_nodes, float* grad_im1, void* stream);
+
 /* Precision forms of the tensor-core pass (fi_piv_pass_tc). */
 #define FI_TC_BF16X1 0 /* one bf16 term per operand                              */
 #define FI_TC_BF16X3 1 /* bf16 hi + lo, products hi*hi + hi*lo + lo*hi           */
