@@ -7,17 +7,17 @@ own image size, dtype, window size (16-64 px), overlap and parameters, run
 together:
 
 * the image minima of every pair in one launch (``fi_images_min_batch``);
-* per window size present, one persistent launch over the windows of every pair
-  of that size, whose blocks take work items from a device counter
-  (``fi_piv_pass_batch``): the per-window computation of ``fi_piv_pass``
-  (works/piv/singlepass.py:262-361 per pair);
+* per window size present, one launch over the windows of every pair of that
+  size, one block per work item, each block taking the next item from a device
+  counter, largest windows first (``fi_piv_pass_batch``): the per-window
+  computation of ``fi_piv_pass`` (works/piv/singlepass.py:262-361 per pair);
 * WorkFIX (works/piv/fix.py:66-133) of every pair in two launches
   (``fi_fix_batch``).
 
 The launches of a run contain no host synchronisation, so a run can be captured in
 a CUDA graph and replayed (``capture``; ``run`` then replays it).  The windows per
-work item and the number of resident blocks of each window size are picked by
-``autotune`` (CUDA-event timing of the candidates on the batch itself).
+work item (the block shape and its register budget) of each window size are picked
+by ``autotune`` (CUDA-event timing of the candidates on the batch itself).
 
 Each job is one pass of ``WorkPIV`` (``params.multipass.number == 1``) without the
 final interpolation; results equal ``WorkPIV(params, interp_last=False).calcul``.
@@ -112,8 +112,7 @@ class PIVBatch:
         self.total_vectors = int(starts[-1])
         self.config = {}
         for n in self.groups:
-            wpb = L.BATCH_WPB[n][0]
-            self._set_config(n, wpb, lib.fi_piv_batch_max_blocks(n, wpb))
+            self._set_config(n, L.BATCH_WPB[n][0])
         self.graph = None
 
     # ------------------------------------------------------------------------------
@@ -123,24 +122,22 @@ class PIVBatch:
         arr = (cls * len(structs))(*structs)
         return torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(self.device)
 
-    def _set_config(self, n, wpb, blocks):
+    def _set_config(self, n, wpb):
         import torch
 
         lib = L.load()
-        if blocks <= 0:
-            L.check(-1, "fi_piv_batch_max_blocks")
         items = [lib.fi_piv_batch_items(n, self.jobs[k].pipe.layouts[0].nvec, wpb)
                  for k in self.groups[n]]
         starts = np.concatenate([[0], np.cumsum(items)]).astype(np.int32)
-        self.config[n] = {"wpb": wpb, "blocks": int(min(blocks, max(1, starts[-1]))),
-                          "item_start": torch.as_tensor(starts, device=self.device),
-                          "items": int(starts[-1])}
+        self.config[n] = {"wpb": wpb, "item_start": torch.as_tensor(starts, device=self.device),
+                          "items": int(starts[-1]),
+                          "resident_blocks": int(lib.fi_piv_batch_max_blocks(n, wpb))}
 
     def _launch_group(self, gi, n, s):
         lib = L.load()
         cfg = self.config[n]
         L.check(lib.fi_piv_pass_batch(L.ptr(self.group_args[n]), L.ptr(cfg["item_start"]),
-                                      len(self.groups[n]), n, cfg["wpb"], cfg["blocks"],
+                                      len(self.groups[n]), n, cfg["wpb"], cfg["items"],
                                       L.ptr(self.counters[gi:gi + 1]), s), "fi_piv_pass_batch")
 
     def launches(self, stream=None):
@@ -178,43 +175,39 @@ class PIVBatch:
         return graph
 
     def autotune(self, reps=2):
-        """Per window size, time the batch launch over its pairs for each candidate
-        (windows per item x resident blocks: all, or half) and keep the fastest;
-        choices are cached per (window size, log2 of its windows)."""
+        """Per window size, time the batch launch over its pairs for each windows-per-
+        item candidate and keep the fastest; choices are cached per (window size,
+        log2 of its windows)."""
         import torch
 
-        lib = L.load()
         choice = {}
         for gi, n in enumerate(self.order):
             nwin = sum(self.jobs[k].pipe.layouts[0].nvec for k in self.groups[n])
             key = (n, int(np.log2(max(nwin, 1))))
             if key in _TUNED:
-                wpb, frac = _TUNED[key]
-                self._set_config(n, wpb, max(1, int(lib.fi_piv_batch_max_blocks(n, wpb) * frac)))
-                choice[n] = {"wpb": wpb, "blocks": self.config[n]["blocks"], "cached": True}
+                self._set_config(n, _TUNED[key])
+                choice[n] = {"wpb": _TUNED[key], "cached": True}
                 continue
             best = None
             for wpb in L.BATCH_WPB[n]:
-                full = lib.fi_piv_batch_max_blocks(n, wpb)
-                for frac in (1.0, 0.5):
-                    self._set_config(n, wpb, max(1, int(full * frac)))
-                    times = []
-                    for _ in range(reps + 1):
-                        e0 = torch.cuda.Event(enable_timing=True)
-                        e1 = torch.cuda.Event(enable_timing=True)
-                        e0.record()
-                        self._launch_group(gi, n, L.stream_handle())
-                        e1.record()
-                        torch.cuda.synchronize()
-                        times.append(e0.elapsed_time(e1))
-                    ms = min(times[1:])
-                    if best is None or ms < best[0]:
-                        best = (ms, wpb, frac)
-            ms, wpb, frac = best
-            _TUNED[key] = (wpb, frac)
-            self._set_config(n, wpb, max(1, int(lib.fi_piv_batch_max_blocks(n, wpb) * frac)))
-            choice[n] = {"wpb": wpb, "blocks": self.config[n]["blocks"], "ms": ms,
-                         "cached": False}
+                self._set_config(n, wpb)
+                times = []
+                for _ in range(reps + 1):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    self._launch_group(gi, n, L.stream_handle())
+                    e1.record()
+                    torch.cuda.synchronize()
+                    times.append(e0.elapsed_time(e1))
+                ms = min(times[1:])
+                if best is None or ms < best[0]:
+                    best = (ms, wpb)
+            ms, wpb = best
+            _TUNED[key] = wpb
+            self._set_config(n, wpb)
+            choice[n] = {"wpb": wpb, "ms": ms, "cached": False,
+                         "resident_blocks": self.config[n]["resident_blocks"]}
         self.graph = None  # a captured graph holds the old configuration
         return choice
 

@@ -440,17 +440,21 @@ static int launch_peaks(float* planes, const double* norms, int count, const Pea
 
 static bool supported_n(int n) { return n == 16 || n == 24 || n == 32 || n == 48 || n == 64; }
 
-// ---- batched passes: one persistent launch per window size over many passes ----
+// ---- batched passes: one launch per window size over many passes ----
 // All passes of one window size n (each its own images, shape, grid and outputs)
-// run in one launch whose blocks take work items from a device counter: an item is
-// WPB consecutive windows of one pass (WPB groups of Cfg<n>::G threads).  Items are
-// numbered pass by pass (item_start); the caller orders the passes.
+// run in one launch of one block per work item: each block takes the next item from
+// a device counter (the queue order is the caller's: largest windows first); an item
+// is WPB consecutive windows of one pass (WPB groups of Cfg<n>::G threads), items
+// numbered pass by pass (item_start).  A block per item, not a persistent loop: the
+// loop kept more registers live across items and spilled (a few hundred bytes per
+// thread at the single-pass kernels' register budgets).
 
-// resident blocks per SM asked of the register allocator: the single-pass kernel's
-// registers per thread (about 80 / 128 / 170 for 16 / 24-32 / 48-64 px windows)
+// resident blocks per SM asked of the register allocator: about 128 / 170 registers
+// for 24-32 / 48-64 px windows; for 16 px windows two budgets (128 registers with 16
+// windows per block, ~100 with 8) for the tuner to choose from
 template <int N, int WPB>
 constexpr int batch_min_blocks() {
-  return N <= 16 ? 48 / WPB : (N <= 32 ? 16 / WPB : 6 / WPB);
+  return N <= 16 ? (WPB == 16 ? 2 : 5) : (N <= 32 ? 16 / WPB : 6 / WPB);
 }
 
 template <int N, int WPB>
@@ -458,42 +462,27 @@ __global__ void __launch_bounds__(WPB * Cfg<N>::G, (batch_min_blocks<N, WPB>()))
     k_piv_batch(const fi_piv_pass_args* __restrict__ passes, const int32_t* __restrict__ item_start,
                 int npass, int32_t* counter) {
   using C = Cfg<N>;
-  constexpr int THREADS = WPB * C::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item, s_pass;
-  __shared__ __align__(16) fi_piv_pass_args s_args;
-  const int total = __ldg(item_start + npass);
-  const int g = threadIdx.x / C::G, t = threadIdx.x % C::G;
-  int cur = -1;  // pass whose arguments are in s_args
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int item = atomicAdd(counter, 1);
-      int lo = 0, hi = npass - 1;  // last pass whose first item is <= item
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(item_start + mid) <= item) lo = mid; else hi = mid - 1;
-      }
-      s_item = item;
-      s_pass = lo;
+  if (threadIdx.x == 0) {
+    const int item = atomicAdd(counter, 1);
+    int lo = 0, hi = npass - 1;  // last pass whose first item is <= item
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(item_start + mid) <= item) lo = mid; else hi = mid - 1;
     }
-    __syncthreads();
-    const int item = s_item, p = s_pass;
-    if (item >= total) break;
-    if (p != cur) {  // the pass arguments, copied to shared memory when the pass changes
-      constexpr int WORDS = sizeof(fi_piv_pass_args) / 4;
-      static_assert(sizeof(fi_piv_pass_args) % 4 == 0, "argument words");
-      for (int i = threadIdx.x; i < WORDS; i += THREADS)
-        reinterpret_cast<uint32_t*>(&s_args)[i] =
-            __ldg(reinterpret_cast<const uint32_t*>(passes + p) + i);
-      cur = p;
-      __syncthreads();
-    }
-    const int w = (item - __ldg(item_start + p)) * WPB + g;
-    if (w < s_args.nx * s_args.ny)
-      piv_window<N, false>(s_args, nullptr, nullptr, w, N / 2 + (N % 2), 1, g, t,
-                           smem_raw + g * C::GROUP_BYTES);
-    __syncthreads();
+    s_item = item;
+    s_pass = lo;
   }
+  __syncthreads();
+  const int item = s_item, p = s_pass;
+  if (item >= __ldg(item_start + npass)) return;
+  const int g = threadIdx.x / C::G, t = threadIdx.x % C::G;
+  const fi_piv_pass_args& a = passes[p];
+  const int w = (item - __ldg(item_start + p)) * WPB + g;
+  if (w < a.nx * a.ny)
+    piv_window<N, false>(a, nullptr, nullptr, w, N / 2 + (N % 2), 1, g, t,
+                         smem_raw + g * C::GROUP_BYTES);
 }
 
 static int group_threads(int n) { return n <= 16 ? 16 : (n <= 32 ? 32 : 64); }
@@ -776,17 +765,17 @@ extern "C" int fi_images_min_batch(const fi_piv_pass_args* pass_args, int npass,
 }
 
 extern "C" int fi_piv_pass_batch(const fi_piv_pass_args* pass_args, const int32_t* item_start,
-                                 int npass, int n, int wpb, int blocks, int32_t* counter,
+                                 int npass, int n, int wpb, int items, int32_t* counter,
                                  void* stream) {
   FI_REQUIRE(pass_args && item_start && counter, "fi_piv_pass_batch: null pointer");
-  FI_REQUIRE(npass > 0 && blocks > 0, "fi_piv_pass_batch: empty batch");
+  FI_REQUIRE(npass > 0 && items > 0, "fi_piv_pass_batch: empty batch");
   FI_REQUIRE(supported_n(n), "fi_piv_pass_batch: window size %d not supported", n);
   FI_REQUIRE(batch_wpb_ok(n, wpb),
              "fi_piv_pass_batch: %d windows per item not available for %d px windows", wpb, n);
   cudaStream_t s = (cudaStream_t)stream;
   FI_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int32_t), s));
 #define FI_BATCH(NN, WW) \
-  if (n == NN && wpb == WW) return launch_batch<NN, WW>(pass_args, item_start, npass, blocks, counter, s);
+  if (n == NN && wpb == WW) return launch_batch<NN, WW>(pass_args, item_start, npass, items, counter, s);
   FI_BATCH(16, 16) FI_BATCH(16, 8) FI_BATCH(24, 8) FI_BATCH(24, 4) FI_BATCH(32, 8) FI_BATCH(32, 4)
   FI_BATCH(48, 2) FI_BATCH(48, 1) FI_BATCH(64, 2) FI_BATCH(64, 1)
 #undef FI_BATCH

@@ -144,3 +144,35 @@ def config3_jobs(params_factory, npairs=256, per_size=4, seed=3000):
         jobs.append((im0, im1, params))
         draws.append((CONFIG3_SIZES[s], n, ov))
     return jobs, draws
+
+
+def config5_field(shape=(2048, 2048), peak=7.0):
+    """Oseen vortex (rc 200 px) plus the sinusoid (sin 2 pi y / 512, cos 2 pi x / 512),
+    scaled together so that the largest displacement is ``peak`` px."""
+    import numpy as np
+
+    oseen = synthetic.oseen_vortex(shape, d_max=1.0, rc=200.0)
+    sinus = synthetic.sinusoid(1.0, 512.0)
+    ys, xs = np.mgrid[0:shape[0]:4, 0:shape[1]:4].astype(np.float64)
+    ou, ov = oseen(xs, ys)
+    su, sv = sinus(xs, ys)
+    scale = peak / float(np.hypot(ou + su, ov + sv).max())
+
+    def field_(x, y):
+        a, b = oseen(x, y)
+        c, d = sinus(x, y)
+        return scale * (a + c), scale * (b + d)
+
+    field_.max_displacement = peak
+    return field_
+
+
+def config5_images(pair=0, shape=(2048, 2048)):
+    """Refinement pair: the particle model of the multipass workload (uint16 12-bit,
+    density 0.05, diameter U[2, 3] px, noise 20), the Oseen-plus-sinusoid field of
+    peak 7 px; returned as float32 images and the field."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = config5_field(shape)
+    im0, im1 = synthetic.make_pair(shape, field, model, seed=5000 + pair)
+    return (im0.astype("float32"), im1.astype("float32")), field

@@ -145,18 +145,18 @@ int fi_piv_pass(const fi_piv_pass_args* args, void* stream);
 /*
  * Batched passes: all passes of window size n of a batch of independent image
  * pairs (each with its own images, shape, dtype, grid, overlap and outputs: one
- * fi_piv_pass_args per pass, in DEVICE memory at pass_args) run in one persistent
- * launch of `blocks` blocks that take work items (wpb consecutive windows of one
- * pass) from the device counter `counter` (reset by the call).  item_start: device
- * int32 [npass + 1], the first item of each pass (fi_piv_batch_items per pass,
- * accumulated).  Same per-window computation and outputs as fi_piv_pass
- * (works/piv/singlepass.py:262-361 for each pass); nb_peaks must be 1.  The role of
- * a topology's parallel executors over a series of couples (topologies/piv.py:143-151,
- * executors/multi_exec_async.py:114-158), on one GPU.  wpb: 16 or 8 (n = 16), 8 or 4
- * (n = 24, 32), 2 or 1 (n = 48, 64).
+ * fi_piv_pass_args per pass, in DEVICE memory at pass_args) run in one launch of
+ * `items` blocks, each of which takes the next work item (wpb consecutive windows of
+ * one pass) from the device counter `counter` (reset by the call).  item_start:
+ * device int32 [npass + 1], the first item of each pass (fi_piv_batch_items per
+ * pass, accumulated; items = item_start[npass]).  Same per-window computation and
+ * outputs as fi_piv_pass (works/piv/singlepass.py:262-361 for each pass); nb_peaks
+ * must be 1.  The role of a topology's parallel executors over a series of couples
+ * (topologies/piv.py:143-151, executors/multi_exec_async.py:114-158), on one GPU.
+ * wpb: 16 or 8 (n = 16), 8 or 4 (n = 24, 32), 2 or 1 (n = 48, 64).
  */
 int fi_piv_pass_batch(const fi_piv_pass_args* pass_args, const int32_t* item_start, int npass,
-                      int n, int wpb, int blocks, int32_t* counter, void* stream);
+                      int n, int wpb, int items, int32_t* counter, void* stream);
 /* Work items of a pass of nvec windows of size n at wpb windows per item (-1: bad). */
 int fi_piv_batch_items(int n, int nvec, int wpb);
 /* Resident blocks of the batch kernel for (n, wpb) on the current device (-1: bad). */
