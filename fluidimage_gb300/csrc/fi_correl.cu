@@ -57,6 +57,89 @@ __global__ void k_subpix_at(const float* planes, int count, int n, const int32_t
   dys[w] = sp.dy32;
 }
 
+// Row `r` of the two windows of an integer image pair (pixels x..x+N-1 of rows y0r
+// and y1r, zero outside the image, minus the image minima) staged into Zrow as
+// (im0, im1) pairs, with the exact row sums, sums of squares and extremes.  Rows
+// inside the image and 16-byte aligned are read by 16-byte loads; others pixel by
+// pixel.
+struct RowStats {
+  unsigned s0 = 0u, s1 = 0u;
+  unsigned long long q0 = 0ull, q1 = 0ull;
+  int lo0 = 0x7fffffff, lo1 = 0x7fffffff, hi0 = -0x7fffffff, hi1 = -0x7fffffff;
+  __device__ __forceinline__ void add(int v0, int v1) {
+    s0 += (unsigned)v0;
+    s1 += (unsigned)v1;
+    q0 += (unsigned long long)((unsigned)v0 * (unsigned)v0);
+    q1 += (unsigned long long)((unsigned)v1 * (unsigned)v1);
+    lo0 = min(lo0, v0);
+    lo1 = min(lo1, v1);
+    hi0 = max(hi0, v0);
+    hi1 = max(hi1, v1);
+  }
+};
+
+template <int N>
+__device__ __forceinline__ void stage_rows_int(const fi_piv_pass_args& a, int y0r, int x0,
+                                               int y1r, int x1, int mini0, int mini1,
+                                               float2* Zrow, RowStats& st) {
+  const int H = a.height, W = a.width;
+  const bool u16 = a.dtype == FI_U16;
+  const int esz = u16 ? 2 : 1;
+  const unsigned char* p0 = reinterpret_cast<const unsigned char*>(a.im0) +
+                            ((int64_t)y0r * W + x0) * esz;
+  const unsigned char* p1 = reinterpret_cast<const unsigned char*>(a.im1) +
+                            ((int64_t)y1r * W + x1) * esz;
+  const bool in0 = y0r >= 0 && y0r < H && x0 >= 0 && x0 + N <= W;
+  const bool in1 = y1r >= 0 && y1r < H && x1 >= 0 && x1 + N <= W;
+  const bool vec = in0 && in1 && (((reinterpret_cast<uintptr_t>(p0) |
+                                     reinterpret_cast<uintptr_t>(p1)) & 15) == 0);
+  if (vec && u16 && (N % 8) == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 8; ++k) {
+      const uint4 A = __ldg(reinterpret_cast<const uint4*>(p0) + k);
+      const uint4 B = __ldg(reinterpret_cast<const uint4*>(p1) + k);
+      const uint32_t wa[4] = {A.x, A.y, A.z, A.w}, wb[4] = {B.x, B.y, B.z, B.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int v0 = (int)((wa[i] >> (16 * h)) & 0xffffu) - mini0;
+          const int v1 = (int)((wb[i] >> (16 * h)) & 0xffffu) - mini1;
+          Zrow[8 * k + 2 * i + h] = make_float2((float)v0, (float)v1);
+          st.add(v0, v1);
+        }
+    }
+    return;
+  }
+  if (vec && !u16 && (N % 16) == 0) {
+#pragma unroll
+    for (int k = 0; k < N / 16; ++k) {
+      const uint4 A = __ldg(reinterpret_cast<const uint4*>(p0) + k);
+      const uint4 B = __ldg(reinterpret_cast<const uint4*>(p1) + k);
+      const uint32_t wa[4] = {A.x, A.y, A.z, A.w}, wb[4] = {B.x, B.y, B.z, B.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int v0 = (int)((wa[i] >> (8 * h)) & 0xffu) - mini0;
+          const int v1 = (int)((wb[i] >> (8 * h)) & 0xffu) - mini1;
+          Zrow[16 * k + 4 * i + h] = make_float2((float)v0, (float)v1);
+          st.add(v0, v1);
+        }
+    }
+    return;
+  }
+  const bool r0 = y0r >= 0 && y0r < H, r1 = y1r >= 0 && y1r < H;
+#pragma unroll 4
+  for (int c = 0; c < N; ++c) {
+    const int xa = x0 + c, xb = x1 + c;
+    const int v0 = (r0 && xa >= 0 && xa < W) ? load_px_int(a.im0, a.dtype, (int64_t)y0r * W + xa) - mini0 : 0;
+    const int v1 = (r1 && xb >= 0 && xb < W) ? load_px_int(a.im1, a.dtype, (int64_t)y1r * W + xb) - mini1 : 0;
+    Zrow[c] = make_float2((float)v0, (float)v1);
+    st.add(v0, v1);
+  }
+}
+
 // One window of a pass, processed by the group g of C::G threads (thread t of it):
 // staging, FFT correlation, peak search, subpixel fit, outputs.  gsm: the group's
 // shared memory (C::GROUP_BYTES).
@@ -85,10 +168,32 @@ __device__ __forceinline__ void piv_window(const fi_piv_pass_args& a, const floa
   unsigned long long qi0 = 0ull, qi1 = 0ull;
   float sf0 = 0.f, sf1 = 0.f, qf0 = 0.f, qf1 = 0.f, cf0 = 0.f, cf1 = 0.f;
   float mm[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
-  if (t < N) {
+  if (intpath) {
+    // integer images: thread t stages row t of both windows (16-byte loads)
+    if (t < N) {
+      RowStats st;
+      if (valid) {
+        stage_rows_int<N>(a, y00 + t, x00, y10 + t, x10, (int)__ldg(a.im_min + 0),
+                          (int)__ldg(a.im_min + 1), Z + t * C::LD, st);
+      } else {
+#pragma unroll 4
+        for (int c = 0; c < N; ++c) {
+          Z[t * C::LD + c] = make_float2(0.f, 0.f);
+          st.add(0, 0);
+        }
+      }
+      si0 = st.s0;
+      si1 = st.s1;
+      qi0 = st.q0;
+      qi1 = st.q1;
+      mm[0] = (float)st.lo0;
+      mm[1] = (float)st.lo1;
+      mm[2] = (float)st.hi0;
+      mm[3] = (float)st.hi1;
+    }
+  } else if (t < N) {
     const float min0 = FROM_WINDOWS ? 0.f : __ldg(a.im_min + 0);
     const float min1 = FROM_WINDOWS ? 0.f : __ldg(a.im_min + 1);
-    const int mini0 = (int)min0, mini1 = (int)min1;
     const int H = a.height, W = a.width;
 #pragma unroll 4
     for (int r = 0; r < N; ++r) {
@@ -100,22 +205,11 @@ __device__ __forceinline__ void piv_window(const fi_piv_pass_args& a, const floa
         const int y0 = y00 + r, x0 = x00 + t, y1 = y10 + r, x1 = x10 + t;
         const bool in0 = y0 >= 0 && y0 < H && x0 >= 0 && x0 < W;
         const bool in1 = y1 >= 0 && y1 < H && x1 >= 0 && x1 < W;
-        if (intpath) {
-          const int i0v = in0 ? load_px_int(a.im0, a.dtype, (int64_t)y0 * W + x0) - mini0 : 0;
-          const int i1v = in1 ? load_px_int(a.im1, a.dtype, (int64_t)y1 * W + x1) - mini1 : 0;
-          v0 = (float)i0v;
-          v1 = (float)i1v;
-          si0 += (unsigned)i0v;
-          si1 += (unsigned)i1v;
-          qi0 += (unsigned long long)((unsigned)i0v * (unsigned)i0v);
-          qi1 += (unsigned long long)((unsigned)i1v * (unsigned)i1v);
-        } else {
-          if (in0) v0 = __fsub_rn(load_px(a.im0, a.dtype, (int64_t)y0 * W + x0), min0);
-          if (in1) v1 = __fsub_rn(load_px(a.im1, a.dtype, (int64_t)y1 * W + x1), min1);
-        }
+        if (in0) v0 = __fsub_rn(load_px(a.im0, a.dtype, (int64_t)y0 * W + x0), min0);
+        if (in1) v1 = __fsub_rn(load_px(a.im1, a.dtype, (int64_t)y1 * W + x1), min1);
       }
       Z[r * C::LD + t] = make_float2(v0, v1);
-      if (!intpath) {
+      {
         sf0 += v0;
         sf1 += v1;
         // Kahan-compensated sums of squares

@@ -684,6 +684,18 @@ struct WinScalars {
   float outscale;  // 0.25 / (N^2 2^-e0 2^-e1)
 };
 
+// Correctly rounded float32 of an unsigned 64-bit integer on the integer pipe: the
+// top 32 significant bits with a sticky bit for the rest (the 64-bit conversion
+// instruction runs on the narrow FP64 pipe of this GPU).
+__device__ __forceinline__ float u64_to_float_rn(unsigned long long v) {
+  const unsigned hi = (unsigned)(v >> 32);
+  if (hi == 0u) return __uint2float_rn((unsigned)v);
+  const int s = 32 - __clz(hi);  // bits beyond the top 32
+  const unsigned long long rest = v & ((1ull << s) - 1ull);
+  const unsigned m = (unsigned)(v >> s) | (rest != 0ull ? 1u : 0u);
+  return __uint2float_rn(m) * __int_as_float((127 + s) << 23);
+}
+
 template <int N>
 __device__ __forceinline__ WinScalars window_scalars(bool intpath,
                                                      const unsigned long long (&u)[4],
@@ -706,8 +718,8 @@ __device__ __forceinline__ WinScalars window_scalars(bool intpath,
       // float64 product rounded to float32
       r.mean0 = ldexpf(__uint2float_rn((unsigned)u[0]), -2 * L);
       r.mean1 = ldexpf(__uint2float_rn((unsigned)u[2]), -2 * L);
-      const float S0f = ldexpf(__ull2float_rn(SN0), -2 * L);
-      const float S1f = ldexpf(__ull2float_rn(SN1), -2 * L);
+      const float S0f = ldexpf(u64_to_float_rn(SN0), -2 * L);
+      const float S1f = ldexpf(u64_to_float_rn(SN1), -2 * L);
       r.normf = __fsqrt_rn(__fmul_rn(S0f, S1f));
       r.norm64 = want_norm64 ? ldexp(sqrt((double)SN0 * (double)SN1), -2 * L) : 0.0;
     } else {

@@ -1,7 +1,8 @@
 """Image deformation and the hand-written adjoint of deform-and-correlate on the GPU.
 
-* warp: equal to the float64 numpy oracle within float32 rounding of the field
-  and the samples (1e-5 of the image range);
+* warp: within the range of the float64 numpy oracle over sample positions moved
+  by two float32 ulps of the image size (the rounding of the float32 positions,
+  which steep particle edges turn into up to ~0.1 counts);
 * soft-argmax read-out r of every 32 x 32 window: within 1e-4 px of the float64
   torch reference on the same deformed image;
 * gradients with respect to the nodes and to im1: the pure-torch autograd
@@ -58,13 +59,16 @@ def test_warp_matches_oracle():
     im0, im1, nodes, truth, xn, yn = _case(B=1)
     got = deform.warp(nodes, xn, yn, im1)
     torch.cuda.synchronize()
-    want = OD.warp(nodes[0].cpu().numpy(), xn.cpu().numpy(), yn.cpu().numpy(),
-                   im1[0].cpu().numpy())
-    np.testing.assert_allclose(got[0].cpu().numpy(), want, rtol=0, atol=1e-5 * 4095)
-    # uint16 images (int16 storage) give the same samples
-    u16 = im1.to(torch.int32).to(torch.int16)
-    np.testing.assert_allclose(deform.warp(nodes, xn, yn, u16)[0].cpu().numpy(), want,
-                               rtol=0, atol=1e-5 * 4095)
+    f, gx, gy, im = (nodes[0].cpu().numpy().astype(np.float64), xn.cpu().numpy(),
+                     yn.cpu().numpy(), im1[0].cpu().numpy())
+    eps = 2 * float(np.spacing(np.float32(max(im.shape))))
+    outs = [OD.warp(f + np.array([du, dv])[:, None, None], gx, gy, im)
+            for du in (-eps, 0.0, eps) for dv in (-eps, 0.0, eps)]
+    lo, hi = np.min(outs, axis=0) - 1e-3, np.max(outs, axis=0) + 1e-3
+    for g in (got[0], deform.warp(nodes, xn, yn, im1.to(torch.int32).to(torch.int16))[0]):
+        g = g.cpu().numpy()  # float32 image, then uint16 (int16 storage): same samples
+        bad = (g < lo) | (g > hi)
+        assert not bad.any(), (int(bad.sum()), float(np.abs(g - outs[4]).max()))
 
 
 def test_readout_matches_torch_reference():
