@@ -102,12 +102,13 @@ _SIGNATURES = {
     "fi_piv_batch_max_blocks": (C.c_int, [C.c_int, C.c_int]),
     "fi_images_min_batch": (C.c_int, [P, C.c_int, P, P]),
     "fi_fix_batch": (C.c_int, [P, P, C.c_int, C.c_int, P]),
-    "fi_dc_warp": (C.c_int, [P, P, C.c_int, P, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_int,
-                             P, P]),
+    "fi_dc_warp": (C.c_int, [P, P, C.c_int, P, C.c_int, C.c_float, P, C.c_int, C.c_int,
+                             C.c_int, C.c_int, P, P]),
     "fi_dc_windows": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_float, P, P, P, P]),
-    "fi_dc_windows_backward": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_float, P, P, P]),
-    "fi_dc_warp_backward": (C.c_int, [P, P, C.c_int, P, C.c_int, P, C.c_int, C.c_int, C.c_int,
-                                      C.c_int, P, P, P, P]),
+    "fi_dc_windows_backward": (C.c_int, [P, P, C.c_int, C.c_int, C.c_int, C.c_float, P, P, P,
+                                         P]),
+    "fi_dc_warp_backward": (C.c_int, [P, P, C.c_int, P, C.c_int, C.c_float, P, C.c_int, C.c_int,
+                                      C.c_int, C.c_int, P, P, P, P]),
     "fi_correl_windows": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P]),
     "fi_peaks_from_planes": (
         C.c_int,

@@ -8,8 +8,10 @@
 // Field: nodes at sorted coordinates xn[nx], yn[ny] (nx, ny >= 2), values u, v as
 // [2][ny][nx] float32; the displacement at a pixel is the bilinear interpolation of
 // the four nodes of its cell, constant beyond the outer nodes.
-// Warp: im1w(x, y) = im1 sampled bilinearly at (x + u, y + v), border pixels
-// replicated outside the image.
+// Warp: imw(x, y) = im sampled bilinearly at (x + s u, y + s v) for a field scale s
+// (the central scheme deforms im0 by s = -1/2 and im1 by s = +1/2, so that a
+// window's displacement belongs to its centre), border pixels replicated outside
+// the image.
 // Windows: the non-overlapping 32 x 32 tiles of the image (H / 32 x W / 32 of them);
 // per window the normalised circular correlation
 //   c(m) = sum_x w0(x) w1(x + m) / (|w0| |w1|),  w = window - its mean
@@ -96,8 +98,8 @@ __device__ __forceinline__ Sample sample(const void* im, int dtype, int H, int W
 }
 
 __global__ void k_warp(const float* __restrict__ fld, const float* __restrict__ xn, int nx,
-                       const float* __restrict__ yn, int ny, const void* im1, int dtype, int B,
-                       int H, int W, float* __restrict__ out) {
+                       const float* __restrict__ yn, int ny, float scale, const void* im1,
+                       int dtype, int B, int H, int W, float* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int b = blockIdx.z;
@@ -108,7 +110,8 @@ __global__ void k_warp(const float* __restrict__ fld, const float* __restrict__ 
   const void* img = (dtype == FI_U8) ? (const void*)((const uint8_t*)im1 + (int64_t)b * H * W)
                     : (dtype == FI_U16) ? (const void*)((const uint16_t*)im1 + (int64_t)b * H * W)
                                         : (const void*)((const float*)im1 + (int64_t)b * H * W);
-  out[((int64_t)b * H + y) * W + x] = sample(img, dtype, H, W, (float)x + u, (float)y + v).v;
+  out[((int64_t)b * H + y) * W + x] =
+      sample(img, dtype, H, W, fmaf(scale, u, (float)x), fmaf(scale, v, (float)y)).v;
 }
 
 __device__ __forceinline__ float wsum(float v) {
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(32 * WPB)
     k_windows(const float* __restrict__ im0, const float* __restrict__ im1w, int B, int H, int W,
               float inv_T, float* __restrict__ r_out, float* __restrict__ cz_out,
               float* __restrict__ cpk_out, const float* __restrict__ grad_r,
-              float* __restrict__ g_im1w) {
+              float* __restrict__ g_im1w, float* __restrict__ g_im0w) {
   extern __shared__ float2 smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwx = W / N, nwy = H / N;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(32 * WPB)
   const bool vec = (W % 4) == 0 && ((reinterpret_cast<uintptr_t>(im0) | reinterpret_cast<uintptr_t>(im1w)) & 15) == 0;
   // ---- windows: means, norms ----
   float2 x[N];
-  float mean1, q1, inv_n;
+  float mean0, mean1, q0, q1, inv_n;
   {
     float a0[N], a1[N];
     load_row(im0 + row, vec, a0);
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(32 * WPB)
       s0 += a0[c];
       s1 += a1[c];
     }
-    const float mean0 = wsum(s0) * (1.f / (N * N));
+    mean0 = wsum(s0) * (1.f / (N * N));
     mean1 = wsum(s1) * (1.f / (N * N));
     float p0 = 0.f, p1 = 0.f;
 #pragma unroll
@@ -216,7 +219,7 @@ __global__ void __launch_bounds__(32 * WPB)
       p1 = fmaf(u1, u1, p1);
       x[c] = make_float2(u0, u1);
     }
-    const float q0 = wsum(p0);
+    q0 = wsum(p0);
     q1 = wsum(p1);
     inv_n = (q0 > 0.f && q1 > 0.f) ? rsqrtf(q0) * rsqrtf(q1) : 0.f;
   }
@@ -283,13 +286,23 @@ __global__ void __launch_bounds__(32 * WPB)
       x[c] = make_float2(g, 0.f);
     }
     S = wsum(S);
-    // ---- conv(y) = sum_m g(m) w0(y - m) = IDFT(G F0)(y) ----
+    // ---- conv(y) = sum_m g(m) w0(y - m) = IDFT(G F0)(y) in the real part, and
+    // xcor(x) = sum_m g(m) w1(x + m) = IDFT(conj(G) F1)(x) in the imaginary part
+    // (both are real: one inverse transform of G F0 + i conj(G) F1)
     fft2_rows_to_cols<false>(x, Wb, lane);
+    {
+      const int lc = (N - lane) & (N - 1);
 #pragma unroll
-    for (int r = 0; r < N; ++r) {
-      const float2 f0 = spec0(Zb, r, lane);
-      const float2 gg = x[r];
-      x[r] = make_float2(gg.x * f0.x - gg.y * f0.y, gg.x * f0.y + gg.y * f0.x);
+      for (int r = 0; r < N; ++r) {
+        const float2 z = Zb[r * LD + lane];
+        const float2 zm = Zb[((N - r) & (N - 1)) * LD + lc];
+        const float2 f0 = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+        const float2 f1 = make_float2(0.5f * (z.y + zm.y), 0.5f * (zm.x - z.x));
+        const float2 gg = x[r];
+        const float2 a0 = make_float2(gg.x * f0.x - gg.y * f0.y, gg.x * f0.y + gg.y * f0.x);
+        const float2 a1 = make_float2(gg.x * f1.x + gg.y * f1.y, gg.x * f1.y - gg.y * f1.x);
+        x[r] = make_float2(a0.x - a1.y, a0.y + a1.x);  // a0 + i a1
+      }
     }
     fft2_cols_to_rows<true>(x, Wb, lane);
     // ---- dL/dw1 = conv / (|w0| |w1|) - S w1 / |w1|^2, then through the mean ----
@@ -307,6 +320,22 @@ __global__ void __launch_bounds__(32 * WPB)
     const float gmean = wsum(gs) * (1.f / (N * N));
 #pragma unroll
     for (int c = 0; c < N; ++c) g_im1w[row + c] = a1[c] - gmean;
+    if (g_im0w) {
+      // dL/dw0 = xcor / (|w0| |w1|) - S w0 / |w0|^2, then through the mean
+      float a0[N];
+      load_row(im0 + row, vec, a0);
+      const float k0 = (q0 > 0.f) ? S / q0 : 0.f;
+      float hs = 0.f;
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        const float gw = x[c].y * kc - k0 * (a0[c] - mean0);
+        a0[c] = gw;
+        hs += gw;
+      }
+      const float hmean = wsum(hs) * (1.f / (N * N));
+#pragma unroll
+      for (int c = 0; c < N; ++c) g_im0w[row + c] = a0[c] - hmean;
+    }
   }
 }
 
@@ -314,9 +343,9 @@ __global__ void __launch_bounds__(32 * WPB)
 // the node contributions of a warp's 32 pixels (one row, at most a few cells) are
 // reduced per cell by shuffles, then added to global memory by one lane.
 __global__ void k_warp_bwd(const float* __restrict__ fld, const float* __restrict__ xn, int nx,
-                           const float* __restrict__ yn, int ny, const void* im1, int dtype, int B,
-                           int H, int W, const float* __restrict__ g_out, float* __restrict__ g_fld,
-                           float* __restrict__ g_im1) {
+                           const float* __restrict__ yn, int ny, float scale, const void* im1,
+                           int dtype, int B, int H, int W, const float* __restrict__ g_out,
+                           float* __restrict__ g_fld, float* __restrict__ g_im1) {
   const int lane = threadIdx.x;
   const int x = blockIdx.x * 32 + lane;
   const int b = blockIdx.z;
@@ -333,10 +362,10 @@ __global__ void k_warp_bwd(const float* __restrict__ fld, const float* __restric
     if (in) {
       q = interp_at(xn, nx, yn, ny, (float)x, (float)y);
       const float u = interp(f, nx, q), v = interp(f + ny * nx, nx, q);
-      const Sample s = sample(img, dtype, H, W, (float)x + u, (float)y + v);
+      const Sample s = sample(img, dtype, H, W, fmaf(scale, u, (float)x), fmaf(scale, v, (float)y));
       const float g = __ldg(g_out + ((int64_t)b * H + y) * W + x);
-      gdx = g * s.gx;
-      gdy = g * s.gy;
+      gdx = scale * g * s.gx;
+      gdy = scale * g * s.gy;
       j0 = q.j0;
       if (g_im1) {
         float* gi = g_im1 + (int64_t)b * H * W;
@@ -397,14 +426,14 @@ static int check_field(const float* nodes, const float* xn, int nx, const float*
 using namespace fi;
 
 extern "C" int fi_dc_warp(const float* nodes, const float* xn, int nx, const float* yn, int ny,
-                          const void* im1, int dtype, int batch, int height, int width, float* out,
-                          void* stream) {
+                          float scale, const void* im1, int dtype, int batch, int height,
+                          int width, float* out, void* stream) {
   if (dc::check_field(nodes, xn, nx, yn, ny, im1, dtype, batch, height, width, "fi_dc_warp") != FI_OK)
     return FI_ERR_INVALID;
   FI_REQUIRE(out, "fi_dc_warp: null output");
   const dim3 block(32, 8), grid((width + 31) / 32, (height + 7) / 8, batch);
-  dc::k_warp<<<grid, block, 0, (cudaStream_t)stream>>>(nodes, xn, nx, yn, ny, im1, dtype, batch,
-                                                       height, width, out);
+  dc::k_warp<<<grid, block, 0, (cudaStream_t)stream>>>(nodes, xn, nx, yn, ny, scale, im1, dtype,
+                                                       batch, height, width, out);
   return check_launch("fi_dc_warp");
 }
 
@@ -422,13 +451,14 @@ extern "C" int fi_dc_windows(const float* im0, const float* im1w, int batch, int
   static SmemLimit limit;
   FI_CUDA_TRY(raise_smem_limit(dc::k_windows<false>, smem, limit));
   dc::k_windows<false><<<blocks, 32 * dc::WPB, smem, (cudaStream_t)stream>>>(
-      im0, im1w, batch, height, width, 1.f / temperature, r, c_zero, c_peak, nullptr, nullptr);
+      im0, im1w, batch, height, width, 1.f / temperature, r, c_zero, c_peak, nullptr, nullptr,
+      nullptr);
   return check_launch("fi_dc_windows");
 }
 
 extern "C" int fi_dc_windows_backward(const float* im0, const float* im1w, int batch, int height,
                                       int width, float temperature, const float* grad_r,
-                                      float* grad_im1w, void* stream) {
+                                      float* grad_im1w, float* grad_im0, void* stream) {
   FI_REQUIRE(im0 && im1w && grad_r && grad_im1w, "fi_dc_windows_backward: null pointer");
   FI_REQUIRE(batch >= 1 && height >= dc::N && width >= dc::N,
              "fi_dc_windows_backward: images smaller than one 32 x 32 window");
@@ -441,14 +471,14 @@ extern "C" int fi_dc_windows_backward(const float* im0, const float* im1w, int b
   FI_CUDA_TRY(raise_smem_limit(dc::k_windows<true>, smem, limit));
   dc::k_windows<true><<<blocks, 32 * dc::WPB, smem, (cudaStream_t)stream>>>(
       im0, im1w, batch, height, width, 1.f / temperature, nullptr, nullptr, nullptr, grad_r,
-      grad_im1w);
+      grad_im1w, grad_im0);
   return check_launch("fi_dc_windows_backward");
 }
 
 extern "C" int fi_dc_warp_backward(const float* nodes, const float* xn, int nx, const float* yn,
-                                   int ny, const void* im1, int dtype, int batch, int height,
-                                   int width, const float* grad_out, float* grad_nodes,
-                                   float* grad_im1, void* stream) {
+                                   int ny, float scale, const void* im1, int dtype, int batch,
+                                   int height, int width, const float* grad_out,
+                                   float* grad_nodes, float* grad_im1, void* stream) {
   if (dc::check_field(nodes, xn, nx, yn, ny, im1, dtype, batch, height, width,
                       "fi_dc_warp_backward") != FI_OK)
     return FI_ERR_INVALID;
@@ -456,8 +486,8 @@ extern "C" int fi_dc_warp_backward(const float* nodes, const float* xn, int nx, 
   const int rows = 8;
   const int gy = min((height + rows - 1) / rows, 64);
   const dim3 block(32, rows), grid((width + 31) / 32, gy, batch);
-  dc::k_warp_bwd<<<grid, block, 0, (cudaStream_t)stream>>>(nodes, xn, nx, yn, ny, im1, dtype,
-                                                           batch, height, width, grad_out,
+  dc::k_warp_bwd<<<grid, block, 0, (cudaStream_t)stream>>>(nodes, xn, nx, yn, ny, scale, im1,
+                                                           dtype, batch, height, width, grad_out,
                                                            grad_nodes, grad_im1);
   return check_launch("fi_dc_warp_backward");
 }

@@ -528,7 +528,7 @@ class PassDevice:
     replaced: object = None  # [nvec, 3] old dx, dy, correl_max of replaced vectors
     tc_status: object = None  # device status word of the tensor-core pass (if it ran)
     fix_work: object = None  # WorkFIX scratch of the pass
-    deformed: object = None  # float32 im1 deformed by the previous pass (deform mode)
+    deformed: object = None  # (im0, im1) deformed by -/+ half the previous pass (deform mode)
     tps_next: Optional[object] = None  # TpsOutput or GridOutput: this pass on the next grid
     tps_final: Optional[object] = None  # TpsOutput or GridOutput: on its own grid
 
@@ -695,31 +695,29 @@ class PIVPipeline:
         return out
 
     def _run_deformed_pass(self, lay, field, im0, im1, stream):
-        """A pass on im1 deformed by ``field`` (the previous pass interpolated on this
-        pass's grid): windows at the grid points, the measured residual plus the
-        field value as the displacement.  The images go to float32 (im0 once per
-        run), the minima are those of the float images."""
+        """A pass on the images deformed by ``field`` (the previous pass interpolated on
+        this pass's grid) with the central scheme, im0 by -d/2 and im1 by +d/2:
+        windows at the grid points, the measured residual plus the field value as
+        the displacement of the grid point.  The minima are those of the float
+        images."""
         torch = _torch()
         lib = L.load()
         from .deform import warp
 
         s = L.stream_handle(stream)
-        im0f = getattr(self, "_im0f", None)
-        if im0f is None or im0f[0] is not im0:
-            self._im0f = (im0, _as_float_image(im0, self.dtype))
-        f0 = self._im0f[1]
         nodes = torch.stack([field.out_x, field.out_y]).to(torch.float32).reshape(
-            1, 2, lay.iyvecs.size, lay.ixvecs.size)
-        xn, yn = lay.dev.setdefault("xn", lay.dev["ixvecs"].float()), \
-            lay.dev.setdefault("yn", lay.dev["iyvecs"].float())
-        im1src = im1.unsqueeze(0)
-        f1 = warp(nodes.contiguous(), xn, yn, im1src, stream)[0]
+            1, 2, lay.iyvecs.size, lay.ixvecs.size).contiguous()
+        if "xn" not in lay.dev:
+            lay.dev["xn"], lay.dev["yn"] = lay.dev["ixvecs"].float(), lay.dev["iyvecs"].float()
+        xn, yn = lay.dev["xn"], lay.dev["yn"]
+        f0 = warp(nodes, xn, yn, im0.unsqueeze(0), -0.5, stream)[0]
+        f1 = warp(nodes, xn, yn, im1.unsqueeze(0), 0.5, stream)[0]
         im_min = torch.empty(2, dtype=torch.float32, device=self.device)
         H, W = self.imshape
         L.check(lib.fi_images_min(L.ptr(f0), L.ptr(f1), L.FI_F32, H * W, L.ptr(im_min), s),
                 "fi_images_min")
         out = self._run_pass(lay, f0, f1, im_min, None, None, L.FI_F32, s)
-        out.deformed = f1
+        out.deformed = (f0, f1)
         # displacement = field at the vector (the grid point) + measured residual
         out.deltaxs_raw += field.out_x.to(torch.float32)
         out.deltays_raw += field.out_y.to(torch.float32)
@@ -806,14 +804,6 @@ class PIVPipeline:
             a.correls_max_out = L.ptr(cur.correls_max)
             a.replaced = L.ptr(cur.replaced)
         return a
-
-
-def _as_float_image(im, dtype):
-    """A device image as float32 (uint16 travels as int16 storage)."""
-    torch = _torch()
-    if np.dtype(dtype) == np.uint16:
-        return (im.to(torch.int32) & 0xFFFF).to(torch.float32)
-    return im.to(torch.float32)
 
 
 # --------------------------------------------------------------------------------

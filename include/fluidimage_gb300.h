@@ -179,10 +179,13 @@ int fi_images_min_batch(const fi_piv_pass_args* pass_args, int npass, uint32_t* 
  * displacement at a pixel is the bilinear interpolation of its cell's four nodes,
  * constant beyond the outer nodes.
  */
-/* out[b][y][x] = im1[b] sampled bilinearly at (x + u, y + v), replicated borders. */
+/*
+ * out[b][y][x] = im[b] sampled bilinearly at (x + scale u, y + scale v), replicated
+ * borders (the central scheme deforms im0 by scale -1/2 and im1 by +1/2).
+ */
 int fi_dc_warp(const float* nodes, const float* xn, int nx, const float* yn, int ny,
-               const void* im1, int dtype, int batch, int height, int width, float* out,
-               void* stream);
+               float scale, const void* im, int dtype, int batch, int height, int width,
+               float* out, void* stream);
 /*
  * Per non-overlapping 32 x 32 window (batch x height/32 x width/32, row-major): the
  * normalised circular correlation c(m) of (im0, im1w) windows (the plane of
@@ -194,20 +197,20 @@ int fi_dc_warp(const float* nodes, const float* xn, int nx, const float* yn, int
 int fi_dc_windows(const float* im0, const float* im1w, int batch, int height, int width,
                   float temperature, float* r, float* c_zero, float* c_peak, void* stream);
 /*
- * Adjoint of fi_dc_windows with respect to im1w: grad_im1w (covered pixels written)
- * from grad_r[w][2].  The correlation planes are recomputed, not stored.
+ * Adjoint of fi_dc_windows: grad_im1w and, when not NULL, grad_im0 (covered pixels
+ * written) from grad_r[w][2].  The correlation planes are recomputed, not stored.
  */
 int fi_dc_windows_backward(const float* im0, const float* im1w, int batch, int height,
                            int width, float temperature, const float* grad_r, float* grad_im1w,
-                           void* stream);
+                           float* grad_im0, void* stream);
 /*
- * Adjoint of fi_dc_warp: grad_nodes (device, zeroed by the caller, accumulated) and,
- * when not NULL, grad_im1 (float32, zeroed by the caller, accumulated) from
+ * Adjoint of fi_dc_warp (same field and scale): grad_nodes (device, accumulated)
+ * and, when not NULL, grad_im (float32, accumulated) from
  * grad_out[batch][height][width].
  */
 int fi_dc_warp_backward(const float* nodes, const float* xn, int nx, const float* yn, int ny,
-                        const void* im1, int dtype, int batch, int height, int width,
-                        const float* grad_out, float* grad_nodes, float* grad_im1, void* stream);
+                        float scale, const void* im, int dtype, int batch, int height, int width,
+                        const float* grad_out, float* grad_nodes, float* grad_im, void* stream);
 
 /* Precision forms of the tensor-core pass (fi_piv_pass_tc). */
 #define FI_TC_BF16X1 0 /* one bf16 term per operand                              */

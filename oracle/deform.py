@@ -35,13 +35,14 @@ def field_at(nodes, xn, yn, H, W):
     return out
 
 
-def warp(nodes, xn, yn, im1):
-    """im1 [H, W] sampled bilinearly at (x + u, y + v), replicated borders (float64)."""
+def warp(nodes, xn, yn, im1, scale=1.0):
+    """im1 [H, W] sampled bilinearly at (x + scale u, y + scale v), replicated borders
+    (float64)."""
     im1 = np.asarray(im1, np.float64)
     H, W = im1.shape
     u, v = field_at(nodes, xn, yn, H, W)
-    px = np.arange(W)[None, :] + u
-    py = np.arange(H)[:, None] + v
+    px = np.arange(W)[None, :] + scale * u
+    py = np.arange(H)[:, None] + scale * v
     x0 = np.floor(px)
     y0 = np.floor(py)
     fx, fy = px - x0, py - y0

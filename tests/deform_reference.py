@@ -16,8 +16,8 @@ def _cell(coords, v):
     return j0, t
 
 
-def warp(nodes, xn, yn, im1):
-    """nodes [B, 2, ny, nx], im1 [B, H, W] -> [B, H, W] (float64)."""
+def warp(nodes, xn, yn, im1, scale=1.0):
+    """nodes [B, 2, ny, nx], im1 [B, H, W] -> im1 at (x + scale d) [B, H, W] (float64)."""
     B, H, W = im1.shape
     dev = im1.device
     xs = torch.arange(W, dtype=torch.float64, device=dev)
@@ -34,8 +34,8 @@ def warp(nodes, xn, yn, im1):
         top = (1 - tx) * f00 + tx * f01
         bot = (1 - tx) * f10 + tx * f11
         comps.append((1 - ty)[:, None] * top + ty[:, None] * bot)
-    px = (xs[None, None, :] + comps[0]).clamp(-1e7, 1e7)
-    py = (ys[None, :, None] + comps[1]).clamp(-1e7, 1e7)
+    px = (xs[None, None, :] + scale * comps[0]).clamp(-1e7, 1e7)
+    py = (ys[None, :, None] + scale * comps[1]).clamp(-1e7, 1e7)
     x0 = torch.floor(px).detach()
     y0 = torch.floor(py).detach()
     fx, fy = px - x0, py - y0
@@ -74,6 +74,9 @@ def windows_r(im0, im1w, temperature):
     return torch.stack([rx, ry], dim=-1)
 
 
-def loss(nodes, im0, im1, xn, yn, temperature=0.1):
-    r = windows_r(im0, warp(nodes, xn, yn, im1), temperature)
+def loss(nodes, im0, im1, xn, yn, temperature=0.1, symmetric=True):
+    if symmetric:
+        r = windows_r(warp(nodes, xn, yn, im0, -0.5), warp(nodes, xn, yn, im1, 0.5), temperature)
+    else:
+        r = windows_r(im0, warp(nodes, xn, yn, im1), temperature)
     return (r * r).sum(dim=-1).mean()

@@ -7,6 +7,7 @@ position inside the stencil (a few percent on a 96 x 128 image); over h = 1e-5 p
 they agree to 1e-4."""
 
 import numpy as np
+import pytest
 import torch
 
 import deform_reference as R
@@ -26,20 +27,22 @@ def _case(seed=0, H=96, W=128):
     return im0.astype(np.float64), im1.astype(np.float64), nodes, xn, yn
 
 
-def test_torch_reference_warp_equals_numpy_oracle():
+@pytest.mark.parametrize("scale", [1.0, 0.5, -0.5])
+def test_torch_reference_warp_equals_numpy_oracle(scale):
     im0, im1, nodes, xn, yn = _case()
     got = R.warp(torch.as_tensor(nodes)[None], torch.as_tensor(xn), torch.as_tensor(yn),
-                 torch.as_tensor(im1)[None])[0].numpy()
-    np.testing.assert_allclose(got, OD.warp(nodes, xn, yn, im1), rtol=0, atol=1e-9)
+                 torch.as_tensor(im1)[None], scale)[0].numpy()
+    np.testing.assert_allclose(got, OD.warp(nodes, xn, yn, im1, scale), rtol=0, atol=1e-9)
 
 
-def test_torch_reference_gradient_equals_central_differences():
+@pytest.mark.parametrize("symmetric", [True, False], ids=["central", "im1_only"])
+def test_torch_reference_gradient_equals_central_differences(symmetric):
     im0, im1, nodes, xn, yn = _case(seed=3)
     t0 = torch.as_tensor(im0)[None]
     t1 = torch.as_tensor(im1)[None]
     txn, tyn = torch.as_tensor(xn), torch.as_tensor(yn)
     p = torch.as_tensor(nodes)[None].clone().requires_grad_(True)
-    R.loss(p, t0, t1, txn, tyn).backward()
+    R.loss(p, t0, t1, txn, tyn, symmetric=symmetric).backward()
     g = p.grad[0].numpy()
     for h, rel in ((1e-3, 5e-2), (1e-5, 1e-4)):
         for c, i, j in [(0, 0, 0), (1, 1, 2), (0, 2, 3), (1, 2, 1)]:
@@ -47,5 +50,6 @@ def test_torch_reference_gradient_equals_central_differences():
             b = a.clone()
             a[0, c, i, j] += h
             b[0, c, i, j] -= h
-            fd = (R.loss(a, t0, t1, txn, tyn) - R.loss(b, t0, t1, txn, tyn)).item() / (2 * h)
+            fd = (R.loss(a, t0, t1, txn, tyn, symmetric=symmetric)
+                  - R.loss(b, t0, t1, txn, tyn, symmetric=symmetric)).item() / (2 * h)
             assert abs(fd - g[c, i, j]) <= rel * max(abs(fd), 1e-3), (h, c, i, j, fd, g[c, i, j])

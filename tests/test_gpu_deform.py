@@ -5,15 +5,16 @@
   which steep particle edges turn into up to ~0.1 counts);
 * soft-argmax read-out r of every 32 x 32 window: within 1e-4 px of the float64
   torch reference on the same deformed image;
-* gradients with respect to the nodes and to im1: the pure-torch autograd
-  reference (float64) within 1e-3 of the gradient's norm; against FP64 central
-  finite differences with h = 1e-3 px within 5 % (the piecewise-linear sampling
-  makes differences over h include pixels that cross an integer position) and with
-  h = 1e-5 px within 1e-3;
+* gradients with respect to the nodes and to im1, central scheme (im0 by -d/2, im1
+  by +d/2) and im1-only scheme: the pure-torch autograd reference (float64) within
+  1e-3 of the gradient's norm; against FP64 central finite differences with
+  h = 1e-3 px within 5 % (the piecewise-linear sampling makes differences over h
+  include pixels that cross an integer position) and with h = 1e-5 px within 1e-3;
 * refinement: 20 Adam steps lower the RMS error against the imposed field;
 * deformation-mode multipass: a deformed pass equals the oracle's pass on the
-  oracle's deformation of im1 by the same field, and lowers the RMS error against
-  the imposed field below the window-shift mode's.
+  oracle's deformation of both images by the same field (im0 by -d/2, im1 by
+  +d/2), and lowers the RMS error against the imposed field below the
+  window-shift mode's.
 """
 
 import numpy as np
@@ -57,18 +58,20 @@ def test_warp_matches_oracle():
     from oracle import deform as OD
 
     im0, im1, nodes, truth, xn, yn = _case(B=1)
-    got = deform.warp(nodes, xn, yn, im1)
-    torch.cuda.synchronize()
     f, gx, gy, im = (nodes[0].cpu().numpy().astype(np.float64), xn.cpu().numpy(),
                      yn.cpu().numpy(), im1[0].cpu().numpy())
     eps = 2 * float(np.spacing(np.float32(max(im.shape))))
-    outs = [OD.warp(f + np.array([du, dv])[:, None, None], gx, gy, im)
-            for du in (-eps, 0.0, eps) for dv in (-eps, 0.0, eps)]
-    lo, hi = np.min(outs, axis=0) - 1e-3, np.max(outs, axis=0) + 1e-3
-    for g in (got[0], deform.warp(nodes, xn, yn, im1.to(torch.int32).to(torch.int16))[0]):
-        g = g.cpu().numpy()  # float32 image, then uint16 (int16 storage): same samples
-        bad = (g < lo) | (g > hi)
-        assert not bad.any(), (int(bad.sum()), float(np.abs(g - outs[4]).max()))
+    for scale in (1.0, 0.5, -0.5):
+        got = deform.warp(nodes, xn, yn, im1, scale)
+        torch.cuda.synchronize()
+        outs = [OD.warp(f + np.array([du, dv])[:, None, None], gx, gy, im, scale)
+                for du in (-eps, 0.0, eps) for dv in (-eps, 0.0, eps)]
+        lo, hi = np.min(outs, axis=0) - 1e-3, np.max(outs, axis=0) + 1e-3
+        as_u16 = deform.warp(nodes, xn, yn, im1.to(torch.int32).to(torch.int16), scale)
+        for g in (got[0], as_u16[0]):
+            g = g.cpu().numpy()  # float32 image, then uint16 (int16 storage): same samples
+            bad = (g < lo) | (g > hi)
+            assert not bad.any(), (scale, int(bad.sum()), float(np.abs(g - outs[4]).max()))
 
 
 def test_readout_matches_torch_reference():
@@ -87,28 +90,29 @@ def test_readout_matches_torch_reference():
     assert (cpk >= cz).all()
 
 
-def _grads_gpu(nodes, im0, im1, xn, yn):
+def _grads_gpu(nodes, im0, im1, xn, yn, symmetric):
     from fluidimage_gb300 import deform
 
     p = nodes.clone().requires_grad_(True)
     q = im1.clone().requires_grad_(True)
-    r = deform.DeformCorrelate.apply(p, im0, q, xn, yn, 0.1)
+    r = deform.DeformCorrelate.apply(p, im0, q, xn, yn, 0.1, symmetric)
     loss = (r * r).sum(dim=-1).mean()
     loss.backward()
     return loss.item(), p.grad, q.grad
 
 
-def test_adjoint_matches_autograd_and_finite_differences():
+@pytest.mark.parametrize("symmetric", [True, False], ids=["central", "im1_only"])
+def test_adjoint_matches_autograd_and_finite_differences(symmetric):
     import torch
 
     import deform_reference as R
 
     im0, im1, nodes, truth, xn, yn = _case()
-    loss, g_nodes, g_im1 = _grads_gpu(nodes, im0, im1, xn, yn)
+    loss, g_nodes, g_im1 = _grads_gpu(nodes, im0, im1, xn, yn, symmetric)
     # pure-torch autograd reference, float64
     p = nodes.double().clone().requires_grad_(True)
     q = im1.double().clone().requires_grad_(True)
-    ref_loss = R.loss(p, im0.double(), q, xn, yn)
+    ref_loss = R.loss(p, im0.double(), q, xn, yn, symmetric=symmetric)
     ref_loss.backward()
     rel_n = ((g_nodes.double() - p.grad).norm() / p.grad.norm()).item()
     rel_i = ((g_im1.double() - q.grad).norm() / q.grad.norm()).item()
@@ -125,8 +129,9 @@ def test_adjoint_matches_autograd_and_finite_differences():
             m = base.clone()
             a[b, c, i, j] += h
             m[b, c, i, j] -= h
-            fd = (R.loss(a, im0.double(), im1.double(), xn, yn)
-                  - R.loss(m, im0.double(), im1.double(), xn, yn)).item() / (2 * h)
+            fd = (R.loss(a, im0.double(), im1.double(), xn, yn, symmetric=symmetric)
+                  - R.loss(m, im0.double(), im1.double(), xn, yn, symmetric=symmetric)
+                  ).item() / (2 * h)
             g = g_nodes[b, c, i, j].item()
             scale = max(abs(fd), 1e-2 * g_nodes.abs().max().item())
             worst[h] = max(worst.get(h, 0.0), abs(g - fd) / scale)
@@ -174,8 +179,9 @@ def test_deformed_multipass_matches_oracle_and_truth():
     xn = np.unique(prev.ixvecs_approx).astype(np.float32)
     yn = np.unique(prev.iyvecs_approx).astype(np.float32)
     nodes32 = nodes.astype(np.float32)
-    warped = OD.warp(nodes32, xn, yn, im1.astype(np.float64)).astype(np.float32)
-    o = O.piv_pass(im0.astype(np.float32), warped, (16, 16), 0.5, apply_subpix=True)
+    w0 = OD.warp(nodes32, xn, yn, im0.astype(np.float64), -0.5).astype(np.float32)
+    w1 = OD.warp(nodes32, xn, yn, im1.astype(np.float64), 0.5).astype(np.float32)
+    o = O.piv_pass(w0, w1, (16, 16), 0.5, apply_subpix=True)
     want_x = o.deltaxs + nodes32[0].ravel()
     raw = np.asarray(last.deltaxs)
     ok = ~np.isnan(raw) & ~np.isnan(want_x) & (np.asarray(last.near_tie_flags) == 0)
