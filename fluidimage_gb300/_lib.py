@@ -156,6 +156,10 @@ _SIGNATURES = {
     "fi_clamp": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P]),
     "fi_sq_sum_max": (C.c_int, [P, C.c_int, C.c_int64, P, P, C.c_int, P]),
     "fi_tanh_rescale": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P]),
+    "fi_min_max": (C.c_int, [P, C.c_int, C.c_int64, P, C.c_int, P]),
+    "fi_rescale_intensity": (C.c_int, [P, C.c_int, C.c_int64, P, C.c_int, C.c_double, C.c_double,
+                                       P, P]),
+    "fi_gamma": (C.c_int, [P, C.c_int, C.c_int64, C.c_double, C.c_double, P, P, P]),
     "fi_gaussian_filter": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P]),
     "fi_sharpen_combine": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_double, P, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),

@@ -11,7 +11,11 @@
 // * img - weight * filtered with numpy's result type (float64 for integer images
 //   and a float weight, float32 for float32 images, wrapping integer arithmetic for
 //   an integer weight), optionally clamped at 0;
-// * clamping (global_threshold) and the tanh rescaling (rescale_intensity_tanh).
+// * clamping (global_threshold) and the tanh rescaling (rescale_intensity_tanh);
+// * the linear rescaling of rescale_intensity (:313-331) and the power law of
+//   gamma_correction (:441-470), which upstream takes from scikit-image 0.24
+//   (exposure.rescale_intensity with in_range='image' and a numeric out_range;
+//   exposure.adjust_gamma), restated from their published definitions.
 #include <cstdint>
 #include <cstring>
 
@@ -386,6 +390,156 @@ __global__ void k_tanh_rescale(const void* in, int dtype, int64_t count, double 
     out[e] = floor(scale * tanh(load_d(in, dtype, e) / thr));
 }
 
+// NaN-propagating min / max (numpy's ndarray.min / max).
+__device__ __forceinline__ double nan_min(double a, double b) {
+  return (a != a || b < a || b != b) ? (a != a ? a : b) : a;
+}
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return (a != a || b > a || b != b) ? (a != a ? a : b) : a;
+}
+
+// Per block: min and max of the image (NaN-propagating); part[0..nparts) the minima,
+// part[nparts..2 nparts) the maxima.
+__global__ void k_min_max_part(const void* in, int dtype, int64_t count, double* part) {
+  __shared__ double smn[32], smx[32];
+  double mn = INFINITY, mx = -INFINITY;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = load_d(in, dtype, e);
+    mn = nan_min(mn, v);
+    mx = nan_max(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = nan_min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = nan_max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    smn[wid] = mn;
+    smx[wid] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      mn = nan_min(mn, smn[w]);
+      mx = nan_max(mx, smx[w]);
+    }
+    part[blockIdx.x] = mn;
+    part[gridDim.x + blockIdx.x] = mx;
+  }
+}
+
+// The block's first warp reduces the nparts partial extremes to (imin, imax).
+__device__ void reduce_parts(const double* part, int nparts, double* out2) {
+  if (threadIdx.x < 32) {
+    double mn = INFINITY, mx = -INFINITY;
+    for (int i = threadIdx.x; i < nparts; i += 32) {
+      mn = nan_min(mn, part[i]);
+      mx = nan_max(mx, part[nparts + i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = nan_min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = nan_max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (threadIdx.x == 0) {
+      out2[0] = mn;
+      out2[1] = mx;
+    }
+  }
+  __syncthreads();
+}
+
+// rescale_intensity(img, out_range=(omin, omax)), in_range = the image's extremes:
+// x clipped to [imin, imax] (a no-op), then (x - imin) / (imax - imin) * (omax - omin)
+// + omin, each operation rounded, in float64 for integer and float64 images and in
+// float32 for float32 images (the Python-float operands rounded to float32, as
+// numpy 2 does with a float32 array); when imin == imax, x clipped to [omin, omax].
+__global__ void k_rescale_linear(const void* in, int dtype, int64_t count, const double* part,
+                                 int nparts, double omin, double omax, void* out) {
+  __shared__ double ext[2];
+  reduce_parts(part, nparts, ext);
+  const double imin = ext[0], imax = ext[1];
+  const bool flat = !(imin != imax);
+  const double span_in = imax - imin, span_out = omax - omin;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = load_d(in, dtype, e);
+    if (dtype == FI_PRE_F32) {
+      const float x = (float)v;
+      float r;
+      if (flat) {
+        const float lo = (float)omin, hi = (float)omax;
+        r = fminf(fmaxf(x, lo), hi);
+        if (x != x) r = x;
+      } else {
+        r = __fdiv_rn(__fsub_rn(x, (float)imin), (float)span_in);
+        r = __fadd_rn(__fmul_rn(r, (float)span_out), (float)omin);
+      }
+      static_cast<float*>(out)[e] = r;
+    } else {
+      double r;
+      if (flat) {
+        r = fmin(fmax(v, omin), omax);
+        if (v != v) r = v;
+      } else {
+        r = __ddiv_rn(__dsub_rn(v, imin), span_in);
+        r = __dadd_rn(__dmul_rn(r, span_out), omin);
+      }
+      static_cast<double*>(out)[e] = r;
+    }
+  }
+}
+
+// x ** g of a float array as numpy evaluates it: exponents 0, 0.5, 1 and 2 by their
+// exact operations (ones, correctly rounded square root, copy, product), others by pow.
+__device__ __forceinline__ double np_pow(double x, double g) {
+  if (g == 1.0) return x;
+  if (g == 2.0) return __dmul_rn(x, x);
+  if (g == 0.5) return __dsqrt_rn(x);
+  if (g == 0.0) return 1.0;
+  return pow(x, g);
+}
+__device__ __forceinline__ float np_powf(float x, float g) {
+  if (g == 1.f) return x;
+  if (g == 2.f) return __fmul_rn(x, x);
+  if (g == 0.5f) return __fsqrt_rn(x);
+  if (g == 0.f) return 1.f;
+  return (float)pow((double)x, (double)g);
+}
+
+// gamma_correction = adjust_gamma(img, gamma, gain): uint8 through the 256-entry
+// table lut; otherwise ((x / scale) ** gamma) * scale * gain cast back to the image
+// dtype, scale = the dtype's upper limit (65535 for uint16, 1 for floats), in float64
+// for uint16 and float64 images and in float32 for float32 images (gamma and gain
+// rounded to float32); the cast to uint16 truncates toward zero and saturates.
+__global__ void k_gamma(const void* in, int dtype, int64_t count, double gamma, double gain,
+                        const uint8_t* __restrict__ lut, void* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    switch (dtype) {
+      case FI_PRE_U8:
+        static_cast<uint8_t*>(out)[e] = lut[static_cast<const uint8_t*>(in)[e]];
+        break;
+      case FI_PRE_U16: {
+        const double x = __ddiv_rn((double)static_cast<const uint16_t*>(in)[e], 65535.0);
+        const double y = __dmul_rn(__dmul_rn(np_pow(x, gamma), 65535.0), gain);
+        const double t = trunc(y);
+        static_cast<uint16_t*>(out)[e] = (uint16_t)(t < 0.0 ? 0.0 : (t > 65535.0 ? 65535.0 : t));
+        break;
+      }
+      case FI_PRE_F32: {
+        const float x = static_cast<const float*>(in)[e];
+        static_cast<float*>(out)[e] = __fmul_rn(np_powf(x, (float)gamma), (float)gain);
+        break;
+      }
+      default: {
+        const double x = static_cast<const double*>(in)[e];
+        static_cast<double*>(out)[e] = __dmul_rn(np_pow(x, gamma), gain);
+      }
+    }
+  }
+}
+
 static int grid_for(int64_t count) {
   const int64_t b = (count + 255) / 256;
   return (int)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
@@ -515,4 +669,36 @@ extern "C" int fi_sharpen_combine(const void* blurred, const void* filtered, int
   k_sharpen_combine<<<blocks, 256, 0, (cudaStream_t)stream>>>(blurred, filtered, dtype, count,
                                                              alpha, out);
   return check_launch("fi_sharpen_combine");
+}
+
+extern "C" int fi_min_max(const void* in, int dtype, int64_t count, double* part, int nparts,
+                          void* stream) {
+  FI_REQUIRE(in && part && count > 0 && nparts > 0 && nparts <= 4096,
+             "fi_min_max: bad arguments");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_min_max: bad dtype %d", dtype);
+  k_min_max_part<<<nparts, 256, 0, (cudaStream_t)stream>>>(in, dtype, count, part);
+  return check_launch("fi_min_max");
+}
+
+extern "C" int fi_rescale_intensity(const void* in, int dtype, int64_t count, const double* part,
+                                    int nparts, double omin, double omax, void* out,
+                                    void* stream) {
+  FI_REQUIRE(in && part && out && count > 0 && nparts > 0 && nparts <= 4096,
+             "fi_rescale_intensity: bad arguments");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_rescale_intensity: bad dtype %d",
+             dtype);
+  k_rescale_linear<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, part,
+                                                                     nparts, omin, omax, out);
+  return check_launch("fi_rescale_intensity");
+}
+
+extern "C" int fi_gamma(const void* in, int dtype, int64_t count, double gamma, double gain,
+                        const uint8_t* lut, void* out, void* stream) {
+  FI_REQUIRE(in && out && count > 0, "fi_gamma: bad arguments");
+  FI_REQUIRE(dtype >= FI_PRE_U8 && dtype <= FI_PRE_F64, "fi_gamma: bad dtype %d", dtype);
+  FI_REQUIRE(dtype != FI_PRE_U8 || lut, "fi_gamma: uint8 images need the table");
+  FI_REQUIRE(gamma >= 0.0, "fi_gamma: gamma must be non-negative");
+  k_gamma<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, gamma, gain, lut,
+                                                            out);
+  return check_launch("fi_gamma");
 }

@@ -16,11 +16,14 @@ works/preproc/_toolbox_py.py:
   filter over the stack with ``window_shape`` (nt, ny, nx), no clamping;
 * ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355);
 * ``sharpen`` (:472-490): scipy.ndimage's gaussian filters (float64 line sums in
-  scipy's order, each axis cast to the image dtype) and the final combination.
+  scipy's order, each axis cast to the image dtype) and the final combination;
+* ``rescale_intensity`` (:313-331) and ``gamma_correction`` (:441-470), which
+  upstream takes from scikit-image 0.24 (``exposure.rescale_intensity`` with
+  ``in_range='image'``, ``exposure.adjust_gamma``): their published elementwise
+  definitions, in the dtypes scikit-image and numpy 2 use.
 
-The tools built on scikit-image (``adaptive_threshold``, ``rescale_intensity``,
-``equalize_hist_*``, ``gamma_correction``) keep their parameters but raise
-``NotImplementedError`` when enabled.
+The other tools built on scikit-image (``adaptive_threshold``, ``equalize_hist_*``)
+keep their parameters but raise ``NotImplementedError`` when enabled.
 """
 
 from __future__ import annotations
@@ -307,6 +310,71 @@ def _tanh_one(img, threshold):
     return out
 
 
+_NPARTS = 152
+
+
+def _extremes(x):
+    """Device partial (min, max) of ``x`` (fi_min_max), 2 x _NPARTS float64."""
+    torch = _torch()
+    part = torch.empty(2 * _NPARTS, dtype=torch.float64, device=x.device)
+    L.check(L.load().fi_min_max(L.ptr(x), _DT[_dtype_of(x)], x.numel(), L.ptr(part), _NPARTS,
+                                L.stream_handle()), "fi_min_max")
+    return part
+
+
+@_per_image
+def rescale_intensity(img, minima=0.0, maxima=4096):
+    """Intensities mapped linearly from [img.min(), img.max()] to [minima, maxima]
+    (_toolbox_py.py:313-331); float32 for float32 images, float64 otherwise; per
+    image for a stack."""
+    x, single = _stack(img)
+    outs = [_rescale_one(x[i], minima, maxima) for i in range(x.shape[0])]
+    return outs[0] if single else _torch().stack(outs)
+
+
+def _rescale_one(img, minima, maxima):
+    torch = _torch()
+    x = img.contiguous()
+    dtype = _dtype_of(x)
+    part = _extremes(x)
+    out_dt = torch.float32 if dtype == np.float32 else torch.float64
+    out = torch.empty(tuple(x.shape), dtype=out_dt, device=x.device)
+    L.check(L.load().fi_rescale_intensity(L.ptr(x), _DT[dtype], x.numel(), L.ptr(part), _NPARTS,
+                                          float(minima), float(maxima), L.ptr(out),
+                                          L.stream_handle()), "fi_rescale_intensity")
+    return out
+
+
+def gamma_table(gamma, gain):
+    """The 256-entry uint8 table of adjust_gamma for uint8 images, from the two
+    parameters: rint(255 gain linspace(0, 1, 256) ** gamma), capped at 255."""
+    lut = 255 * gain * (np.linspace(0, 1, 256) ** gamma)
+    return np.minimum(np.rint(lut), 255).astype("uint8")
+
+
+@_per_image
+def gamma_correction(img, gamma=1.0, gain=1.0):
+    """gain * img ** gamma on intensities scaled to [0, 1] by the dtype's range
+    (_toolbox_py.py:441-470), in the image dtype."""
+    torch = _torch()
+    if gamma < 0:
+        raise ValueError("Gamma should be a non-negative real number.")
+    x = img.contiguous()
+    dtype = _dtype_of(x)
+    lut = None
+    if dtype == np.uint8:
+        lut = torch.as_tensor(gamma_table(gamma, gain), device=x.device)
+    elif dtype.kind == "f":
+        part = _extremes(x).cpu().numpy()
+        if part[:_NPARTS].min() < 0:
+            raise ValueError("Image Correction methods work correctly only on images with "
+                             "non-negative values. Use skimage.exposure.rescale_intensity.")
+    out = _empty(tuple(x.shape), dtype, x.device)
+    L.check(L.load().fi_gamma(L.ptr(x), _DT[dtype], x.numel(), float(gamma), float(gain),
+                              L.ptr(lut), L.ptr(out), L.stream_handle()), "fi_gamma")
+    return out
+
+
 def _gauss_weights(sigma, truncate=4.0):
     """scipy.ndimage's ``_gaussian_kernel1d`` (order 0, ndimage/_filters.py), reversed
     for the correlation as ``gaussian_filter1d`` does, and its radius."""
@@ -370,6 +438,8 @@ TOOLS = {
     "temporal_percentile": temporal_percentile,
     "global_threshold": global_threshold,
     "rescale_intensity_tanh": rescale_intensity_tanh,
+    "rescale_intensity": rescale_intensity,
+    "gamma_correction": gamma_correction,
     "sharpen": sharpen,
 }
 for _name in AVAILABLE_TOOLS:

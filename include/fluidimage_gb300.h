@@ -619,6 +619,33 @@ int fi_tanh_rescale(const void* in, int dtype, int64_t count, double threshold, 
                     double* out, void* stream);
 
 /*
+ * Partial extremes of img (NaN-propagating like ndarray.min / max), one pair per
+ * block: part[0, nparts) the minima, part[nparts, 2 nparts) the maxima; nparts <= 4096.
+ */
+int fi_min_max(const void* in, int dtype, int64_t count, double* part, int nparts, void* stream);
+
+/*
+ * rescale_intensity (_toolbox_py.py:313-331, skimage.exposure.rescale_intensity of
+ * scikit-image 0.24 with in_range='image', out_range=(omin, omax)): the image's
+ * extremes come from fi_min_max's partials on the device (no host round trip);
+ * out = (x - imin) / (imax - imin) * (omax - omin) + omin, float32 for float32 images
+ * and float64 otherwise; x clipped to [omin, omax] when imin == imax.
+ */
+int fi_rescale_intensity(const void* in, int dtype, int64_t count, const double* part, int nparts,
+                         double omin, double omax, void* out, void* stream);
+
+/*
+ * gamma_correction (_toolbox_py.py:441-470, skimage.exposure.adjust_gamma of
+ * scikit-image 0.24): uint8 images through a 256-entry device table lut
+ * (rint(255 gain linspace(0, 1, 256) ** gamma), capped at 255); other dtypes
+ * ((x / scale) ** gamma) scale gain in the image dtype, scale = 65535 for uint16 and
+ * 1 for floats, the uint16 result truncated.  gamma >= 0; the caller rejects
+ * negative images (upstream raises ValueError).
+ */
+int fi_gamma(const void* in, int dtype, int64_t count, double gamma, double gain,
+             const uint8_t* lut, void* out, void* stream);
+
+/*
  * scipy.ndimage.gaussian_filter of each image of a (nt, ny, nx) stack (axis y then x;
  * the call of sharpen, _toolbox_py.py:486-487): one symmetric 1-D correlation per
  * axis in float64 ('reflect' boundaries; out = w_0 x_0, then the tap pairs from the

@@ -5,6 +5,14 @@ module provides, with upstream's stack handling (works/preproc/io.py:46-84): the
 sliding tools, global_threshold and rescale_intensity_tanh run image by image into
 a float64 stack; the temporal tools see the whole stack.  The arithmetic is
 numpy's (NEP 50 scalar promotion), the filters scipy.ndimage's.
+
+rescale_intensity and gamma_correction call scikit-image (0.24.0 in the reference's
+lock file), which is not installed here: they are restated from scikit-image's
+published definitions of ``exposure.rescale_intensity`` (in_range='image', a
+numeric out_range; output float64 for integer images, the float type otherwise)
+and ``exposure.adjust_gamma`` (uint8 through a 256-entry table, other dtypes
+scaled by the dtype's range, power law, cast back).  Parity for these two is
+unpinned: no scikit-image output exists here to record.
 """
 
 from __future__ import annotations
@@ -114,3 +122,45 @@ def sharpen(img, sigma1=3.0, sigma2=1.0, alpha=30.0):
         return blurred + alpha * (blurred - filter_blurred)
 
     return _per_image(one, img)
+
+
+def rescale_intensity(img, minima=0.0, maxima=4096):
+    """_toolbox_py.py:313-331 (skimage.exposure.rescale_intensity(img,
+    out_range=(minima, maxima)))."""
+
+    def one(im):
+        out_dtype = np.float32 if im.dtype == np.float32 else np.float64
+        imin, imax = float(im.min()), float(im.max())
+        omin, omax = float(minima), float(maxima)
+        im = np.clip(im, imin, imax)
+        if imin != imax:
+            im = (im - imin) / (imax - imin)
+            return np.asarray(im * (omax - omin) + omin, dtype=out_dtype)
+        return np.clip(im, omin, omax).astype(out_dtype)
+
+    return _per_image(one, img)
+
+
+def gamma_correction(img, gamma=1.0, gain=1.0, with_raw=False):
+    """_toolbox_py.py:441-470 (skimage.exposure.adjust_gamma(img, gamma, gain)).
+    ``with_raw``: also the float values before the cast to uint16 (for tests at
+    truncation boundaries)."""
+    if gamma < 0:
+        raise ValueError("Gamma should be a non-negative real number.")
+    raws = []
+
+    def one(im):
+        if im.dtype == np.uint8:
+            lut = 255 * gain * (np.linspace(0, 1, 256) ** gamma)
+            lut = np.minimum(np.rint(lut), 255).astype("uint8")
+            return lut[im]
+        if im.min() < 0:
+            raise ValueError("Image Correction methods work correctly only on images with "
+                             "non-negative values. Use skimage.exposure.rescale_intensity.")
+        scale = 65535.0 if im.dtype == np.uint16 else 1.0
+        raw = ((im / scale) ** gamma) * scale * gain
+        raws.append(raw)
+        return raw.astype(im.dtype)
+
+    out = _per_image(one, img)
+    return (out, raws) if with_raw else out

@@ -71,3 +71,74 @@ def test_work_preproc_sequence():
                               maxima=100)
     got = np.array([res.data[n] for n in names])
     np.testing.assert_array_equal(got, want)
+
+
+def _ulps(got, want):
+    got, want = np.asarray(got), np.asarray(want)
+    return np.abs(got - want) / np.spacing(np.maximum(np.abs(want), np.finfo(want.dtype).tiny))
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32", "f64"])
+@pytest.mark.parametrize("lo_hi", [(0.0, 4096.0), (-1.0, 1.0), (0.0, 65535.0)])
+def test_rescale_intensity_matches_oracle(image, lo_hi):
+    """rescale_intensity: the same IEEE operations in the same order as numpy, so the
+    float64 and float32 results are equal to the oracle's."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    img = Z["img_f32"].astype(np.float64) * 1.37 if image == "f64" else Z["img_" + image]
+    got = P.to_host(P.rescale_intensity(P.to_device(img), *lo_hi))
+    want = O.rescale_intensity(img.copy(), *lo_hi)
+    assert got.dtype == want.dtype
+    np.testing.assert_array_equal(got, want)
+    one = P.to_host(P.rescale_intensity(P.to_device(img[0]), *lo_hi))
+    want1 = O.rescale_intensity(img[0].copy(), *lo_hi)
+    assert one.dtype == want1.dtype
+    np.testing.assert_array_equal(one, want1)
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32", "f64"])
+@pytest.mark.parametrize("gamma_gain", [(1.0, 1.0), (0.5, 1.0), (2.0, 0.8), (0.7, 1.0),
+                                        (1.8, 1.3)])
+def test_gamma_correction_matches_oracle(image, gamma_gain):
+    """gamma_correction: uint8 exact (the same table); the exponents 0.5, 1 and 2 exact
+    (numpy's sqrt, copy and product); other exponents through CUDA's pow, within
+    2 ulps of the libm power for floats, and for uint16 equal except where the
+    oracle's value before truncation lies within 1e-12 relative of an integer."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    gamma, gain = gamma_gain
+    if image == "f64":
+        img = np.abs(Z["img_f32"].astype(np.float64)) * 1.37
+    elif image == "f32":
+        img = np.abs(Z["img_f32"])
+    else:
+        img = Z["img_" + image]
+    x = img[0]
+    got = P.to_host(P.gamma_correction(P.to_device(x), gamma, gain))
+    want, raws = O.gamma_correction(x.copy(), gamma, gain, with_raw=True)
+    assert got.dtype == want.dtype
+    exact = image == "u8" or gamma in (0.5, 1.0, 2.0)
+    if exact:
+        np.testing.assert_array_equal(got, want)
+    elif image == "u16":
+        raw = raws[0]
+        near = np.abs(raw - np.rint(raw)) <= 1e-12 * np.maximum(np.abs(raw), 1.0)
+        bad = (got != want) & ~near
+        assert not bad.any(), int(bad.sum())
+        assert np.abs(got.astype(np.int64) - want.astype(np.int64)).max() <= 1
+    else:
+        assert _ulps(got, want).max() <= 2.0
+    stack = P.to_host(P.gamma_correction(P.to_device(img), gamma, gain))
+    assert stack.dtype == np.float64
+    np.testing.assert_array_equal(stack[0], got.astype(np.float64))
+
+
+def test_gamma_correction_rejects_negative_float_images():
+    from fluidimage_gb300 import preproc as P
+
+    img = Z["img_f32"][0].copy()
+    img[3, 4] = -1.0
+    with pytest.raises(ValueError):
+        P.gamma_correction(P.to_device(img), 0.7)

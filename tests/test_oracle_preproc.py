@@ -21,3 +21,44 @@ def test_oracle_matches_upstream_tools(name):
     want = Z["out_" + name]
     assert got.dtype == want.dtype
     np.testing.assert_array_equal(got, want)
+
+
+def test_rescale_intensity_known_answers():
+    """scikit-image's rescale_intensity(in_range='image', out_range=(lo, hi)) by its
+    definition: the image's extremes go to lo and hi, linearly in between; float64
+    for integer images, float32 for float32 images; a flat image is clipped."""
+    a = np.array([[10, 20], [30, 50]], np.uint16)
+    got = O.rescale_intensity(a, 0.0, 4.0)
+    assert got.dtype == np.float64
+    np.testing.assert_array_equal(got, [[0.0, 1.0], [2.0, 4.0]])
+    f = np.array([[-1.0, 0.0, 3.0]], np.float32)
+    got = O.rescale_intensity(f, 0.0, 8.0)
+    assert got.dtype == np.float32
+    np.testing.assert_array_equal(got, np.array([[0.0, 2.0, 8.0]], np.float32))
+    flat = np.full((2, 3), 7, np.uint8)
+    np.testing.assert_array_equal(O.rescale_intensity(flat, 0.0, 5.0), np.full((2, 3), 5.0))
+    stack = np.stack([a, 2 * a])  # per image: both map to the same values
+    got = O.rescale_intensity(stack, 0.0, 4.0)
+    np.testing.assert_array_equal(got[0], got[1])
+
+
+def test_gamma_correction_known_answers():
+    """adjust_gamma by its definition: gain * (x / range) ** gamma * range, in the
+    image dtype; uint8 through the rounded 256-entry table."""
+    u8 = np.array([[0, 255, 128, 64]], np.uint8)
+    got = O.gamma_correction(u8, 0.5, 1.0)
+    want = np.minimum(np.rint(255 * np.sqrt(u8 / 255.0)), 255).astype(np.uint8)
+    np.testing.assert_array_equal(got, want)
+    assert got.dtype == np.uint8
+    u16 = np.array([[0, 65535, 32768]], np.uint16)
+    got = O.gamma_correction(u16, 2.0, 1.0)
+    assert got.dtype == np.uint16
+    assert got[0, 0] == 0 and got[0, 1] == 65535
+    assert got[0, 2] == int(32768.0 ** 2 / 65535.0)
+    f = np.array([[0.25, 1.0, 4.0]], np.float32)
+    np.testing.assert_array_equal(O.gamma_correction(f, 2.0, 0.5),
+                                  np.array([[0.03125, 0.5, 8.0]], np.float32))
+    with pytest.raises(ValueError):
+        O.gamma_correction(np.array([[-1.0]], np.float32))
+    with pytest.raises(ValueError):
+        O.gamma_correction(u8, -1.0)
