@@ -54,7 +54,7 @@ constexpr int OFF_B1 = 0;
 constexpr int OFF_B2 = OFF_B1 + 2 * B1_BYTES;
 constexpr int OFF_B4 = OFF_B2 + 2 * B2_BYTES;
 constexpr int OFF_A = OFF_B4 + 2 * B4_BYTES;  // stage operands, then the planes
-constexpr int A_BYTES = 64 * 1024 + 2048;
+constexpr int A_BYTES = 64 * 1024;
 constexpr int OFF_X = OFF_A + A_BYTES;         // kx' = 0 rows exchanged between warps
 constexpr int X_BYTES = WIN * 2 * 64 * 4;
 constexpr int OFF_W = OFF_X + X_BYTES;         // per-window scalars
@@ -64,12 +64,6 @@ constexpr int RED_BYTES = WIN * 256;
 constexpr int OFF_BAR = OFF_RED + RED_BYTES;   // mbarrier, TMEM base
 constexpr int SMEM = OFF_BAR + 64;
 static_assert(WIN * N * LDP * 4 <= A_BYTES, "planes must fit the operand region");
-// the next tile's window rows, prefetched into the operand region behind the planes
-// while the current tile's peak search runs: [window][image][row] x 64 bytes
-constexpr int PF_OFF = 34816;
-constexpr int PF_ROW = 64;
-static_assert(WIN * N * LDP * 4 <= PF_OFF, "the prefetch must not overlap the planes");
-static_assert(PF_OFF + WIN * 2 * N * PF_ROW <= A_BYTES, "prefetch region");
 
 // operand sub-regions of the A region
 constexpr int A1_PART = 128 * 32 * 2;  // [img][tile][part]: 128 rows x K 32
@@ -151,23 +145,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
   }
   return done != 0;
-}
-
-// Row prefetch by the bulk-copy engine: `bytes` (multiple of 16, both addresses
-// 16-byte aligned) from global to shared memory, completing on the mbarrier.
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes,
-                                          uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t addr, float (&v)[16]) {
@@ -366,47 +343,6 @@ __device__ __forceinline__ void load_row_f32(const float* im, int H, int W, int 
   }
 }
 
-// A window row that the bulk copy can fetch: integer image, inside the image, 16-byte
-// aligned; its source address and size (u16: 64 bytes, u8: 32 bytes).
-__device__ __forceinline__ bool pf_row(const void* im, int dtype, int H, int W, int y, int x0,
-                                       const void** src, uint32_t* bytes) {
-  if (dtype == FI_F32 || y < 0 || y >= H || x0 < 0 || x0 + N > W) return false;
-  const size_t esz = (dtype == FI_U16) ? 2 : 1;
-  const unsigned char* p = reinterpret_cast<const unsigned char*>(im) + ((size_t)y * W + x0) * esz;
-  if ((reinterpret_cast<uintptr_t>(p) & 15) != 0) return false;
-  *src = p;
-  *bytes = (uint32_t)(N * esz);
-  return true;
-}
-
-// The 32 pixels of a prefetched row (shared memory), minus the image minimum.
-__device__ __forceinline__ void unpack_row(const unsigned char* row, int dtype, int mini,
-                                           int (&v)[N]) {
-  const uint4* q = reinterpret_cast<const uint4*>(row);
-  if (dtype == FI_U16) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint4 u = q[k];
-      const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        v[8 * k + 2 * i] = (int)(w4[i] & 0xffffu) - mini;
-        v[8 * k + 2 * i + 1] = (int)(w4[i] >> 16) - mini;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint4 u = q[k];
-      const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) v[16 * k + 4 * i + b] = (int)((w4[i] >> (8 * b)) & 0xffu) - mini;
-    }
-  }
-}
-
 template <int FORM>
 __global__ void __launch_bounds__(THREADS, 2)
     k_piv_pass_tc(const fi_piv_pass_args a, int nvec, int npad, int ntiles, float tie_rel,
@@ -420,14 +356,11 @@ __global__ void __launch_bounds__(THREADS, 2)
   TcWin* wins = reinterpret_cast<TcWin*>(sm + OFF_W);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + OFF_BAR);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + OFF_BAR + 8);
-  uint64_t* bar_pf = reinterpret_cast<uint64_t*>(sm + OFF_BAR + 16);
-  unsigned char* pf = sA + PF_OFF;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   fill_constants<F16>(sm);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar_pf)), "r"(THREADS));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -476,31 +409,6 @@ __global__ void __launch_bounds__(THREADS, 2)
   const uint32_t sA_u = smem_u32(sA), sB1 = smem_u32(sm + OFF_B1), sB2 = smem_u32(sm + OFF_B2),
                  sB4 = smem_u32(sm + OFF_B4);
   bool ok = true;
-  // every thread fetches its row of its warp's window of tile `tn`, both images, and
-  // arrives on bar_pf with the bytes it expects
-  uint32_t pf_phase = 0;
-  bool pf_pending = false;
-  auto prefetch = [&](int tn) {
-    uint32_t bytes = 0;
-    const void* src[2] = {nullptr, nullptr};
-    uint32_t nb[2] = {0u, 0u};
-    const int vn = tn * WIN + warp;
-    if (intpath && vn < nvec) {
-      const WinPos wq = window_positions<N>(a, vn, npad);
-      if (wq.valid) {
-        if (pf_row(a.im0, a.dtype, a.height, a.width, wq.y0 + lane, wq.x0, &src[0], &nb[0]))
-          bytes += nb[0];
-        if (pf_row(a.im1, a.dtype, a.height, a.width, wq.y1 + lane, wq.x1, &src[1], &nb[1]))
-          bytes += nb[1];
-      }
-    }
-    arrive_expect_tx(bar_pf, bytes);
-    for (int img = 0; img < 2; ++img)
-      if (nb[img]) bulk_copy(pf + ((warp * 2 + img) * N + lane) * PF_ROW, src[img], nb[img], bar_pf);
-    pf_pending = true;
-  };
-  if (blockIdx.x < ntiles) prefetch(blockIdx.x);
-
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int vec = tile * WIN + warp;  // this warp's window
     const bool active = vec < nvec;
@@ -513,24 +421,11 @@ __global__ void __launch_bounds__(THREADS, 2)
       unsigned long long u[4] = {0ull, 0ull, 0ull, 0ull};
       double sums[4] = {0.0, 0.0, 0.0, 0.0};
       float mm[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
-      // the rows prefetched for this tile have landed
-      ok = mbar_wait(bar_pf, pf_phase);
-      pf_phase ^= 1u;
-      pf_pending = false;
-      if (__syncthreads_or(!ok)) break;
       if (intpath) {
         int v0[32], v1[32];
         if (load) {
-          const void* sp;
-          uint32_t nbp;
-          if (pf_row(a.im0, a.dtype, a.height, a.width, wp.y0 + lane, wp.x0, &sp, &nbp))
-            unpack_row(pf + ((warp * 2 + 0) * N + lane) * PF_ROW, a.dtype, (int)min0, v0);
-          else
-            load_row_int(a.im0, a.dtype, a.height, a.width, wp.y0 + lane, wp.x0, (int)min0, v0);
-          if (pf_row(a.im1, a.dtype, a.height, a.width, wp.y1 + lane, wp.x1, &sp, &nbp))
-            unpack_row(pf + ((warp * 2 + 1) * N + lane) * PF_ROW, a.dtype, (int)min1, v1);
-          else
-            load_row_int(a.im1, a.dtype, a.height, a.width, wp.y1 + lane, wp.x1, (int)min1, v1);
+          load_row_int(a.im0, a.dtype, a.height, a.width, wp.y0 + lane, wp.x0, (int)min0, v0);
+          load_row_int(a.im1, a.dtype, a.height, a.width, wp.y1 + lane, wp.x1, (int)min1, v1);
         } else {
 #pragma unroll
           for (int i = 0; i < 32; ++i) v0[i] = v1[i] = 0;
@@ -622,8 +517,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         tw.valid = load ? 1 : 0;
         wins[warp] = tw;
       }
-      // every warp has read its prefetched rows before the operands overwrite them
-      __syncthreads();
+      __syncwarp();
       const float s0 = pow2f(-wins[warp].e0), s1 = pow2f(-wins[warp].e1);
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
@@ -790,8 +684,6 @@ __global__ void __launch_bounds__(THREADS, 2)
     });
     if (!ok) break;
     // ---------------- epilogue 4: the plane, peak search, subpixel fit ----------------
-    // (the next tile's rows are fetched meanwhile, behind the planes)
-    if (tile + (int)gridDim.x < ntiles) prefetch(tile + gridDim.x);
     {
       const int t = warp >> 2;
       float c[32];
@@ -863,7 +755,6 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
   }
   if (!ok && tid == 0 && status) atomicOr(status, 1);
-  if (pf_pending) mbar_wait(bar_pf, pf_phase);  // copies in flight land before exit
   fence_before();
   __syncthreads();
   fence_after();
