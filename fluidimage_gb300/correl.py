@@ -42,6 +42,11 @@ class CorrelGB300:
     """FFT cross-correlation of one window pair (or a batch) on the GPU."""
 
     _tag = "gb300"
+    #: class of the errors the per-window methods raise; ``register_upstream`` makes
+    #: it a subclass of the installed fluidimage's PIVError as well, so that
+    #: upstream's ``except PIVError`` (works/piv/singlepass.py:328, 339;
+    #: works/piv/fix.py:202) catches it
+    _piv_error = PIVError
 
     def __init__(self, im0_shape, im1_shape=None, method_subpix="2d_gaussian2", nsubpix=None,
                  displacement_max=None, particle_radius=3, nb_peaks_to_search=1, mode=None):
@@ -190,7 +195,7 @@ class CorrelGB300:
         if e == 5:
             raise AssertionError("correlation plane without finite value")
         if e:
-            error = PIVError(explanation=ERROR_STRINGS[e])
+            error = self._piv_error(explanation=ERROR_STRINGS[e])
             error.results = (int(dx[0]), int(dy[0]), cmax)
             raise error
         return int(dx[0]), int(dy[0]), cmax, (None if other is None else other[0])
@@ -213,7 +218,7 @@ class CorrelGB300:
                                  L.ptr(err), L.stream_handle()), "fi_subpix_at")
         e = int(err.item())
         if e:
-            raise PIVError(explanation=ERROR_STRINGS[e], result_compute_subpix=(iy, ix))
+            raise self._piv_error(explanation=ERROR_STRINGS[e], result_compute_subpix=(iy, ix))
         return float(ox.item()), float(oy.item())
 
 
@@ -229,7 +234,18 @@ def register_upstream():
     """
     try:
         from fluidimage.calcul import correl as upstream
+        from fluidimage.calcul.errors import PIVError as UpstreamPIVError
     except Exception:
         return False
+
+    class _PIVError(PIVError, UpstreamPIVError):
+        """A PIVError of both packages (upstream's handlers catch their own class)."""
+
+        def __init__(self, *args, **kwargs):
+            Exception.__init__(self, *args)
+            self.explanation = "General no peak error"
+            self.__dict__.update(kwargs)
+
+    CorrelGB300._piv_error = _PIVError
     upstream.correlation_classes[CorrelGB300._tag] = CorrelGB300
     return True

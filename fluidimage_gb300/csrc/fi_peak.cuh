@@ -289,40 +289,42 @@ __device__ PeakOut find_peak(const float* PL, const uint8_t* mask, const SearchB
 }
 
 // compute_subpix_2d_gaussian2 (subpix.py:16-61) in float32 with the upstream
-// operation order.  False when |depl|^2 > 4.5 (upstream then falls back to the
-// centroid).
-static __device__ bool gauss2_depl(const float (&c)[9], float* deplx_o, float* deply_o,
-                            bool* min_tie) {
-  float n[9];
+// operation order, in two halves.  First half, for element k of the 3x3 crop:
+// (c - min) / (max - min), the 1e-8 floor of zeros and the float32 log; `low`: the
+// normalised value lies within 1e-5 of the minimum.
+static __device__ __forceinline__ float gauss2_log(const float (&c)[9], int k, bool* low) {
   float cmin = c[0];
 #pragma unroll
-  for (int k = 1; k < 9; ++k) cmin = (c[k] < cmin) ? c[k] : cmin;
+  for (int q = 1; q < 9; ++q) cmin = (c[q] < cmin) ? c[q] : cmin;
+  float n[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) n[k] = __fsub_rn(c[k], cmin);
+  for (int q = 0; q < 9; ++q) n[q] = __fsub_rn(c[q], cmin);
   float cmx = n[0];
 #pragma unroll
-  for (int k = 1; k < 9; ++k) cmx = (n[k] > cmx) ? n[k] : cmx;
-  int nlow = 0;  // crop values within 1e-5 of the minimum (relative to the range)
+  for (int q = 1; q < 9; ++q) cmx = (n[q] > cmx) ? n[q] : cmx;
+  float nk = n[0];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    n[k] = __fdiv_rn(n[k], cmx);
-    nlow += (n[k] < 1e-5f) ? 1 : 0;
-    if (n[k] == 0.0f) n[k] = 1e-8f;
-  }
-  // two or more values at the minimum: the 1e-8 floor makes the fit depend on
-  // which of them rounds to exactly zero (a near-tie of the subpixel fit)
-  *min_tie = nlow >= 2;
+  for (int q = 1; q < 9; ++q) nk = (q == k) ? n[q] : nk;  // static indices: registers
+  float v = __fdiv_rn(nk, cmx);
+  *low = v < 1e-5f;
+  if (v == 0.0f) v = 1e-8f;
+  return logf(v);
+}
+
+// Second half: the least-squares coefficients of the nine logs and the offsets.
+// False when |depl|^2 > 4.5 (upstream then falls back to the centroid).
+static __device__ bool gauss2_fit(const float (&l)[9], float* deplx_o, float* deply_o) {
   float c10 = 0.f, c01 = 0.f, c11 = 0.f, c20 = 0.f, c02 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      const float l = logf(n[3 * a + b]);
-      c10 = __fadd_rn(c10, __fmul_rn((float)(b - 1), l));
-      c01 = __fadd_rn(c01, __fmul_rn((float)(a - 1), l));
-      c11 = __fadd_rn(c11, __fmul_rn((float)((b - 1) * (a - 1)), l));
-      c20 = __fadd_rn(c20, __fmul_rn((float)(3 * (b - 1) * (b - 1) - 2), l));
-      c02 = __fadd_rn(c02, __fmul_rn((float)(3 * (a - 1) * (a - 1) - 2), l));
+      const float lv = l[3 * a + b];
+      c10 = __fadd_rn(c10, __fmul_rn((float)(b - 1), lv));
+      c01 = __fadd_rn(c01, __fmul_rn((float)(a - 1), lv));
+      c11 = __fadd_rn(c11, __fmul_rn((float)((b - 1) * (a - 1)), lv));
+      c20 = __fadd_rn(c20, __fmul_rn((float)(3 * (b - 1) * (b - 1) - 2), lv));
+      c02 = __fadd_rn(c02, __fmul_rn((float)(3 * (a - 1) * (a - 1) - 2), lv));
     }
   c10 = __fdiv_rn(c10, 6.f);
   c01 = __fdiv_rn(c01, 6.f);
@@ -340,38 +342,44 @@ static __device__ bool gauss2_depl(const float (&c)[9], float* deplx_o, float* d
   return !(r2 > 4.5f);
 }
 
-// '2d_gaussian2' with the centroid fallback on a 3x3 crop (subpix.py:184-216).
-// Returns 0 or FI_VEC_WRONG_SUBPIX; (dx, dy) displacement.
-static __device__ int subpix_gaussian2_vals(const float (&c)[9], int i0, int i1, int ix0, int iy0,
-                                     float* dxo, float* dyo, bool* min_tie) {
-  float deplx, deply;
-  if (gauss2_depl(c, &deplx, &deply, min_tie)) {
-    *dxo = __fsub_rn((float)ix0, __fadd_rn(deplx, (float)i1));
-    *dyo = __fsub_rn((float)iy0, __fadd_rn(deply, (float)i0));
-    return FI_VEC_OK;
-  }
-  // centroid on the 3x3 crop (float32 sum, float64 moments)
-  float s = 0.f;
+// Both halves on one thread.  min_tie: two or more crop values at the minimum (the
+// 1e-8 floor then makes the fit depend on which of them rounds to exactly zero).
+static __device__ bool gauss2_depl(const float (&c)[9], float* deplx_o, float* deply_o,
+                                   bool* min_tie) {
+  float l[9];
+  int nlow = 0;
 #pragma unroll
-  for (int k = 0; k < 9; ++k) s = __fadd_rn(s, c[k]);
-  double mx = 0.0, my = 0.0;
+  for (int k = 0; k < 9; ++k) {
+    bool low;
+    l[k] = gauss2_log(c, k, &low);
+    nlow += low ? 1 : 0;
+  }
+  *min_tie = nlow >= 2;
+  return gauss2_fit(l, deplx_o, deply_o);
+}
+
+// The first half on threads 0..8 of a group of G threads (one crop element each):
+// the nine logs into lg[0..8] (shared memory, read by thread 0 after the call) and
+// the count of values at the minimum (returned on every thread).
+template <int G>
+__device__ __forceinline__ int gauss2_logs_group(const float* PL, int ld, int i0, int i1,
+                                                 const NanBox& cbox, int t, float* lg) {
+  float c[9];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      mx = __dadd_rn(mx, __dmul_rn((double)(b - 1), (double)c[3 * a + b]));
-      my = __dadd_rn(my, __dmul_rn((double)(a - 1), (double)c[3 * a + b]));
+      const int r = i0 - 1 + a, q = i1 - 1 + b;
+      c[3 * a + b] = cbox.has(r, q) ? NAN : PL[r * ld + q];
     }
-  const double cx = __ddiv_rn(mx, (double)s);
-  const double cy = __ddiv_rn(my, (double)s);
-  if (__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)) > 4.5) {
-    *dxo = (float)(ix0 - i1);
-    *dyo = (float)(iy0 - i0);
-    return FI_VEC_WRONG_SUBPIX;
-  }
-  *dxo = (float)__dsub_rn((double)ix0, __dadd_rn(cx, (double)i1));
-  *dyo = (float)__dsub_rn((double)iy0, __dadd_rn(cy, (double)i0));
-  return FI_VEC_OK;
+  bool low = false;
+  const float l = gauss2_log(c, t < 9 ? t : 0, &low);
+  if (t < 9) lg[t] = l;
+  const unsigned m = seg_mask<G>();
+  const unsigned base = (G == 16) ? (threadIdx.x & 16u) : 0u;
+  const unsigned bits = __ballot_sync(m, low && t < 9);
+  __syncwarp(m);  // threads 0..8 and thread 0 share a warp
+  return __popc((bits >> base) & 0x1FFu);
 }
 
 // Subpixel fit with any method (SubPix.compute_subpix, subpix.py:107-218) at the
@@ -389,9 +397,10 @@ struct SubpixOut {
 
 // want64: also the float64 displacement (dx64, dy64) of the '2d_gaussian2' fit and
 // of integer results (the other methods compute in float64 anyway).
+// logs9 / nlow9: the first half of '2d_gaussian2' computed by gauss2_logs_group.
 static __device__ int subpix_any(const float* PL, int ld, int N, int i0, int i1, int method, int nsub,
                           const double* minv, const NanBox& cbox, SubpixOut* o,
-                          bool want64 = false) {
+                          bool want64 = false, const float* logs9 = nullptr, int nlow9 = 0) {
   const int ix0 = N / 2 - 1, iy0 = N / 2 - 1;
   const int n = (method == FI_SUBPIX_GAUSSIAN2) ? 1 : nsub;
   o->tie = false;
@@ -416,13 +425,23 @@ static __device__ int subpix_any(const float* PL, int ld, int N, int i0, int i1,
   const double lim = 2.0 * (0.5 + n) * (0.5 + n);
   int m = method;
   if (m == FI_SUBPIX_GAUSSIAN2) {
-    float c[9];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) c[3 * a + b] = val(i0 - 1 + a, i1 - 1 + b);
     float deplx, deply;
-    if (gauss2_depl(c, &deplx, &deply, &o->tie)) {
+    bool fit;
+    if (logs9) {
+      float l[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) l[k] = logs9[k];
+      o->tie = nlow9 >= 2;
+      fit = gauss2_fit(l, &deplx, &deply);
+    } else {
+      float c[9];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) c[3 * a + b] = val(i0 - 1 + a, i1 - 1 + b);
+      fit = gauss2_depl(c, &deplx, &deply, &o->tie);
+    }
+    if (fit) {
       o->dx32 = __fsub_rn((float)ix0, __fadd_rn(deplx, (float)i1));
       o->dy32 = __fsub_rn((float)iy0, __fadd_rn(deply, (float)i0));
       if (want64) {
@@ -553,13 +572,21 @@ __device__ VecResult peak_and_subpix(const float* PL, const PeakArgs& pa, float 
   // upstream's caller plane holds the second-chance box unless the displacement
   // mask made the search work on a copy (CorrelFFTBase, correl.py:561-568)
   const NanBox cbox = (pa.mask == nullptr) ? r.nb : NanBox{0, 0, 0, 0};
-  if (fin.err == FI_VEC_OK && pa.apply_subpix && t == 0) {
-    SubpixOut sp;
-    r.err = subpix_any(PL, Cfg<N>::LDP, N, fin.i0, fin.i1, pa.subpix_method, pa.nsubpix,
-                       pa.minv, cbox, &sp);
-    r.subpix_tie = sp.tie;
-    r.dx = sp.dx32;
-    r.dy = sp.dy32;
+  if (fin.err == FI_VEC_OK && pa.apply_subpix) {
+    // '2d_gaussian2': the nine divisions and logs on nine threads (through the
+    // group's scratch, past the words the reductions use), the fit on one
+    float* lg = reinterpret_cast<float*>(red + 24);
+    const bool g2 = pa.subpix_method == FI_SUBPIX_GAUSSIAN2;
+    const int nlow = g2 ? gauss2_logs_group<Cfg<N>::G>(PL, Cfg<N>::LDP, fin.i0, fin.i1, cbox, t, lg)
+                        : 0;
+    if (t == 0) {
+      SubpixOut sp;
+      r.err = subpix_any(PL, Cfg<N>::LDP, N, fin.i0, fin.i1, pa.subpix_method, pa.nsubpix,
+                         pa.minv, cbox, &sp, false, g2 ? lg : nullptr, nlow);
+      r.subpix_tie = sp.tie;
+      r.dx = sp.dx32;
+      r.dy = sp.dy32;
+    }
   }
   // other peaks (correl.py:250-273): NaN box around the last peak, search again
   if (so != nullptr && pa.nb_peaks > 1) {
