@@ -17,13 +17,14 @@ works/preproc/_toolbox_py.py:
 * ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355);
 * ``sharpen`` (:472-490): scipy.ndimage's gaussian filters (float64 line sums in
   scipy's order, each axis cast to the image dtype) and the final combination;
-* ``rescale_intensity`` (:313-331) and ``gamma_correction`` (:441-470), which
-  upstream takes from scikit-image 0.24 (``exposure.rescale_intensity`` with
-  ``in_range='image'``, ``exposure.adjust_gamma``): their published elementwise
-  definitions, in the dtypes scikit-image and numpy 2 use.
+* ``rescale_intensity`` (:313-331), ``gamma_correction`` (:441-470) and
+  ``adaptive_threshold`` (:292-308), which upstream takes from scikit-image 0.24
+  (``exposure.rescale_intensity`` with ``in_range='image'``,
+  ``exposure.adjust_gamma``, ``filters.threshold_local`` with its gaussian method):
+  their published definitions, in the dtypes scikit-image and numpy 2 use.
 
-The other tools built on scikit-image (``adaptive_threshold``, ``equalize_hist_*``)
-keep their parameters but raise ``NotImplementedError`` when enabled.
+The histogram equalisations (``equalize_hist_*``), also built on scikit-image, keep
+their parameters but raise ``NotImplementedError`` when enabled.
 """
 
 from __future__ import annotations
@@ -403,6 +404,31 @@ def gaussian_filter(img, sigma):
     return out[0] if single else out
 
 
+def _as_float(x, ft):
+    """A device image as float32 / float64 (uint16 travels as int16 storage)."""
+    torch = _torch()
+    if x.dtype == torch.int16:
+        return (x.to(torch.int32) & 0xFFFF).to(ft)
+    return x.to(ft)
+
+
+@_per_image
+def adaptive_threshold(img, window_size=5, offset=0):
+    """The local threshold image of a gaussian-weighted neighbourhood
+    (_toolbox_py.py:292-308; scikit-image's filters.threshold_local with method
+    'gaussian'): the image as float64 (float32 images stay float32), scipy's
+    gaussian filter with sigma = (window_size - 1) / 6 and 'reflect' borders,
+    minus offset."""
+    torch = _torch()
+    if int(window_size) != window_size or int(window_size) % 2 == 0:
+        raise ValueError(f"block_size must be odd! Given block_size {window_size} is even.")
+    ft = torch.float32 if _dtype_of(img) == np.float32 else torch.float64
+    x = _as_float(img.contiguous(), ft)
+    sigma = (int(window_size) - 1) / 6.0
+    out = gaussian_filter(x, sigma) if sigma > 1e-15 else x.clone()
+    return out - offset
+
+
 @_per_image
 def sharpen(img, sigma1=3.0, sigma2=1.0, alpha=30.0):
     """_toolbox_py.py:472-490: two chained gaussian filters in the image dtype, then
@@ -440,6 +466,7 @@ TOOLS = {
     "rescale_intensity_tanh": rescale_intensity_tanh,
     "rescale_intensity": rescale_intensity,
     "gamma_correction": gamma_correction,
+    "adaptive_threshold": adaptive_threshold,
     "sharpen": sharpen,
 }
 for _name in AVAILABLE_TOOLS:

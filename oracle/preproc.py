@@ -6,13 +6,16 @@ sliding tools, global_threshold and rescale_intensity_tanh run image by image in
 a float64 stack; the temporal tools see the whole stack.  The arithmetic is
 numpy's (NEP 50 scalar promotion), the filters scipy.ndimage's.
 
-rescale_intensity and gamma_correction call scikit-image (0.24.0 in the reference's
-lock file), which is not installed here: they are restated from scikit-image's
-published definitions of ``exposure.rescale_intensity`` (in_range='image', a
-numeric out_range; output float64 for integer images, the float type otherwise)
-and ``exposure.adjust_gamma`` (uint8 through a 256-entry table, other dtypes
-scaled by the dtype's range, power law, cast back).  Parity for these two is
-unpinned: no scikit-image output exists here to record.
+rescale_intensity, gamma_correction and adaptive_threshold call scikit-image (0.24.0
+in the reference's lock file), which is not installed here: they are restated from
+scikit-image's published definitions of ``exposure.rescale_intensity``
+(in_range='image', a numeric out_range; output float64 for integer images, the
+float type otherwise), ``exposure.adjust_gamma`` (uint8 through a 256-entry table,
+other dtypes scaled by the dtype's range, power law, cast back) and
+``filters.threshold_local`` with method 'gaussian' (scipy's gaussian filter of the
+float image, sigma = (block_size - 1) / 6, 'reflect', minus the offset).  Parity for
+these three is unpinned: no scikit-image output exists here to record (the
+gaussian filter itself is scipy's).
 """
 
 from __future__ import annotations
@@ -164,3 +167,19 @@ def gamma_correction(img, gamma=1.0, gain=1.0, with_raw=False):
 
     out = _per_image(one, img)
     return (out, raws) if with_raw else out
+
+
+def adaptive_threshold(img, window_size=5, offset=0):
+    """_toolbox_py.py:292-308 (skimage.filters.threshold_local(img, window_size,
+    offset=offset), method 'gaussian')."""
+    if int(window_size) % 2 == 0:
+        raise ValueError("block_size must be odd")
+
+    def one(im):
+        ft = np.float32 if im.dtype == np.float32 else np.float64
+        x = im.astype(ft, copy=False)
+        out = np.zeros(x.shape, dtype=ft)
+        ndi.gaussian_filter(x, (window_size - 1) / 6.0, output=out, mode="reflect", cval=0)
+        return out - offset
+
+    return _per_image(one, img)

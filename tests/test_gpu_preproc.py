@@ -142,3 +142,21 @@ def test_gamma_correction_rejects_negative_float_images():
     img[3, 4] = -1.0
     with pytest.raises(ValueError):
         P.gamma_correction(P.to_device(img), 0.7)
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32"])
+@pytest.mark.parametrize("window_offset", [(5, 0), (11, 3), (31, -2.5), (1, 1)])
+def test_adaptive_threshold_matches_scipy(image, window_offset):
+    """adaptive_threshold: scipy's gaussian filter of the float image (float64 line
+    sums, the float type after each axis), so equal to the oracle bit for bit."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    ws, off = window_offset
+    img = Z["img_" + image]
+    got = P.to_host(P.adaptive_threshold(P.to_device(img[0]), ws, off))
+    want = O.adaptive_threshold(img[0].copy(), ws, off)
+    assert got.dtype == want.dtype
+    np.testing.assert_array_equal(got, want)
+    stack = P.to_host(P.adaptive_threshold(P.to_device(img), ws, off))
+    np.testing.assert_array_equal(stack, O.adaptive_threshold(img.copy(), ws, off))

@@ -62,3 +62,16 @@ def test_gamma_correction_known_answers():
         O.gamma_correction(np.array([[-1.0]], np.float32))
     with pytest.raises(ValueError):
         O.gamma_correction(u8, -1.0)
+
+
+def test_adaptive_threshold_definition():
+    """threshold_local's gaussian method: a constant image is its own threshold (minus
+    the offset); the weights sum to one; even windows are rejected."""
+    flat = np.full((9, 11), 7, np.uint16)
+    got = O.adaptive_threshold(flat, 5, 2)
+    assert got.dtype == np.float64
+    np.testing.assert_allclose(got, 5.0, rtol=0, atol=1e-12)
+    f = np.full((9, 11), 3.0, np.float32)
+    assert O.adaptive_threshold(f, 7, 0).dtype == np.float32
+    with pytest.raises(ValueError):
+        O.adaptive_threshold(flat, 4)
