@@ -753,11 +753,12 @@ def refinement_workload(args, dev, pairs=8, steps=20):
     txn, tyn = torch.as_tensor(xn, device=dev), torch.as_tensor(yn, device=dev)
     params = workloads.config2_params(WorkPIV.create_default_params())
     work = WorkPIV(params, device=dev)
+    work_deform = WorkPIV(params, device=dev, deform=True)
 
-    def plain():
+    def plain(w=work):
         nodes = []
         for k in range(pairs):
-            outs = work.calcul_device(t0[k], t1[k])
+            outs = w.calcul_device(t0[k], t1[k])
             fin = outs[-1].tps_final
             lay = outs[-1].layout
             fx = fin.out_x.view(lay.iyvecs.size, lay.ixvecs.size)[1::4, 1::4]
@@ -767,28 +768,43 @@ def refinement_workload(args, dev, pairs=8, steps=20):
 
     for _ in range(max(1, args.warmup)):
         nodes0 = plain()
+        plain(work_deform)
         deform.refine(nodes0, t0, t1, txn, tyn, steps=2)
     torch.cuda.synchronize()
-    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    e[0].record()
-    nodes0 = plain()
-    e[1].record()
-    nodes1 = deform.refine(nodes0, t0, t1, txn, tyn, steps=steps, lr=0.05)
-    e[2].record()
-    torch.cuda.synchronize()
+
+    def timed(f):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = f()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
     inner = (slice(None), slice(None), slice(2, -2), slice(2, -2))
 
     def rms(n):
         return float(((n - truth)[inner] ** 2).sum(dim=1).mean().sqrt())
 
+    nodes0, ms_plain = timed(plain)
+    nodes_d, ms_deform = timed(lambda: plain(work_deform))
+    frontier = [{"form": "3-pass window shift", "ms": ms_plain, "rms_px": rms(nodes0)},
+                {"form": "3-pass deformation (central)", "ms": ms_deform, "rms_px": rms(nodes_d)}]
+    refined = {}
+    for k in sorted({5, 10, steps}):
+        nodes_k, ms_k = timed(lambda: deform.refine(nodes0, t0, t1, txn, tyn, steps=k, lr=0.05))
+        refined[k] = (nodes_k, ms_k)
+        frontier.append({"form": f"3-pass window shift + {k} Adam steps", "ms": ms_plain + ms_k,
+                         "rms_px": rms(nodes_k)})
     return {
         "workload": f"{pairs} pairs 2048x2048 float32 (uint16 12-bit particles), Oseen + "
                     "sinusoid field of peak 7 px; nodes 64x64x2 per pair at the 32 px window "
                     "centres; loss mean |soft-argmax residual|^2 of the 32 px windows, T 0.1",
-        "plain_3pass_ms": e[0].elapsed_time(e[1]),
-        "refine_ms": e[1].elapsed_time(e[2]), "adam_steps": steps,
-        "rms_error_px": {"plain_3pass": rms(nodes0), "refined": rms(nodes1)},
-        "error_note": "vector error |d - truth| at the inner nodes (2-node margin)",
+        "plain_3pass_ms": ms_plain,
+        "refine_ms": refined[steps][1], "adam_steps": steps,
+        "rms_error_px": {"plain_3pass": rms(nodes0), "refined": rms(refined[steps][0])},
+        "time_vs_error": frontier,
+        "error_note": "vector error |d - truth| at the inner nodes (2-node margin); times are "
+                      "device times of all 8 pairs (CUDA events)",
     }
 
 
