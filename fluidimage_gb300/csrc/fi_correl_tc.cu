@@ -54,28 +54,16 @@ constexpr int OFF_B1 = 0;
 constexpr int OFF_B2 = OFF_B1 + 2 * B1_BYTES;
 constexpr int OFF_B4 = OFF_B2 + 2 * B2_BYTES;
 constexpr int OFF_A = OFF_B4 + 2 * B4_BYTES;  // stage operands, then the planes
-constexpr int A_BYTES = 64 * 1024 + 2048;  // + the top of the prefetch region
+constexpr int A_BYTES = 64 * 1024;
 constexpr int OFF_X = OFF_A + A_BYTES;         // kx' = 0 rows exchanged between warps
 constexpr int X_BYTES = WIN * 2 * 64 * 4;
 constexpr int OFF_W = OFF_X + X_BYTES;         // per-window scalars
 constexpr int W_BYTES = WIN * 64;
 constexpr int OFF_RED = OFF_W + W_BYTES;       // per-window peak-search scratch
 constexpr int RED_BYTES = WIN * 256;
-constexpr int OFF_POS = OFF_RED + RED_BYTES;   // the next tile's window positions
-constexpr int POS_BYTES = WIN * 48;
-constexpr int OFF_BAR = OFF_POS + POS_BYTES;   // mbarrier, TMEM base
+constexpr int OFF_BAR = OFF_RED + RED_BYTES;   // mbarrier, TMEM base
 constexpr int SMEM = OFF_BAR + 64;
 static_assert(WIN * N * LDP * 4 <= A_BYTES, "planes must fit the operand region");
-// The next tile's window rows are copied (cp.async, 16 bytes per instruction) into
-// the operand region above the planes while the current tile's stages 3-4 and peak
-// search run: [window][image][row] x 64 bytes.  Stage 3 and 4 operands and the planes
-// stay below PF_OFF; the region is free once stage 2's MMAs have completed.
-constexpr int PF_OFF = 34816;
-constexpr int PF_ROW = 64;
-constexpr int A34_BYTES = 2 * 128 * 64 * 2;  // A3 (two parts) or A4 (two tiles, two parts)
-static_assert(WIN * N * LDP * 4 <= PF_OFF && A34_BYTES <= PF_OFF, "prefetch overlap");
-static_assert(PF_OFF + WIN * 2 * N * PF_ROW <= A_BYTES, "prefetch region");
-static_assert(PF_OFF % 16 == 0, "cp.async alignment");
 
 // operand sub-regions of the A region
 constexpr int A1_PART = 128 * 32 * 2;  // [img][tile][part]: 128 rows x K 32
@@ -99,14 +87,6 @@ struct TcWin {
   int dinx, diny;   // input shift (passes >= 1)
 };
 static_assert(sizeof(TcWin) <= 64, "per-window scalars");
-
-// Window positions of a window of the next tile, kept in shared memory.
-struct TcPos {
-  int y0, x0, y1, x1;
-  int sx, sy, dinx, diny;
-  int valid;
-};
-static_assert(sizeof(TcPos) <= 48, "positions");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -365,56 +345,6 @@ __device__ __forceinline__ void load_row_f32(const float* im, int H, int W, int 
   }
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-}
-
-// Source of a window row that cp.async can copy (an integer image, the row inside
-// the image, 16-byte aligned), else nullptr; bytes: 64 (u16) or 32 (u8).
-__device__ __forceinline__ const unsigned char* pf_src(const fi_piv_pass_args& a, const void* im,
-                                                       int y, int x0) {
-  if (a.dtype == FI_F32 || y < 0 || y >= a.height || x0 < 0 || x0 + N > a.width) return nullptr;
-  const size_t esz = (a.dtype == FI_U16) ? 2 : 1;
-  const unsigned char* p =
-      reinterpret_cast<const unsigned char*>(im) + ((size_t)y * a.width + x0) * esz;
-  return (reinterpret_cast<uintptr_t>(p) & 15) ? nullptr : p;
-}
-
-// The 32 pixels of a copied row, minus the image minimum.
-__device__ __forceinline__ void unpack_row(const unsigned char* row, bool u16, int mini,
-                                           int (&v)[N]) {
-  const uint4* q = reinterpret_cast<const uint4*>(row);
-  if (u16) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint4 u = q[k];
-      const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        v[8 * k + 2 * i] = (int)(w4[i] & 0xffffu) - mini;
-        v[8 * k + 2 * i + 1] = (int)(w4[i] >> 16) - mini;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const uint4 u = q[k];
-      const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) v[16 * k + 4 * i + b] = (int)((w4[i] >> (8 * b)) & 0xffu) - mini;
-    }
-  }
-}
-
 template <int FORM>
 __global__ void __launch_bounds__(THREADS, 2)
     k_piv_pass_tc(const fi_piv_pass_args a, int nvec, int npad, int ntiles, float tie_rel,
@@ -451,8 +381,7 @@ __global__ void __launch_bounds__(THREADS, 2)
   const bool intpath = a.dtype != FI_F32;
 
   // one stage: operands written -> MMAs issued by thread 0 -> bounded wait
-  // (`during` runs on every thread while the MMAs execute)
-  auto run_stage = [&](auto issue, auto during) -> bool {
+  auto run_stage = [&](auto issue) -> bool {
     fence_async_smem();
     fence_before();
     __syncthreads();
@@ -461,7 +390,6 @@ __global__ void __launch_bounds__(THREADS, 2)
       issue();
       mma_commit(bar);
     }
-    during();
     const bool ok = mbar_wait(bar, phase);
     phase ^= 1u;
     if (__syncthreads_or(!ok)) return false;
@@ -482,31 +410,19 @@ __global__ void __launch_bounds__(THREADS, 2)
   };
   const uint32_t sA_u = smem_u32(sA), sB1 = smem_u32(sm + OFF_B1), sB2 = smem_u32(sm + OFF_B2),
                  sB4 = smem_u32(sm + OFF_B4);
-  TcPos* npos = reinterpret_cast<TcPos*>(sm + OFF_POS);
-  unsigned char* pf = sA + PF_OFF;
-  const bool u16 = a.dtype == FI_U16;
-  const auto nothing = [] {};
   bool ok = true;
-  bool have_pf = false;  // this tile's positions and rows were fetched during the last one
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int vec = tile * WIN + warp;  // this warp's window
     const bool active = vec < nvec;
     // ---------------- stage the two windows (warp = window, lane = row) ----------------
     {
-      TcPos wp;
-      wp.valid = 0;
-      if (have_pf) {
-        wp = npos[warp];
-      } else if (active) {
-        const WinPos w = window_positions<N>(a, vec, npad);
-        wp = TcPos{w.y0, w.x0, w.y1, w.x1, w.ixs0 + w.ixs1, w.iys0 + w.iys1, w.dinx, w.diny,
-                   w.valid ? 1 : 0};
-      }
+      WinPos wp;
+      if (active) wp = window_positions<N>(a, vec, npad);
       const bool load = active && wp.valid;
-      if (lane == 0) {
+      if (lane == 0) {  // the vector position and input shift, for the outputs
         TcWin* W = wins + warp;
-        W->sx = wp.sx;
-        W->sy = wp.sy;
+        W->sx = wp.ixs0 + wp.ixs1;
+        W->sy = wp.iys0 + wp.iys1;
         W->dinx = wp.dinx;
         W->diny = wp.diny;
       }
@@ -516,18 +432,9 @@ __global__ void __launch_bounds__(THREADS, 2)
       float mm[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
       if (intpath) {
         int v0[32], v1[32];
-        if (have_pf) cp_async_wait_all();  // this thread's copies have landed
         if (load) {
-          const unsigned char* c0 = have_pf ? pf_src(a, a.im0, wp.y0 + lane, wp.x0) : nullptr;
-          const unsigned char* c1 = have_pf ? pf_src(a, a.im1, wp.y1 + lane, wp.x1) : nullptr;
-          if (c0)
-            unpack_row(pf + ((warp * 2 + 0) * N + lane) * PF_ROW, u16, (int)min0, v0);
-          else
-            load_row_int(a.im0, a.dtype, a.height, a.width, wp.y0 + lane, wp.x0, (int)min0, v0);
-          if (c1)
-            unpack_row(pf + ((warp * 2 + 1) * N + lane) * PF_ROW, u16, (int)min1, v1);
-          else
-            load_row_int(a.im1, a.dtype, a.height, a.width, wp.y1 + lane, wp.x1, (int)min1, v1);
+          load_row_int(a.im0, a.dtype, a.height, a.width, wp.y0 + lane, wp.x0, (int)min0, v0);
+          load_row_int(a.im1, a.dtype, a.height, a.width, wp.y1 + lane, wp.x1, (int)min1, v1);
         } else {
 #pragma unroll
           for (int i = 0; i < 32; ++i) v0[i] = v1[i] = 0;
@@ -618,11 +525,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         tw.outscale = ldexpf(1.0f, e0 + e1 + SCALE_P + SCALE_Q - 10);
         tw.valid = load ? 1 : 0;
       }
-      // the operands below overwrite the copied rows of the other warps
-      if (have_pf)
-        __syncthreads();
-      else
-        __syncwarp();
+      __syncwarp();
       const float s0 = pow2f(-wins[warp].e0), s1 = pow2f(-wins[warp].e1);
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
@@ -645,7 +548,7 @@ __global__ void __launch_bounds__(THREADS, 2)
           for (int ks = 0; ks < 2; ++ks)
             mma_terms(tmem + 64 * t + 32 * img, sA_u + ((img * 2 + t) * 2) * A1_PART + ks * 256,
                       A1_PART, 128, 512, sB1 + ks * 256, B1_BYTES, 128, 512, id, ks == 0);
-    }, nothing);
+    });
     if (!ok) break;
     // ---------------- epilogue 1: DC removal, pack kx = 0 and 16, operand of stage 2 ----
     {
@@ -684,7 +587,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         for (int ks = 0; ks < 4; ++ks)
           mma_terms(tmem + 128 + 64 * img, sA_u + (img * 2) * A2_PART + ks * 4096, A2_PART, 2048,
                     128, sB2 + ks * 256, B2_BYTES, 128, 1024, id, ks == 0);
-    }, nothing);
+    });
     if (!ok) break;
     // ---------------- epilogue 2: cross spectrum P = conj(F0) F1 ----------------
     {
@@ -754,41 +657,12 @@ __global__ void __launch_bounds__(THREADS, 2)
       }
     }
     // ---------------- stage 3: Q = inverse DFT over ky ----------------
-    // (meanwhile: the next tile's window positions and rows, into the region above
-    // the stage 3-4 operands, which stage 2's completed MMAs no longer read)
-    const bool pf_next = tile + (int)gridDim.x < ntiles;
-    ok = run_stage(
-        [&] {
-          const uint32_t id = idesc(F16, false, 64);
-          for (int ks = 0; ks < 4; ++ks)
-            mma_terms(tmem, sA_u + ks * 256, A3_PART, 128, 1024, sB2 + ks * 256, B2_BYTES, 128,
-                      1024, id, ks == 0);
-        },
-        [&] {
-          if (!pf_next) return;
-          const int vn = (tile + (int)gridDim.x) * WIN + warp;
-          TcPos q;
-          q.valid = 0;
-          if (vn < nvec) {
-            const WinPos w = window_positions<N>(a, vn, npad);
-            q = TcPos{w.y0, w.x0, w.y1, w.x1, w.ixs0 + w.ixs1, w.iys0 + w.iys1, w.dinx, w.diny,
-                      w.valid ? 1 : 0};
-          }
-          if (q.valid) {
-            const int nb = u16 ? 64 : 32;
-            const unsigned char* c0 = pf_src(a, a.im0, q.y0 + lane, q.x0);
-            const unsigned char* c1 = pf_src(a, a.im1, q.y1 + lane, q.x1);
-            unsigned char* d0 = pf + ((warp * 2 + 0) * N + lane) * PF_ROW;
-            unsigned char* d1 = pf + ((warp * 2 + 1) * N + lane) * PF_ROW;
-            for (int k = 0; k < nb; k += 16) {
-              if (c0) cp_async16(d0 + k, c0 + k);
-              if (c1) cp_async16(d1 + k, c1 + k);
-            }
-          }
-          cp_async_commit();
-          if (lane == 0) npos[warp] = q;
-        });
-    have_pf = pf_next;
+    ok = run_stage([&] {
+      const uint32_t id = idesc(F16, false, 64);
+      for (int ks = 0; ks < 4; ++ks)
+        mma_terms(tmem, sA_u + ks * 256, A3_PART, 128, 1024, sB2 + ks * 256, B2_BYTES, 128, 1024,
+                  id, ks == 0);
+    });
     if (!ok) break;
     // ---------------- epilogue 3: operand of the real inverse over kx ----------------
     {
@@ -815,7 +689,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         for (int ks = 0; ks < 2; ++ks)
           mma_terms(tmem + 128 + 32 * t, sA_u + (t * 2) * A4_PART + ks * 4096, A4_PART, 2048, 128,
                     sB4 + ks * 256, B4_BYTES, 128, 512, id, ks == 0);
-    }, nothing);
+    });
     if (!ok) break;
     // ---------------- epilogue 4: the plane, peak search, subpixel fit ----------------
     {
@@ -887,7 +761,6 @@ __global__ void __launch_bounds__(THREADS, 2)
     }
   }
   if (!ok && tid == 0 && status) atomicOr(status, 1);
-  cp_async_wait_all();  // no copy lands after the CTA ends
   fence_before();
   __syncthreads();
   fence_after();
