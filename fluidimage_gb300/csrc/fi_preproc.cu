@@ -540,6 +540,146 @@ __global__ void k_gamma(const void* in, int dtype, int64_t count, double gamma, 
   }
 }
 
+// ---------------------------------------------------------- histogram equalisation
+// equalize_hist_global = skimage.exposure.equalize_hist (scikit-image 0.24): the
+// cumulative distribution of the image's histogram, interpolated at every pixel.
+// Integer images: one bin per integer value (the histogram of the raw values; the
+// bins below the minimum are empty, so the cumulative sums equal those from the
+// minimum), out = cdf[x] exactly (np.interp at its nodes).  Float images: numpy's
+// uniform histogram of nbins bins over [min, max] — bin index
+// ((x - first) / denom) * nbins truncated, then moved by one where x lies below its
+// bin's left edge or at or above the next edge (the last bin is closed) — in the
+// image's float type, with the edges computed by the caller exactly as numpy does.
+__global__ void k_hist_int(const void* in, int dtype, int64_t count, unsigned* hist) {
+  __shared__ unsigned sh[256];
+  const bool u8 = dtype == FI_PRE_U8;
+  if (u8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = 0u;
+    __syncthreads();
+  }
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (u8)
+      atomicAdd(&sh[static_cast<const uint8_t*>(in)[e]], 1u);
+    else
+      atomicAdd(&hist[static_cast<const uint16_t*>(in)[e]], 1u);
+  }
+  if (u8) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ int np_bin(T x, const T* edges, int nbins, T first, T denom) {
+  T f;
+  if constexpr (sizeof(T) == 4)
+    f = __fmul_rn(__fdiv_rn(__fsub_rn(x, first), denom), (float)nbins);
+  else
+    f = __dmul_rn(__ddiv_rn(__dsub_rn(x, first), denom), (double)nbins);
+  int i = (int)f;
+  if (i == nbins) --i;
+  if (x < edges[i]) --i;
+  if (i != nbins - 1 && x >= edges[i + 1]) ++i;
+  return i;
+}
+
+// edges: nbins + 1 values in the image's float type (float32 images: float
+// values stored as float), first / denom likewise (as doubles, exact).
+__global__ void k_hist_float(const void* in, int dtype, int64_t count, const void* edges,
+                             int nbins, double first, double denom, unsigned* hist) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int i;
+    if (dtype == FI_PRE_F32) {
+      const float x = static_cast<const float*>(in)[e];
+      i = np_bin<float>(x, static_cast<const float*>(edges), nbins, (float)first, (float)denom);
+    } else {
+      const double x = static_cast<const double*>(in)[e];
+      i = np_bin<double>(x, static_cast<const double*>(edges), nbins, first, denom);
+    }
+    atomicAdd(&hist[i], 1u);
+  }
+}
+
+// One block: cdf[i] = (sum of hist[0..i]) / total (float64), rounded to float32
+// and back when round32 (the cdf of float32 images).
+__global__ void k_cdf(const unsigned* hist, int nbins, int round32, double* cdf) {
+  __shared__ unsigned long long part[1024];
+  const int per = (nbins + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  unsigned long long s = 0;
+  for (int i = b0; i < b0 + per && i < nbins; ++i) s += hist[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  // inclusive scan of the per-thread sums (Hillis-Steele over the block)
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    const unsigned long long v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0ull;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const double total = (double)part[blockDim.x - 1];
+  unsigned long long run = threadIdx.x ? part[threadIdx.x - 1] : 0ull;
+  for (int i = b0; i < b0 + per && i < nbins; ++i) {
+    run += hist[i];
+    const double c = __ddiv_rn((double)run, total);
+    cdf[i] = round32 ? (double)(float)c : c;
+  }
+}
+
+// Integer images: out = cdf[x] (float64).
+__global__ void k_equalize_int(const void* in, int dtype, int64_t count, const double* cdf,
+                               double* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int v = dtype == FI_PRE_U8 ? (int)static_cast<const uint8_t*>(in)[e]
+                                     : (int)static_cast<const uint16_t*>(in)[e];
+    out[e] = cdf[v];
+  }
+}
+
+// np.interp(x, xp, fp) in float64 (xp increasing, n >= 1): fp[0] below xp[0],
+// fp[n-1] from xp[n-1] on, the node value at a node, else the slope form
+// slope (x - xp[j]) + fp[j] without contraction (then from the right node if NaN).
+// Output in the image's float type.
+__global__ void k_interp(const void* in, int dtype, int64_t count, const double* xp,
+                         const double* fp, int n, void* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double x = load_d(in, dtype, e);
+    double r;
+    if (x > xp[n - 1] || x == xp[n - 1]) {
+      r = fp[n - 1];
+    } else if (x < xp[0]) {
+      r = fp[0];
+    } else if (x != x) {
+      r = x;
+    } else {
+      int lo = 0, hi = n - 1;  // xp[lo] <= x < xp[hi]
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (xp[mid] <= x) lo = mid; else hi = mid;
+      }
+      if (xp[lo] == x) {
+        r = fp[lo];
+      } else {
+        const double slope = __ddiv_rn(__dsub_rn(fp[lo + 1], fp[lo]), __dsub_rn(xp[lo + 1], xp[lo]));
+        r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[lo])), fp[lo]);
+        if (r != r) {
+          r = __dadd_rn(__dmul_rn(slope, __dsub_rn(x, xp[lo + 1])), fp[lo + 1]);
+          if (r != r && fp[lo] == fp[lo + 1]) r = fp[lo];
+        }
+      }
+    }
+    if (dtype == FI_PRE_F32)
+      static_cast<float*>(out)[e] = (float)r;
+    else
+      static_cast<double*>(out)[e] = r;
+  }
+}
+
 static int grid_for(int64_t count) {
   const int64_t b = (count + 255) / 256;
   return (int)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
@@ -701,4 +841,34 @@ extern "C" int fi_gamma(const void* in, int dtype, int64_t count, double gamma, 
   k_gamma<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, gamma, gain, lut,
                                                             out);
   return check_launch("fi_gamma");
+}
+
+extern "C" int fi_equalize_hist_int(const void* in, int dtype, int64_t count, unsigned* hist,
+                                    double* cdf, double* out, void* stream) {
+  FI_REQUIRE(in && hist && cdf && out && count > 0, "fi_equalize_hist_int: bad arguments");
+  FI_REQUIRE(dtype == FI_PRE_U8 || dtype == FI_PRE_U16, "fi_equalize_hist_int: bad dtype %d",
+             dtype);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nbins = dtype == FI_PRE_U8 ? 256 : 65536;
+  FI_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * nbins, s));
+  k_hist_int<<<grid_for(count), 256, 0, s>>>(in, dtype, count, hist);
+  k_cdf<<<1, 1024, 0, s>>>(hist, nbins, 0, cdf);
+  k_equalize_int<<<grid_for(count), 256, 0, s>>>(in, dtype, count, cdf, out);
+  return check_launch("fi_equalize_hist_int", 3);
+}
+
+extern "C" int fi_equalize_hist_float(const void* in, int dtype, int64_t count, const void* edges,
+                                      int nbins, double first, double denom,
+                                      const double* centers, unsigned* hist, double* cdf,
+                                      void* out, void* stream) {
+  FI_REQUIRE(in && edges && centers && hist && cdf && out && count > 0 && nbins > 0,
+             "fi_equalize_hist_float: bad arguments");
+  FI_REQUIRE(dtype == FI_PRE_F32 || dtype == FI_PRE_F64, "fi_equalize_hist_float: bad dtype %d",
+             dtype);
+  cudaStream_t s = (cudaStream_t)stream;
+  FI_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * nbins, s));
+  k_hist_float<<<grid_for(count), 256, 0, s>>>(in, dtype, count, edges, nbins, first, denom, hist);
+  k_cdf<<<1, 1024, 0, s>>>(hist, nbins, dtype == FI_PRE_F32 ? 1 : 0, cdf);
+  k_interp<<<grid_for(count), 256, 0, s>>>(in, dtype, count, centers, cdf, nbins, out);
+  return check_launch("fi_equalize_hist_float", 3);
 }

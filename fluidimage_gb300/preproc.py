@@ -17,14 +17,16 @@ works/preproc/_toolbox_py.py:
 * ``global_threshold`` (:265-289) and ``rescale_intensity_tanh`` (:332-355);
 * ``sharpen`` (:472-490): scipy.ndimage's gaussian filters (float64 line sums in
   scipy's order, each axis cast to the image dtype) and the final combination;
-* ``rescale_intensity`` (:313-331), ``gamma_correction`` (:441-470) and
-  ``adaptive_threshold`` (:292-308), which upstream takes from scikit-image 0.24
-  (``exposure.rescale_intensity`` with ``in_range='image'``,
-  ``exposure.adjust_gamma``, ``filters.threshold_local`` with its gaussian method):
-  their published definitions, in the dtypes scikit-image and numpy 2 use.
+* ``rescale_intensity`` (:313-331), ``gamma_correction`` (:441-470),
+  ``adaptive_threshold`` (:292-308) and ``equalize_hist_global`` (:357-379), which
+  upstream takes from scikit-image 0.24 (``exposure.rescale_intensity`` with
+  ``in_range='image'``, ``exposure.adjust_gamma``, ``filters.threshold_local`` with
+  its gaussian method, ``exposure.equalize_hist``): their published definitions, in
+  the dtypes scikit-image and numpy 2 use.
 
-The histogram equalisations (``equalize_hist_*``), also built on scikit-image, keep
-their parameters but raise ``NotImplementedError`` when enabled.
+The adaptive equalisations (``equalize_hist_adapt``, CLAHE, and ``equalize_hist_local``,
+a rank filter over a disk), also built on scikit-image, keep their parameters but
+raise ``NotImplementedError`` when enabled.
 """
 
 from __future__ import annotations
@@ -376,6 +378,61 @@ def gamma_correction(img, gamma=1.0, gain=1.0):
     return out
 
 
+def histogram_edges(vmin, vmax, nbins, dtype):
+    """The outer edges, the bin edges and the range of numpy's uniform histogram
+    (``np.histogram(a, bins=nbins)`` with the range taken from the data) of an
+    array of float ``dtype`` with extremes vmin, vmax: computed on numpy scalars of
+    that type, as numpy does."""
+    dt = np.dtype(dtype).type
+    first, last = dt(vmin), dt(vmax)
+    if not (np.isfinite(first) and np.isfinite(last)):
+        raise ValueError(f"autodetected range of [{first}, {last}] is not finite")
+    if first == last:
+        first = first - 0.5
+        last = last + 0.5
+    bin_type = np.result_type(first, last, np.dtype(dtype))
+    edges = np.linspace(first, last, nbins + 1, endpoint=True, dtype=bin_type)
+    denom = np.subtract(last, first, dtype=bin_type)
+    return first, edges, denom
+
+
+@_per_image
+def equalize_hist_global(img, nbins=256):
+    """Histogram equalisation (_toolbox_py.py:357-379; scikit-image's
+    exposure.equalize_hist): the cumulative distribution of the image's histogram
+    (one bin per integer value for integer images, ``nbins`` uniform bins for float
+    images) interpolated at every pixel; float64 (float32 for float32 images)."""
+    torch = _torch()
+    lib = L.load()
+    x = img.contiguous()
+    dtype = _dtype_of(x)
+    dev = x.device
+    s = L.stream_handle()
+    if dtype.kind in "ui":
+        nb = 256 if dtype == np.uint8 else 65536
+        hist = torch.empty(nb, dtype=torch.int32, device=dev)
+        cdf = torch.empty(nb, dtype=torch.float64, device=dev)
+        out = torch.empty(tuple(x.shape), dtype=torch.float64, device=dev)
+        L.check(lib.fi_equalize_hist_int(L.ptr(x), _DT[dtype], x.numel(), L.ptr(hist), L.ptr(cdf),
+                                         L.ptr(out), s), "fi_equalize_hist_int")
+        return out
+    part = _extremes(x).cpu().numpy()
+    vmin, vmax = part[:_NPARTS].min(), part[_NPARTS:].max()
+    if np.isnan(part).any():
+        vmin = vmax = np.nan
+    first, edges, denom = histogram_edges(vmin, vmax, int(nbins), dtype)
+    centers = ((edges[:-1] + edges[1:]) / 2.0).astype(np.float64)
+    d_edges = torch.as_tensor(edges, device=dev)
+    d_centers = torch.as_tensor(centers, device=dev)
+    hist = torch.empty(int(nbins), dtype=torch.int32, device=dev)
+    cdf = torch.empty(int(nbins), dtype=torch.float64, device=dev)
+    out = _empty(tuple(x.shape), dtype, dev)
+    L.check(lib.fi_equalize_hist_float(L.ptr(x), _DT[dtype], x.numel(), L.ptr(d_edges), int(nbins),
+                                       float(first), float(denom), L.ptr(d_centers), L.ptr(hist),
+                                       L.ptr(cdf), L.ptr(out), s), "fi_equalize_hist_float")
+    return out
+
+
 def _gauss_weights(sigma, truncate=4.0):
     """scipy.ndimage's ``_gaussian_kernel1d`` (order 0, ndimage/_filters.py), reversed
     for the correlation as ``gaussian_filter1d`` does, and its radius."""
@@ -467,6 +524,7 @@ TOOLS = {
     "rescale_intensity": rescale_intensity,
     "gamma_correction": gamma_correction,
     "adaptive_threshold": adaptive_threshold,
+    "equalize_hist_global": equalize_hist_global,
     "sharpen": sharpen,
 }
 for _name in AVAILABLE_TOOLS:

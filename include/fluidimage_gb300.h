@@ -646,6 +646,26 @@ int fi_gamma(const void* in, int dtype, int64_t count, double gamma, double gain
              const uint8_t* lut, void* out, void* stream);
 
 /*
+ * equalize_hist_global (_toolbox_py.py:357-379, skimage.exposure.equalize_hist of
+ * scikit-image 0.24) of integer images: the histogram of the raw values (hist:
+ * 256 / 65536 uint32 scratch), cdf (same length, float64) = cumulative counts /
+ * pixels, out (float64) = cdf[x].
+ */
+int fi_equalize_hist_int(const void* in, int dtype, int64_t count, unsigned* hist, double* cdf,
+                         double* out, void* stream);
+
+/*
+ * equalize_hist_global of float images: numpy's uniform histogram of nbins bins
+ * (edges: nbins + 1 values in the image's float type, first = edges[0], denom =
+ * the range, both exactly as numpy computes them), the cumulative distribution
+ * (float32 for float32 images), and np.interp of the pixels at the bin centres
+ * (centers: nbins float64), out in the image's float type.
+ */
+int fi_equalize_hist_float(const void* in, int dtype, int64_t count, const void* edges, int nbins,
+                           double first, double denom, const double* centers, unsigned* hist,
+                           double* cdf, void* out, void* stream);
+
+/*
  * scipy.ndimage.gaussian_filter of each image of a (nt, ny, nx) stack (axis y then x;
  * the call of sharpen, _toolbox_py.py:486-487): one symmetric 1-D correlation per
  * axis in float64 ('reflect' boundaries; out = w_0 x_0, then the tap pairs from the

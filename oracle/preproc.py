@@ -6,15 +6,18 @@ sliding tools, global_threshold and rescale_intensity_tanh run image by image in
 a float64 stack; the temporal tools see the whole stack.  The arithmetic is
 numpy's (NEP 50 scalar promotion), the filters scipy.ndimage's.
 
-rescale_intensity, gamma_correction and adaptive_threshold call scikit-image (0.24.0
-in the reference's lock file), which is not installed here: they are restated from
-scikit-image's published definitions of ``exposure.rescale_intensity``
+rescale_intensity, gamma_correction, adaptive_threshold and equalize_hist_global call
+scikit-image (0.24.0 in the reference's lock file), which is not installed here: they
+are restated from scikit-image's published definitions of ``exposure.equalize_hist``
+(one histogram bin per integer value for integer images, numpy's uniform histogram
+of nbins bins otherwise; np.interp of the cumulative distribution at the bin
+centres), ``exposure.rescale_intensity``
 (in_range='image', a numeric out_range; output float64 for integer images, the
 float type otherwise), ``exposure.adjust_gamma`` (uint8 through a 256-entry table,
 other dtypes scaled by the dtype's range, power law, cast back) and
 ``filters.threshold_local`` with method 'gaussian' (scipy's gaussian filter of the
 float image, sigma = (block_size - 1) / 6, 'reflect', minus the offset).  Parity for
-these three is unpinned: no scikit-image output exists here to record (the
+these four is unpinned: no scikit-image output exists here to record (the
 gaussian filter itself is scipy's).
 """
 
@@ -181,5 +184,26 @@ def adaptive_threshold(img, window_size=5, offset=0):
         out = np.zeros(x.shape, dtype=ft)
         ndi.gaussian_filter(x, (window_size - 1) / 6.0, output=out, mode="reflect", cval=0)
         return out - offset
+
+    return _per_image(one, img)
+
+
+def equalize_hist_global(img, nbins=256):
+    """_toolbox_py.py:357-379 (skimage.exposure.equalize_hist(img, nbins=nbins))."""
+
+    def one(im):
+        if np.issubdtype(im.dtype, np.integer):
+            lo, hi = int(im.min()), int(im.max())
+            centers = np.arange(lo, hi + 1)
+            hist = np.bincount((im.ravel().astype(np.int64) - lo), minlength=hi - lo + 1)
+            cdf_dtype = np.float64
+        else:
+            hist, edges = np.histogram(im, bins=nbins)
+            centers = (edges[:-1] + edges[1:]) / 2.0
+            cdf_dtype = np.float32 if im.dtype == np.float32 else np.float64
+        cdf = hist.cumsum()
+        cdf = (cdf / float(cdf[-1])).astype(cdf_dtype, copy=False)
+        out = np.interp(im.ravel(), centers, cdf).reshape(im.shape)
+        return out.astype(np.float32 if im.dtype == np.float32 else np.float64, copy=False)
 
     return _per_image(one, img)

@@ -160,3 +160,27 @@ def test_adaptive_threshold_matches_scipy(image, window_offset):
     np.testing.assert_array_equal(got, want)
     stack = P.to_host(P.adaptive_threshold(P.to_device(img), ws, off))
     np.testing.assert_array_equal(stack, O.adaptive_threshold(img.copy(), ws, off))
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32", "f64"])
+@pytest.mark.parametrize("nbins", [256, 100])
+def test_equalize_hist_global_matches_oracle(image, nbins):
+    """equalize_hist_global: integer images exactly (the cumulative fraction at the
+    pixel's value); float images with the same bins as np.histogram and np.interp
+    within 2 ulps (numpy's interpolation may contract the slope form into an FMA
+    on some hosts)."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    img = Z["img_f32"].astype(np.float64) * 1.37 if image == "f64" else Z["img_" + image]
+    x = img[0]
+    got = P.to_host(P.equalize_hist_global(P.to_device(x), nbins))
+    want = O.equalize_hist_global(x.copy(), nbins)
+    assert got.dtype == want.dtype
+    if image in ("u8", "u16"):
+        np.testing.assert_array_equal(got, want)
+    else:
+        assert _ulps(got, want).max() <= 2.0
+    stack = P.to_host(P.equalize_hist_global(P.to_device(img), nbins))
+    assert stack.dtype == np.float64
+    np.testing.assert_array_equal(stack[0], got.astype(np.float64))

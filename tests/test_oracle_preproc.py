@@ -75,3 +75,33 @@ def test_adaptive_threshold_definition():
     assert O.adaptive_threshold(f, 7, 0).dtype == np.float32
     with pytest.raises(ValueError):
         O.adaptive_threshold(flat, 4)
+
+
+def test_equalize_hist_known_answers():
+    """equalize_hist by its definition: integer images, one bin per value and the
+    cumulative fraction of pixels at or below each pixel's value; float images, a
+    uniform histogram over [min, max] interpolated at the bin centres."""
+    a = np.array([[1, 2], [2, 5]], np.uint8)
+    got = O.equalize_hist_global(a)
+    assert got.dtype == np.float64
+    np.testing.assert_array_equal(got, [[0.25, 0.75], [0.75, 1.0]])
+    f = np.array([[0.0, 1.0], [1.0, 3.0]], np.float32)
+    got = O.equalize_hist_global(f, nbins=3)
+    assert got.dtype == np.float32
+    np.testing.assert_array_equal(got, np.array([[0.25, 0.5], [0.5, 1.0]], np.float32))
+
+
+def test_histogram_edges_follow_numpy():
+    """The host computation of numpy's histogram edges (used by the device
+    equalisation) equals np.histogram_bin_edges, flat images included."""
+    from fluidimage_gb300.preproc import histogram_edges
+
+    rng = np.random.default_rng(5)
+    for dt in (np.float32, np.float64):
+        for arr in (rng.random((7, 9)).astype(dt) * 3.7 - 1.1, np.full((3, 4), 2.5, dt)):
+            for nb in (1, 7, 256):
+                first, edges, denom = histogram_edges(arr.min(), arr.max(), nb, dt)
+                want = np.histogram_bin_edges(arr, bins=nb)
+                assert edges.dtype == want.dtype
+                np.testing.assert_array_equal(edges, want)
+                assert first == want[0]
