@@ -83,8 +83,6 @@ struct TcWin {
   int flat;
   int e0, e1;       // input scales 2^-e
   int valid;
-  int sx, sy;       // sums of the two window centres (the vector position x 2)
-  int dinx, diny;   // input shift (passes >= 1)
 };
 static_assert(sizeof(TcWin) <= 64, "per-window scalars");
 
@@ -419,13 +417,6 @@ __global__ void __launch_bounds__(THREADS, 2)
       WinPos wp;
       if (active) wp = window_positions<N>(a, vec, npad);
       const bool load = active && wp.valid;
-      if (lane == 0) {  // the vector position and input shift, for the outputs
-        TcWin* W = wins + warp;
-        W->sx = wp.ixs0 + wp.ixs1;
-        W->sy = wp.iys0 + wp.iys1;
-        W->dinx = wp.dinx;
-        W->diny = wp.diny;
-      }
       float f0[32], f1[32];
       unsigned long long u[4] = {0ull, 0ull, 0ull, 0ull};
       double sums[4] = {0.0, 0.0, 0.0, 0.0};
@@ -501,7 +492,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       if (lane == 0) {
         const bool flat0 = mm[0] == mm[2], flat1 = mm[1] == mm[3];
         const WinScalars ws = window_scalars<N>(intpath, u, sums, flat0, flat1, a.norms != nullptr);
-        TcWin& tw = wins[warp];
+        TcWin tw;
         // input scales: unit RMS, and the maximum below 2^15 (FP16 range)
         int e0 = ws.e0, e1 = ws.e1, x0, x1;
         frexpf(fmaxf(fabsf(mm[2]), fabsf(mm[0])), &x0);
@@ -524,6 +515,7 @@ __global__ void __launch_bounds__(THREADS, 2)
         // plane = c 2^(e0 + e1 + SCALE_P + SCALE_Q) / N^2
         tw.outscale = ldexpf(1.0f, e0 + e1 + SCALE_P + SCALE_Q - 10);
         tw.valid = load ? 1 : 0;
+        wins[warp] = tw;
       }
       __syncwarp();
       const float s0 = pow2f(-wins[warp].e0), s1 = pow2f(-wins[warp].e1);
@@ -697,7 +689,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       float c[32];
       tmem_ld32(tmem + lane_base + 128 + 32 * t, c);
       tmem_wait_ld();
-      const TcWin& tw = wins[warp];
+      const TcWin tw = wins[warp];
       float* PL = reinterpret_cast<float*>(sA) + warp * (N * LDP);
       double* red = reinterpret_cast<double*>(sm + OFF_RED + warp * 256);
       const int i0 = shift_index<N>(lane);
@@ -707,6 +699,7 @@ __global__ void __launch_bounds__(THREADS, 2)
       __syncwarp();
       if (active) {
         const bool valid = tw.valid != 0;
+        WinPos wp = window_positions<N>(a, vec, npad);
         PeakArgs pa;
         pa.mask = a.mask;
         pa.box = SearchBox{a.box_i0_start, a.box_i0_stop, a.box_i1_start, a.box_i1_stop};
@@ -717,8 +710,8 @@ __global__ void __launch_bounds__(THREADS, 2)
         pa.minv = a.subpix_minv;
         pa.nb_peaks = a.nb_peaks;
         pa.tie_rel = tie_rel;
-        SecondaryOut so{a.peaks_count, a.peaks, a.peaks_err, vec, a.dxin != nullptr, tw.dinx,
-                        tw.diny};
+        SecondaryOut so{a.peaks_count, a.peaks, a.peaks_err, vec, a.dxin != nullptr, wp.dinx,
+                        wp.diny};
         VecResult res = peak_and_subpix<N>(PL, pa, tw.normf, lane, warp, red,
                                            a.nb_peaks > 1 ? &so : nullptr);
         if (!valid && a.nb_peaks > 1 && lane == 0) a.peaks_count[vec] = -1;
@@ -740,8 +733,8 @@ __global__ void __launch_bounds__(THREADS, 2)
             err = FI_VEC_BAD_CROP;
           }
           if (a.dxin) {
-            dxo = add_shift(dxo, tw.dinx);
-            dyo = add_shift(dyo, tw.diny);
+            dxo = add_shift(dxo, wp.dinx);
+            dyo = add_shift(dyo, wp.diny);
           }
           a.deltaxs[vec] = dxo;
           a.deltays[vec] = dyo;
@@ -752,8 +745,9 @@ __global__ void __launch_bounds__(THREADS, 2)
                                              (res.subpix_tie ? FI_FLAG_SUBPIX_TIE : 0) |
                                              (res.sec_tie ? FI_FLAG_SECONDARY_TIE : 0))
                                  : (uint8_t)0;
-          a.xs[vec] = midpoint(tw.sx);
-          a.ys[vec] = midpoint(tw.sy);
+          const int sx = wp.ixs0 + wp.ixs1, sy = wp.iys0 + wp.iys1;
+          a.xs[vec] = midpoint(sx);
+          a.ys[vec] = midpoint(sy);
         }
       }
       // the planes alias the operand region of the next tile
