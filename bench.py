@@ -187,7 +187,8 @@ def run_reference(args):
     sample = (f"{cores} worker processes x one {SAMPLE_SHAPE[0]}x{SAMPLE_SHAPE[1]} pair of "
               "the workload each per step (numpy oracle, 1 thread per process)")
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "device": f"host CPU, {cores} cores (no GPU used)",
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": WORKLOAD, "same_config": True,

@@ -401,7 +401,14 @@ def equalize_hist_global(img, nbins=256):
     """Histogram equalisation (_toolbox_py.py:357-379; scikit-image's
     exposure.equalize_hist): the cumulative distribution of the image's histogram
     (one bin per integer value for integer images, ``nbins`` uniform bins for float
-    images) interpolated at every pixel; float64 (float32 for float32 images)."""
+    images) interpolated at every pixel; float64 (float32 for float32 images); per
+    image for a stack."""
+    x, single = _stack(img)
+    outs = [_equalize_one(x[i], nbins) for i in range(x.shape[0])]
+    return outs[0] if single else _torch().stack(outs)
+
+
+def _equalize_one(img, nbins):
     torch = _torch()
     lib = L.load()
     x = img.contiguous()
