@@ -772,9 +772,28 @@ __device__ __forceinline__ WinScalars window_scalars(bool intpath,
     }
     // scale of the inverse FFT: 0.25 / (N^2 sc0 sc1) = 2^(e0 + e1 - 2 - 2L)
     r.outscale = ldexpf(1.0f, e0 + e1 - 2 - 2 * L);
+  } else if (intpath) {
+    // 24 and 48 px windows of integer images: N^2 S exact in 64 bits as above; the
+    // scales 2^-e from its bit length (any power of two gives the same planes: the
+    // FFT commutes with exact scalings; this one keeps the values near unit RMS); the
+    // means, S and the norm in float32 (the DC bin is zeroed, so the mean only
+    // centres the values); FP64 only for the caller's norms array
+    constexpr unsigned long long NN = (unsigned long long)N * N;
+    constexpr int LB = 64 - __builtin_clzll(NN * NN);  // bit length of N^4
+    const unsigned long long SN0 = flat0 ? 0ull : NN * u[1] - u[0] * u[0];
+    const unsigned long long SN1 = flat1 ? 0ull : NN * u[3] - u[2] * u[2];
+    if (SN0 != 0ull) e0 = ((64 - __clzll((long long)SN0)) - LB + 1) >> 1;
+    if (SN1 != 0ull) e1 = ((64 - __clzll((long long)SN1)) - LB + 1) >> 1;
+    const float nnf = (float)NN;
+    r.mean0 = __fdiv_rn(__uint2float_rn((unsigned)u[0]), nnf);
+    r.mean1 = __fdiv_rn(__uint2float_rn((unsigned)u[2]), nnf);
+    const float S0f = __fdiv_rn(u64_to_float_rn(SN0), nnf);
+    const float S1f = __fdiv_rn(u64_to_float_rn(SN1), nnf);
+    r.normf = __fsqrt_rn(__fmul_rn(S0f, S1f));
+    r.norm64 = want_norm64 ? sqrt((double)SN0 * (double)SN1) / (double)NN : 0.0;
+    // scale of the inverse FFT: 0.25 / (N^2 2^-e0 2^-e1)
+    r.outscale = ldexpf(__fdiv_rn(0.25f, nnf), e0 + e1);
   } else {
-    if (intpath)
-      for (int i = 0; i < 4; ++i) sums[i] = (double)u[i];
     const double NN = (double)N * (double)N;
     const double S0 = flat0 ? 0.0 : fmax(sums[1] - sums[0] * sums[0] / NN, 0.0);
     const double S1 = flat1 ? 0.0 : fmax(sums[3] - sums[2] * sums[2] / NN, 0.0);
