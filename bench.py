@@ -95,6 +95,9 @@ def parse_args():
                     help="forms of the precision sweep (fp32_fft, bf16x1, bf16x3, fp16x3)")
     ap.add_argument("--sweep-size", type=int, default=4096,
                     help="image side of the precision sweep (4096 = the workload)")
+    ap.add_argument("--window-sizes", default=None,
+                    help="run only single passes of these window sizes (e.g. 16,24,32,48,64; "
+                         "one JSON line)")
     ap.add_argument("--preproc", action="store_true",
                     help="time the preprocessing tools instead (second JSON line format)")
     return ap.parse_args()
@@ -438,6 +441,7 @@ def run_gpu(args):
     }
     if not args.no_precision_sweep:
         line["precision_sweep"] = precision_sweep(args, dev, flush, peaks, peak_kind)
+    line["window_sizes"] = window_size_passes(args, dev)
     if not args.no_batched:
         line["batched"] = batched_workload(args, dev, flush)
     if not args.no_refinement:
@@ -894,6 +898,50 @@ def run_preproc(args):
     print(json.dumps(out), flush=True)
 
 
+def window_size_passes(args, dev, sizes=(16, 24, 32, 48, 64), reps=10):
+    """One FP32 pass (with WorkFIX) per window size on the 2048^2 pair of the
+    multipass workload, overlap 0.5, no interpolation: the window count, the best of
+    ``reps`` CUDA-event timings and the time per window."""
+    import torch
+
+    from fluidimage_gb300 import WorkPIV, workloads
+
+    (im0, im1), _ = workloads.config2_images(pair=0, shape=(args.size, args.size))
+    d0 = torch.as_tensor(im0.view(np.int16), device=dev)
+    d1 = torch.as_tensor(im1.view(np.int16), device=dev)
+    out = {}
+    for n in sizes:
+        params = WorkPIV.create_default_params()
+        params.piv0.shape_crop_im0 = n
+        params.multipass.number = 1
+        params.multipass.use_tps = False
+        params.fix.threshold_diff_neighbour = None
+        work = WorkPIV(params, device=dev, interp_last=False)
+        for _ in range(3):
+            work.calcul_device(d0, d1)
+        torch.cuda.synchronize()
+        nvec = work._pipelines[next(iter(work._pipelines))].layouts[0].nvec
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            work.calcul_device(d0, d1)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = min(times)
+        out[str(n)] = {"windows": nvec, "ms": ms, "ns_per_window": ms * 1e6 / nvec}
+    return {"workload": f"one {args.size}x{args.size} uint16 pair, single FP32 pass + WorkFIX "
+                        "per window size, overlap 0.5", "passes": out}
+
+
+def run_window_sizes_only(args):
+    import torch
+
+    sizes = tuple(int(v) for v in args.window_sizes.split(","))
+    print(json.dumps(window_size_passes(args, torch.device("cuda"), sizes)), flush=True)
+
+
 def run_sweep_only(args):
     """The precision sweep alone (no accuracy check), one JSON line."""
     import torch
@@ -915,6 +963,8 @@ def main():
         run_batched_only(args)
     elif args.refinement_only:
         run_refinement_only(args)
+    elif args.window_sizes:
+        run_window_sizes_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -548,7 +548,7 @@ static bool supported_n(int n) { return n == 16 || n == 24 || n == 32 || n == 48
 // windows per block, ~100 with 8) for the tuner to choose from
 template <int N, int WPB>
 constexpr int batch_min_blocks() {
-  return N <= 16 ? (WPB == 16 ? 2 : 5) : (N <= 32 ? 16 / WPB : 6 / WPB);
+  return N <= 16 ? (WPB == 16 ? 2 : 5) : (N <= 32 ? 16 / WPB : (N == 48 ? 8 : 6) / WPB);
 }
 
 template <int N, int WPB>

@@ -23,8 +23,10 @@ struct Cfg {
   static constexpr int WPB = (G == 16) ? 16 : ((G == 32) ? 8 : 2);  // windows / block
   static constexpr int THREADS = G * WPB;
   // resident CTAs per SM asked of the register allocator (16-px windows: 3, i.e.
-  // 24 warps, at <= 85 registers)
-  static constexpr int MIN_BLOCKS = (N <= 16) ? 3 : 1;
+  // 24 warps, at <= 85 registers; 48-px windows: 4, i.e. 16 warps at 128 registers,
+  // 6 % faster than 12 warps at 166 registers despite 72 bytes of spills; 16-px
+  // windows at 2 CTAs and 128 registers were 5 % slower)
+  static constexpr int MIN_BLOCKS = (N <= 16) ? 3 : ((N == 48) ? 4 : 1);
   static constexpr int LD = N + 1;   // row stride (float2) of the complex buffer
   static constexpr int LDP = N + 1;  // row stride (float) of the plane
   static constexpr int ZBYTES = N * LD * 8;
