@@ -356,6 +356,26 @@ def run_gpu(args):
         dist.barrier()
     ms = statistics.mean(step_ms)
 
+    # ---- the same step writing every correlation plane to device memory, as
+    # upstream's HeavyPIVResults.correls holds them (keep_correls=True)
+    work_planes = WorkPIV(params, device=dev, keep_correls=True)
+    for _ in range(2):
+        outs_p = work_planes.calcul_device(t0, t1)
+    planes_ms = []
+    for _ in range(5):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        outs_p = work_planes.calcul_device(t0, t1)
+        ev1.record()
+        torch.cuda.synchronize()
+        planes_ms.append(ev0.elapsed_time(ev1))
+    planes_bytes = int(sum(pd.planes.numel() * pd.planes.element_size() for pd in outs_p
+                           if pd.planes is not None))
+    del outs_p, work_planes
+
     # ---- end to end through the public API (pinned host images -> host results)
     h0 = torch.from_numpy(im0.view(np.int16)).pin_memory()
     h1 = torch.from_numpy(im1.view(np.int16)).pin_memory()
@@ -437,6 +457,11 @@ def run_gpu(args):
         "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kern.items()},
         "roofline": roof,
         "correlation": pass_lines(kern, outs, work),
+        "planes_kept": {"ms_per_step": statistics.mean(planes_ms),
+                        "plane_bytes_per_step": planes_bytes,
+                        "note": "the timed step with every correlation plane written to "
+                                "device memory (keep_correls=True; upstream keeps them in "
+                                "HeavyPIVResults.correls); not part of value"},
         "clocks": clk,
     }
     if not args.no_precision_sweep:
