@@ -75,6 +75,10 @@ class PIVBatch:
                 raise ValueError("PIVBatch runs single-pass works (params.multipass.number == 1)")
             if int(params.piv0.nb_peaks_to_search) != 1:
                 raise NotImplementedError("PIVBatch: nb_peaks_to_search must be 1")
+            if params.piv0.method_correl not in ("gb300", "np.fft", "fftw"):
+                raise NotImplementedError(
+                    "PIVBatch runs the FP32 FFT correlation (method_correl 'gb300', "
+                    f"'np.fft' or 'fftw'), not {params.piv0.method_correl!r}")
             t0, t1 = _to_dev(im0, dev), _to_dev(im1, dev)
             key = (id(params), tuple(t0.shape), _np_dtype(t0))
             if key not in pipes:

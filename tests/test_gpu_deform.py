@@ -200,3 +200,29 @@ def test_deformed_multipass_matches_oracle_and_truth():
     e_def, e_shift = rms(res_def.passes[-1]), rms(res_shift.passes[-1])
     print("RMS error vs imposed field: deformation", e_def, "window shift", e_shift)
     assert e_def < e_shift
+
+
+def test_deformed_multipass_with_tensor_core_pass():
+    """Deformation mode with the 32 px passes on the tensor cores (fp16 3-term): the
+    deformed images are float32, which the tensor-core pass takes like integer
+    images; the final field stays within 5e-3 px of the FP32 FFT form's."""
+    import torch
+
+    from fluidimage_gb300 import WorkPIV, synthetic, workloads
+
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = synthetic.oseen_vortex((512, 512), d_max=6.0, rc=60.0)
+    im0, im1 = synthetic.make_pair((512, 512), field, model, seed=78)
+    params = workloads.config2_params(WorkPIV.create_default_params())
+    ref = WorkPIV(params, deform=True).calcul({"arrays": (im0, im1), "names": ("a", "b")})
+    params_tc = workloads.config2_params(WorkPIV.create_default_params())
+    params_tc.piv0.method_correl = "gb300_tc_fp16x3"
+    got = WorkPIV(params_tc, deform=True).calcul({"arrays": (im0, im1), "names": ("a", "b")})
+    torch.cuda.synchronize()
+    a, b = ref.passes[-1], got.passes[-1]
+    d = np.hypot(a.deltaxs_final - b.deltaxs_final, a.deltays_final - b.deltays_final)
+    print("deformed multipass, tensor-core vs FFT 32 px pass: max", d.max(), "median",
+          np.median(d))
+    assert np.median(d) < 1e-4
+    assert np.mean(d < 5e-3) > 0.99
