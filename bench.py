@@ -406,7 +406,7 @@ def run_gpu(args):
 
     for _ in work.calcul_series(couples(len(series))):
         pass
-    n_series = max(args.e2e_steps, 16)
+    n_series = max(args.e2e_steps, 32)
     torch.cuda.synchronize()
     t_start = time.perf_counter()
     for _ in work.calcul_series(couples(n_series)):
