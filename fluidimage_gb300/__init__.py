@@ -8,9 +8,14 @@
 * ``WorkBOS``: background-oriented schlieren (PIV against a reference image kept
   on the GPU).
 * ``PIVBatch``: single-pass PIV of many pairs of mixed image and window sizes in a
-  few persistent launches (one per window size), replayable as a CUDA graph.
+  few launches (one per window size, blocks fed by a device work queue),
+  replayable as a CUDA graph.
 * ``params.piv0.method_correl = "gb300_tc_fp16x3"`` (or ``_bf16x3``, ``_bf16x1``):
   32 px passes on the tensor cores (DFT as dense contractions).
+* ``WorkPIV(params, deform=True)``: passes after the first on deformed images;
+  ``deform``: the differentiable deform-and-correlate chain (hand-written adjoint)
+  and its gradient refinement.
+* ``preproc.WorkPreproc``: the preprocessing tools on the device.
 
 Importing the package is cheap: the CUDA library is loaded on first use by
 ``fluidimage_gb300._lib`` and fails loudly when it is missing (no CPU fallback).
