@@ -169,8 +169,38 @@ __device__ __forceinline__ void piv_window(const fi_piv_pass_args& a, const floa
   float sf0 = 0.f, sf1 = 0.f, qf0 = 0.f, qf1 = 0.f, cf0 = 0.f, cf1 = 0.f;
   float mm[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
   if (intpath) {
-    // integer images: thread t stages row t of both windows (16-byte loads)
-    if (t < N) {
+    // integer images: with both windows' rows 16-byte aligned (the grid of a first
+    // pass), thread t stages row t (16-byte loads); otherwise (shifted windows)
+    // thread t stages column t, so that the group's loads of a row are coalesced
+    const int esz = a.dtype == FI_U16 ? 2 : 1;
+    const bool rowwise =
+        !valid || ((esz == 2 || N % 16 == 0) && (((x00 | x10) * esz) & 15) == 0 &&
+                   ((a.width * esz) & 15) == 0 &&
+                   ((reinterpret_cast<uintptr_t>(a.im0) | reinterpret_cast<uintptr_t>(a.im1)) &
+                    15) == 0);
+    if (t < N && !rowwise) {
+      RowStats st;
+      const int H = a.height, W = a.width;
+      const int mini0 = (int)__ldg(a.im_min + 0), mini1 = (int)__ldg(a.im_min + 1);
+#pragma unroll 4
+      for (int r = 0; r < N; ++r) {
+        const int y0 = y00 + r, xa = x00 + t, y1 = y10 + r, xb = x10 + t;
+        const int v0 = (y0 >= 0 && y0 < H && xa >= 0 && xa < W)
+                           ? load_px_int(a.im0, a.dtype, (int64_t)y0 * W + xa) - mini0 : 0;
+        const int v1 = (y1 >= 0 && y1 < H && xb >= 0 && xb < W)
+                           ? load_px_int(a.im1, a.dtype, (int64_t)y1 * W + xb) - mini1 : 0;
+        Z[r * C::LD + t] = make_float2((float)v0, (float)v1);
+        st.add(v0, v1);
+      }
+      si0 = st.s0;
+      si1 = st.s1;
+      qi0 = st.q0;
+      qi1 = st.q1;
+      mm[0] = (float)st.lo0;
+      mm[1] = (float)st.lo1;
+      mm[2] = (float)st.hi0;
+      mm[3] = (float)st.hi1;
+    } else if (t < N) {
       RowStats st;
       if (valid) {
         stage_rows_int<N>(a, y00 + t, x00, y10 + t, x10, (int)__ldg(a.im_min + 0),
