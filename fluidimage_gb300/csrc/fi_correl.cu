@@ -171,12 +171,12 @@ __device__ __forceinline__ void piv_window(const fi_piv_pass_args& a, const floa
   if (intpath) {
     // integer images: with both windows' rows 16-byte aligned (the grid of a first
     // pass), thread t stages row t (16-byte loads); otherwise (shifted windows) thread
-    // t stages column t for windows of 32 px and more, so that the group's loads of a
-    // row are coalesced (measured: the shifted 32 px pass of the 2048^2 multipass
-    // 0.193 -> 0.168 ms; 16 and 24 px windows were faster row by row)
+    // t stages column t for 32 px windows, so that the warp's loads of a row are
+    // coalesced (measured: the shifted 32 px pass of the 2048^2 multipass 0.193 ->
+    // 0.168 ms; 16, 24 and 48 px windows were faster row by row)
     const int esz = a.dtype == FI_U16 ? 2 : 1;
     const bool rowwise =
-        N < 32 || !valid ||
+        N != 32 || !valid ||
         ((esz == 2 || N % 16 == 0) && (((x00 | x10) * esz) & 15) == 0 &&
                    ((a.width * esz) & 15) == 0 &&
                    ((reinterpret_cast<uintptr_t>(a.im0) | reinterpret_cast<uintptr_t>(a.im1)) &

@@ -1,0 +1,86 @@
+"""Edge cases of a pass against the oracle: constant images (every window flat:
+zero planes, norm 0, correls_max 0, the peak at the last maximum of an all-zero
+plane), images with constant regions (flat and textured windows side by side), a
+single window per image, and images of one window plus a ragged border.  The GPU
+pass equals the oracle's pass: same errors, same NaN pattern, displacements within
+5e-3 px, correls_max within 2e-5 relative."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_PX = 5e-3
+
+
+def _pass(im0, im1, n, overlap, dtype):
+    import torch
+
+    from fluidimage_gb300 import WorkPIV
+
+    params = WorkPIV.create_default_params()
+    params.piv0.shape_crop_im0 = n
+    params.piv0.grid.overlap = overlap
+    params.multipass.number = 1
+    params.fix.threshold_diff_neighbour = None
+    params.fix.correl_min = float("-inf")
+    res = WorkPIV(params, interp_last=False).calcul(
+        {"arrays": (im0.astype(dtype), im1.astype(dtype)), "names": ("a", "b")})
+    torch.cuda.synchronize()
+    return res.passes[0]
+
+
+def _compare(got, want):
+    a = np.asarray(got.deltaxs, np.float64)
+    b = np.asarray(want.deltaxs, np.float64)
+    assert a.shape == b.shape
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    ok = ~np.isnan(b)
+    if ok.any():
+        assert np.abs(a[ok] - b[ok]).max() <= TOL_PX
+        assert np.abs(np.asarray(got.deltays)[ok] - want.deltays[ok]).max() <= TOL_PX
+        np.testing.assert_allclose(np.asarray(got.correls_max)[ok], want.correls_max[ok],
+                                   rtol=2e-5, atol=1e-7)
+    assert dict(got.errors) == want.errors
+
+
+def _images(kind, shape, seed=5):
+    from fluidimage_gb300 import synthetic
+
+    model = synthetic.ParticleModel(density=0.05, noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair(shape, synthetic.uniform_shift(2.3, -1.4), model, seed=seed)
+    im0, im1 = im0.astype(np.float64), im1.astype(np.float64)
+    if kind == "constant":
+        im0[:] = 37.0
+        im1[:] = 37.0
+    elif kind == "constant_im1":
+        im1[:] = 12.0
+    elif kind == "flat_regions":
+        im0[:, : shape[1] // 3] = 50.0
+        im1[:, : shape[1] // 3] = 50.0
+        im0[shape[0] // 2:, shape[1] // 2:] = 0.0
+    return im0, im1
+
+
+@pytest.mark.parametrize("dtype", ["uint8", "uint16", "float32"])
+@pytest.mark.parametrize("kind", ["constant", "constant_im1", "flat_regions"])
+def test_flat_windows_match_oracle(kind, dtype):
+    from oracle import piv as O
+
+    im0, im1 = _images(kind, (128, 160))
+    n = 32
+    got = _pass(im0, im1, n, 0.5, dtype)
+    want = O.piv_pass(im0.astype(dtype), im1.astype(dtype), (n, n), 0.5)
+    _compare(got, want)
+
+
+@pytest.mark.parametrize("shape, n", [((32, 32), 32), ((35, 41), 32), ((16, 16), 16),
+                                      ((64, 70), 48), ((24, 30), 24)])
+def test_one_window_and_ragged_borders_match_oracle(shape, n):
+    from oracle import piv as O
+
+    im0, im1 = _images("particles", shape, seed=9)
+    got = _pass(im0, im1, n, 0.5, "uint16")
+    want = O.piv_pass(im0.astype("uint16"), im1.astype("uint16"), (n, n), 0.5)
+    assert np.asarray(got.deltaxs).size >= 1
+    _compare(got, want)
