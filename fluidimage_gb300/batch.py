@@ -32,6 +32,7 @@ import numpy as np
 
 from . import _lib as L
 from .engine import PIVPipeline, _DTYPES
+from .errors import GridError
 
 #: autotuner choices, kept per (window size, log2 of the windows of that size)
 _TUNED = {}
@@ -92,6 +93,10 @@ class PIVBatch:
         self.min_keys = torch.empty(2 * n_jobs, dtype=torch.int32, device=dev)
         for k, job in enumerate(self.jobs):
             lay = job.pipe.layouts[0]
+            if (job.params.fix.threshold_diff_neighbour is not None
+                    and (lay.ixvecs.size < 2 or lay.iyvecs.size < 2)):
+                raise GridError(f"job {k}: WorkFIX's neighbour test needs a vector grid of at "
+                                f"least 2 x 2 (this one is {lay.iyvecs.size} x {lay.ixvecs.size})")
             job.out, job.args = job.pipe.make_pass(lay, job.im0, job.im1, self.im_min[k],
                                                    None, None, _DTYPES[job.pipe.dtype])
             job.fix = job.pipe.make_fix(job.out, job.params.fix)

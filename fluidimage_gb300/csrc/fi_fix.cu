@@ -193,9 +193,13 @@ __global__ void k_fix_batch_b(const fi_fix_args* __restrict__ args,
     const int p = batch_pass_of(vec_start, npass, i);
     const fi_fix_args& a = args[p];
     if (!a.use_threshold) continue;
-    const int nvec = a.nx * a.ny;
-    fix_b_one(a, i - __ldg(vec_start + p), a.work, a.work + nvec,
-              __fmul_rn(a.threshold, a.threshold));
+    const int nvec = a.nx * a.ny, j = i - __ldg(vec_start + p);
+    if (a.nx < 2 || a.ny < 2) {  // no neighbour stencil (callers reject such passes)
+      a.deltaxs_out[j] = a.work[j];
+      a.deltays_out[j] = a.work[nvec + j];
+      continue;
+    }
+    fix_b_one(a, j, a.work, a.work + nvec, __fmul_rn(a.threshold, a.threshold));
   }
 }
 
@@ -276,7 +280,9 @@ using namespace fi;
 extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
   FI_REQUIRE(args, "fi_fix: null args");
   const fi_fix_args& a = *args;
-  FI_REQUIRE(a.nx >= 2 && a.ny >= 2, "fi_fix: vector grid must be at least 2 x 2");
+  FI_REQUIRE(a.nx >= 1 && a.ny >= 1, "fi_fix: empty vector grid");
+  FI_REQUIRE(!a.use_threshold || (a.nx >= 2 && a.ny >= 2),
+             "fi_fix: the neighbour test needs a vector grid of at least 2 x 2");
   FI_REQUIRE(a.deltaxs && a.deltays && a.correls_max && a.errors && a.deltaxs_out &&
                  a.deltays_out && a.fix_flags,
              "fi_fix: null pointer");
@@ -309,7 +315,9 @@ extern "C" int fi_fix(const fi_fix_args* args, void* stream) {
 extern "C" int fi_fix_static(const fi_fix_args* args, void* stream) {
   FI_REQUIRE(args, "fi_fix_static: null args");
   const fi_fix_args& a = *args;
-  FI_REQUIRE(a.nx >= 2 && a.ny >= 2, "fi_fix_static: vector grid must be at least 2 x 2");
+  FI_REQUIRE(a.nx >= 1 && a.ny >= 1, "fi_fix_static: empty vector grid");
+  FI_REQUIRE(!a.use_threshold || (a.nx >= 2 && a.ny >= 2),
+             "fi_fix_static: the neighbour test needs a vector grid of at least 2 x 2");
   FI_REQUIRE((int64_t)a.nx * a.ny <= FI_FIX_STATIC_MAX_VECTORS,
              "fi_fix_static: %lld vectors exceed the static scratch limit of %d vectors "
              "(use fi_fix with a caller-provided work buffer)",

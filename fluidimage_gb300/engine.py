@@ -24,7 +24,7 @@ from typing import List, Optional
 import numpy as np
 
 from . import _lib as L
-from .errors import ERROR_STRINGS, InterpError  # noqa: F401  (ERROR_STRINGS re-exported)
+from .errors import ERROR_STRINGS, GridError, InterpError  # noqa: F401  (ERROR_STRINGS re-exported)
 
 _DTYPES = {np.dtype(np.uint8): L.FI_U8, np.dtype(np.uint16): L.FI_U16,
            np.dtype(np.float32): L.FI_F32}
@@ -104,7 +104,7 @@ def make_grid(imshape, shape_crop, overlap):
     iyvec_max = len_y - stop[0]
     iyvecs = np.arange(start[0], iyvec_max, stepy, dtype=int)
     if ixvecs.size == 0 or iyvecs.size == 0:
-        raise ValueError("image smaller than the interrogation window")
+        raise GridError("image smaller than the interrogation window")
     if ixvec_max - ixvecs[-1] > stepx // 2.5:
         ixvecs = np.append(ixvecs, ixvec_max)
     if iyvec_max - iyvecs[-1] > stepy // 2.5:
@@ -774,6 +774,9 @@ class PIVPipeline:
     def _run_fix(self, cur: PassDevice, fx, s):
         lib = L.load()
         a = self.make_fix(cur, fx)
+        if a.use_threshold and (a.nx < 2 or a.ny < 2):
+            raise GridError(f"WorkFIX's neighbour test needs a vector grid of at least 2 x 2 "
+                            f"(this one is {a.ny} x {a.nx})")
         with _timed("fi_fix"):
             L.check(lib.fi_fix(C.byref(a), s), "fi_fix")
 

@@ -20,6 +20,13 @@ class InterpError(ValueError):
     pass
 
 
+class GridError(ValueError, IndexError):
+    """A vector grid the work cannot run on.  Upstream fails there with an
+    IndexError (an empty window grid, singlepass.py:128-133; WorkFIX's neighbour
+    mean on a grid narrower than 2, mean_neighbors.py:5-125); this error is an
+    IndexError too, with the reason."""
+
+
 ERROR_STRINGS = {
     1: "Correlation peak touching boundary.",
     2: "Correlation peak touching nan.",

@@ -315,7 +315,8 @@ int fi_fix(const fi_fix_args* args, void* stream);
  * in two launches: fix_args, device array [npass] (each with its own work buffer
  * when use_threshold); vec_start: device int32 [npass + 1], first vector of each
  * pass; total = vec_start[npass].  Secondary peaks (nb_peaks > 1) are not handled
- * here (fi_fix per pass).
+ * here (fi_fix per pass).  A pass with the neighbour test needs a grid of at least
+ * 2 x 2 (its vectors are otherwise passed through untested; fi_fix rejects it).
  */
 int fi_fix_batch(const fi_fix_args* fix_args, const int32_t* vec_start, int npass, int total,
                  void* stream);

@@ -78,9 +78,11 @@ def test_flat_windows_match_oracle(kind, dtype):
     _compare(got, want)
 
 
-@pytest.mark.parametrize("shape, n", [((32, 32), 32), ((35, 41), 32), ((16, 16), 16),
-                                      ((64, 70), 48), ((24, 30), 24)])
-def test_one_window_and_ragged_borders_match_oracle(shape, n):
+@pytest.mark.parametrize("shape, n", [((35, 41), 32), ((33, 33), 32), ((40, 33), 32),
+                                      ((64, 70), 48), ((30, 50), 24), ((17, 18), 16)])
+def test_small_grids_and_ragged_borders_match_oracle(shape, n):
+    """Grids of 1 x 1, 1 x 2 and 2 x 1 vectors and ragged borders, WorkFIX without the
+    neighbour test (upstream's neighbour mean needs 2 x 2, see below)."""
     from oracle import piv as O
 
     im0, im1 = _images("particles", shape, seed=9)
@@ -88,3 +90,41 @@ def test_one_window_and_ragged_borders_match_oracle(shape, n):
     want = O.piv_pass(im0.astype("uint16"), im1.astype("uint16"), (n, n), 0.5)
     assert np.asarray(got.deltaxs).size >= 1
     _compare(got, want)
+
+
+@pytest.mark.parametrize("shape, n", [((32, 32), 32), ((16, 16), 16), ((24, 30), 24)])
+def test_empty_grid_raises_index_error_like_upstream(shape, n):
+    """An image the size of the window has an empty grid: upstream's
+    _prepare_with_image fails with an IndexError (singlepass.py:128-133); so does the
+    oracle, and the work raises an IndexError too (GridError)."""
+    from fluidimage_gb300 import WorkPIV
+    from oracle import piv as O
+
+    im0, im1 = _images("particles", shape, seed=9)
+    with pytest.raises(IndexError):
+        O.make_grid(shape, (n, n), 0.5)
+    params = WorkPIV.create_default_params()
+    params.piv0.shape_crop_im0 = n
+    params.multipass.number = 1
+    with pytest.raises(IndexError):
+        WorkPIV(params).calcul({"arrays": (im0.astype("uint16"), im1.astype("uint16")),
+                                "names": ("a", "b")})
+
+
+def test_neighbour_test_on_a_one_row_grid_raises_index_error_like_upstream():
+    """WorkFIX's neighbour mean on a grid of one row fails with an IndexError upstream
+    (mean_neighbors.py:5-125); the oracle and the work do the same."""
+    from fluidimage_gb300 import WorkPIV
+    from oracle import piv as O
+
+    im0, im1 = _images("particles", (35, 41), seed=9)
+    want = O.piv_pass(im0.astype("uint16"), im1.astype("uint16"), (32, 32), 0.5)
+    with pytest.raises(IndexError):
+        O.fix(want, correl_min=0.2, threshold_diff_neighbour=2.0)
+    params = WorkPIV.create_default_params()
+    params.piv0.shape_crop_im0 = 32
+    params.multipass.number = 1
+    params.fix.threshold_diff_neighbour = 2.0
+    with pytest.raises(IndexError):
+        WorkPIV(params, interp_last=False).calcul(
+            {"arrays": (im0.astype("uint16"), im1.astype("uint16")), "names": ("a", "b")})
