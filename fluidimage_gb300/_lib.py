@@ -79,6 +79,10 @@ class FixArgs(C.Structure):
     ]
 
 
+#: bytes of a TPS plan buffer (header + compaction scratch), FI_TPS_PLAN_BYTES
+TPS_PLAN_BYTES = 256 + 24 * 1024
+
+
 class TpsPlan(C.Structure):
     _fields_ = [
         ("num_centers", C.c_int), ("nb_subdomx", C.c_int), ("nb_subdomy", C.c_int),

@@ -145,6 +145,46 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return __longlong_as_double((long long)d);
 }
 
+// The plan header from the count of valid vectors and their extremes
+// (ThinPlateSplineSubdom.__init__, thin_plate_spline_subdom.py:38-91).
+__device__ fi_tps_plan plan_header(int base, double xmin, double xmax, double ymin, double ymax,
+                                   int subdom_size, double smoothing_coef, double pct) {
+  fi_tps_plan p{};
+  p.num_centers = base;
+  if (base == 0) {
+    p.status = 1;
+    return p;
+  }
+  p.x_min = xmin;
+  p.x_max = xmax;
+  p.y_min = ymin;
+  p.y_max = ymax;
+  const double range_x = __dsub_rn(xmax, xmin), range_y = __dsub_rn(ymax, ymin);
+  const double aspect = __ddiv_rn(range_y, range_x);
+  const double nb_subdom = __ddiv_rn((double)base, (double)subdom_size);
+  const double fx = floor(__dsqrt_rn(__ddiv_rn(nb_subdom, aspect)));
+  const double fy = ceil(__dsqrt_rn(__dmul_rn(nb_subdom, aspect)));
+  if (!(fx < 1e6) || !(fy < 1e6)) {  // upstream fails (int(inf) / int(nan))
+    p.status = 2;
+    return p;
+  }
+  int nbx = (int)fx, nby = (int)fy;
+  if (nbx == 0) nbx = 1;
+  if (nby == 0) nby = 1;
+  p.nb_subdomx = nbx;
+  p.nb_subdomy = nby;
+  const double x0 = linspace_at(xmin, xmax, nbx + 1, 0), x1 = linspace_at(xmin, xmax, nbx + 1, 1);
+  const double y0 = linspace_at(ymin, ymax, nby + 1, 0), y1 = linspace_at(ymin, ymax, nby + 1, 1);
+  const double per = __ddiv_rn((double)base, (double)(nbx * nby));
+  p.smoothing = __dmul_rn(
+      smoothing_coef, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dsub_rn(x1, x0), __dsub_rn(y1, y0)), per)));
+  const double coef_buffer = __ddiv_rn(pct, 100.0);
+  p.buffer_x = __ddiv_rn(__dmul_rn(coef_buffer, range_x), (double)nbx);
+  p.buffer_y = __ddiv_rn(__dmul_rn(coef_buffer, range_y), (double)nby);
+  p.status = 0;
+  return p;
+}
+
 // Compaction of the valid vectors (no NaN component) in index order, limits and
 // subdomain layout; one block of 32 warps, each over one contiguous segment of the
 // vectors: the warps count their valid vectors, one block scan places the segments,
@@ -219,42 +259,170 @@ __global__ void __launch_bounds__(1024)
   ymin = block_reduce_d(ymin, red, false);
   ymax = block_reduce_d(ymax, red, true);
   if (threadIdx.x != 0) return;
-  fi_tps_plan p{};
-  p.num_centers = base;
-  if (base == 0) {
-    p.status = 1;
-    *plan = p;
-    return;
+  *plan = plan_header(base, xmin, xmax, ymin, ymax, subdom_size, smoothing_coef, pct);
+}
+
+// The same compaction over many blocks (large passes), in three launches with the
+// per-block data in the scratch that follows the plan header (FI_TPS_PLAN_BYTES):
+// (1) each block counts the valid vectors of its contiguous chunk and their float32
+// extremes; (2) one block scans the counts, reduces the extremes and writes the
+// header; (3) each block writes its chunk's valid vectors from its offset, in order.
+struct PlanScratch {
+  int count[FI_TPS_PLAN_MAX_BLOCKS];
+  int offset[FI_TPS_PLAN_MAX_BLOCKS];
+  float ext[FI_TPS_PLAN_MAX_BLOCKS][4];  // min x, max x, min y, max y
+};
+
+__device__ __forceinline__ PlanScratch* plan_scratch(fi_tps_plan* plan) {
+  return reinterpret_cast<PlanScratch*>(reinterpret_cast<unsigned char*>(plan) + 256);
+}
+
+__device__ __forceinline__ void plan_chunk(int nvec, int& s0, int& s1) {
+  const int chunk = (((nvec + gridDim.x - 1) / gridDim.x) + 31) & ~31;
+  s0 = min(nvec, (int)blockIdx.x * chunk);
+  s1 = min(nvec, s0 + chunk);
+}
+
+__global__ void __launch_bounds__(256)
+    k_tps_plan_count(const float* xs, const float* ys, const float* dx, const float* dy,
+                     int nvec, fi_tps_plan* plan) {
+  __shared__ int s_cnt[8];
+  __shared__ float s_ext[8][4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int s0, s1;
+  plan_chunk(nvec, s0, s1);
+  int cnt = 0;
+  float e[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+  for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+    if (isnan(dx[i]) || isnan(dy[i])) continue;
+    ++cnt;
+    const float x = xs[i], y = ys[i];
+    e[0] = fminf(e[0], x);
+    e[1] = fmaxf(e[1], x);
+    e[2] = fminf(e[2], y);
+    e[3] = fmaxf(e[3], y);
   }
-  p.x_min = xmin;
-  p.x_max = xmax;
-  p.y_min = ymin;
-  p.y_max = ymax;
-  const double range_x = __dsub_rn(xmax, xmin), range_y = __dsub_rn(ymax, ymin);
-  const double aspect = __ddiv_rn(range_y, range_x);
-  const double nb_subdom = __ddiv_rn((double)base, (double)subdom_size);
-  const double fx = floor(__dsqrt_rn(__ddiv_rn(nb_subdom, aspect)));
-  const double fy = ceil(__dsqrt_rn(__dmul_rn(nb_subdom, aspect)));
-  if (!(fx < 1e6) || !(fy < 1e6)) {  // upstream fails (int(inf) / int(nan))
-    p.status = 2;
-    *plan = p;
-    return;
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    e[0] = fminf(e[0], __shfl_xor_sync(0xffffffffu, e[0], o));
+    e[1] = fmaxf(e[1], __shfl_xor_sync(0xffffffffu, e[1], o));
+    e[2] = fminf(e[2], __shfl_xor_sync(0xffffffffu, e[2], o));
+    e[3] = fmaxf(e[3], __shfl_xor_sync(0xffffffffu, e[3], o));
   }
-  int nbx = (int)fx, nby = (int)fy;
-  if (nbx == 0) nbx = 1;
-  if (nby == 0) nby = 1;
-  p.nb_subdomx = nbx;
-  p.nb_subdomy = nby;
-  const double x0 = linspace_at(xmin, xmax, nbx + 1, 0), x1 = linspace_at(xmin, xmax, nbx + 1, 1);
-  const double y0 = linspace_at(ymin, ymax, nby + 1, 0), y1 = linspace_at(ymin, ymax, nby + 1, 1);
-  const double per = __ddiv_rn((double)base, (double)(nbx * nby));
-  p.smoothing = __dmul_rn(
-      smoothing_coef, __dsqrt_rn(__ddiv_rn(__dmul_rn(__dsub_rn(x1, x0), __dsub_rn(y1, y0)), per)));
-  const double coef_buffer = __ddiv_rn(pct, 100.0);
-  p.buffer_x = __ddiv_rn(__dmul_rn(coef_buffer, range_x), (double)nbx);
-  p.buffer_y = __ddiv_rn(__dmul_rn(coef_buffer, range_y), (double)nby);
-  p.status = 0;
-  *plan = p;
+  if (lane == 0) {
+    s_cnt[wid] = cnt;
+    for (int k = 0; k < 4; ++k) s_ext[wid][k] = e[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    PlanScratch* sc = plan_scratch(plan);
+    int c = 0;
+    float f[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      c += s_cnt[w];
+      f[0] = fminf(f[0], s_ext[w][0]);
+      f[1] = fmaxf(f[1], s_ext[w][1]);
+      f[2] = fminf(f[2], s_ext[w][2]);
+      f[3] = fmaxf(f[3], s_ext[w][3]);
+    }
+    sc->count[blockIdx.x] = c;
+    for (int k = 0; k < 4; ++k) sc->ext[blockIdx.x][k] = f[k];
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+    k_tps_plan_head(int nblocks, int subdom_size, double smoothing_coef, double pct,
+                    fi_tps_plan* plan) {
+  __shared__ int s_wsum[32];
+  __shared__ float s_ext[32][4];
+  PlanScratch* sc = plan_scratch(plan);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int b = threadIdx.x;
+  const int v = b < nblocks ? sc->count[b] : 0;
+  float e[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+  if (b < nblocks)
+    for (int k = 0; k < 4; ++k) e[k] = sc->ext[b][k];
+  int incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    e[0] = fminf(e[0], __shfl_xor_sync(0xffffffffu, e[0], o));
+    e[1] = fmaxf(e[1], __shfl_xor_sync(0xffffffffu, e[1], o));
+    e[2] = fminf(e[2], __shfl_xor_sync(0xffffffffu, e[2], o));
+    e[3] = fmaxf(e[3], __shfl_xor_sync(0xffffffffu, e[3], o));
+  }
+  if (lane == 31) s_wsum[wid] = incl;
+  if (lane == 0)
+    for (int k = 0; k < 4; ++k) s_ext[wid][k] = e[k];
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < wid; ++w) before += s_wsum[w];
+  if (b < nblocks) sc->offset[b] = before + incl - v;
+  if (threadIdx.x == 0) {
+    int base = 0;
+    float f[4] = {INFINITY, -INFINITY, INFINITY, -INFINITY};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      base += s_wsum[w];
+      f[0] = fminf(f[0], s_ext[w][0]);
+      f[1] = fmaxf(f[1], s_ext[w][1]);
+      f[2] = fminf(f[2], s_ext[w][2]);
+      f[3] = fmaxf(f[3], s_ext[w][3]);
+    }
+    // the float32 extremes are exact in float64 (the positions are float32)
+    *plan = plan_header(base, (double)f[0], (double)f[1], (double)f[2], (double)f[3],
+                        subdom_size, smoothing_coef, pct);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_tps_plan_write(const float* xs, const float* ys, const float* dx, const float* dy,
+                     int nvec, const fi_tps_plan* plan, double* cx, double* cy, float* ux,
+                     float* uy, int32_t* sel) {
+  constexpr int R = 4;
+  __shared__ int warp_off[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int s0, s1;
+  plan_chunk(nvec, s0, s1);
+  // the block's chunk in one contiguous segment per warp
+  const int seg = (((s1 - s0) + nw - 1) / nw + 31) & ~31;
+  const int w0 = min(s1, s0 + wid * seg), w1 = min(s1, w0 + seg);
+  int cnt = 0;
+  for (int i = w0 + lane; i < w1; i += 32) cnt += (isnan(dx[i]) || isnan(dy[i])) ? 0 : 1;
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) warp_off[wid] = cnt;
+  __syncthreads();
+  int pos = reinterpret_cast<const PlanScratch*>(reinterpret_cast<const unsigned char*>(plan) + 256)
+                ->offset[blockIdx.x];
+  for (int w = 0; w < wid; ++w) pos += warp_off[w];
+  for (int c0 = w0; c0 < w1; c0 += R * 32) {
+    float vx[R], vy[R], px[R], py[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = c0 + 32 * r + lane;
+      const bool in = i < w1;
+      vx[r] = in ? dx[i] : NAN;
+      vy[r] = in ? dy[i] : NAN;
+      px[r] = in ? xs[i] : 0.f;
+      py[r] = in ? ys[i] : 0.f;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = c0 + 32 * r + lane;
+      const bool ok = !(isnan(vx[r]) || isnan(vy[r]));
+      const unsigned bal = __ballot_sync(0xffffffffu, ok);
+      if (ok) {
+        const int at = pos + __popc(bal & ((1u << lane) - 1u));
+        cx[at] = f2d_exact(px[r]);
+        cy[at] = f2d_exact(py[r]);
+        ux[at] = vx[r];
+        uy[at] = vy[r];
+        if (sel) sel[at] = i;
+      }
+      pos += __popc(bal);
+    }
+  }
 }
 
 __global__ void k_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
@@ -1114,10 +1282,20 @@ extern "C" int fi_tps_plan_make(const float* xs, const float* ys, const float* d
                                 void* stream) {
   FI_REQUIRE(xs && ys && dx && dy && plan && cx && cy && ux && uy, "fi_tps_plan_make: null pointer");
   FI_REQUIRE(nvec > 0 && subdom_size > 0, "fi_tps_plan_make: bad sizes");
-  k_tps_plan<<<1, 1024, 0, (cudaStream_t)stream>>>(xs, ys, dx, dy, nvec, subdom_size,
-                                                   smoothing_coef, percent_buffer_area, plan, cx,
-                                                   cy, ux, uy, selection);
-  return check_launch("fi_tps_plan_make");
+  cudaStream_t s = (cudaStream_t)stream;
+  // one block for small passes; chunks of about 1024 vectors per block otherwise
+  const int nblocks = min(FI_TPS_PLAN_MAX_BLOCKS, (nvec + 1023) / 1024);
+  if (nblocks <= 4) {
+    k_tps_plan<<<1, 1024, 0, s>>>(xs, ys, dx, dy, nvec, subdom_size, smoothing_coef,
+                                  percent_buffer_area, plan, cx, cy, ux, uy, selection);
+    return check_launch("fi_tps_plan_make");
+  }
+  k_tps_plan_count<<<nblocks, 256, 0, s>>>(xs, ys, dx, dy, nvec, plan);
+  k_tps_plan_head<<<1, 1024, 0, s>>>(nblocks, subdom_size, smoothing_coef, percent_buffer_area,
+                                      plan);
+  k_tps_plan_write<<<nblocks, 256, 0, s>>>(xs, ys, dx, dy, nvec, plan, cx, cy, ux, uy,
+                                            selection);
+  return check_launch("fi_tps_plan_make", 3);
 }
 
 extern "C" int fi_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,

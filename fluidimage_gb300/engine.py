@@ -355,7 +355,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     u8_, i32_, i64_, f32_, f64_ = (torch.uint8, torch.int32, torch.int64, torch.float32,
                                    torch.float64)
     # the plan and the compacted centres; the host needs the plan header first
-    cA = _Carved(dev, [(C.sizeof(L.TpsPlan), u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
+    cA = _Carved(dev, [(L.TPS_PLAN_BYTES, u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
                        (nvec, f32_), (nvec, i32_)])
     plan, cx, cy, ux, uy, sel = cA.addr
     with _timed("fi_tps_plan_make"):
@@ -458,7 +458,7 @@ def run_griddata(xs, ys, dx, dy, nvec, grid, px, py, npts, stream):
     s = L.stream_handle(stream)
     ixvecs, iyvecs, nx, ny = grid
     u8_, i32_, f32_, f64_ = torch.uint8, torch.int32, torch.float32, torch.float64
-    cA = _Carved(dev, [(C.sizeof(L.TpsPlan), u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
+    cA = _Carved(dev, [(L.TPS_PLAN_BYTES, u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
                        (nvec, f32_), (nvec, i32_)])
     plan, cx, cy, ux, uy, sel = cA.addr
     # the compaction of the valid vectors (the subdomain layout it also computes is

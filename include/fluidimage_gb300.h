@@ -347,6 +347,14 @@ int fi_fix_static(const fi_fix_args* args, void* stream);
  * vectors, subdomain populations) are read back between stages.
  * ------------------------------------------------------------------------- */
 
+/*
+ * A TPS plan buffer (device memory) holds the header below at its start and, from
+ * byte 256, the scratch of the multi-block compaction: callers of fi_tps_plan_make
+ * provide FI_TPS_PLAN_BYTES bytes.
+ */
+#define FI_TPS_PLAN_MAX_BLOCKS 1024
+#define FI_TPS_PLAN_BYTES (256 + 24 * FI_TPS_PLAN_MAX_BLOCKS)
+
 /* Header of a TPS plan (device memory, written by fi_tps_plan). */
 typedef struct fi_tps_plan {
   int num_centers;      /* valid (non-NaN) vectors                        */
@@ -364,6 +372,7 @@ typedef struct fi_tps_plan {
  * the values ux, uy (float32) and, if not NULL, the original index of each
  * selected vector.  The header *plan is written in device memory; the host reads
  * num_centers, nb_subdomx, nb_subdomy and status from it before the next stages.
+ * plan points to FI_TPS_PLAN_BYTES bytes (header and compaction scratch).
  */
 int fi_tps_plan_make(const float* xs, const float* ys, const float* dx, const float* dy,
                      int nvec, int subdom_size, double smoothing_coef,

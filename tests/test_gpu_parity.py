@@ -329,7 +329,7 @@ def test_members_index_range_matches_full_scan(order):
     f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)  # noqa: E731
     tx, ty, tdx, tdy = f32(xs), f32(ys), f32(dx), f32(dy)
     n = xs.size
-    plan = torch.empty(C.sizeof(L.TpsPlan), dtype=torch.uint8, device=dev)
+    plan = torch.empty(L.TPS_PLAN_BYTES, dtype=torch.uint8, device=dev)
     cx = torch.empty(n, dtype=torch.float64, device=dev)
     cy = torch.empty(n, dtype=torch.float64, device=dev)
     ux = torch.empty(n, dtype=torch.float32, device=dev)
