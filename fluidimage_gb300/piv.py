@@ -11,6 +11,7 @@ false-vector removal and the TPS interpolation run on the GPU.
 
 from __future__ import annotations
 
+import threading
 import time
 
 import numpy as np
@@ -122,12 +123,18 @@ class WorkPIV:
     """
 
     @classmethod
-    def create_default_params(cls):
-        params = ParamContainer(tag="params")
+    def _complete_params_with_default(cls, params):
+        """Add this work's parameters to ``params`` (multipass.py:47-105): what a PIV
+        topology calls on its ``WorkVelocimetry`` class (topologies/piv.py:58-76)."""
         _complete_params_series(params)
         _complete_params_piv0(params)
         _complete_params_fix(params)
         _complete_params_multipass(params)
+
+    @classmethod
+    def create_default_params(cls):
+        params = ParamContainer(tag="params")
+        cls._complete_params_with_default(params)
         return params
 
     def __init__(self, params=None, keep_correls=False, device=None, verbose=False,
@@ -148,17 +155,33 @@ class WorkPIV:
         self.deform = deform
         self.device = device
         self.verbose = verbose
+        # nothing here touches CUDA: a topology builds its works in the parent process
+        # and a multi-process executor forks its workers afterwards (each worker then
+        # makes its own CUDA context on its first couple)
         self._pipelines = {}
+        self._lock = threading.Lock()
+
+    def __getstate__(self):
+        # pickled works (spawned workers) rebuild their pipelines on first use
+        state = self.__dict__.copy()
+        state["_pipelines"] = {}
+        del state["_lock"]
+        return state
+
+    def __setstate__(self, state):
+        self.__dict__.update(state)
+        self._lock = threading.Lock()
 
     # --------------------------------------------------------------------
     def _pipeline(self, imshape, dtype):
         key = (tuple(imshape), np.dtype(dtype).str)
-        if key not in self._pipelines:
-            self._pipelines[key] = PIVPipeline(self.params, imshape, dtype, device=self.device,
-                                               keep_correls=self.keep_correls,
-                                               interp_last=self.interp_last,
-                                               deform=self.deform)
-        return self._pipelines[key]
+        with self._lock:
+            if key not in self._pipelines:
+                self._pipelines[key] = PIVPipeline(
+                    self.params, imshape, dtype, device=self.device,
+                    keep_correls=self.keep_correls, interp_last=self.interp_last,
+                    deform=self.deform)
+            return self._pipelines[key]
 
     def _xy_offsets(self):
         strcrop = self.params.mask.strcrop
@@ -175,7 +198,11 @@ class WorkPIV:
         return pipe.run(im0, im1, stream=stream)
 
     def calcul(self, couple):
-        """Compute a multipass PIV field from a couple of images."""
+        """Compute a multipass PIV field from a couple of images.
+
+        Several host threads may call it at once (a topology's thread executors run
+        the "compute piv" work that way, topologies/piv.py:143-149): each thread runs
+        its couples on a CUDA stream of its own, so their kernels overlap."""
         import torch
 
         if isinstance(couple, dict):
@@ -184,11 +211,13 @@ class WorkPIV:
             raise ValueError(f"not isinstance(couple, ArrayCouple), {type(couple) = }")
         couple.apply_mask(self.params.mask)
         im0, im1 = couple.get_arrays()
-        dev = torch.device(self.device or "cuda")
-        t0 = _to_device(im0, dev)
-        t1 = _to_device(im1, dev)
-        outs = self.calcul_device(t0, t1)
-        return self.results_to_host(outs, couple)
+        dev = _cuda_device(self.device)
+        stream = _thread_stream(dev)
+        with torch.cuda.stream(stream):
+            t0 = _to_device(im0, dev)
+            t1 = _to_device(im1, dev)
+            outs = self.calcul_device(t0, t1, stream=stream)
+            return self.results_to_host(outs, couple)
 
     def calcul_from_arrays(self, *arrays, names=None):
         names = [f"array{i}" for i in range(len(arrays))]
@@ -216,12 +245,11 @@ class WorkPIV:
         (topologies/piv.py:143-151) for this work.
         """
         import collections
-        import threading
 
         import torch
         from concurrent.futures import ThreadPoolExecutor
 
-        dev = torch.device(self.device or "cuda")
+        dev = _cuda_device(self.device)
         local = threading.local()
 
         def run(couple):
@@ -471,6 +499,37 @@ def _np_dtype(t):
     import torch
 
     return {torch.uint8: np.uint8, torch.int16: np.uint16, torch.float32: np.float32}[t.dtype]
+
+
+_THREAD = threading.local()
+
+
+def _cuda_device(device):
+    """The torch device of a work; refuses to start CUDA in a process forked from one
+    that had already started it (a forked child cannot use its parent's context)."""
+    import torch
+
+    in_bad_fork = getattr(torch.cuda, "_is_in_bad_fork", lambda: False)
+    if in_bad_fork():
+        raise RuntimeError(
+            "CUDA was initialised in the parent of this forked process: create the "
+            "work in the parent but run it only in the workers (the work itself "
+            "initialises nothing before its first couple), or start the workers "
+            "with 'spawn'")
+    return torch.device(device or "cuda")
+
+
+def _thread_stream(dev):
+    """The CUDA stream of the calling host thread on ``dev`` (made on first use)."""
+    import torch
+
+    streams = getattr(_THREAD, "streams", None)
+    if streams is None:
+        streams = _THREAD.streams = {}
+    key = (dev.type, dev.index if dev.index is not None else torch.cuda.current_device())
+    if key not in streams:
+        streams[key] = torch.cuda.Stream(device=dev)
+    return streams[key]
 
 
 def _to_device(a, dev):
