@@ -205,10 +205,7 @@ class WorkPIV:
         its couples on a CUDA stream of its own, so their kernels overlap."""
         import torch
 
-        if isinstance(couple, dict):
-            couple = ArrayCouple(**couple)
-        if not isinstance(couple, ArrayCouple):
-            raise ValueError(f"not isinstance(couple, ArrayCouple), {type(couple) = }")
+        couple = _as_couple(couple)
         couple.apply_mask(self.params.mask)
         im0, im1 = couple.get_arrays()
         dev = _cuda_device(self.device)
@@ -267,11 +264,7 @@ class WorkPIV:
         pending = collections.deque()
         with ThreadPoolExecutor(max_workers=nstreams) as pool:
             for couple in couples:
-                if isinstance(couple, dict):
-                    couple = ArrayCouple(**couple)
-                if not isinstance(couple, ArrayCouple):
-                    raise ValueError(
-                        f"not isinstance(couple, ArrayCouple), {type(couple) = }")
+                couple = _as_couple(couple)
                 couple.apply_mask(self.params.mask)
                 im0, _ = couple.get_arrays()
                 self._pipeline(tuple(im0.shape), _host_dtype(im0))  # built here, once
@@ -502,6 +495,19 @@ def _np_dtype(t):
 
 
 _THREAD = threading.local()
+
+
+def _as_couple(couple):
+    """A couple of arrays: this package's ``ArrayCouple``, one built from a dict of
+    its arguments, or a couple object of an installed fluidimage (what the couples
+    queue of its PIV topology holds, topologies/piv.py:203-226: any object with
+    ``get_arrays`` and ``apply_mask``)."""
+    if isinstance(couple, dict):
+        couple = ArrayCouple(**couple)
+    if not isinstance(couple, ArrayCouple) and not (
+            hasattr(couple, "get_arrays") and hasattr(couple, "apply_mask")):
+        raise ValueError(f"not isinstance(couple, ArrayCouple), {type(couple) = }")
+    return couple
 
 
 def _cuda_device(device):
