@@ -167,6 +167,10 @@ _SIGNATURES = {
     "fi_equalize_hist_int": (C.c_int, [P, C.c_int, C.c_int64, P, P, P, P]),
     "fi_equalize_hist_float": (C.c_int, [P, C.c_int, C.c_int64, P, C.c_int, C.c_double,
                                          C.c_double, P, P, P, P, P]),
+    "fi_clahe": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                           P, P, P]),
+    "fi_to_ubyte": (C.c_int, [P, C.c_int, C.c_int64, P, P]),
+    "fi_rank_equalize": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P, P]),
     "fi_gaussian_filter": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P]),
     "fi_sharpen_combine": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_double, P, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),

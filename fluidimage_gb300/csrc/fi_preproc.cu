@@ -685,6 +685,229 @@ static int grid_for(int64_t count) {
   return (int)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
 }
 
+// ------------------------------------------------------------------ CLAHE
+// Contrast-limited adaptive histogram equalisation (Zuiderveld, Graphics Gems IV,
+// 1994) in the variant of scikit-image 0.24 (equalize_adapthist / _clahe /
+// clip_histogram / map_histogram), the core of equalize_hist_adapt
+// (_toolbox_py.py:383-409).  Grey levels: 2^14.
+constexpr int CLAHE_GREYS = 16384;
+constexpr int CLAHE_NT = 256;
+
+// numpy 'reflect' padding index for i >= 0 (mirror without repeating the edge)
+__device__ __forceinline__ int reflect_index(int i, int n) {
+  if (n == 1) return 0;
+  const int period = 2 * (n - 1);
+  const int m = i % period;
+  return m >= n ? period - m : m;
+}
+
+// the grey level of a pixel of the image rescaled to [0, 2^14 - 1]: astype(uint16)
+// (truncation), clamped into the table range
+__device__ __forceinline__ int clahe_level(const void* y, int dtype, int64_t e) {
+  const double v = load_d(y, dtype, e);
+  if (!(v >= 0.0)) return 0;
+  if (v >= (double)(CLAHE_GREYS - 1)) return CLAHE_GREYS - 1;
+  return (int)v;
+}
+
+// sum over the block of one int per thread (all threads call it); sh: 33 ints
+__device__ __forceinline__ int block_sum_int(int v, int* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[32] = v;
+  }
+  __syncthreads();
+  v = sh[32];
+  __syncthreads();
+  return v;
+}
+
+// One block per contextual region (i, j) of k0 x k1 pixels starting at image pixel
+// (i k0, j k1), the image extended at its end by reflection: histogram of the bins
+// level / bin_size, clipped at clim with the excess handed out again, and the map
+// min(cdf * scale, 2^14 - 1) truncated, stored as uint16 (maps[(i m1 + j) nbins + b]).
+// The redistribution: excess // nbins to every bin below clim - that, the bins
+// between that and clim filled to it, then one count at a time to the bins below
+// clim in strides of max(1, (bins below clim) // excess) from each start bin in turn
+// until no excess is left or a full pass hands out nothing (bounded: each pass that
+// continues hands out at least one count of an excess of at most k0 k1).
+__global__ void __launch_bounds__(CLAHE_NT)
+    k_clahe_maps(const void* levels, int dtype, int s0, int s1, int k0, int k1, int m1,
+                 int nbins, int bin_size, int clim, double scale, uint16_t* maps) {
+  extern __shared__ int hist[];
+  __shared__ int red[33];
+  const int i = blockIdx.x / m1, j = blockIdx.x % m1;
+  for (int b = threadIdx.x; b < nbins; b += CLAHE_NT) hist[b] = 0;
+  __syncthreads();
+  const int npix = k0 * k1;
+  for (int t = threadIdx.x; t < npix; t += CLAHE_NT) {
+    const int r = t / k1, c = t - r * k1;
+    const int row = reflect_index(i * k0 + r, s0), col = reflect_index(j * k1 + c, s1);
+    atomicAdd(&hist[clahe_level(levels, dtype, (int64_t)row * s1 + col) / bin_size], 1);
+  }
+  __syncthreads();
+  // the bins above the limit are cut
+  int part = 0;
+  for (int b = threadIdx.x; b < nbins; b += CLAHE_NT) {
+    const int h = hist[b];
+    if (h > clim) {
+      part += h - clim;
+      hist[b] = clim;
+    }
+  }
+  int excess = block_sum_int(part, red);
+  const int incr = excess / nbins, upper = clim - incr;
+  part = 0;
+  for (int b = threadIdx.x; b < nbins; b += CLAHE_NT) {
+    int h = hist[b];
+    if (h < upper) {
+      h += incr;
+      part += incr;
+    }
+    if (h >= upper && h < clim) {
+      part += clim - h;
+      h = clim;
+    }
+    hist[b] = h;
+  }
+  excess -= block_sum_int(part, red);
+  while (excess > 0) {
+    const int before = excess;
+    for (int start = 0; start < nbins; ++start) {
+      int under = 0;
+      for (int b = threadIdx.x; b < nbins; b += CLAHE_NT) under += hist[b] < clim;
+      under = block_sum_int(under, red);
+      const int stride = max(1, under / excess);
+      int given = 0;
+      for (int p = start + threadIdx.x * stride; p < nbins; p += CLAHE_NT * stride) {
+        if (hist[p] < clim) {
+          hist[p] += 1;
+          ++given;
+        }
+      }
+      excess -= block_sum_int(given, red);
+      if (excess <= 0) break;
+    }
+    if (before == excess) break;
+  }
+  // cumulative counts (each thread a run of bins) and the grey-level map
+  const int per = (nbins + CLAHE_NT - 1) / CLAHE_NT;
+  const int b0 = min(nbins, (int)threadIdx.x * per), b1 = min(nbins, b0 + per);
+  int local = 0;
+  for (int b = b0; b < b1; ++b) local += hist[b];
+  // exclusive scan of the per-thread sums
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) red[wid] = incl;
+  __syncthreads();
+  int before_warp = 0;
+  for (int w = 0; w < wid; ++w) before_warp += red[w];
+  int run = before_warp + incl - local;
+  uint16_t* map = maps + (int64_t)blockIdx.x * nbins;
+  for (int b = b0; b < b1; ++b) {
+    run += hist[b];
+    const double v = fmin(__dmul_rn((double)run, scale), (double)(CLAHE_GREYS - 1));
+    map[b] = (uint16_t)(int)v;
+  }
+}
+
+// Each pixel: the blend of the maps of the four regions around it.  In the image
+// shifted by half a region (k0 / 2, k1 / 2), the pixel sits in block (bi, bj) at
+// (r, c); the coefficients are r / k0 and c / k1 (float64), the blocks' maps those of
+// regions (bi - 1 + e0, bj - 1 + e1) clamped to the grid.  Each term map * weight is
+// rounded to float32 and added in float32 in the order (0, 0), (0, 1), (1, 0),
+// (1, 1); the sum is truncated to an integer level, written in the image's float type.
+__global__ void k_clahe_blend(const void* levels, int dtype, int s0, int s1, int k0, int k1,
+                              int m0, int m1, int nbins, int bin_size, const uint16_t* maps,
+                              void* out) {
+  const int64_t count = (int64_t)s0 * s1;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int y = (int)(e / s1), x = (int)(e - (int64_t)y * s1);
+    const int py = y + k0 / 2, px = x + k1 / 2;
+    const int bi = py / k0, bj = px / k1;
+    const double cy = __ddiv_rn((double)(py - bi * k0), (double)k0);
+    const double cx = __ddiv_rn((double)(px - bj * k1), (double)k1);
+    const int b = clahe_level(levels, dtype, e) / bin_size;
+    float acc = 0.f;
+#pragma unroll
+    for (int e0 = 0; e0 < 2; ++e0) {
+      const int ri = min(max(bi + e0 - 1, 0), m0 - 1);
+      const double wy = e0 ? cy : __dsub_rn(1.0, cy);
+#pragma unroll
+      for (int e1 = 0; e1 < 2; ++e1) {
+        const int rj = min(max(bj + e1 - 1, 0), m1 - 1);
+        const double wx = e1 ? cx : __dsub_rn(1.0, cx);
+        const int mapped = maps[((int64_t)ri * m1 + rj) * nbins + b];
+        acc = __fadd_rn(acc, __double2float_rn(__dmul_rn((double)mapped, __dmul_rn(wx, wy))));
+      }
+    }
+    const int level = (int)acc;
+    if (dtype == FI_PRE_F32)
+      static_cast<float*>(out)[e] = (float)level;
+    else
+      static_cast<double*>(out)[e] = (double)level;
+  }
+}
+
+// scikit-image's img_as_ubyte of a float image in [0, 1]: rint(x * 255) in the
+// image's float type, clipped to [0, 255] (NaN gives 0).
+__global__ void k_to_ubyte(const void* in, int dtype, int64_t count, uint8_t* out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double r;
+    if (dtype == FI_PRE_F32)
+      r = (double)rintf(__fmul_rn(static_cast<const float*>(in)[e], 255.f));
+    else
+      r = rint(__dmul_rn(static_cast<const double*>(in)[e], 255.0));
+    out[e] = (r >= 0.0) ? (uint8_t)(int)fmin(r, 255.0) : (uint8_t)0;
+  }
+}
+
+// scikit-image's filters.rank.equalize over disk(radius) of a uint8 image: of the
+// disk's pixels inside the image (pop), the count n of values at most the centre's;
+// out = (255 n) / pop truncated.  The disk's half-width per row, floor(sqrt(r^2 -
+// dy^2)), is found in integers (one per row, in shared memory); rows are scanned as
+// runs clipped to the image.
+__global__ void k_rank_equalize(const uint8_t* __restrict__ in, int ny, int nx, int radius,
+                                uint8_t* __restrict__ out) {
+  extern __shared__ int halfw[];
+  for (int d = threadIdx.x; d <= 2 * radius; d += blockDim.x) {
+    const int dy = d - radius;
+    const int q = radius * radius - dy * dy;
+    int w = (int)sqrt((double)q);
+    while (w > 0 && w * w > q) --w;
+    while ((w + 1) * (w + 1) <= q) ++w;
+    halfw[d] = w;
+  }
+  __syncthreads();
+  const int64_t count = (int64_t)ny * nx;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int y = (int)(e / nx), x = (int)(e - (int64_t)y * nx);
+    const int g = in[e];
+    int pop = 0, n = 0;
+    const int d0 = max(0, radius - y), d1 = min(2 * radius, radius + ny - 1 - y);
+    for (int d = d0; d <= d1; ++d) {
+      const int w = halfw[d];
+      const int xa = max(0, x - w), xb = min(nx - 1, x + w);
+      const uint8_t* row = in + (int64_t)(y + d - radius) * nx;
+      pop += xb - xa + 1;
+      for (int xx = xa; xx <= xb; ++xx) n += __ldg(row + xx) <= g;
+    }
+    out[e] = (uint8_t)(int)__ddiv_rn((double)(255 * n), (double)pop);
+  }
+}
+
 }  // namespace fi
 
 using namespace fi;
@@ -871,4 +1094,47 @@ extern "C" int fi_equalize_hist_float(const void* in, int dtype, int64_t count, 
   k_cdf<<<1, 1024, 0, s>>>(hist, nbins, dtype == FI_PRE_F32 ? 1 : 0, cdf);
   k_interp<<<grid_for(count), 256, 0, s>>>(in, dtype, count, centers, cdf, nbins, out);
   return check_launch("fi_equalize_hist_float", 3);
+}
+
+extern "C" int fi_clahe(const void* levels, int dtype, int ny, int nx, int k0, int k1,
+                        int nbins, double clip_limit, uint16_t* maps, void* out, void* stream) {
+  FI_REQUIRE(levels && maps && out, "fi_clahe: null pointer");
+  FI_REQUIRE(dtype == FI_PRE_F32 || dtype == FI_PRE_F64, "fi_clahe: bad dtype %d", dtype);
+  FI_REQUIRE(ny >= 1 && nx >= 1 && k0 >= 1 && k1 >= 1, "fi_clahe: bad sizes");
+  FI_REQUIRE(nbins >= 1 && nbins <= 12000, "fi_clahe: nbins must be in [1, 12000], not %d",
+             nbins);
+  FI_REQUIRE((int64_t)k0 * k1 <= (1 << 24), "fi_clahe: kernel of %d x %d too large", k0, k1);
+  const int m0 = (ny + k0 - 1) / k0, m1 = (nx + k1 - 1) / k1;
+  FI_REQUIRE((int64_t)m0 * m1 <= INT32_MAX, "fi_clahe: too many regions");
+  const int npix = k0 * k1;
+  const double lim = clip_limit * (double)npix;
+  const int clim = clip_limit > 0.0 ? (int)(lim > 1.0 ? lim : 1.0) : npix;
+  const double scale = (double)(CLAHE_GREYS - 1) / (double)npix;
+  const int bin_size = 1 + CLAHE_GREYS / nbins;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_clahe_maps<<<m0 * m1, CLAHE_NT, sizeof(int) * nbins, s>>>(
+      levels, dtype, ny, nx, k0, k1, m1, nbins, bin_size, clim, scale, maps);
+  const int64_t count = (int64_t)ny * nx;
+  k_clahe_blend<<<grid_for(count), 256, 0, s>>>(levels, dtype, ny, nx, k0, k1, m0, m1, nbins,
+                                               bin_size, maps, out);
+  return check_launch("fi_clahe", 2);
+}
+
+extern "C" int fi_to_ubyte(const void* in, int dtype, int64_t count, uint8_t* out,
+                           void* stream) {
+  FI_REQUIRE(in && out && count > 0, "fi_to_ubyte: bad arguments");
+  FI_REQUIRE(dtype == FI_PRE_F32 || dtype == FI_PRE_F64, "fi_to_ubyte: bad dtype %d", dtype);
+  k_to_ubyte<<<grid_for(count), 256, 0, (cudaStream_t)stream>>>(in, dtype, count, out);
+  return check_launch("fi_to_ubyte");
+}
+
+extern "C" int fi_rank_equalize(const uint8_t* in, int ny, int nx, int radius, uint8_t* out,
+                                void* stream) {
+  FI_REQUIRE(in && out && ny >= 1 && nx >= 1, "fi_rank_equalize: bad arguments");
+  FI_REQUIRE(radius >= 0 && radius <= 4096, "fi_rank_equalize: radius %d out of [0, 4096]",
+             radius);
+  const int64_t count = (int64_t)ny * nx;
+  k_rank_equalize<<<grid_for(count), 256, sizeof(int) * (2 * radius + 1),
+                    (cudaStream_t)stream>>>(in, ny, nx, radius, out);
+  return check_launch("fi_rank_equalize");
 }

@@ -24,9 +24,10 @@ works/preproc/_toolbox_py.py:
   its gaussian method, ``exposure.equalize_hist``): their published definitions, in
   the dtypes scikit-image and numpy 2 use.
 
-The adaptive equalisations (``equalize_hist_adapt``, CLAHE, and ``equalize_hist_local``,
-a rank filter over a disk), also built on scikit-image, keep their parameters but
-raise ``NotImplementedError`` when enabled.
+The adaptive equalisations, also built on scikit-image, are restated the same way:
+``equalize_hist_adapt`` (:383-409, ``exposure.equalize_adapthist``: CLAHE on 2^14
+grey levels, ``fi_clahe``) and ``equalize_hist_local`` (:412-438,
+``filters.rank.equalize`` over ``morphology.disk``: ``fi_rank_equalize``).
 """
 
 from __future__ import annotations
@@ -509,14 +510,87 @@ def sharpen(img, sigma1=3.0, sigma2=1.0, alpha=30.0):
     return out
 
 
-def _not_provided(name):
-    def tool(img, **kwargs):
-        raise NotImplementedError(
-            f"preprocessing tool {name!r} is not provided by this backend (upstream builds it "
-            "on scikit-image)")
+#: grey levels of scikit-image's CLAHE (2^14)
+NR_OF_GRAY = 2 ** 14
 
-    tool.__name__ = name
-    return tool
+
+def _host_extremes(x):
+    """(min, max) of a device image as Python floats (upstream's ``img.min()``,
+    ``img.max()`` passed on as an output range)."""
+    part = _extremes(x).cpu().numpy()
+    return float(part[:_NPARTS].min()), float(part[_NPARTS:].max())
+
+
+def _kernel_size(window_shape, shape):
+    """``kernel_size`` as scikit-image's equalize_adapthist takes it: None gives
+    1/8 of each dimension (at least 1), a number is used for both dimensions."""
+    if window_shape is None:
+        return tuple(max(s // 8, 1) for s in shape)
+    if np.isscalar(window_shape):
+        return (int(window_shape),) * 2
+    if len(window_shape) != 2:
+        raise ValueError(f"Incorrect value of `kernel_size`: {window_shape}")
+    return tuple(int(k) for k in window_shape)
+
+
+@_per_image
+def equalize_hist_adapt(img, window_shape=(10, 10), nbins=256):
+    """Contrast-limited adaptive histogram equalisation (_toolbox_py.py:383-409;
+    scikit-image 0.24's exposure.equalize_adapthist with kernel_size=window_shape,
+    clip_limit 0.01): the image rescaled to [0, 1], then to grey levels
+    [0, 2^14 - 1] (truncated), ``fi_clahe``, rescaled to [0, 1] and back to the
+    image's [min, max]; float32 for float32 images, float64 otherwise; per image
+    for a stack."""
+    x, single = _stack(img)
+    outs = [_clahe_one(x[i], window_shape, nbins) for i in range(x.shape[0])]
+    return outs[0] if single else _torch().stack(outs)
+
+
+def _clahe_one(img, window_shape, nbins):
+    torch = _torch()
+    x = img.contiguous()
+    ny, nx = x.shape
+    k0, k1 = _kernel_size(window_shape, (ny, nx))
+    if k0 < 1 or k1 < 1:
+        raise ValueError(f"Incorrect value of `kernel_size`: {window_shape}")
+    lo, hi = _host_extremes(x)
+    levels = _rescale_one(_rescale_one(x, 0, 1), 0, NR_OF_GRAY - 1)
+    m0, m1 = -(-ny // k0), -(-nx // k1)
+    maps = torch.empty(m0 * m1 * int(nbins), dtype=torch.int16, device=x.device)
+    eq = torch.empty_like(levels)
+    L.check(L.load().fi_clahe(L.ptr(levels), _DT[_dtype_of(levels)], ny, nx, k0, k1, int(nbins),
+                              0.01, L.ptr(maps), L.ptr(eq), L.stream_handle()), "fi_clahe")
+    return _rescale_one(_rescale_one(eq, 0, 1), lo, hi)
+
+
+@_per_image
+def equalize_hist_local(img, radius=10):
+    """Local histogram equalisation over a disk (_toolbox_py.py:412-438;
+    scikit-image's filters.rank.equalize with morphology.disk(radius)): the image
+    rescaled to [0, 1], to uint8 (img_as_ubyte), the rank equalisation
+    (``fi_rank_equalize``), rescaled to the image's [min, max] (float64); per image
+    for a stack."""
+    x, single = _stack(img)
+    outs = [_local_one(x[i], radius) for i in range(x.shape[0])]
+    return outs[0] if single else _torch().stack(outs)
+
+
+def _local_one(img, radius):
+    torch = _torch()
+    if int(radius) != radius or radius < 0:
+        raise ValueError(f"radius must be a non-negative integer, not {radius!r}")
+    x = img.contiguous()
+    ny, nx = x.shape
+    lo, hi = _host_extremes(x)
+    unit = _rescale_one(x, 0, 1)
+    lib, s = L.load(), L.stream_handle()
+    u8 = torch.empty((ny, nx), dtype=torch.uint8, device=x.device)
+    L.check(lib.fi_to_ubyte(L.ptr(unit), _DT[_dtype_of(unit)], unit.numel(), L.ptr(u8), s),
+            "fi_to_ubyte")
+    eq = torch.empty_like(u8)
+    L.check(lib.fi_rank_equalize(L.ptr(u8), ny, nx, int(radius), L.ptr(eq), s),
+            "fi_rank_equalize")
+    return _rescale_one(eq, lo, hi)
 
 
 TOOLS = {
@@ -532,10 +606,11 @@ TOOLS = {
     "gamma_correction": gamma_correction,
     "adaptive_threshold": adaptive_threshold,
     "equalize_hist_global": equalize_hist_global,
+    "equalize_hist_adapt": equalize_hist_adapt,
+    "equalize_hist_local": equalize_hist_local,
     "sharpen": sharpen,
 }
-for _name in AVAILABLE_TOOLS:
-    TOOLS.setdefault(_name, _not_provided(_name))
+assert set(TOOLS) == set(AVAILABLE_TOOLS)
 
 
 class PreprocToolsGB300:

@@ -676,6 +676,36 @@ int fi_equalize_hist_float(const void* in, int dtype, int64_t count, const void*
                            double* cdf, void* out, void* stream);
 
 /*
+ * The core of equalize_hist_adapt (_toolbox_py.py:383-409; scikit-image 0.24's
+ * exposure.equalize_adapthist, CLAHE): levels = the (ny, nx) image rescaled to
+ * [0, 2^14 - 1] (float32 or float64, dtype), truncated to grey levels; contextual
+ * regions of k0 x k1 pixels (the image extended at its end by reflection), each
+ * region's histogram of nbins bins (1 <= nbins <= 12000) clipped at
+ * max(clip_limit k0 k1, 1) with the excess redistributed, its grey-level map (maps:
+ * ceil(ny / k0) * ceil(nx / k1) * nbins uint16 scratch), and the bilinear blend of
+ * the four maps around each pixel summed in float32 and truncated: out (same dtype
+ * as levels) holds the equalised grey levels.
+ */
+int fi_clahe(const void* levels, int dtype, int ny, int nx, int k0, int k1, int nbins,
+             double clip_limit, uint16_t* maps, void* out, void* stream);
+
+/*
+ * scikit-image's img_as_ubyte of a float image in [0, 1] (the step before the rank
+ * equalisation of equalize_hist_local, _toolbox_py.py:433-435): rint(x * 255) in the
+ * image's float type, clipped to [0, 255].
+ */
+int fi_to_ubyte(const void* in, int dtype, int64_t count, uint8_t* out, void* stream);
+
+/*
+ * equalize_hist_local's rank equalisation (_toolbox_py.py:412-438; scikit-image's
+ * filters.rank.equalize over morphology.disk(radius)) of a (ny, nx) uint8 image: out
+ * = 255 n / pop truncated, pop the disk's pixels inside the image, n those at most
+ * the centre pixel.
+ */
+int fi_rank_equalize(const uint8_t* in, int ny, int nx, int radius, uint8_t* out,
+                     void* stream);
+
+/*
  * scipy.ndimage.gaussian_filter of each image of a (nt, ny, nx) stack (axis y then x;
  * the call of sharpen, _toolbox_py.py:486-487): one symmetric 1-D correlation per
  * axis in float64 ('reflect' boundaries; out = w_0 x_0, then the tap pairs from the

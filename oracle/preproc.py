@@ -207,3 +207,175 @@ def equalize_hist_global(img, nbins=256):
         return out.astype(np.float32 if im.dtype == np.float32 else np.float64, copy=False)
 
     return _per_image(one, img)
+
+
+# ---------------------------------------------------------------- adaptive equalisation
+#: grey levels of scikit-image's CLAHE (exposure/_adapthist.py: NR_OF_GRAY = 2**14)
+NR_OF_GRAY = 2 ** 14
+
+
+def _rescale_one(im, minima, maxima):
+    return rescale_intensity(im, minima, maxima)
+
+
+def clip_histogram(hist, clim):
+    """Contrast limiting of one contextual-region histogram (Zuiderveld, "Contrast
+    Limited Adaptive Histogram Equalization", Graphics Gems IV, 1994, in the
+    variant of scikit-image 0.24's ``clip_histogram``): bins above the limit are
+    cut and the excess is handed out again — first ``excess // nbins`` to every
+    bin below ``clim - that``, bins between that and the limit filled to it, then
+    one count at a time to bins below the limit, in strides of
+    ``max(1, (bins below the limit) // excess)`` from every start bin in turn,
+    until no excess is left or a full pass hands out nothing."""
+    h = np.array(hist, dtype=np.int64)
+    nb = h.size
+    excess = int(np.maximum(h - clim, 0).sum())
+    h = np.minimum(h, clim)
+    incr = excess // nb
+    upper = clim - incr
+    for b in range(nb):
+        if h[b] < upper:
+            h[b] += incr
+            excess -= incr
+        if upper <= h[b] < clim:
+            excess -= clim - h[b]
+            h[b] = clim
+    while excess > 0:
+        before = excess
+        for start in range(nb):
+            under = h < clim
+            stride = max(1, int(np.count_nonzero(under)) // excess)
+            given = 0
+            for p in range(start, nb, stride):
+                if under[p]:
+                    h[p] += 1
+                    given += 1
+            excess -= given
+            if excess <= 0:
+                break
+        if before == excess:
+            break
+    return h
+
+
+def _reflect(idx, size):
+    """numpy's 'reflect' padding index (mirror without repeating the edge)."""
+    if size == 1:
+        return np.zeros_like(idx)
+    period = 2 * (size - 1)
+    m = np.mod(idx, period)
+    return np.where(m >= size, period - m, m)
+
+
+def clahe_levels(v, kernel_size, nbins, clip_limit=0.01):
+    """scikit-image 0.24's ``_clahe`` restated (exposure/_adapthist.py) on a 2-D
+    image ``v`` of grey levels in [0, NR_OF_GRAY): the image, extended at its end
+    by reflection to whole regions of ``kernel_size``, is cut into contextual
+    regions; each region's histogram of ``v // (1 + NR_OF_GRAY // nbins)`` is
+    clipped at ``max(clip_limit * region size, 1)`` (truncated) and turned into the
+    grey-level map ``min(cdf * ((NR_OF_GRAY - 1) / region size), NR_OF_GRAY - 1)``
+    (float64, truncated); each pixel takes the bilinear blend of the maps of the
+    four regions around it (coefficients ``r / k`` from the pixel's place in the
+    block shifted by half a region, edge maps repeated), each term rounded to
+    float32 and summed in float32 in the order (0, 0), (0, 1), (1, 0), (1, 1), the
+    sum truncated to uint16."""
+    s0, s1 = v.shape
+    k0, k1 = (int(k) for k in kernel_size)
+    m0, m1 = -(-s0 // k0), -(-s1 // k1)
+    npix = k0 * k1
+    clim = int(max(clip_limit * npix, 1)) if clip_limit > 0 else npix
+    bins = v.astype(np.int64) // (1 + NR_OF_GRAY // nbins)
+    ext = bins[np.ix_(_reflect(np.arange(m0 * k0), s0), _reflect(np.arange(m1 * k1), s1))]
+    scale = np.float64(NR_OF_GRAY - 1) / np.float64(npix)
+    maps = np.empty((m0, m1, nbins), np.int64)
+    for i in range(m0):
+        for j in range(m1):
+            region = ext[i * k0:(i + 1) * k0, j * k1:(j + 1) * k1].ravel()
+            h = clip_histogram(np.bincount(region, minlength=nbins), clim)
+            cdf = np.cumsum(h).astype(np.float64)
+            maps[i, j] = np.minimum(cdf * scale, NR_OF_GRAY - 1).astype(np.int64)
+    yy, xx = np.meshgrid(np.arange(s0), np.arange(s1), indexing="ij")
+    py, px = yy + k0 // 2, xx + k1 // 2
+    bi, bj = py // k0, px // k1
+    cy = (py - bi * k0) / np.float64(k0)
+    cx = (px - bj * k1) / np.float64(k1)
+    out = np.zeros((s0, s1), np.float32)
+    for e0 in (0, 1):
+        for e1 in (0, 1):
+            ri = np.clip(bi + e0 - 1, 0, m0 - 1)
+            rj = np.clip(bj + e1 - 1, 0, m1 - 1)
+            mapped = maps[ri, rj, bins]
+            w = (cx if e1 else 1.0 - cx) * (cy if e0 else 1.0 - cy)
+            out += (mapped * w).astype(np.float32)
+    return out.astype(np.uint16)
+
+
+def equalize_hist_adapt(img, window_shape=(10, 10), nbins=256):
+    """_toolbox_py.py:383-409: the image rescaled to [0, 1], scikit-image's
+    ``exposure.equalize_adapthist`` (kernel_size=window_shape, clip_limit 0.01:
+    rescaled to grey levels [0, NR_OF_GRAY - 1] and truncated, ``clahe_levels``,
+    rescaled to [0, 1] in the float type), rescaled back to the image's [min, max].
+    float32 images stay float32, others give float64."""
+
+    def one(im):
+        ft = np.float32 if im.dtype == np.float32 else np.float64
+        if window_shape is None:  # scikit-image: 1/8 of each dimension
+            kernel = tuple(max(s // 8, 1) for s in im.shape)
+        elif np.isscalar(window_shape):
+            kernel = (int(window_shape),) * 2
+        else:
+            kernel = tuple(int(k) for k in window_shape)
+        lo, hi = im.min(), im.max()
+        y = _rescale_one(_rescale_one(im, 0, 1), 0, NR_OF_GRAY - 1)
+        levels = clahe_levels(y.astype(np.uint16), kernel, nbins)
+        z = _rescale_one(levels.astype(ft), 0, 1)
+        return _rescale_one(z, lo, hi)
+
+    return _per_image(one, img)
+
+
+def disk(radius):
+    """scikit-image's ``morphology.disk(radius)``: x^2 + y^2 <= radius^2 on the
+    (2 radius + 1)^2 grid."""
+    r = np.arange(-radius, radius + 1)
+    return ((r[:, None] ** 2 + r[None, :] ** 2) <= radius ** 2).astype(np.uint8)
+
+
+def to_ubyte(y):
+    """scikit-image's ``img_as_ubyte`` of a float image in [0, 1]: rint(y * 255)
+    computed in the image's float type, clipped to [0, 255]."""
+    prod = np.multiply(y, 255, dtype=y.dtype)
+    return np.clip(np.rint(prod), 0, 255).astype(np.uint8)
+
+
+def rank_equalize(u8, footprint):
+    """scikit-image's ``filters.rank.equalize`` of a uint8 image: at each pixel, of
+    the footprint's pixels inside the image (``pop``), the number ``n`` whose value
+    is at most the centre's; the output is ``(256 - 1) * n / pop`` truncated to
+    uint8."""
+    s0, s1 = u8.shape
+    fr = footprint.shape[0] // 2
+    g = u8.astype(np.int64)
+    n = np.zeros((s0, s1), np.int64)
+    pop = np.zeros((s0, s1), np.int64)
+    pad = np.full((s0 + 2 * fr, s1 + 2 * fr), -1, np.int64)
+    pad[fr:fr + s0, fr:fr + s1] = g
+    for dy, dx in zip(*np.nonzero(footprint)):
+        win = pad[dy:dy + s0, dx:dx + s1]
+        inside = win >= 0
+        pop += inside
+        n += inside & (win <= g)
+    return ((255 * n) / pop.astype(np.float64)).astype(np.uint8)
+
+
+def equalize_hist_local(img, radius=10):
+    """_toolbox_py.py:412-438: the image rescaled to [0, 1], to uint8
+    (``to_ubyte``), ``rank_equalize`` over ``disk(radius)``, rescaled to the image's
+    [min, max] (float64)."""
+
+    def one(im):
+        lo, hi = im.min(), im.max()
+        u8 = to_ubyte(_rescale_one(im, 0, 1))
+        return _rescale_one(rank_equalize(u8, disk(radius)), lo, hi)
+
+    return _per_image(one, img)

@@ -184,3 +184,92 @@ def test_equalize_hist_global_matches_oracle(image, nbins):
     stack = P.to_host(P.equalize_hist_global(P.to_device(img), nbins))
     assert stack.dtype == np.float64
     np.testing.assert_array_equal(stack[0], got.astype(np.float64))
+
+
+def _adapt_image(image, shape=None):
+    img = Z["img_f32"].astype(np.float64) * 1.37 if image == "f64" else Z["img_" + image]
+    if shape is not None:
+        rng = np.random.default_rng(11)
+        hi = {"u8": 255, "u16": 4095}.get(image, 1)
+        img = rng.integers(0, hi + 1, (2,) + shape).astype(img.dtype) if image in ("u8", "u16") \
+            else (rng.random((2,) + shape) * 900.0).astype(img.dtype)
+    return img
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32", "f64"])
+@pytest.mark.parametrize("window_nbins", [((10, 10), 256), ((7, 12), 100), ((16, 16), 256),
+                                          (5, 64), (None, 256), ((64, 80), 256)])
+def test_equalize_hist_adapt_matches_oracle(image, window_nbins):
+    """equalize_hist_adapt (CLAHE): the same grey levels, clipped histograms, maps and
+    float32 blend as the restatement of scikit-image's algorithm, so the result is
+    equal to the oracle's (regions past the image's end reflected; a kernel as large
+    as the image)."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    window, nbins = window_nbins
+    img = _adapt_image(image)
+    x = img[0]
+    got = P.to_host(P.equalize_hist_adapt(P.to_device(x), window, nbins))
+    want = O.equalize_hist_adapt(x.copy(), window, nbins)
+    assert got.dtype == want.dtype
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32"])
+@pytest.mark.parametrize("shape", [(97, 131), (33, 250), (9, 9)])
+def test_equalize_hist_adapt_ragged_shapes(image, shape):
+    """Images that are not multiples of the kernel, and smaller than it; a stack is
+    equalised image by image (float64)."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    img = _adapt_image(image, shape)
+    got = P.to_host(P.equalize_hist_adapt(P.to_device(img), (10, 10), 256))
+    want = O.equalize_hist_adapt(img.copy(), (10, 10), 256)
+    assert got.dtype == np.float64 and want.dtype == np.float64
+    np.testing.assert_array_equal(got, want)
+
+
+def test_equalize_hist_adapt_flat_image():
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    x = np.full((40, 50), 700, np.uint16)
+    got = P.to_host(P.equalize_hist_adapt(P.to_device(x)))
+    np.testing.assert_array_equal(got, O.equalize_hist_adapt(x.copy()))
+
+
+@pytest.mark.parametrize("image", ["u8", "u16", "f32", "f64"])
+@pytest.mark.parametrize("radius", [0, 1, 4, 10])
+def test_equalize_hist_local_matches_oracle(image, radius):
+    """equalize_hist_local: img_as_ubyte (rint in the image's float type), the rank
+    equalisation over the disk with the pixels outside the image left out, and the
+    rescaling, equal to the oracle's."""
+    from fluidimage_gb300 import preproc as P
+    from oracle import preproc as O
+
+    img = _adapt_image(image)
+    got = P.to_host(P.equalize_hist_local(P.to_device(img[:2]), radius))
+    want = O.equalize_hist_local(img[:2].copy(), radius)
+    assert got.dtype == want.dtype == np.float64
+    np.testing.assert_array_equal(got, want)
+    one = P.to_host(P.equalize_hist_local(P.to_device(img[0]), radius))
+    np.testing.assert_array_equal(one, want[0])
+
+
+def test_work_preproc_adaptive_equalisations():
+    from fluidimage_gb300.preproc import WorkPreproc
+    from oracle import preproc as O
+
+    params = WorkPreproc.create_default_params()
+    params.tools.sequence = ["equalize_hist_adapt", "equalize_hist_local"]
+    params.tools.equalize_hist_adapt.enable = True
+    params.tools.equalize_hist_local.enable = True
+    params.tools.equalize_hist_local.radius = 3
+    imgs = Z["img_u16"][:3]
+    names = [f"im{i}" for i in range(len(imgs))]
+    res = WorkPreproc(params).calcul({"arrays": list(imgs), "names": names})
+    want = O.equalize_hist_local(O.equalize_hist_adapt(imgs.copy()), radius=3)
+    got = np.array([res.data[n] for n in names])
+    np.testing.assert_array_equal(got, want)

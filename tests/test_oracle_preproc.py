@@ -105,3 +105,46 @@ def test_histogram_edges_follow_numpy():
                 assert edges.dtype == want.dtype
                 np.testing.assert_array_equal(edges, want)
                 assert first == want[0]
+
+
+def test_clip_histogram_known_answers():
+    """Hand-traced cases of the contrast limiting: no increment (the remaining excess
+    handed out in strides, overshooting by 2), a per-bin increment, and bins filled
+    to the limit (the excess goes negative: no redistribution)."""
+    from oracle import preproc as O
+
+    np.testing.assert_array_equal(O.clip_histogram([5, 0, 0, 3, 0, 0, 0, 1], 2),
+                                  [2, 1, 1, 2, 1, 1, 1, 2])
+    np.testing.assert_array_equal(O.clip_histogram([10, 0, 0, 0], 4), [4, 2, 2, 2])
+    np.testing.assert_array_equal(O.clip_histogram([20, 3, 2, 0, 0, 0, 0, 0], 4), [4] * 8)
+    np.testing.assert_array_equal(O.clip_histogram([1, 2, 0], 5), [1, 2, 0])
+
+
+def test_clahe_levels_flat_regions():
+    """One grey level everywhere: each region's clipped histogram is [1, 1, 1, 1]
+    (limit 1 for 2 x 2 regions), the map of bin 0 is floor(16383 / 4) and the blend
+    weights sum to 1 exactly."""
+    from oracle import preproc as O
+
+    out = O.clahe_levels(np.zeros((4, 6), np.uint16), (2, 2), 4)
+    np.testing.assert_array_equal(out, np.full((4, 6), 4095, np.uint16))
+
+
+def test_rank_equalize_known_answer():
+    from oracle import preproc as O
+
+    u8 = np.array([[10, 20, 30], [40, 50, 60], [70, 80, 90]], np.uint8)
+    out = O.rank_equalize(u8, O.disk(1))
+    # (0, 0): 10, 20, 40 -> 1 of 3; (0, 1): 10, 20, 30, 50 -> 2 of 4; (1, 1): 5 of 5 -> 3
+    assert out[0, 0] == 255 // 3 and out[0, 1] == 127 and out[1, 1] == 153
+    assert out[2, 2] == 255
+    np.testing.assert_array_equal(O.disk(1), [[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    assert O.disk(10).sum() == 317
+
+
+def test_to_ubyte_rounds_half_to_even():
+    from oracle import preproc as O
+
+    y = np.array([0.0, 1.0, 127.5 / 255, 0.5 / 255], np.float64)
+    np.testing.assert_array_equal(O.to_ubyte(y), np.rint(y * 255).astype(np.uint8))
+    assert O.to_ubyte(np.array([1.0], np.float32))[0] == 255
