@@ -885,6 +885,8 @@ def run_preproc(args):
         ("sliding_median", dict(window_size=30), t_img, im0),
         ("temporal_minima", dict(), t_stack, frames),
         ("sharpen", dict(), t_img, im0),
+        ("equalize_hist_adapt", dict(), t_img, im0),
+        ("equalize_hist_local", dict(radius=10), t_img, im0),
     ]
     out = {"metric": "preprocessing Mpixel/s", "unit": "Mpixel/s", "workload":
            f"{args.size}x{args.size} uint16 frames of the config-2 pair", "tools": {}}
