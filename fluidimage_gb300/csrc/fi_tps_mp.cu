@@ -134,11 +134,20 @@ __device__ __forceinline__ double bmax(double v, double* sh) {
 
 constexpr int TS = 36;  // row stride (floats) of the 32 x 32 shared tiles: float4-aligned rows
 
+// Start moving [p, p + bytes) from memory into L2 without waiting for it (bulk
+// prefetch by the copy engine; p 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // rho = g - B z for two right-hand sides, in double-float; B (m x m, symmetric, both
-// triangles, column-major, leading dimension ld) holds (hi, lo) pairs, read with the
-// streaming hint (B is twice the FP32 factor, which should stay in L2).  Each warp
-// takes four columns at a time (one row per lane), then reduce-scatters its eight
-// sums over the warp.  rho is rounded to float.
+// triangles, column-major, leading dimension ld, a multiple of 4; 32-byte aligned)
+// holds (hi, lo) pairs, read with the streaming hint (B is twice the FP32 factor,
+// which should stay in L2).  Each warp takes four columns at a time (one row per
+// lane), then reduce-scatters its eight sums over the warp.  B is streamed from
+// memory: each warp has the copy engine prefetch its next two column groups into L2
+// (contiguous, 32 ld bytes per column) while it works on the current one, so that
+// its loads wait on L2 rather than on memory.  rho is rounded to float.
 template <int NT>
 __device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const float2* zx,
                              const float2* zy, const float2* gx, const float2* gy, float* rx,
@@ -146,7 +155,14 @@ __device__ void residual_df2(const float2* __restrict__ B, int m, int ld, const 
   constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
+  auto prefetch_group = [&](int c) {
+    if (lane == 0 && c < m)
+      prefetch_l2(B + (int64_t)c * ld, (unsigned)(min(4, m - c) * ld * sizeof(float2)));
+  };
+  prefetch_group(4 * wid);
+  prefetch_group(4 * wid + 4 * NW);
   for (int c0 = 4 * wid; c0 < m; c0 += 4 * NW) {
+    prefetch_group(c0 + 8 * NW);
     // column q: x sums in lane .x, y sums in lane .y of the pairs (packed FP32x2)
     float2 H[4], Lo[4];
 #pragma unroll
