@@ -425,9 +425,20 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Valid centres and subdomains of a plan as the layout kernels read them on the device
+// (none when the plan failed), each clamped to the capacity the host sized for.
+__device__ __forceinline__ int plan_centers(const fi_tps_plan* p, int cap) {
+  return p->status == 0 ? min(cap, p->num_centers) : 0;
+}
+__device__ __forceinline__ int plan_subdoms(const fi_tps_plan* p, int cap) {
+  return p->status == 0 ? min(cap, p->nb_subdomx * p->nb_subdomy) : 0;
+}
+
+// count_plan (nullable): the number of points is the plan's centre count (at most npts)
 __global__ void k_tps_lattice(const double* px, const double* py, int npts, int32_t* xy2,
-                              int32_t* on_lattice) {
+                              int32_t* on_lattice, const fi_tps_plan* count_plan) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (count_plan != nullptr) npts = plan_centers(count_plan, npts);
   if (i >= npts) return;
   const double X = 2.0 * px[i], Y = 2.0 * py[i];
   const bool ok = X == rint(X) && Y == rint(Y) && fabs(X) < 1073741824.0 &&
@@ -461,9 +472,12 @@ __device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsig
 }
 
 __global__ void __launch_bounds__(YB_TILE) k_y_tiles(const double* py, int n, double* tmax,
-                                                      double* tmin) {
+                                                      double* tmin,
+                                                      const fi_tps_plan* count_plan) {
   __shared__ unsigned long long smx[YB_TILE / 32], smn[YB_TILE / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // with count_plan, n is the plan's centre count; tiles past it stay neutral
+  if (count_plan != nullptr) n = plan_centers(count_plan, n);
   const int i = blockIdx.x * YB_TILE + threadIdx.x;
   const double y = (i < n) ? py[i] : NAN;
   unsigned long long kx = isnan(y) ? dkey(-INFINITY) : dkey(y);
@@ -588,7 +602,9 @@ constexpr int ORDER_MAX = 8192;
 __global__ void __launch_bounds__(1024)
     k_tps_offsets(const int32_t* counts, const int32_t* ncounts, int nsub, int64_t* off,
                   int64_t* noff, int64_t* moff, int64_t* woff, int64_t* summary,
-                  int32_t* order) {
+                  int32_t* order, const fi_tps_plan* count_plan) {
+  // with count_plan, nsub is a capacity and the plan gives the subdomains
+  if (count_plan != nullptr) nsub = plan_subdoms(count_plan, nsub);
   __shared__ int64_t wsum[33];
   __shared__ int s_max[2];
   if (threadIdx.x == 0) s_max[0] = s_max[1] = 0;
@@ -677,12 +693,17 @@ __device__ __forceinline__ double coef_norm_hoisted(const double* c, double x, d
 
 // Ordered membership of points in subdomain blockIdx.x; mode 0 counts, mode 1 fills.
 // With the tile index y_pmax / y_smin of py (k_y_tiles) only the tiles that can hold
-// the subdomain's y band are scanned.
+// the subdomain's y band are scanned.  subdoms_from_plan: the grid is a capacity,
+// blocks past the plan's subdomains return; centres_from_plan: the points are the
+// plan's centres (npts a capacity).
 __global__ void __launch_bounds__(512)
     k_tps_members(const fi_tps_plan* plan_ptr, const double* px, const double* py, int npts,
                   int mode, int32_t* counts, const int64_t* offsets, int32_t* indices,
                   double* coefs, const int32_t* xy2, const int32_t* on_lattice,
-                  const double* y_pmax, const double* y_smin) {
+                  const double* y_pmax, const double* y_smin, int subdoms_from_plan,
+                  int centres_from_plan) {
+  if (subdoms_from_plan && (int)blockIdx.x >= plan_subdoms(plan_ptr, gridDim.x)) return;
+  if (centres_from_plan) npts = plan_centers(plan_ptr, npts);
   __shared__ int warp_tot[33];
   __shared__ int s_range[2], s_box[4];
   __shared__ Limits sL;
@@ -1303,7 +1324,7 @@ extern "C" int fi_tps_lattice(const double* px, const double* py, int npts, int3
   FI_REQUIRE(px && py && xy2 && on_lattice && npts > 0, "fi_tps_lattice: bad arguments");
   cudaStream_t s = (cudaStream_t)stream;
   k_set_int<<<1, 1, 0, s>>>(on_lattice, 1);
-  k_tps_lattice<<<(npts + 255) / 256, 256, 0, s>>>(px, py, npts, xy2, on_lattice);
+  k_tps_lattice<<<(npts + 255) / 256, 256, 0, s>>>(px, py, npts, xy2, on_lattice, nullptr);
   return check_launch("fi_tps_lattice", 2);
 }
 
@@ -1311,7 +1332,7 @@ extern "C" int fi_tps_y_bounds(const double* py, int npts, double* y_pmax, doubl
                                void* stream) {
   FI_REQUIRE(py && y_pmax && y_smin && npts > 0, "fi_tps_y_bounds: bad arguments");
   const int nt = (npts + YB_TILE - 1) / YB_TILE;
-  k_y_tiles<<<nt, YB_TILE, 0, (cudaStream_t)stream>>>(py, npts, y_pmax, y_smin);
+  k_y_tiles<<<nt, YB_TILE, 0, (cudaStream_t)stream>>>(py, npts, y_pmax, y_smin, nullptr);
   k_y_tiles_scan<<<1, 1024, 0, (cudaStream_t)stream>>>(nt, y_pmax, y_smin);
   return check_launch("fi_tps_y_bounds", 2);
 }
@@ -1325,7 +1346,7 @@ extern "C" int fi_tps_offsets(const int32_t* counts, const int32_t* ncounts, int
              "fi_tps_offsets: bad arguments");
   k_tps_offsets<<<1, 1024, 0, (cudaStream_t)stream>>>(counts, ncounts, nb_subdom, offsets,
                                                       noffsets, mat_offsets, w_offsets, summary,
-                                                      order);
+                                                      order, nullptr);
   return check_launch("fi_tps_offsets");
 }
 
@@ -1340,7 +1361,7 @@ extern "C" int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const doub
   FI_REQUIRE(((uintptr_t)xy2 & 7) == 0, "fi_tps_members: xy2 must be 8-byte aligned");
   k_tps_members<<<nb_subdom, 512, 0, (cudaStream_t)stream>>>(plan, px, py, npts, mode, counts,
                                                             offsets, indices, coefs, xy2,
-                                                            on_lattice, y_pmax, y_smin);
+                                                            on_lattice, y_pmax, y_smin, 0, 0);
   return check_launch("fi_tps_members");
 }
 
@@ -1354,23 +1375,32 @@ extern "C" int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const doubl
                  pbounds && counts && ncounts && offsets && nb_subdom > 0 &&
                  num_centers > 0 && npts > 0,
              "fi_tps_layout: bad arguments");
+  FI_REQUIRE(((uintptr_t)cxy2 & 7) == 0 && ((uintptr_t)pxy2 & 7) == 0,
+             "fi_tps_layout: xy2 must be 8-byte aligned");
+  // nb_subdom and num_centers are capacities: the kernels take the plan's counts
+  cudaStream_t s = (cudaStream_t)stream;
   const int ctiles = (num_centers + YB_TILE - 1) / YB_TILE;
   const int ptiles = (npts + YB_TILE - 1) / YB_TILE;
-  int rc = fi_tps_lattice(cx, cy, num_centers, cxy2, clat, stream);
-  if (rc == FI_OK && !p_given) rc = fi_tps_lattice(px, py, npts, pxy2, plat, stream);
-  if (rc == FI_OK) rc = fi_tps_y_bounds(cy, num_centers, cbounds, cbounds + ctiles, stream);
-  if (rc == FI_OK) rc = fi_tps_y_bounds(py, npts, pbounds, pbounds + ptiles, stream);
-  if (rc == FI_OK)
-    rc = fi_tps_members(plan, nb_subdom, cx, cy, num_centers, 0, counts, nullptr, nullptr,
-                        nullptr, cxy2, clat, cbounds, cbounds + ctiles, stream);
-  if (rc == FI_OK)
-    rc = fi_tps_members(plan, nb_subdom, px, py, npts, 0, ncounts, nullptr, nullptr, nullptr,
-                        pxy2, plat, pbounds, pbounds + ptiles, stream);
-  if (rc == FI_OK)
-    rc = fi_tps_offsets(counts, ncounts, nb_subdom, offsets, offsets + nb_subdom,
-                        offsets + 2 * nb_subdom, offsets + 3 * nb_subdom,
-                        offsets + 4 * nb_subdom, order, stream);
-  return rc;
+  k_set_int<<<1, 1, 0, s>>>(clat, 1);
+  k_tps_lattice<<<ctiles, 256, 0, s>>>(cx, cy, num_centers, cxy2, clat, plan);
+  int launched = 2;
+  if (!p_given) {
+    k_set_int<<<1, 1, 0, s>>>(plat, 1);
+    k_tps_lattice<<<ptiles, 256, 0, s>>>(px, py, npts, pxy2, plat, nullptr);
+    launched += 2;
+  }
+  k_y_tiles<<<ctiles, YB_TILE, 0, s>>>(cy, num_centers, cbounds, cbounds + ctiles, plan);
+  k_y_tiles_scan<<<1, 1024, 0, s>>>(ctiles, cbounds, cbounds + ctiles);
+  k_y_tiles<<<ptiles, YB_TILE, 0, s>>>(py, npts, pbounds, pbounds + ptiles, nullptr);
+  k_y_tiles_scan<<<1, 1024, 0, s>>>(ptiles, pbounds, pbounds + ptiles);
+  k_tps_members<<<nb_subdom, 512, 0, s>>>(plan, cx, cy, num_centers, 0, counts, nullptr, nullptr,
+                                          nullptr, cxy2, clat, cbounds, cbounds + ctiles, 1, 1);
+  k_tps_members<<<nb_subdom, 512, 0, s>>>(plan, px, py, npts, 0, ncounts, nullptr, nullptr,
+                                          nullptr, pxy2, plat, pbounds, pbounds + ptiles, 1, 0);
+  k_tps_offsets<<<1, 1024, 0, s>>>(counts, ncounts, nb_subdom, offsets, offsets + nb_subdom,
+                                   offsets + 2 * nb_subdom, offsets + 3 * nb_subdom,
+                                   offsets + 4 * nb_subdom, order, plan);
+  return check_launch("fi_tps_layout", launched + 7);
 }
 
 extern "C" int fi_tps_members_fill(const fi_tps_plan* plan, int nb_subdom, const double* cx,
@@ -1384,14 +1414,19 @@ extern "C" int fi_tps_members_fill(const fi_tps_plan* plan, int nb_subdom, const
   FI_REQUIRE(plan && cx && cy && px && py && cbounds && pbounds && offsets && indices &&
                  coefs && nindices && ncoefs && nb_subdom > 0 && num_centers > 0 && npts > 0,
              "fi_tps_members_fill: bad arguments");
+  FI_REQUIRE(((uintptr_t)cxy2 & 7) == 0 && ((uintptr_t)pxy2 & 7) == 0,
+             "fi_tps_members_fill: xy2 must be 8-byte aligned");
+  // the capacities of fi_tps_layout: the kernels take the plan's counts
+  cudaStream_t s = (cudaStream_t)stream;
   const int ctiles = (num_centers + YB_TILE - 1) / YB_TILE;
   const int ptiles = (npts + YB_TILE - 1) / YB_TILE;
-  int rc = fi_tps_members(plan, nb_subdom, cx, cy, num_centers, 1, nullptr, offsets, indices,
-                          coefs, cxy2, clat, cbounds, cbounds + ctiles, stream);
-  if (rc == FI_OK)
-    rc = fi_tps_members(plan, nb_subdom, px, py, npts, 1, nullptr, offsets + nb_subdom,
-                        nindices, ncoefs, pxy2, plat, pbounds, pbounds + ptiles, stream);
-  return rc;
+  k_tps_members<<<nb_subdom, 512, 0, s>>>(plan, cx, cy, num_centers, 1, nullptr, offsets,
+                                          indices, coefs, cxy2, clat, cbounds, cbounds + ctiles,
+                                          1, 1);
+  k_tps_members<<<nb_subdom, 512, 0, s>>>(plan, px, py, npts, 1, nullptr, offsets + nb_subdom,
+                                          nindices, ncoefs, pxy2, plat, pbounds,
+                                          pbounds + ptiles, 1, 0);
+  return check_launch("fi_tps_members_fill", 2);
 }
 
 extern "C" int fi_tps_solve(const fi_tps_plan* plan, int nb_subdom, int max_members,

@@ -284,19 +284,31 @@ class GridOutput:
 _PINNED = threading.local()
 
 
-def _readback_raw(addr, nbytes, stream=None):
-    """``nbytes`` at device address ``addr`` -> bytes, through a pinned buffer kept
-    per host thread (one synchronisation of the stream)."""
+def _readback_many(regions, stream=None):
+    """Device regions ``(address, nbytes)`` -> one bytes object each, through a pinned
+    buffer kept per host thread, with one synchronisation of the stream."""
     torch = _torch()
+    spans, total = [], 0
+    for _, nbytes in regions:
+        spans.append((total, nbytes))
+        total += -(-nbytes // 16) * 16
     buf = getattr(_PINNED, "small", None)
-    if buf is None or buf.numel() < nbytes:
-        buf = torch.empty(max(4096, nbytes), dtype=torch.uint8, pin_memory=True)
+    if buf is None or buf.numel() < total:
+        buf = torch.empty(max(4096, total), dtype=torch.uint8, pin_memory=True)
         _PINNED.small = buf
     strm = stream or torch.cuda.current_stream()
-    L.check(L.load().fi_memcpy_d2h(buf.data_ptr(), addr, nbytes, strm.cuda_stream),
-            "fi_memcpy_d2h")
+    lib = L.load()
+    for (addr, nbytes), (off, _) in zip(regions, spans):
+        L.check(lib.fi_memcpy_d2h(buf.data_ptr() + off, addr, nbytes, strm.cuda_stream),
+                "fi_memcpy_d2h")
     strm.synchronize()
-    return bytes(buf.numpy()[:nbytes])
+    raw = buf.numpy()
+    return [bytes(raw[off:off + nbytes]) for off, nbytes in spans]
+
+
+def _readback_raw(addr, nbytes, stream=None):
+    """``nbytes`` at device address ``addr`` -> bytes (one synchronisation)."""
+    return _readback_many([(addr, nbytes)], stream)[0]
 
 
 def _readback(t, stream=None):
@@ -342,6 +354,16 @@ class _Carved:
         return self.buf[o:o + count * dtype.itemsize].view(dtype)
 
 
+def tps_subdomain_capacity(nvec, subdom_size):
+    """Subdomains the layout buffers of a TPS over ``nvec`` vectors are sized for: the
+    layout has nbx nby subdomains, nbx = floor(sqrt(nb / r)), nby = ceil(sqrt(nb r)),
+    nb = (valid vectors) / subdom_size, r the aspect ratio of their extent, so about
+    nb + sqrt(nb / r) (thin_plate_spline_subdom.py:56-62); the margin covers ratios down
+    to ~1/16 (beyond, the layout runs again with the plan's count)."""
+    nb = nvec / max(int(subdom_size), 1)
+    return int(2 * nb + 4 * math.sqrt(nb)) + 16
+
+
 def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
             threshold, want_smooth, stream, p_lattice=None):
     """apply_interp with ThinPlateSplineSubdom on device (singlepass.py:466-548).
@@ -354,7 +376,7 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     s = L.stream_handle(stream)
     u8_, i32_, i64_, f32_, f64_ = (torch.uint8, torch.int32, torch.int64, torch.float32,
                                    torch.float64)
-    # the plan and the compacted centres; the host needs the plan header first
+    # the plan and the compacted centres
     cA = _Carved(dev, [(L.TPS_PLAN_BYTES, u8_), (nvec, f64_), (nvec, f64_), (nvec, f32_),
                        (nvec, f32_), (nvec, i32_)])
     plan, cx, cy, ux, uy, sel = cA.addr
@@ -363,30 +385,38 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                      int(subdom_size), float(smoothing_coef), 20.0, plan, cx,
                                      cy, ux, uy, sel, s),
                 "fi_tps_plan_make")
-    hdr = L.TpsPlan.from_buffer_copy(_readback_raw(plan, C.sizeof(L.TpsPlan), stream))
-    if hdr.status == 1:
-        raise InterpError("Only nan.")
-    if hdr.status != 0:
-        raise ValueError("TPS subdomain layout is degenerate (all vectors on one line)")
-    nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
-    ctiles, ptiles = -(-nv // 256), -(-npts // 256)
+    # layout (lattice coordinates, y bounds, member counts, offsets) in buffers sized by
+    # capacities: the kernels take the valid centres and the subdomains from the plan on
+    # the device, and the host reads the plan header and the 6 totals in one
+    # synchronisation (a plan with more subdomains than the estimate is laid out again)
     p_given = p_lattice is not None
-    # layout: lattice coordinates, y bounds, member counts, offsets (one call)
-    specs = [(2 * nv, i32_), (1, i32_), (2 * ctiles, f64_), (2 * ptiles, f64_), (nsub, i32_),
-             (nsub, i32_), (4 * nsub + 6, i64_), (nsub, i32_)]
-    if not p_given:
-        specs += [(2 * npts, i32_), (1, i32_)]
-    cB = _Carved(dev, specs)
-    cxy2, clat, cbounds, pbounds, counts, ncounts, offs, order = cB.addr[:8]
-    pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[8:]
-    L.check(lib.fi_tps_layout(plan, nsub, cx, cy, nv, L.ptr(px), L.ptr(py), npts,
-                              int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds, counts,
-                              ncounts, offs, order, s),
-            "fi_tps_layout")
-    off_d, noff_d, moff_d, woff_d = (offs + 8 * k * nsub for k in range(4))
-    # the host reads back the 6 totals only
-    tot, ntot, msum, wsum, maxc, maxnc = (
-        int(v) for v in np.frombuffer(_readback_raw(offs + 32 * nsub, 48, stream), np.int64))
+    nv_cap, nsub_cap = nvec, tps_subdomain_capacity(nvec, subdom_size)
+    while True:
+        ctiles, ptiles = -(-nv_cap // 256), -(-npts // 256)
+        specs = [(2 * nv_cap, i32_), (1, i32_), (2 * ctiles, f64_), (2 * ptiles, f64_),
+                 (nsub_cap, i32_), (nsub_cap, i32_), (4 * nsub_cap + 6, i64_), (nsub_cap, i32_)]
+        if not p_given:
+            specs += [(2 * npts, i32_), (1, i32_)]
+        cB = _Carved(dev, specs)
+        cxy2, clat, cbounds, pbounds, counts, ncounts, offs, order = cB.addr[:8]
+        pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[8:]
+        L.check(lib.fi_tps_layout(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py), npts,
+                                  int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds,
+                                  counts, ncounts, offs, order, s),
+                "fi_tps_layout")
+        raw_hdr, raw_tot = _readback_many(
+            [(plan, C.sizeof(L.TpsPlan)), (offs + 32 * nsub_cap, 48)], stream)
+        hdr = L.TpsPlan.from_buffer_copy(raw_hdr)
+        if hdr.status == 1:
+            raise InterpError("Only nan.")
+        if hdr.status != 0:
+            raise ValueError("TPS subdomain layout is degenerate (all vectors on one line)")
+        nv, nsub = hdr.num_centers, hdr.nb_subdomx * hdr.nb_subdomy
+        if nsub <= nsub_cap:
+            break
+        nsub_cap = nsub
+    off_d, noff_d, moff_d, woff_d = (offs + 8 * k * nsub_cap for k in range(4))
+    tot, ntot, msum, wsum, maxc, maxnc = (int(v) for v in np.frombuffer(raw_tot, np.int64))
     use_mp = maxc <= MP_MAX_MEMBERS
     t1, nt1 = max(tot, 1), max(ntot, 1)
     # scratch of this call (the matrices dominate) apart from the outputs that the
@@ -401,9 +431,9 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
         (2 * nsub, i32_), (nsub, i32_), (nsub, i32_), (nsub, i32_), (npts, i32_), (npts, i32_)])
     (weights, max_udiff, out_x, out_y, smooth_x, smooth_y, iters, nfixed, singular, status,
      sweeps, rx, ry) = cO.addr
-    L.check(lib.fi_tps_members_fill(plan, nsub, cx, cy, nv, L.ptr(px), L.ptr(py), npts, cxy2,
-                                    clat, pxy2, plat, cbounds, pbounds, offs, idx, coefs, nidx,
-                                    ncoefs, s),
+    L.check(lib.fi_tps_members_fill(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py), npts,
+                                    cxy2, clat, pxy2, plat, cbounds, pbounds, offs, idx, coefs,
+                                    nidx, ncoefs, s),
             "fi_tps_members_fill")
     use_thr = threshold is not None
     thr = float(threshold) if use_thr else 0.0
@@ -438,8 +468,8 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     # tensors for what the caller keeps (built while the GPU works)
     out = TpsOutput(
         out_x=cO.tensor(2), out_y=cO.tensor(3), rx=cO.tensor(11), ry=cO.tensor(12),
-        selection=cA.tensor(5), num_centers=nv, nb_subdom=nsub, counts_d=cB.tensor(4),
-        w_offsets_d=cB.tensor(6)[3 * nsub:4 * nsub], weights=cO.tensor(0),
+        selection=cA.tensor(5), num_centers=nv, nb_subdom=nsub, counts_d=cB.tensor(4)[:nsub],
+        w_offsets_d=cB.tensor(6)[3 * nsub_cap:3 * nsub_cap + nsub], weights=cO.tensor(0),
         singular=cO.tensor(8), iters=cO.tensor(6), nfixed=cO.tensor(7),
         max_udiff=cO.tensor(1), mp_status=cO.tensor(9), mp_sweeps=cO.tensor(10),
     )

@@ -433,10 +433,16 @@ int fi_tps_members(const fi_tps_plan* plan, int nb_subdom, const double* px, con
  * The layout stages of one TPS interpolation in one call: fi_tps_lattice of the
  * centres (cx, cy) and, unless p_given, of the new positions (px, py) (else pxy2 /
  * plat are read); fi_tps_y_bounds of both; the member counts of both
- * (fi_tps_members mode 0) and fi_tps_offsets.  Buffers: cxy2 [2 num_centers],
- * pxy2 [2 npts], clat / plat [1], cbounds / pbounds [2 ceil(n / 256)] (y_pmax then
- * y_smin), counts / ncounts [nb_subdom], offsets [4 nb_subdom + 6] (offsets,
- * noffsets, mat_offsets, w_offsets, summary), order (nullable, [nb_subdom]) as in
+ * (fi_tps_members mode 0) and fi_tps_offsets.  nb_subdom and num_centers are
+ * capacities (at least the plan's subdomains and valid centres, e.g. nvec for the
+ * centres): the kernels read the actual counts from *plan on the device, so that the
+ * host needs no copy of the plan before this call and reads the plan header and the
+ * summary after it in one synchronisation; with a plan of more subdomains than
+ * nb_subdom, only the first nb_subdom are laid out and the caller calls again with
+ * the plan's count.  Buffers: cxy2 [2 num_centers], pxy2 [2 npts], clat / plat [1],
+ * cbounds / pbounds [2 ceil(n / 256)] (y_pmax then y_smin, n = num_centers / npts),
+ * counts / ncounts [nb_subdom], offsets [4 nb_subdom + 6] (offsets, noffsets,
+ * mat_offsets, w_offsets, summary), order (nullable, [nb_subdom]) as in
  * fi_tps_offsets.  No reference counterpart (the
  * bookkeeping of ThinPlateSplineSubdom.__init__ / init_with_new_positions,
  * thin_plate_spline_subdom.py:25-127, 160-206).
@@ -448,10 +454,10 @@ int fi_tps_layout(const fi_tps_plan* plan, int nb_subdom, const double* cx, cons
                   int32_t* order, void* stream);
 
 /*
- * Both membership fills (fi_tps_members mode 1) after fi_tps_layout: the centres
- * into indices / coefs at offsets[0:nb_subdom], the new positions into nindices /
- * ncoefs at offsets[nb_subdom:2 nb_subdom]; the other buffers as fi_tps_layout
- * wrote them.
+ * Both membership fills (fi_tps_members mode 1) after fi_tps_layout, with the same
+ * capacities nb_subdom and num_centers: the centres into indices / coefs at
+ * offsets[0:nb_subdom], the new positions into nindices / ncoefs at
+ * offsets[nb_subdom:2 nb_subdom]; the other buffers as fi_tps_layout wrote them.
  */
 int fi_tps_members_fill(const fi_tps_plan* plan, int nb_subdom, const double* cx,
                         const double* cy, int num_centers, const double* px, const double* py,
