@@ -354,6 +354,12 @@ class _Carved:
         return self.buf[o:o + count * dtype.itemsize].view(dtype)
 
 
+#: subdomains a point can belong to: the buffered subdomains (20 % of a subdomain's
+#: width added on each side, thin_plate_spline_subdom.py:80-88) overlap at most
+#: pairwise along each axis, so the membership lists hold at most 4 entries per point
+MEMBERS_PER_POINT = 4
+
+
 def tps_subdomain_capacity(nvec, subdom_size):
     """Subdomains the layout buffers of a TPS over ``nvec`` vectors are sized for: the
     layout has nbx nby subdomains, nbx = floor(sqrt(nb / r)), nby = ceil(sqrt(nb r)),
@@ -394,16 +400,24 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
     while True:
         ctiles, ptiles = -(-nv_cap // 256), -(-npts // 256)
         specs = [(2 * nv_cap, i32_), (1, i32_), (2 * ctiles, f64_), (2 * ptiles, f64_),
-                 (nsub_cap, i32_), (nsub_cap, i32_), (4 * nsub_cap + 6, i64_), (nsub_cap, i32_)]
+                 (nsub_cap, i32_), (nsub_cap, i32_), (4 * nsub_cap + 6, i64_), (nsub_cap, i32_),
+                 (MEMBERS_PER_POINT * nv_cap, i32_), (MEMBERS_PER_POINT * nv_cap, f64_),
+                 (MEMBERS_PER_POINT * npts, i32_), (MEMBERS_PER_POINT * npts, f64_)]
         if not p_given:
             specs += [(2 * npts, i32_), (1, i32_)]
         cB = _Carved(dev, specs)
-        cxy2, clat, cbounds, pbounds, counts, ncounts, offs, order = cB.addr[:8]
-        pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[8:]
+        (cxy2, clat, cbounds, pbounds, counts, ncounts, offs, order, idx, coefs, nidx,
+         ncoefs) = cB.addr[:12]
+        pxy2, plat = (L.ptr(p_lattice[0]), L.ptr(p_lattice[1])) if p_given else cB.addr[12:]
         L.check(lib.fi_tps_layout(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py), npts,
                                   int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds,
                                   counts, ncounts, offs, order, s),
                 "fi_tps_layout")
+        # the membership lists need no host value either: they run while the host waits
+        L.check(lib.fi_tps_members_fill(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py),
+                                        npts, cxy2, clat, pxy2, plat, cbounds, pbounds, offs,
+                                        idx, coefs, nidx, ncoefs, s),
+                "fi_tps_members_fill")
         raw_hdr, raw_tot = _readback_many(
             [(plan, C.sizeof(L.TpsPlan)), (offs + 32 * nsub_cap, 48)], stream)
         hdr = L.TpsPlan.from_buffer_copy(raw_hdr)
@@ -417,24 +431,22 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
         nsub_cap = nsub
     off_d, noff_d, moff_d, woff_d = (offs + 8 * k * nsub_cap for k in range(4))
     tot, ntot, msum, wsum, maxc, maxnc = (int(v) for v in np.frombuffer(raw_tot, np.int64))
+    if tot > MEMBERS_PER_POINT * nv_cap or ntot > MEMBERS_PER_POINT * npts:
+        raise RuntimeError("TPS layout: more subdomain members than the bound")
     use_mp = maxc <= MP_MAX_MEMBERS
     t1, nt1 = max(tot, 1), max(ntot, 1)
     # scratch of this call (the matrices dominate) apart from the outputs that the
     # results keep (weights, interpolated fields, per-subdomain statistics)
     cS = _Carved(dev, [
-        (msum, f64_), (msum if use_mp else 0, f32_), (t1, f64_), (nt1, f64_), (t1, f64_),
-        (t1, f64_), (nt1, f64_), (nt1, f64_), (t1, i32_), (nt1, i32_), (tot + 3 * nsub, i32_)])
-    matrices, matrices32, coefs, ncoefs, smx, smy, partx, party, idx, nidx, pivots = cS.addr
+        (msum, f64_), (msum if use_mp else 0, f32_), (t1, f64_), (t1, f64_), (nt1, f64_),
+        (nt1, f64_), (tot + 3 * nsub, i32_)])
+    matrices, matrices32, smx, smy, partx, party, pivots = cS.addr
     cO = _Carved(dev, [
         (wsum, f64_), (2 * nsub, f64_), (npts, f64_), (npts, f64_),
         (nv if want_smooth else 0, f64_), (nv if want_smooth else 0, f64_), (2 * nsub, i32_),
         (2 * nsub, i32_), (nsub, i32_), (nsub, i32_), (nsub, i32_), (npts, i32_), (npts, i32_)])
     (weights, max_udiff, out_x, out_y, smooth_x, smooth_y, iters, nfixed, singular, status,
      sweeps, rx, ry) = cO.addr
-    L.check(lib.fi_tps_members_fill(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py), npts,
-                                    cxy2, clat, pxy2, plat, cbounds, pbounds, offs, idx, coefs,
-                                    nidx, ncoefs, s),
-            "fi_tps_members_fill")
     use_thr = threshold is not None
     thr = float(threshold) if use_thr else 0.0
     table = L.ptr(phi_table(dev))
