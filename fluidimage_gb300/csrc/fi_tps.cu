@@ -20,6 +20,7 @@
 
 #include "fi_common.cuh"
 #include "fi_df.cuh"
+#include "fi_lattice.cuh"
 
 namespace fi {
 
@@ -1142,14 +1143,20 @@ __global__ void k_tps_blend_centers(const fi_tps_plan* plan_ptr, const double* c
 // Part of each subdomain's TPS at its new positions: coef * (sum_j w_j phi_j + affine)
 // (interpolate, thin_plate_spline_subdom.py:224-234).  On the lattice with the
 // (hi, lo) table the kernel sum runs in double-float on the FP32 pipe (~1e-14
-// relative per term), else in FP64.
+// relative per term), else in FP64.  When the block's positions and the centres lie
+// on one grid of the lattice whose offsets fit tab_cap entries (EVAL_TABLE, or 0 when
+// the launch has no room for them), the block reads the (hi, lo) values of the grid's
+// offsets from shared memory (the same table entries).
+constexpr int EVAL_TABLE = 2048;
+
 __global__ void __launch_bounds__(256)
     k_tps_eval(const int32_t* counts, const int64_t* offsets, const int32_t* indices,
                const int64_t* w_off, const double* weights, const double* cx, const double* cy,
                const int32_t* ncounts, const int64_t* noffsets, const int32_t* nindices,
                const double* ncoefs, const double* px, const double* py, double* partx,
                double* party, const double* table, const float2* table2, int64_t tsize,
-               const int32_t* cxy2, const int32_t* c_on_lattice, int max_members) {
+               const int32_t* cxy2, const int32_t* c_on_lattice, int max_members,
+               int tab_cap) {
   extern __shared__ double sh[];
   const int sd = blockIdx.y;
   const int N = counts[sd], n = N + 3, M = ncounts[sd];
@@ -1163,7 +1170,8 @@ __global__ void __launch_bounds__(256)
   int2* sxy2 = reinterpret_cast<int2*>(swy + NM + 3);   // lattice coordinates of the centres
   float2* dwx = reinterpret_cast<float2*>(sxy2 + NM);  // weights as (hi, lo) pairs
   float2* dwy = dwx + NM;
-  __shared__ int s_lat;
+  float2* tab = dwy + NM;  // tab_cap pairs: kernel values of the grid offsets
+  __shared__ int s_lat, s_red[6 * 32];
   const int64_t off = offsets[sd];
   const double* w = weights + w_off[sd];
   if (threadIdx.x == 0) s_lat = (cxy2 != nullptr && c_on_lattice != nullptr) ? *c_on_lattice : 0;
@@ -1182,16 +1190,62 @@ __global__ void __launch_bounds__(256)
     }
   }
   __syncthreads();
-  if (k >= M) return;
   const int64_t noff = noffsets[sd];
-  const int q = nindices[noff + k];
-  const double x = px[q], y = py[q];
+  const int q = k < M ? nindices[noff + k] : 0;
+  const double x = k < M ? px[q] : 0.0, y = k < M ? py[q] : 0.0;
   double vx = 0.0, vy = 0.0;
   const double X2 = 2.0 * x, Y2 = 2.0 * y;
-  const bool qlat = s_lat && table != nullptr && X2 == rint(X2) && Y2 == rint(Y2) &&
+  const bool qlat = k < M && s_lat && table != nullptr && X2 == rint(X2) && Y2 == rint(Y2) &&
                     fabs(X2) < 1073741824.0 && fabs(Y2) < 1073741824.0;
-  if (qlat && table2 != nullptr) {  // 4 r^2 in integers, double-float sums
-    const int tsz32 = (int)(tsize < (int64_t)INT_MAX ? tsize : (int64_t)INT_MAX);
+  const int tsz32 = (int)(tsize < (int64_t)INT_MAX ? tsize : (int64_t)INT_MAX);
+  // the grid through the centres and the block's lattice positions (origin: the first
+  // centre; every lattice coordinate is below 2^30 in magnitude, so offsets fit)
+  int tw = 0, QA = 0, QB = 0;
+  if (s_lat && table != nullptr && table2 != nullptr) {
+    const int2 o = sxy2[0];
+    int v[6];
+    lat_grid_init(v);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) lat_grid_add(v, sxy2[j].x - o.x, sxy2[j].y - o.y);
+    if (qlat) lat_grid_add(v, (int)X2 - o.x, (int)Y2 - o.y);
+    lat_grid_block(v, s_red);
+    const LatTable g = lat_table_of(v, tab_cap, tsz32);
+    if (g.ok) {  // centres to grid indices, the table, this position's grid indices
+      tw = g.wx;
+      const int ax0 = v[2], ay0 = v[4];  // smallest offsets: index 0 of each axis
+      for (int j = threadIdx.x; j < N; j += blockDim.x)
+        sxy2[j] = make_int2((sxy2[j].x - o.x - ax0) / g.gx, (sxy2[j].y - o.y - ay0) / g.gy);
+      for (int e = threadIdx.x; e < g.wx * g.wy; e += blockDim.x) {
+        const int b = e / g.wx, a = e - b * g.wx;
+        tab[e] = table2[(g.gy * b) * (g.gy * b) + (g.gx * a) * (g.gx * a)];
+      }
+      if (qlat) {
+        QA = ((int)X2 - o.x - ax0) / g.gx;
+        QB = ((int)Y2 - o.y - ay0) / g.gy;
+      }
+      __syncthreads();
+    }
+  }
+  if (k >= M) return;
+  if (qlat && tw > 0) {  // grid offsets in the shared table, double-float sums
+    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+    constexpr int U = 8;
+    for (int j0 = 0; j0 < N; j0 += U) {
+      float2 f[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int2 c = sxy2[min(j0 + u, N - 1)];
+        f[u] = tab[abs(QB - c.y) * tw + abs(QA - c.x)];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (j0 + u >= N) break;
+        df_mac(dwx[j0 + u], f[u], hx, lx);
+        df_mac(dwy[j0 + u], f[u], hy, ly);
+      }
+    }
+    vx += (double)hx + (double)lx;
+    vy += (double)hy + (double)ly;
+  } else if (qlat && table2 != nullptr) {  // 4 r^2 in integers, double-float sums
     const int QX = (int)X2, QY = (int)Y2;
     float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
     constexpr int U = 8;  // table loads issued ahead of their use
@@ -1487,11 +1541,14 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
              "fi_tps_interpolate: null pointer");
   FI_REQUIRE(nb_subdom > 0 && npts > 0, "fi_tps_interpolate: bad sizes");
   cudaStream_t s = (cudaStream_t)stream;
-  const size_t smem = (size_t)(4 * max_members + 6) * sizeof(double) +
+  const size_t base = (size_t)(4 * max_members + 6) * sizeof(double) +
                       (size_t)max_members * sizeof(int2) +
                       (size_t)2 * max_members * sizeof(float2);
-  FI_REQUIRE(smem <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
+  FI_REQUIRE(base <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
              max_members);
+  // the grid-offset table where it fits beside the subdomain's centres
+  const int tab_cap = base + (size_t)EVAL_TABLE * sizeof(float2) <= 200 * 1024 ? EVAL_TABLE : 0;
+  const size_t smem = base + (size_t)tab_cap * sizeof(float2);
   static SmemLimit limit;
   FI_CUDA_TRY(raise_smem_limit(k_tps_eval, smem, limit));
   if (max_new_members > 0) {
@@ -1500,7 +1557,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
     k_tps_eval<<<grid, threads, smem, s>>>(
         counts, offsets, indices, w_offsets, weights, cx, cy, ncounts, noffsets, nindices, ncoefs,
         px, py, partx, party, phi_table, reinterpret_cast<const float2*>(phi_table2), table_size,
-        cxy2, c_on_lattice, max_members);
+        cxy2, c_on_lattice, max_members, tab_cap);
     add_launches(1);
   }
   const int threads = 256;

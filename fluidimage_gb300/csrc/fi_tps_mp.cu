@@ -23,7 +23,9 @@
 //
 // K entries come from a table of phi(r^2) = r^2 log(r^2) / 2 indexed by 4 r^2,
 // exact for window centres on the half-integer lattice (the integer window shifts
-// put every PIV vector there); other distances use log() directly.
+// put every PIV vector there); other distances use log() directly.  When a
+// subdomain's centres lie on a grid of the lattice, the block keeps the (hi, lo)
+// values of every grid offset in shared memory (the same table entries).
 #include <cooperative_groups.h>
 
 #include <climits>
@@ -31,6 +33,7 @@
 
 #include "fi_common.cuh"
 #include "fi_df.cuh"
+#include "fi_lattice.cuh"
 
 namespace fi {
 
@@ -838,12 +841,40 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   }
   __syncthreads();
   const bool lat = s_lat != 0;
+  // Centres on the lattice: cxy becomes the grid indices ((2x - 2x_0) / gx,
+  // (2y - 2y_0) / gy) of the grid of steps (gx, gy) through them, and, when every
+  // offset of the grid's extent fits, tab holds the (hi, lo) kernel value of each
+  // offset (a, b) at tab[b tw + a] (tw = 0: no table).  The table lives in W's last n
+  // doubles, free until the refinement.
+  int gx = 1, gy = 1, tw = 0;
+  float2* tab = reinterpret_cast<float2*>(W + 3 * n);
+  const int tsz32 = (int)(table_size < (int64_t)INT_MAX ? table_size : (int64_t)INT_MAX);
+  if (lat) {
+    const int2 o = cxy[0];
+    int v[6];
+    lat_grid_init(v);
+    for (int i = threadIdx.x; i < N; i += NT) lat_grid_add(v, cxy[i].x - o.x, cxy[i].y - o.y);
+    lat_grid_block(v, reinterpret_cast<int*>(sh));
+    const LatTable g = lat_table_of(v, n, tsz32);
+    gx = g.gx;
+    gy = g.gy;
+    for (int i = threadIdx.x; i < N; i += NT)
+      cxy[i] = make_int2((cxy[i].x - o.x) / gx, (cxy[i].y - o.y) / gy);
+    if (g.ok && phi_table2 != nullptr) {
+      tw = g.wx;
+      for (int e = threadIdx.x; e < g.wx * g.wy; e += NT) {
+        const int b = e / g.wx, a = e - b * g.wx;
+        tab[e] = phi_table2[(gy * b) * (gy * b) + (gx * a) * (gx * a)];
+      }
+    }
+    __syncthreads();
+  }
   // A = K + lam I, entry (r, c); on the lattice 4 r^2 is an integer table index
   auto a_entry = [&](int r, int c) -> double {
     if (r == c) return lam;
     if (lat) {
       const int2 ca = cxy[r], cb = cxy[c];
-      const int64_t dx = (int64_t)(ca.x - cb.x), dy = (int64_t)(ca.y - cb.y);
+      const int64_t dx = (int64_t)gx * (ca.x - cb.x), dy = (int64_t)gy * (ca.y - cb.y);
       const int64_t kq = dy * dy + dx * dx;
       if (kq < table_size) return __ldg(phi_table + kq);
       return phi_pair(xc[r], yc[r], xc[c], yc[c], nullptr, 0);
@@ -856,7 +887,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
     if (i == j) return lam2;
     if (lat) {
       const int2 cj = cxy[j];
-      const int64_t dx = (int64_t)(ci.x - cj.x), dy = (int64_t)(ci.y - cj.y);
+      const int64_t dx = (int64_t)gx * (ci.x - cj.x), dy = (int64_t)gy * (ci.y - cj.y);
       const int64_t kq = dy * dy + dx * dx;
       if (kq < table_size)
         return phi_table2 != nullptr ? phi_table2[kq] : df_split(__ldg(phi_table + kq));
@@ -867,9 +898,21 @@ __global__ void __launch_bounds__(NT, 512 / NT)
   // entries (i, j0 .. j0 + cnt - 1) of A as pairs (0 < cnt <= 8, the rest zero): on the
   // lattice the eight table loads are issued before any is used (the loads, mostly
   // L2 hits, bound these phases), the diagonal and far entries patched afterwards
-  const int tsz32 = (int)(table_size < (int64_t)INT_MAX ? table_size : (int64_t)INT_MAX);
   auto a_batch_df = [&](int i, int2 ci, int j0, int cnt, float2(&out)[8]) {
-    if (lat && phi_table2 != nullptr) {
+    if (lat && tw > 0) {  // every offset in the shared table
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int2 cj = cxy[j0 + min(u, cnt - 1)];
+        out[u] = tab[abs(ci.y - cj.y) * tw + abs(ci.x - cj.x)];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (u >= cnt)
+          out[u] = make_float2(0.f, 0.f);
+        else if (j0 + u == i)
+          out[u] = lam2;
+      }
+    } else if (lat && phi_table2 != nullptr) {
       // 4 r^2 in 32-bit integers: the lattice coordinates are below 2^30 in magnitude,
       // so their differences fit, and |dx|, |dy| <= 32767 keeps dx^2 + dy^2 below
       // 2^31; farther pairs (beyond the table anyway) take the direct kernel value
@@ -877,7 +920,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int2 cj = cxy[j0 + min(u, cnt - 1)];
-        const int dx = ci.x - cj.x, dy = ci.y - cj.y;
+        const int dx = gx * (ci.x - cj.x), dy = gy * (ci.y - cj.y);
         const bool near = (unsigned)dx + 32767u <= 65534u && (unsigned)dy + 32767u <= 65534u;
         kq[u] = near ? dy * dy + dx * dx : INT_MAX;
         out[u] = phi_table2[kq[u] < tsz32 ? kq[u] : 0];
