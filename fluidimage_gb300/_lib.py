@@ -173,6 +173,9 @@ _SIGNATURES = {
     "fi_rank_equalize": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P, P]),
     "fi_gaussian_filter": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P]),
     "fi_sharpen_combine": (C.c_int, [P, P, C.c_int, C.c_int64, C.c_double, P, P]),
+    "fi_image_unpack": (C.c_int, [P, C.c_int64, P, C.c_int, C.c_int, C.c_int, C.c_int, P,
+                                  C.c_int, P, P, P]),
+    "fi_png_unfilter": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
     "fi_griddata": (
         C.c_int,

@@ -730,6 +730,30 @@ int fi_gaussian_filter(const void* in, void* out, void* tmp, int dtype, int nt, 
 int fi_sharpen_combine(const void* blurred, const void* filtered, int dtype, int64_t count,
                        double alpha, void* out, void* stream);
 
+/*
+ * Image decode (fluidimage.util.imread, util/util.py:46-59, which reads the image
+ * files through fluiddyn.io.image): writes the (height, width) image `out` (uint8 for
+ * 1-byte samples, uint16 for 2-byte samples) from a container's pixel payload `raw`
+ * (raw_bytes bytes on the device).  Row r starts at byte row_offsets[r] (device,
+ * height int64): TIFF strips, bottom-up BMP rows and row padding are offsets.
+ * 2-byte samples are big-endian when big_endian is set, else little-endian; lut
+ * (device, 256 bytes, nullable) maps 1-byte samples (a BMP palette); invert maps
+ * WhiteIsZero images to BlackIsZero (255 - v, 65535 - v).  A row outside the payload
+ * is written as zeros and sets *status to 1 (status: device int32, nullable).
+ */
+int fi_image_unpack(const uint8_t* raw, int64_t raw_bytes, const int64_t* row_offsets,
+                    int height, int width, int bytes_per_sample, int big_endian,
+                    const uint8_t* lut, int invert, void* out, int32_t* status, void* stream);
+
+/*
+ * PNG scanline reconstruction (the PNG files read by fluiddyn.io.image for
+ * fluidimage.util.imread; RFC 2083 section 6 filters None, Sub, Up, Average, Paeth).
+ * HOST memory, synchronous: `filtered` holds height rows of 1 + row_bytes bytes (the
+ * filter type byte, then the row), out receives height * row_bytes bytes; bpp = bytes
+ * per complete pixel (at least 1).  FI_ERR_INVALID on an undefined filter type.
+ */
+int fi_png_unfilter(const uint8_t* filtered, int height, int row_bytes, int bpp, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif
