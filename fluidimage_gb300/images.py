@@ -222,9 +222,11 @@ def imread(path) -> np.ndarray:
 
 
 def imread_device(path, device="cuda", stream=None):
-    """The image of ``path`` decoded into a (height, width) uint8 or uint16 torch tensor
-    on ``device``: one host-to-device copy of the pixel payload (with the row offsets
-    and the palette), then ``fi_image_unpack`` on the stream."""
+    """The image of ``path`` decoded into a (height, width) torch tensor on ``device``:
+    one host-to-device copy of the pixel payload (with the row offsets and the
+    palette), then ``fi_image_unpack`` on the stream.  8-bit images are uint8; 16-bit
+    images are uint16 values kept bit for bit in an int16 tensor, the device image
+    type of ``WorkPIV.calcul_device`` (``.view(torch.uint16)`` reads them as such)."""
     import torch
 
     p = read_payload(path)
@@ -240,7 +242,7 @@ def imread_device(path, device="cuda", stream=None):
     dev = torch.device(device)
     strm = stream if stream is not None else torch.cuda.current_stream(dev)
     out = torch.empty((p.height, p.width),
-                      dtype=torch.uint8 if p.bytes_per_sample == 1 else torch.uint16, device=dev)
+                      dtype=torch.uint8 if p.bytes_per_sample == 1 else torch.int16, device=dev)
     with torch.cuda.stream(strm):
         buf = torch.empty_like(host, device=dev)
         buf.copy_(host, non_blocking=True)

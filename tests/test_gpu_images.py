@@ -19,8 +19,8 @@ def test_imread_device_known_content(tmp_path, name, data, expected):
     path.write_bytes(data)
     got = images.imread_device(path, "cuda:0")
     assert got.device.type == "cuda" and got.shape == expected.shape
-    want = torch.from_numpy(expected.astype(np.int32))
-    assert torch.equal(got.cpu().to(torch.int32), want)
+    assert got.dtype == (torch.uint8 if expected.dtype == np.uint8 else torch.int16)
+    assert np.array_equal(got.cpu().numpy().view(expected.dtype), expected)
 
 
 def test_imread_device_full_size_frame(tmp_path):
@@ -36,4 +36,31 @@ def test_imread_device_full_size_frame(tmp_path):
     path.write_bytes(tiff_bytes(img, big_endian=True, rows_per_strip=37))
     assert np.array_equal(O.decode(path), img)
     got = images.imread_device(path, "cuda:0")
-    assert torch.equal(got.cpu().to(torch.int32), torch.from_numpy(img.astype(np.int32)))
+    assert np.array_equal(got.cpu().numpy().view(np.uint16), img)
+
+
+def test_decoded_frames_feed_the_pipeline(tmp_path):
+    """imread_device output goes straight into WorkPIV.calcul_device: the same field
+    as the host images through WorkPIV.calcul."""
+    import torch
+
+    from fluidimage_gb300 import WorkPIV, synthetic
+    from fluidimage_gb300.images import imread_device
+
+    model = synthetic.ParticleModel(density=0.05, noise=20.0, dtype="uint16")
+    im0, im1 = synthetic.make_pair((256, 320), synthetic.uniform_shift(2.3, -1.4), model,
+                                   seed=4)
+    p0, p1 = tmp_path / "a.tif", tmp_path / "b.tif"
+    p0.write_bytes(tiff_bytes(im0, rows_per_strip=16))
+    p1.write_bytes(tiff_bytes(im1, big_endian=True))
+    params = WorkPIV.create_default_params()
+    params.piv0.shape_crop_im0 = 32
+    params.multipass.number = 2
+    work = WorkPIV(params, device="cuda:0")
+    ref = work.calcul({"arrays": (im0, im1), "names": ("a", "b")})
+    outs = work.calcul_device(imread_device(p0, "cuda:0"), imread_device(p1, "cuda:0"))
+    torch.cuda.synchronize()
+    got = work.results_to_host(outs, None)
+    for k in range(2):
+        np.testing.assert_array_equal(got.passes[k].deltaxs, ref.passes[k].deltaxs)
+        np.testing.assert_array_equal(got.passes[k].deltays, ref.passes[k].deltays)
