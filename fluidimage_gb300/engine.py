@@ -287,6 +287,15 @@ _PINNED = threading.local()
 def _readback_many(regions, stream=None):
     """Device regions ``(address, nbytes)`` -> one bytes object each, through a pinned
     buffer kept per host thread, with one synchronisation of the stream."""
+    return _readback_finish(_readback_start(regions, stream, event=False))
+
+
+def _readback_start(regions, stream=None, event=True):
+    """Enqueue the copies of ``_readback_many`` on the stream; with ``event`` an event
+    recorded after them lets ``_readback_finish`` wait for the copies alone, so the
+    host can take the bytes while later work of the stream runs.  The thread's pinned
+    buffer is reused by the next readback of the thread: finish before starting
+    another."""
     torch = _torch()
     spans, total = [], 0
     for _, nbytes in regions:
@@ -301,7 +310,21 @@ def _readback_many(regions, stream=None):
     for (addr, nbytes), (off, _) in zip(regions, spans):
         L.check(lib.fi_memcpy_d2h(buf.data_ptr() + off, addr, nbytes, strm.cuda_stream),
                 "fi_memcpy_d2h")
-    strm.synchronize()
+    done = None
+    if event:
+        done = getattr(_PINNED, "event", None)
+        if done is None:
+            done = _PINNED.event = torch.cuda.Event()
+        done.record(strm)
+    return buf, spans, strm, done
+
+
+def _readback_finish(handle):
+    buf, spans, strm, done = handle
+    if done is not None:
+        done.synchronize()
+    else:
+        strm.synchronize()
     raw = buf.numpy()
     return [bytes(raw[off:off + nbytes]) for off, nbytes in spans]
 
@@ -413,13 +436,16 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                   int(p_given), cxy2, clat, pxy2, plat, cbounds, pbounds,
                                   counts, ncounts, offs, order, s),
                 "fi_tps_layout")
-        # the membership lists need no host value either: they run while the host waits
+        # the plan header and the totals are final after the layout: their copy goes
+        # first, and the membership lists (which need no host value) fill while the
+        # host reads them and prepares the solve
+        pending = _readback_start([(plan, C.sizeof(L.TpsPlan)), (offs + 32 * nsub_cap, 48)],
+                                  stream)
         L.check(lib.fi_tps_members_fill(plan, nsub_cap, cx, cy, nv_cap, L.ptr(px), L.ptr(py),
                                         npts, cxy2, clat, pxy2, plat, cbounds, pbounds, offs,
                                         idx, coefs, nidx, ncoefs, s),
                 "fi_tps_members_fill")
-        raw_hdr, raw_tot = _readback_many(
-            [(plan, C.sizeof(L.TpsPlan)), (offs + 32 * nsub_cap, 48)], stream)
+        raw_hdr, raw_tot = _readback_finish(pending)
         hdr = L.TpsPlan.from_buffer_copy(raw_hdr)
         if hdr.status == 1:
             raise InterpError("Only nan.")
