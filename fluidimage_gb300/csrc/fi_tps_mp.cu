@@ -1489,6 +1489,35 @@ extern "C" int fi_tps_phi_table2(float* table2, int64_t count, void* stream) {
   return check_launch("fi_tps_phi_table2");
 }
 
+// The tail of a launch of narrow blocks: with slots resident blocks per GPU, a solve
+// of slots < nb < 2 slots subdomains (in decreasing size) runs the first wave on the
+// caller's stream and the last nb - slots subdomains as clusters of two blocks on a
+// side stream (fork and join by events), queued behind the first wave: a cluster
+// shares a subdomain's build and projection over two blocks, so the small last
+// subdomains, which otherwise run alone after the first wave, finish sooner.  One
+// side stream and two events per host thread and device, created on first use.
+struct TailStreams {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+static cudaError_t tail_streams(int dev, TailStreams** out) {
+  static thread_local TailStreams per_dev[FI_SMEM_DEVICES];
+  if (dev < 0 || dev >= FI_SMEM_DEVICES) return cudaErrorInvalidDevice;
+  TailStreams& t = per_dev[dev];
+  if (t.side == nullptr) {
+    cudaError_t e = cudaStreamCreateWithFlags(&t.side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      t.side = nullptr;
+      return e;
+    }
+  }
+  *out = &t;
+  return cudaSuccess;
+}
+
 extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members,
                                const double* cx, const double* cy, const float* ux,
                                const float* uy, const int32_t* counts, const int64_t* offsets,
@@ -1546,11 +1575,47 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                    table_size, cxy2, c_on_lattice, threshold,
                                    use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
                                    iters, nfixed, status, max_udiff, sweeps, order, 60, N));
-  } else
-    k_tps_solve_mp<256><<<nb_subdom, 256, smem, (cudaStream_t)stream>>>(
+  } else {
+    int per_sm = 0;
+    FI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tps_solve_mp<256>,
+                                                              256, smem));
+    const int slots = per_sm * nsm;
+    const int head = (order != nullptr && slots > 0 && nb_subdom > slots &&
+                      nb_subdom < 2 * slots) ? slots : nb_subdom;
+    k_tps_solve_mp<256><<<head, 256, smem, (cudaStream_t)stream>>>(
         plan, cx, cy, ux, uy, counts, offsets, indices, mat_offsets, matrices, matrices32,
         phi_table, reinterpret_cast<const float2*>(phi_table2), table_size, cxy2, c_on_lattice,
         threshold, use_threshold, w_offsets, weights,
         smoothed_x, smoothed_y, iters, nfixed, status, max_udiff, sweeps, order, 60, N);
+    if (head < nb_subdom) {  // the last subdomains in clusters of two, on the side stream
+      FI_CUDA_TRY(cudaGetLastError());
+      TailStreams* ts = nullptr;
+      FI_CUDA_TRY(tail_streams(dev, &ts));
+      FI_CUDA_TRY(cudaEventRecord(ts->fork, (cudaStream_t)stream));
+      FI_CUDA_TRY(cudaStreamWaitEvent(ts->side, ts->fork, 0));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)(2 * (nb_subdom - head)));
+      cfg.blockDim = dim3(256);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = ts->side;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 2;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      FI_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_tps_solve_mp<256>, plan, cx, cy, ux, uy, counts,
+                                     offsets, indices, mat_offsets, matrices, matrices32,
+                                     phi_table, reinterpret_cast<const float2*>(phi_table2),
+                                     table_size, cxy2, c_on_lattice, threshold,
+                                     use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
+                                     iters, nfixed, status, max_udiff, sweeps, order + head, 60,
+                                     N));
+      FI_CUDA_TRY(cudaEventRecord(ts->join, ts->side));
+      FI_CUDA_TRY(cudaStreamWaitEvent((cudaStream_t)stream, ts->join, 0));
+      return check_launch("fi_tps_solve_mp", 2);
+    }
+  }
   return check_launch("fi_tps_solve_mp");
 }

@@ -516,7 +516,10 @@ int fi_tps_phi_table2(float* table2, int64_t count, void* stream);
  * Cholesky breakdown or no convergence.  sweeps (nullable, [nb_subdom]): refinement
  * sweeps (one FP32 solve each) per subdomain.  order (nullable, fi_tps_offsets):
  * the subdomains in the order the blocks take them (largest first shortens the
- * last wave).
+ * last wave).  With order, a solve of more subdomains than one wave of resident
+ * blocks but fewer than two runs its last subdomains as clusters of two blocks on a
+ * side stream of the library (one per host thread and device, created on the first
+ * such call), joined back into `stream` by an event before the call returns.
  */
 int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_members, const double* cx,
                     const double* cy, const float* ux, const float* uy, const int32_t* counts,
