@@ -1576,9 +1576,24 @@ extern "C" int fi_tps_solve_mp(const fi_tps_plan* plan, int nb_subdom, int max_m
                                    use_threshold, w_offsets, weights, smoothed_x, smoothed_y,
                                    iters, nfixed, status, max_udiff, sweeps, order, 60, N));
   } else {
-    int per_sm = 0;
-    FI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tps_solve_mp<256>,
-                                                              256, smem));
+    // resident narrow blocks per SM for this shared-memory size (queried once per
+    // device and size: the call sits between the host's readback and the launch)
+    static size_t occ_smem[FI_SMEM_DEVICES] = {};
+    static int occ_blocks[FI_SMEM_DEVICES] = {};
+    int per_sm = -1;
+    {
+      std::lock_guard<std::mutex> lock(smem_limit_mutex());
+      if (dev < FI_SMEM_DEVICES && occ_smem[dev] == smem) per_sm = occ_blocks[dev];
+    }
+    if (per_sm < 0) {
+      FI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tps_solve_mp<256>,
+                                                                256, smem));
+      std::lock_guard<std::mutex> lock(smem_limit_mutex());
+      if (dev < FI_SMEM_DEVICES) {
+        occ_smem[dev] = smem;
+        occ_blocks[dev] = per_sm;
+      }
+    }
     const int slots = per_sm * nsm;
     const int head = (order != nullptr && slots > 0 && nb_subdom > slots &&
                       nb_subdom < 2 * slots) ? slots : nb_subdom;
