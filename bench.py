@@ -11,8 +11,8 @@ field's (65025 per pair).
   (a 512 MiB write) between steps outside the timed events.
 * ``e2e``: the public API from pinned host images to host ``MultipassPIVResults``
   (host<->device copies inside the timed region): ``WorkPIV.calcul_series`` over a
-  series of pairs (three pairs in flight, each on its own host thread and CUDA
-  stream: 3.9 ms per pair against 4.1 with two and 4.5 with four), and
+  series of pairs (two pairs in flight, each on its own host thread and CUDA
+  stream: 3.8-4.1 ms per pair against 4.1-4.5 with three), and
   ``single_call``: ``WorkPIV.calcul``, one pair per call.
 * ``roofline``: the dominant kernel (the TPS subdomain solve), timed with CUDA
   events inside the timed steps: its algorithmic bytes (one write and one read of
@@ -390,7 +390,7 @@ def run_gpu(args):
         res = work.calcul({"arrays": (h0, h1), "names": ("im0", "im1")})
         torch.cuda.synchronize()
         single_ms.append(1e3 * (time.perf_counter() - t_start))
-    # a series of pairs (WorkPIV.calcul_series: three pairs in flight, each on its own
+    # a series of pairs (WorkPIV.calcul_series: two pairs in flight, each on its own
     # host thread and CUDA stream, so that one pair's kernels fill the GPU while the
     # other waits on the host); four distinct pinned pairs in rotation
     # (circular shifts of the pair), each step moving > 0.5 GB of TPS matrices
@@ -443,7 +443,7 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(im0.nbytes + im1.nbytes),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": series_ms,
-                "api": f"WorkPIV.calcul_series over {n_series} pairs, 3 pairs in flight "
+                "api": f"WorkPIV.calcul_series over {n_series} pairs, 2 pairs in flight "
                        "(own host thread and CUDA stream each)",
                 "single_call": {"value": single_value, "unit": UNIT,
                                 "ms_per_step": single_mean,

@@ -234,7 +234,7 @@ class WorkPIV:
         handle = _fetch_start(list(want.values()))
         return self._host_results(outs, couple, dict(zip(want, _fetch_finish(handle))))
 
-    def calcul_series(self, couples, streams=3):
+    def calcul_series(self, couples, streams=2):
         """Results of a series of couples, in order (a generator).  ``streams`` couples
         are in flight at once, each on its own host thread and CUDA stream: the GPU
         works on one couple's kernels while another couple's host-side steps (the TPS
