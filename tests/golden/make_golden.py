@@ -384,6 +384,27 @@ def case_preproc():
     print("wrote preproc.npz")
 
 
+def case_minimal_piv_oseen():
+    """The configuration of upstream's own test_minimal_piv (works/piv/test_piv.py:16-34)
+    on its Oseen sample pair (image_samples/Oseen/Images/Oseen_center_01/02.tif, 8-bit
+    TIFF, read with this package's image reader since PIL is absent here): 32 -> 16 px
+    windows at overlap -3 (windows 96 px apart in the first pass), two peaks searched,
+    TPS between the passes on a grid of 3 x 2 vectors, fix.displacement_max 3."""
+    from fluidimage_gb300.images import imread
+
+    import os
+
+    samples = Path(os.environ[refharness.SRC_ENV]).parent / "image_samples" / "Oseen" / "Images"
+    im0 = imread(samples / "Oseen_center_01.tif")
+    im1 = imread(samples / "Oseen_center_02.tif")
+    run_workpiv("minimal_piv_oseen", im0, im1, {
+        "piv0.shape_crop_im0": 32, "piv0.grid.overlap": -3,
+        "piv0.nb_peaks_to_search": 2,
+        "multipass.number": 2, "multipass.use_tps": True,
+        "fix.displacement_max": 3, "fix.threshold_diff_neighbour": 2,
+    })
+
+
 CASES = {
     "correl_window": case_correl_window,
     "single_pass_c1": case_single_pass_c1,
@@ -397,6 +418,7 @@ CASES = {
     "multipass_48_24": case_window_48_24,
     "overlap_075": case_overlap_075,
     "preproc": case_preproc,
+    "minimal_piv_oseen": case_minimal_piv_oseen,
 }
 
 if __name__ == "__main__":

@@ -211,7 +211,8 @@ def _compare_secondary(z, ip, r, tie, report):
                                   "griddata_two_pass", "griddata_oseen_three_pass",
                                   "subpix_gaussian_single", "subpix_centroid2_single",
                                   "subpix_none_single", "multipass_48_24",
-                                  "single_pass_24_ov75", "multipass_64_32_ov75"])
+                                  "single_pass_24_ov75", "multipass_64_32_ov75",
+                                  "minimal_piv_oseen"])
 def test_workpiv_matches_reference(name):
     z, res = _run(name)
     assert len(res.passes) == int(z["nb_passes"])
