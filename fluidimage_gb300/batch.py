@@ -80,6 +80,12 @@ class PIVBatch:
                 raise NotImplementedError(
                     "PIVBatch runs the FP32 FFT correlation (method_correl 'gb300', "
                     f"'np.fft' or 'fftw'), not {params.piv0.method_correl!r}")
+            n = int(params.piv0.shape_crop_im0) if not isinstance(
+                params.piv0.shape_crop_im0, (list, tuple)) else -1
+            if n not in L.BATCH_WPB:
+                raise NotImplementedError(
+                    f"PIVBatch: windows of {params.piv0.shape_crop_im0} px (batched sizes: "
+                    f"{sorted(L.BATCH_WPB)})")
             t0, t1 = _to_dev(im0, dev), _to_dev(im1, dev)
             key = (id(params), tuple(t0.shape), _np_dtype(t0))
             if key not in pipes:

@@ -132,12 +132,12 @@ __global__ void k_min_batch_decode(const fi_piv_pass_args* __restrict__ passes, 
 using namespace fi;
 
 extern "C" int fi_piv_batch_items(int n, int nvec, int wpb) {
-  if (!supported_n(n) || nvec <= 0 || !batch_wpb_ok(n, wpb)) return -1;
+  if (!supported_n_batch(n) || nvec <= 0 || !batch_wpb_ok(n, wpb)) return -1;
   return (nvec + wpb - 1) / wpb;
 }
 
 extern "C" int fi_piv_batch_max_blocks(int n, int wpb) {
-  if (!supported_n(n) || !batch_wpb_ok(n, wpb)) return -1;
+  if (!supported_n_batch(n) || !batch_wpb_ok(n, wpb)) return -1;
   const int threads = wpb * group_threads(n);
   const int smem = wpb * batch_group_bytes_n(n);
   int per_sm = 0;
@@ -176,7 +176,7 @@ extern "C" int fi_piv_pass_batch(const fi_piv_pass_args* pass_args, const int32_
                                  void* stream) {
   FI_REQUIRE(pass_args && item_start && counter, "fi_piv_pass_batch: null pointer");
   FI_REQUIRE(npass > 0 && items > 0, "fi_piv_pass_batch: empty batch");
-  FI_REQUIRE(supported_n(n), "fi_piv_pass_batch: window size %d not supported", n);
+  FI_REQUIRE(supported_n_batch(n), "fi_piv_pass_batch: window size %d not supported", n);
   FI_REQUIRE(batch_wpb_ok(n, wpb),
              "fi_piv_pass_batch: %d windows per item not available for %d px windows", wpb, n);
   cudaStream_t s = (cudaStream_t)stream;

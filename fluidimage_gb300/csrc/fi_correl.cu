@@ -263,7 +263,7 @@ extern "C" int fi_images_min(const void* im0, const void* im1, int dtype, int64_
 extern "C" int fi_piv_pass(const fi_piv_pass_args* args, void* stream) {
   FI_REQUIRE(args, "fi_piv_pass: null args");
   const fi_piv_pass_args& a = *args;
-  FI_REQUIRE(supported_n(a.n), "fi_piv_pass: window size %d not supported (16, 24, 32, 48, 64)",
+  FI_REQUIRE(supported_n(a.n), "fi_piv_pass: window size %d not supported (8, 12, 16, 24, 32, 48, 64)",
              a.n);
   FI_REQUIRE(a.im0 && a.im1 && a.im_min && a.ixvecs && a.iyvecs, "fi_piv_pass: null input");
   FI_REQUIRE(a.deltaxs && a.deltays && a.correls_max && a.errors && a.xs && a.ys,
@@ -292,6 +292,8 @@ extern "C" int fi_piv_pass(const fi_piv_pass_args* args, void* stream) {
   const int npad = a.n / 2 + (a.n % 2);
   cudaStream_t s = (cudaStream_t)stream;
   switch (a.n) {
+    case 8: return launch_pass<8, false>(a, nullptr, nullptr, nvec, npad, 1, s);
+    case 12: return launch_pass<12, false>(a, nullptr, nullptr, nvec, npad, 1, s);
     case 16: return launch_pass<16, false>(a, nullptr, nullptr, nvec, npad, 1, s);
     case 24: return launch_pass<24, false>(a, nullptr, nullptr, nvec, npad, 1, s);
     case 32: return launch_pass<32, false>(a, nullptr, nullptr, nvec, npad, 1, s);
@@ -311,6 +313,8 @@ extern "C" int fi_correl_windows(const float* win0, const float* win1, int count
   a.norms = norms;
   cudaStream_t s = (cudaStream_t)stream;
   switch (n) {
+    case 8: return launch_pass<8, true>(a, win0, win1, count, 0, 0, s);
+    case 12: return launch_pass<12, true>(a, win0, win1, count, 0, 0, s);
     case 16: return launch_pass<16, true>(a, win0, win1, count, 0, 0, s);
     case 24: return launch_pass<24, true>(a, win0, win1, count, 0, 0, s);
     case 32: return launch_pass<32, true>(a, win0, win1, count, 0, 0, s);
@@ -378,6 +382,8 @@ extern "C" int fi_peaks_from_planes(float* planes, const double* norms, int coun
     return launch_peaks<NN>(planes, norms, count, pa, deltaxs, deltays, correls_max, errors, \
                             peak_i0, peak_i1, peaks_count, peaks, peaks_err, s);
   switch (n) {
+    FI_PEAKS_CASE(8)
+    FI_PEAKS_CASE(12)
     FI_PEAKS_CASE(16)
     FI_PEAKS_CASE(24)
     FI_PEAKS_CASE(32)

@@ -29,7 +29,7 @@ from .errors import ERROR_STRINGS, GridError, InterpError  # noqa: F401  (ERROR_
 _DTYPES = {np.dtype(np.uint8): L.FI_U8, np.dtype(np.uint16): L.FI_U16,
            np.dtype(np.float32): L.FI_F32}
 
-SUPPORTED_WINDOWS = (16, 24, 32, 48, 64)
+SUPPORTED_WINDOWS = (8, 12, 16, 24, 32, 48, 64)
 
 
 def _torch():

@@ -405,6 +405,26 @@ def case_minimal_piv_oseen():
     })
 
 
+def case_small_windows():
+    """Windows of 12 and 8 px: upstream's default parameters with three passes (48 ->
+    24 -> 12 px, use_tps 'last': griddata between the passes, TPS at the end) on a
+    288x320 uint16 12-bit Oseen pair, and 16 -> 8 px with TPS between the passes on a
+    160x192 uint8 pair moving by under 2 px."""
+    model = synthetic.ParticleModel(density=0.05, diameter=(2.0, 3.0), intensity=(1000, 4000),
+                                    noise=20.0, dtype="uint16", max_value=4095)
+    field = synthetic.oseen_vortex((288, 320), d_max=5.0, rc=50.0)
+    im0, im1 = synthetic.make_pair((288, 320), field, model, seed=9100)
+    run_workpiv("multipass_48_24_12", im0, im1, {"multipass.number": 3})
+    model8 = synthetic.ParticleModel(density=0.06, noise=2.0, dtype="uint8")
+    im0, im1 = synthetic.make_pair((160, 192), synthetic.sinusoid(1.6, 96.0), model8, seed=9101)
+    run_workpiv("multipass_16_8", im0, im1, {
+        "piv0.shape_crop_im0": 16, "piv0.grid.overlap": 0.5,
+        "multipass.number": 2, "multipass.use_tps": True,
+        "multipass.subdom_size": 100, "multipass.smoothing_coef": 1.0,
+        "fix.threshold_diff_neighbour": 2,
+    })
+
+
 CASES = {
     "correl_window": case_correl_window,
     "single_pass_c1": case_single_pass_c1,
@@ -419,6 +439,7 @@ CASES = {
     "overlap_075": case_overlap_075,
     "preproc": case_preproc,
     "minimal_piv_oseen": case_minimal_piv_oseen,
+    "small_windows": case_small_windows,
 }
 
 if __name__ == "__main__":
