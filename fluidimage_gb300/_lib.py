@@ -177,6 +177,8 @@ _SIGNATURES = {
                                   C.c_int, P, P, P]),
     "fi_png_unfilter": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P]),
     "fi_tps_blend_centers": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P, P, P]),
+    "fi_tps_smooth_fields": (C.c_int, [P, P, C.c_int, P, P, C.c_int, C.c_double, C.c_double, P,
+                                       C.c_int, P, P, P, P, P, P, P, P, P]),
     "fi_griddata": (
         C.c_int,
         [P, P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, C.c_int, P, P, P, P, P, P, P,

@@ -1523,6 +1523,69 @@ extern "C" int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, co
   return check_launch("fi_tps_blend_centers");
 }
 
+// The *_smooth fields of the last pass (singlepass.py:515-529).  First the final grid:
+// its positions (px + offx, py + offy rounded to float32) and the interpolated field.
+__global__ void k_smooth_grid(const double* __restrict__ px, const double* __restrict__ py,
+                              int npts, double offx, double offy,
+                              const double* __restrict__ out_x,
+                              const double* __restrict__ out_y, float* xs_s, float* ys_s,
+                              double* dx_s, double* dy_s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npts; i += gridDim.x * blockDim.x) {
+    xs_s[i] = __double2float_rn(__dadd_rn(px[i], offx));
+    ys_s[i] = __double2float_rn(__dadd_rn(py[i], offy));
+    dx_s[i] = out_x[i];
+    dy_s[i] = out_y[i];
+  }
+}
+
+// Then, at the selected vectors (sel[k]: their index on the grid), their own positions
+// (the pass's xs / ys when vec_xy, else the grid's) and their smoothed values.
+__global__ void k_smooth_sel(const int32_t* __restrict__ sel, int n_sel,
+                             const double* __restrict__ px, const double* __restrict__ py,
+                             const float* __restrict__ xs, const float* __restrict__ ys,
+                             int npts, int vec_xy, double offx, double offy,
+                             const double* __restrict__ smooth_x,
+                             const double* __restrict__ smooth_y, float* xs_s, float* ys_s,
+                             double* dx_s, double* dy_s) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_sel; k += gridDim.x * blockDim.x) {
+    const int i = sel[k];
+    if (i < 0 || i >= npts) continue;
+    const double x = vec_xy ? (double)xs[i] : px[i];
+    const double y = vec_xy ? (double)ys[i] : py[i];
+    xs_s[i] = __double2float_rn(__dadd_rn(x, offx));
+    ys_s[i] = __double2float_rn(__dadd_rn(y, offy));
+    dx_s[i] = smooth_x[k];
+    dy_s[i] = smooth_y[k];
+  }
+}
+
+extern "C" int fi_tps_smooth_fields(const double* px, const double* py, int npts, const float* xs,
+                                    const float* ys, int vec_xy, double offx, double offy,
+                                    const int32_t* sel, int n_sel, const double* out_x,
+                                    const double* out_y, const double* smooth_x,
+                                    const double* smooth_y, float* xs_s, float* ys_s,
+                                    double* dx_s, double* dy_s, void* stream) {
+  FI_REQUIRE(px && py && out_x && out_y && xs_s && ys_s && dx_s && dy_s && npts > 0,
+             "fi_tps_smooth_fields: bad arguments");
+  FI_REQUIRE(n_sel >= 0 && (n_sel == 0 || (sel && smooth_x && smooth_y)) &&
+                 (!vec_xy || (xs && ys)),
+             "fi_tps_smooth_fields: bad selection arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int threads = 256;
+  const int gb = (npts + threads - 1) / threads;
+  k_smooth_grid<<<gb < 1024 ? gb : 1024, threads, 0, s>>>(px, py, npts, offx, offy, out_x, out_y,
+                                                          xs_s, ys_s, dx_s, dy_s);
+  int launched = 1;
+  if (n_sel > 0) {
+    const int sb = (n_sel + threads - 1) / threads;
+    k_smooth_sel<<<sb < 1024 ? sb : 1024, threads, 0, s>>>(sel, n_sel, px, py, xs, ys, npts,
+                                                           vec_xy, offx, offy, smooth_x,
+                                                           smooth_y, xs_s, ys_s, dx_s, dy_s);
+    ++launched;
+  }
+  return check_launch("fi_tps_smooth_fields", launched);
+}
+
 extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                                   int max_new_members, const double* cx, const double* cy,
                                   const int32_t* counts, const int64_t* offsets,

@@ -305,19 +305,23 @@ class WorkPIV:
                 if tag == "tps_final":
                     # the *_smooth fields (singlepass.py:515-529): the grid with the
                     # selected vectors' values scattered in, built on the device
+                    import torch
+
                     lay = pd.layout
-                    sel = tps.selection[: tps.num_centers].long()
-                    gx, gy = lay.dev["px"] + offx, lay.dev["py"] + offy
-                    sx = gx if lay.index == 0 else pd.xs.double() + offx
-                    sy = gy if lay.index == 0 else pd.ys.double() + offy
-                    xs_s, ys_s = gx.float(), gy.float()
-                    xs_s[sel] = sx[sel].float()
-                    ys_s[sel] = sy[sel].float()
+                    npts = lay.nvec
+                    xs_s = torch.empty(npts, dtype=torch.float32, device=tps.out_x.device)
+                    ys_s = torch.empty_like(xs_s)
+                    dx_s = torch.empty_like(tps.out_x)
+                    dy_s = torch.empty_like(tps.out_y)
+                    _lib.check(_lib.load().fi_tps_smooth_fields(
+                        _lib.ptr(lay.dev["px"]), _lib.ptr(lay.dev["py"]), npts, _lib.ptr(pd.xs),
+                        _lib.ptr(pd.ys), int(lay.index != 0), float(offx), float(offy),
+                        _lib.ptr(tps.selection), int(tps.num_centers), _lib.ptr(tps.out_x),
+                        _lib.ptr(tps.out_y), _lib.ptr(tps.smooth_x), _lib.ptr(tps.smooth_y),
+                        _lib.ptr(xs_s), _lib.ptr(ys_s), _lib.ptr(dx_s), _lib.ptr(dy_s),
+                        _lib.stream_handle()), "fi_tps_smooth_fields")
                     want[(k, tag, "xs_smooth")], want[(k, tag, "ys_smooth")] = xs_s, ys_s
-                    want[(k, tag, "dx_smooth")] = tps.out_x.clone().index_copy_(
-                        0, sel, tps.smooth_x)
-                    want[(k, tag, "dy_smooth")] = tps.out_y.clone().index_copy_(
-                        0, sel, tps.smooth_y)
+                    want[(k, tag, "dx_smooth")], want[(k, tag, "dy_smooth")] = dx_s, dy_s
         return want
 
     def _host_results(self, outs, couple, got):

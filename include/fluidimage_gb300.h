@@ -566,6 +566,19 @@ int fi_tps_blend_centers(const fi_tps_plan* plan, int num_centers, const double*
                          const double* smoothed_y, double* out_x, double* out_y, void* stream);
 
 /*
+ * The *_smooth fields of the last pass (works/piv/singlepass.py:515-529): xs_s/ys_s
+ * (float32) = px/py + offx/offy of the final grid, dx_s/dy_s = out_x/out_y, except at
+ * the n_sel selected vectors (sel[k], int32: their index on the grid), which take
+ * their own positions (xs/ys float32 + offsets when vec_xy, else the grid's) and the
+ * smoothed values smooth_x[k]/smooth_y[k].  Sums in float64, rounded to float32.
+ */
+int fi_tps_smooth_fields(const double* px, const double* py, int npts, const float* xs,
+                         const float* ys, int vec_xy, double offx, double offy,
+                         const int32_t* sel, int n_sel, const double* out_x,
+                         const double* out_y, const double* smooth_x, const double* smooth_y,
+                         float* xs_s, float* ys_s, double* dx_s, double* dy_s, void* stream);
+
+/*
  * Interpolation at npts new positions (init_with_new_positions + interpolate,
  * thin_plate_spline_subdom.py:161-234): out_x/out_y float64 and, if not NULL,
  * out_rx/out_ry = round-half-even to int32 (the window shifts of the next pass,
