@@ -205,7 +205,10 @@ def read_payload(path) -> Payload:
     reader = _READERS.get(data[:2])
     if reader is None:
         raise NotImplementedError(f"{path}: image format not supported (TIFF, BMP, PNG)")
-    return reader(data).check()
+    try:
+        return reader(data).check()
+    except (KeyError, IndexError, struct.error, zlib.error) as error:
+        raise ValueError(f"{path}: malformed or truncated image file ({error!r})") from error
 
 
 def imread(path) -> np.ndarray:

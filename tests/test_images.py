@@ -76,3 +76,15 @@ def test_unsupported_and_corrupt_files(tmp_path):
     unknown.write_bytes(b"\0" * 64)
     with pytest.raises(NotImplementedError, match="not supported"):
         images.imread(unknown)
+
+
+def test_truncated_files_raise_value_error(tmp_path):
+    from imagefiles import bmp_bytes, tiff_bytes
+
+    img = np.arange(64, dtype=np.uint8).reshape(8, 8)
+    for name, data in (("t.tif", tiff_bytes(img)[:40]), ("t.bmp", bmp_bytes(img)[:60]),
+                       ("t.png", png_bytes(img)[:45])):
+        path = tmp_path / name
+        path.write_bytes(data)
+        with pytest.raises(ValueError):
+            images.imread(path)
