@@ -38,7 +38,8 @@ TC_FORMS = {"bf16x1": 0, "bf16x3": 1, "fp16x3": 2}
 #: window size of the tensor-core pass
 TC_WINDOW = 32
 #: windows per work item of the batch kernel, per window size (autotuner choices)
-BATCH_WPB = {16: (16, 8), 24: (8, 4), 32: (8, 4), 48: (2, 1), 64: (2, 1)}
+BATCH_WPB = {8: (16, 8), 12: (16, 8), 16: (16, 8), 24: (8, 4), 32: (8, 4), 48: (2, 1),
+             64: (2, 1)}
 MAX_NSUBPIX = 4
 MAX_PEAKS = 4
 PEAK_FIELDS = 5

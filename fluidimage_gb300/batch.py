@@ -3,7 +3,7 @@
 A series of couples is what a PIV topology feeds to its works, one couple per
 process in the reference (topologies/piv.py:143-151 with the executors of
 executors/multi_exec_async.py:114-158).  Here the couples of a batch, each with its
-own image size, dtype, window size (16-64 px), overlap and parameters, run
+own image size, dtype, window size (8-64 px), overlap and parameters, run
 together:
 
 * the image minima of every pair in one launch (``fi_images_min_batch``);

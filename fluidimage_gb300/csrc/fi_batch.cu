@@ -64,6 +64,8 @@ static int group_threads(int n) { return n <= 16 ? 16 : (n <= 32 ? 32 : 64); }
 
 static int batch_group_bytes_n(int n) {
   switch (n) {
+    case 8: return Cfg<8>::GROUP_BYTES;
+    case 12: return Cfg<12>::GROUP_BYTES;
     case 16: return Cfg<16>::GROUP_BYTES;
     case 24: return Cfg<24>::GROUP_BYTES;
     case 32: return Cfg<32>::GROUP_BYTES;
@@ -76,7 +78,7 @@ static int batch_group_bytes_n(int n) {
 // kernel's windows per block and half of it
 static bool batch_wpb_ok(int n, int wpb) {
   switch (n) {
-    case 16: return wpb == 16 || wpb == 8;
+    case 8: case 12: case 16: return wpb == 16 || wpb == 8;
     case 24: case 32: return wpb == 8 || wpb == 4;
     default: return wpb == 2 || wpb == 1;
   }
@@ -150,6 +152,7 @@ extern "C" int fi_piv_batch_max_blocks(int n, int wpb) {
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_piv_batch<NN, WW>, threads, \
                                                         (size_t)smem);                         \
   }
+  FI_OCC(8, 16) FI_OCC(8, 8) FI_OCC(12, 16) FI_OCC(12, 8)
   FI_OCC(16, 16) FI_OCC(16, 8) FI_OCC(24, 8) FI_OCC(24, 4) FI_OCC(32, 8) FI_OCC(32, 4)
   FI_OCC(48, 2) FI_OCC(48, 1) FI_OCC(64, 2) FI_OCC(64, 1)
 #undef FI_OCC
@@ -183,6 +186,7 @@ extern "C" int fi_piv_pass_batch(const fi_piv_pass_args* pass_args, const int32_
   FI_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int32_t), s));
 #define FI_BATCH(NN, WW) \
   if (n == NN && wpb == WW) return launch_batch<NN, WW>(pass_args, item_start, npass, items, counter, s);
+  FI_BATCH(8, 16) FI_BATCH(8, 8) FI_BATCH(12, 16) FI_BATCH(12, 8)
   FI_BATCH(16, 16) FI_BATCH(16, 8) FI_BATCH(24, 8) FI_BATCH(24, 4) FI_BATCH(32, 8) FI_BATCH(32, 4)
   FI_BATCH(48, 2) FI_BATCH(48, 1) FI_BATCH(64, 2) FI_BATCH(64, 1)
 #undef FI_BATCH

@@ -12,14 +12,11 @@
 namespace fi {
 
 // Window sizes of the passes (square windows; 2^a 3^b register FFTs).
-// window sizes of the single-pass kernels (register FFTs of 2^a 3^b points) and of the
-// batched kernels (tuned work-item sizes)
+// window sizes of the single-pass and batched kernels (register FFTs of 2^a 3^b points)
 inline bool supported_n(int n) {
   return n == 8 || n == 12 || n == 16 || n == 24 || n == 32 || n == 48 || n == 64;
 }
-inline bool supported_n_batch(int n) {
-  return n == 16 || n == 24 || n == 32 || n == 48 || n == 64;
-}
+inline bool supported_n_batch(int n) { return supported_n(n); }
 
 // Row `r` of the two windows of an integer image pair (pixels x..x+N-1 of rows y0r
 // and y1r, zero outside the image, minus the image minima) staged into Zrow as

@@ -1,5 +1,5 @@
 """Batched single-pass PIV (PIVBatch): pairs of mixed image sizes, dtypes, window
-sizes (16-64 px) and overlaps in one batch give the results of WorkPIV on each
+sizes (8-64 px) and overlaps in one batch give the results of WorkPIV on each
 pair alone, with direct launches, after autotuning and through a CUDA graph replay.
 The per-window code is the same, compiled into another kernel, so float32 rounding
 may differ by an ulp: validity, error strings and vector positions must be equal,
@@ -23,6 +23,8 @@ def _jobs():
         ((256, 256), "float32", 64, 0.5, synthetic.uniform_shift(-5.2, -2.7)),
         ((192, 160), "uint16", 16, 0.75, synthetic.sinusoid(3.0, 160.0)),
         ((320, 256), "uint8", 32, 0.75, synthetic.uniform_shift(1.3, 5.1)),
+        ((96, 128), "uint8", 12, 0.5, synthetic.uniform_shift(1.4, -0.8)),
+        ((80, 112), "uint16", 8, 0.5, synthetic.uniform_shift(-0.7, 1.2)),
     ]
     jobs = []
     for k, (shape, dtype, n, ov, field) in enumerate(specs):
@@ -66,7 +68,7 @@ def test_batch_matches_workpiv():
     want = [WorkPIV(p, interp_last=False).calcul({"arrays": (a, b), "names": ("a", "b")}).passes[0]
             for a, b, p in jobs]
     batch = PIVBatch(jobs)
-    assert set(batch.groups) == {16, 24, 32, 48, 64}
+    assert set(batch.groups) == {8, 12, 16, 24, 32, 48, 64}
     batch.run()
     torch.cuda.synchronize()
     _check(batch.results(), want)
