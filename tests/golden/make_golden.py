@@ -120,6 +120,8 @@ def case_correl_window():
         ("sq24", (24, 24), (2.6, -3.1), None),
         ("sq48", (48, 48), (-5.3, 4.4), None),
         ("sq48_dmax", (48, 48), (-5.3, 4.4), 9.0),
+        ("sq12", (12, 12), (1.6, -2.2), None),
+        ("sq8", (8, 8), (1.2, 0.7), None),
     ]
     for icase, (tag, shape, shift, dmax) in enumerate(rng_cases):
         model = synthetic.ParticleModel(density=0.06, noise=2.0, dtype="uint8")
