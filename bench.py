@@ -925,7 +925,7 @@ def run_preproc(args):
     print(json.dumps(out), flush=True)
 
 
-def window_size_passes(args, dev, sizes=(16, 24, 32, 48, 64), reps=10):
+def window_size_passes(args, dev, sizes=(8, 12, 16, 24, 32, 48, 64), reps=10):
     """One FP32 pass (with WorkFIX) per window size on the 2048^2 pair of the
     multipass workload, overlap 0.5, no interpolation: the window count, the best of
     ``reps`` CUDA-event timings and the time per window."""
