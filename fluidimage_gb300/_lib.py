@@ -189,7 +189,7 @@ _SIGNATURES = {
     "fi_tps_interpolate": (
         C.c_int,
         [P, C.c_int, C.c_int, C.c_int, P, P, P, P, P, P, P, P, P, C.c_int, P, P, P, P, P, P,
-         P, P, P, P, P, P, C.c_int64, P, P, P],
+         P, P, P, P, P, P, C.c_int64, P, P, C.c_int, P],
     ),
 }
 

@@ -1144,9 +1144,10 @@ __global__ void k_tps_blend_centers(const fi_tps_plan* plan_ptr, const double* c
 // (interpolate, thin_plate_spline_subdom.py:224-234).  On the lattice with the
 // (hi, lo) table the kernel sum runs in double-float on the FP32 pipe (~1e-14
 // relative per term), else in FP64.  When the block's positions and the centres lie
-// on one grid of the lattice whose offsets fit tab_cap entries (EVAL_TABLE, or 0 when
-// the launch has no room for them), the block reads the (hi, lo) values of the grid's
-// offsets from shared memory (the same table entries).
+// on one grid of the lattice, or the centres half a pixel off it along an axis (the
+// final evaluation, on the grid of the pass's own windows), and the grid's offsets fit
+// tab_cap entries (0 when the launch has no room for them), the block reads the
+// (hi, lo) values of the grid's offsets from shared memory (the same table entries).
 constexpr int EVAL_TABLE = 2048;
 
 __global__ void __launch_bounds__(256)
@@ -1200,7 +1201,7 @@ __global__ void __launch_bounds__(256)
   const int tsz32 = (int)(tsize < (int64_t)INT_MAX ? tsize : (int64_t)INT_MAX);
   // the grid through the centres and the block's lattice positions (origin: the first
   // centre; every lattice coordinate is below 2^30 in magnitude, so offsets fit)
-  int tw = 0, QA = 0, QB = 0;
+  int tw = 0, jw = 0, QA = 0, QB = 0;
   if (s_lat && table != nullptr && table2 != nullptr) {
     const int2 o = sxy2[0];
     int v[6];
@@ -1223,10 +1224,100 @@ __global__ void __launch_bounds__(256)
         QB = ((int)Y2 - o.y - ay0) / g.gy;
       }
       __syncthreads();
+    } else {
+      // The positions on a grid of steps (gx, gy) >= 4 (origin: the block's first
+      // position) and every centre on it or half a pixel (one lattice unit) after it
+      // along each axis (the midpoints of odd window shifts): a centre is at
+      // o + g A + e (e in {0, 1}), an offset p - c = g k - e, so |p - c| is g |k|, g |k| + 1
+      // (e = 1, k <= 0) or g k - 1 (e = 1, k >= 1): the table holds the kernel value of
+      // each (|k|, case) pair per axis, row length jw = 3 Kx.
+      const int q0 = nindices[noff + (int64_t)blockIdx.x * blockDim.x];
+      const double PX2 = 2.0 * px[q0], PY2 = 2.0 * py[q0];
+      const bool oklat = PX2 == rint(PX2) && PY2 == rint(PY2) && fabs(PX2) < 1073741824.0 &&
+                         fabs(PY2) < 1073741824.0;
+      if (oklat) {  // uniform: every thread read the same position
+        const int OX = (int)PX2, OY = (int)PY2;
+        int vp[6];
+        lat_grid_init(vp);
+        if (qlat) lat_grid_add(vp, (int)X2 - OX, (int)Y2 - OY);
+        lat_grid_block(vp, s_red);
+        const int gpx = vp[0], gpy = vp[1];
+        // every position of the block is on the lattice when qlat holds for all of
+        // them: count the others (in the gcd slot, as 0 / 1) with the centres below
+        if (gpx >= 4 && gpy >= 4) {
+          int vc[6];
+          lat_grid_init(vc);
+          vc[0] = (k < M && !qlat) ? 1 : 0;
+          for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            const int dx = sxy2[j].x - OX, dy = sxy2[j].y - OY;
+            const int ax = (dx >= 0) ? dx / gpx : -((-dx + gpx - 1) / gpx);  // floor
+            const int ay = (dy >= 0) ? dy / gpy : -((-dy + gpy - 1) / gpy);
+            const int ex = dx - ax * gpx, ey = dy - ay * gpy;
+            if (ex > 1 || ey > 1) vc[0] = 1;
+            vc[2] = min(vc[2], ax);
+            vc[3] = max(vc[3], ax);
+            vc[4] = min(vc[4], ay);
+            vc[5] = max(vc[5], ay);
+          }
+          lat_grid_block(vc, s_red);
+          // grid indices of the positions: offsets / g (exact)
+          const int pax0 = vp[2] / gpx, pax1 = vp[3] / gpx, pay0 = vp[4] / gpy,
+                    pay1 = vp[5] / gpy;
+          const int kx = max(pax1 - vc[2], vc[3] - pax0) + 1;
+          const int ky = max(pay1 - vc[4], vc[5] - pay0) + 1;
+          const int64_t ex = (int64_t)gpx * kx + 1, ey = (int64_t)gpy * ky + 1;
+          if (vc[0] == 0 && vc[2] <= vc[3] && kx > 0 && ky > 0 &&
+              (int64_t)9 * kx * ky <= tab_cap && ex <= 32767 && ey <= 32767 &&
+              ex * ex + ey * ey < (int64_t)tsz32) {
+            jw = 3 * kx;
+            for (int j = threadIdx.x; j < N; j += blockDim.x) {
+              const int dx = sxy2[j].x - OX, dy = sxy2[j].y - OY;
+              const int ax = (dx >= 0) ? dx / gpx : -((-dx + gpx - 1) / gpx);
+              const int ay = (dy >= 0) ? dy / gpy : -((-dy + gpy - 1) / gpy);
+              sxy2[j] = make_int2(2 * ax + (dx - ax * gpx), 2 * ay + (dy - ay * gpy));
+            }
+            for (int e = threadIdx.x; e < 9 * kx * ky; e += blockDim.x) {
+              const int r = e / jw, c = e - r * jw;
+              const int axx = c / 3, sx = c - 3 * axx, ayy = r / 3, sy = r - 3 * ayy;
+              const int adx = gpx * axx + (sx == 1 ? 1 : (sx == 2 ? -1 : 0));
+              const int ady = gpy * ayy + (sy == 1 ? 1 : (sy == 2 ? -1 : 0));
+              tab[e] = (adx < 0 || ady < 0) ? make_float2(0.f, 0.f)
+                                            : table2[ady * ady + adx * adx];
+            }
+            if (qlat) {
+              QA = ((int)X2 - OX) / gpx;
+              QB = ((int)Y2 - OY) / gpy;
+            }
+          }
+          __syncthreads();
+        }
+      }
     }
   }
   if (k >= M) return;
-  if (qlat && tw > 0) {  // grid offsets in the shared table, double-float sums
+  if (qlat && jw > 0) {  // offsets of the jittered grid in the shared table
+    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
+    constexpr int U = 8;
+    for (int j0 = 0; j0 < N; j0 += U) {
+      float2 f[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int2 c = sxy2[min(j0 + u, N - 1)];
+        const int kx = QA - (c.x >> 1), ky = QB - (c.y >> 1);
+        const int sx = (c.x & 1) ? (kx <= 0 ? 1 : 2) : 0;
+        const int sy = (c.y & 1) ? (ky <= 0 ? 1 : 2) : 0;
+        f[u] = tab[(3 * abs(ky) + sy) * jw + 3 * abs(kx) + sx];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (j0 + u >= N) break;
+        df_mac(dwx[j0 + u], f[u], hx, lx);
+        df_mac(dwy[j0 + u], f[u], hy, ly);
+      }
+    }
+    vx += (double)hx + (double)lx;
+    vy += (double)hy + (double)ly;
+  } else if (qlat && tw > 0) {  // grid offsets in the shared table, double-float sums
     float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
     constexpr int U = 8;
     for (int j0 = 0; j0 < N; j0 += U) {
@@ -1597,7 +1688,7 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                                   int32_t* out_ry, const double* phi_table,
                                   const float* phi_table2, int64_t table_size,
                                   const int32_t* cxy2, const int32_t* c_on_lattice,
-                                  void* stream) {
+                                  int table_entries, void* stream) {
   FI_REQUIRE(plan && cx && cy && counts && offsets && indices && w_offsets && weights && px &&
                  py && ncounts && noffsets && nindices && ncoefs && partx && party && out_x &&
                  out_y,
@@ -1609,8 +1700,12 @@ extern "C" int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int ma
                       (size_t)2 * max_members * sizeof(float2);
   FI_REQUIRE(base <= 200 * 1024, "fi_tps_interpolate: subdomain of %d vectors too large",
              max_members);
-  // the grid-offset table where it fits beside the subdomain's centres
-  const int tab_cap = base + (size_t)EVAL_TABLE * sizeof(float2) <= 200 * 1024 ? EVAL_TABLE : 0;
+  // the grid-offset table (at least EVAL_TABLE entries) where it fits beside the
+  // subdomain's centres
+  FI_REQUIRE(table_entries >= 0 && table_entries <= 16384,
+             "fi_tps_interpolate: table_entries %d out of [0, 16384]", table_entries);
+  const int want = table_entries > EVAL_TABLE ? table_entries : EVAL_TABLE;
+  const int tab_cap = base + (size_t)want * sizeof(float2) <= 200 * 1024 ? want : 0;
   const size_t smem = base + (size_t)tab_cap * sizeof(float2);
   static SmemLimit limit;
   FI_CUDA_TRY(raise_smem_limit(k_tps_eval, smem, limit));

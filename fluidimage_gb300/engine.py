@@ -222,6 +222,9 @@ class TpsOutput:
 #: phi(k / 4) for k < PHI_TABLE_SIZE covers distances up to ~1024 px on the
 #: half-integer lattice (32 MiB per device); larger distances use log() directly.
 PHI_TABLE_SIZE = 1 << 22
+#: entries of the shared table of kernel values that the final TPS evaluation asks
+#: for (9 K^2 for offsets up to K - 1 grid steps: K = 26 covers subdomains of ~25 steps)
+FINAL_EVAL_TABLE = 6144
 #: largest subdomain handled by the mixed-precision solver (shared-memory bound)
 MP_MAX_MEMBERS = 800
 _PHI_TABLES = {}
@@ -498,10 +501,13 @@ def run_tps(xs, ys, dx, dy, nvec, px, py, npts, subdom_size, smoothing_coef,
                                          smooth_x, smooth_y, s),
                 "fi_tps_blend_centers")
     with _timed("fi_tps_interpolate"):
+        # the final evaluation (on the grid of the pass's own windows, whose vectors
+        # sit on it or half a pixel off it) gets the larger shared table of offsets
         L.check(lib.fi_tps_interpolate(plan, nsub, maxc, maxnc, cx, cy, counts, off_d, idx,
                                        woff_d, weights, L.ptr(px), L.ptr(py), npts, ncounts,
                                        noff_d, nidx, ncoefs, partx, party, out_x, out_y, rx, ry,
-                                       table, table2, PHI_TABLE_SIZE, cxy2, clat, s),
+                                       table, table2, PHI_TABLE_SIZE, cxy2, clat,
+                                       FINAL_EVAL_TABLE if want_smooth else 0, s),
                 "fi_tps_interpolate")
     # tensors for what the caller keeps (built while the GPU works)
     out = TpsOutput(

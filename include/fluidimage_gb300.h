@@ -587,6 +587,10 @@ int fi_tps_smooth_fields(const double* px, const double* py, int npts, const flo
  * as nindices.  cxy2/c_on_lattice (nullable, from fi_tps_lattice on the centres)
  * enable integer 4 r^2 table indices; with phi_table2 (nullable, fi_tps_phi_table2)
  * the kernel sums on the lattice run in double-float (~1e-14 relative per term).
+ * table_entries (0: 2048, at most 16384): capacity of the per-block shared-memory
+ * copy of the kernel values of a grid's offsets, used where the new positions lie on
+ * a grid and the centres on it or half a pixel off it (a larger table costs shared
+ * memory, and so L1 capacity, on every block of the launch).
  */
 int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        int max_new_members, const double* cx, const double* cy,
@@ -597,7 +601,7 @@ int fi_tps_interpolate(const fi_tps_plan* plan, int nb_subdom, int max_members,
                        double* partx, double* party, double* out_x, double* out_y,
                        int32_t* out_rx, int32_t* out_ry, const double* phi_table,
                        const float* phi_table2, int64_t table_size, const int32_t* cxy2,
-                       const int32_t* c_on_lattice, void* stream);
+                       const int32_t* c_on_lattice, int table_entries, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Image preprocessing (works/preproc/_toolbox_py.py)
