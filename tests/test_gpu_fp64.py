@@ -6,7 +6,6 @@ interpolated field within 0.005 px; correlation planes within 2e-6 relative to
 each plane's maximum (FP32 FFTs of mean-removed, power-of-two-scaled windows).
 """
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu

@@ -4,8 +4,6 @@ grids with holes.  Points the kernel flags (cells of cocircular centres, where
 several Delaunay triangulations exist and scipy follows Qhull's, or equidistant
 nearest centres) are counted and left out; elsewhere the values agree to 1e-9."""
 
-import ctypes as C
-
 import numpy as np
 import pytest
 

@@ -333,8 +333,6 @@ def test_members_index_range_matches_full_scan(order):
     """fi_tps_members restricted by fi_tps_y_bounds gives the same ordered members as
     the scan over every point, for row-ordered and for shuffled points (on and off
     the half-integer lattice)."""
-    import ctypes as C
-
     import torch
 
     from fluidimage_gb300 import _lib as L, engine

@@ -5,8 +5,6 @@ ones, against numpy's compaction and the oracle's layout: the centres, values an
 selection exactly, the header (count, subdomain grid, smoothing, extremes, buffers)
 exactly."""
 
-import ctypes as C
-
 import numpy as np
 import pytest
 

@@ -5,7 +5,6 @@ topology, and the fork guard (CPU); thread and fork executors on the GPU
 import pytest
 
 from fluidimage_gb300 import ParamContainer, WorkPIV
-from fluidimage_gb300 import piv as piv_mod
 from fluidimage_gb300.topology import topology_piv_class
 
 
